@@ -1,0 +1,954 @@
+/*
+ * ecmg_oracle.c -- CPU oracle (test infrastructure, see ecmg_oracle.h).
+ *
+ * Each function restates one reference function; the comment above it gives
+ * the file:line it follows.  Operand order of every float expression is the
+ * reference's; build with -ffp-contract=off.
+ */
+#include "ecmg_oracle.h"
+#include "../ecmgenerator_gb300/csrc/ecmg_tmath.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define OG_EPS 0.0001f /* Utility::EPSILON, ECMGenerator/Configuration.h:14 */
+
+/* ---------------------------------------------------------------------------
+ * Vec2 / Point algebra, ECMGenerator/ECMDataTypes.h:13-104 and
+ * MathUtility, ECMGenerator/UtilityFunctions.cpp:15-349
+ * ------------------------------------------------------------------------- */
+static inline og_v2 v2(float x, float y) { og_v2 r; r.x = x; r.y = y; return r; }
+static inline og_v2 vadd(og_v2 a, og_v2 b) { return v2(a.x + b.x, a.y + b.y); }
+static inline og_v2 vsub(og_v2 a, og_v2 b) { return v2(a.x - b.x, a.y - b.y); }
+static inline og_v2 vmul(og_v2 a, float s) { return v2(a.x * s, a.y * s); }
+static inline og_v2 vdiv(og_v2 a, float s) { return v2(a.x / s, a.y / s); }
+static inline float vlen(og_v2 a) { return sqrtf(a.x * a.x + a.y * a.y); }
+static inline float vlen2(og_v2 a) { return a.x * a.x + a.y * a.y; }
+static inline float vdot(og_v2 a, og_v2 b) { return a.x * b.x + a.y * b.y; }
+static inline float vdet(og_v2 a, og_v2 b) { return a.x * b.y - a.y * b.x; }
+static inline og_v2 vright(og_v2 a) { return v2(a.y, -a.x); }
+static inline og_v2 vleft(og_v2 a) { return v2(-a.y, a.x); }
+/* Vec2::Normalize (ECMDataTypes.h:45-52) */
+static inline og_v2 vnormalize(og_v2 a)
+{
+    float l = vlen(a);
+    if (l == 0.0f) return a;
+    a.x /= l;
+    a.y /= l;
+    return a;
+}
+/* Vec2::Normalized (ECMDataTypes.h:54-60); the reference returns an
+   uninitialised Vec2 for a zero vector, this returns (0,0). */
+static inline og_v2 vnormalized(og_v2 a)
+{
+    float l = vlen(a);
+    if (l == 0.0f) return v2(0.0f, 0.0f);
+    return v2(a.x / l, a.y / l);
+}
+/* Point::Approximate (ECMDataTypes.cpp:97-100) */
+static inline int vapprox(og_v2 p, og_v2 a)
+{
+    return p.x < (a.x + OG_EPS) && p.x > (a.x - OG_EPS) && p.y < (a.y + OG_EPS) && p.y > (a.y - OG_EPS);
+}
+/* MathUtility::SquareDistance(Point,Point) (UtilityFunctions.cpp:32-39): p2 - p1 */
+static inline float vsqdist(og_v2 p1, og_v2 p2)
+{
+    float dx = p2.x - p1.x, dy = p2.y - p1.y;
+    return dx * dx + dy * dy;
+}
+/* MathUtility::GetClosestPointOnSegment (UtilityFunctions.cpp:287-306) */
+static og_v2 closest_on_segment(og_v2 point, og_v2 s1, og_v2 s2)
+{
+    if (vapprox(s1, s2)) return s1;
+    og_v2 seg = vsub(s2, s1);
+    og_v2 pts = vsub(point, s1);
+    float tsq = vsqdist(s1, s2);
+    float d = (pts.x * seg.x + pts.y * seg.y) / tsq;
+    if (d > 1.0f) d = 1.0f;
+    if (d < 0.0f) d = 0.0f;
+    return v2(s1.x + d * seg.x, s1.y + d * seg.y);
+}
+/* MathUtility::RotateVector (UtilityFunctions.cpp:233-242) */
+static og_v2 rotate(og_v2 v, float rad, int libm)
+{
+    float cs, sn;
+    if (libm) {
+        cs = cosf(rad);
+        sn = sinf(rad);
+    } else {
+        ecmg_sincosf(rad, &sn, &cs);
+    }
+    float px = v.x * cs - v.y * sn;
+    float py = v.x * sn + v.y * cs;
+    return v2(px, py);
+}
+
+/* ---------------------------------------------------------------------------
+ * kNN
+ * ------------------------------------------------------------------------- */
+
+/* Exact k nearest neighbours, ordered by (d2, id).  This is the neighbour
+   definition the GPU grid query must reproduce bit for bit; the reference's
+   kd-tree (below) is a different, approximate query.  d2 is computed exactly
+   as KDTree.cpp:107-108 computes it, self and coincident agents are excluded
+   by the same d2 > EPSILON test (KDTree.cpp:112). */
+int og_knn_exact(const og_state* s, int agent, int k, float r2, int* out_ids, float* out_d2)
+{
+    og_v2 t = s->pos[agent];
+    int n = 0;
+    for (int j = 0; j <= s->last_idx; j++) {
+        if (!s->active[j]) continue;
+        float dx = s->pos[j].x - t.x;
+        float dy = s->pos[j].y - t.y;
+        float d2 = dx * dx + dy * dy;
+        if (!(d2 > OG_EPS) || !(d2 < r2)) continue;
+        /* insertion into the sorted top-k list */
+        if (n == k && !(d2 < out_d2[k - 1])) continue; /* ties: ids arrive ascending */
+        int pos = n < k ? n : k - 1;
+        while (pos > 0 && d2 < out_d2[pos - 1]) {
+            out_d2[pos] = out_d2[pos - 1];
+            out_ids[pos] = out_ids[pos - 1];
+            pos--;
+        }
+        out_d2[pos] = d2;
+        out_ids[pos] = j;
+        if (n < k) n++;
+    }
+    return n;
+}
+
+struct og_kdtree {
+    int k;
+    int* tree;
+    int tree_cap;
+    int tree_size;
+    int max_depth;
+    int* cache;   /* ORCA::m_NeighborCache, persists across agents and ticks */
+    float* dist;  /* nearestSqDistances (fresh per query)                   */
+    int* idx;
+    int idx_cap;
+    const og_v2* sort_pos;
+};
+
+og_kdtree* og_kdtree_create(int k)
+{
+    og_kdtree* t = (og_kdtree*)calloc(1, sizeof(og_kdtree));
+    t->k = k;
+    t->cache = (int*)calloc((size_t)k, sizeof(int)); /* std::vector<int>::resize -> 0 */
+    t->dist = (float*)malloc(sizeof(float) * (size_t)k);
+    return t;
+}
+
+void og_kdtree_destroy(og_kdtree* t)
+{
+    if (!t) return;
+    free(t->tree);
+    free(t->cache);
+    free(t->dist);
+    free(t->idx);
+    free(t);
+}
+
+/* stable merge sort of ids by one coordinate (std::sort in the reference;
+   identical result whenever the coordinates are distinct) */
+static void msort(int* a, int* tmp, int n, const og_v2* pos, int axis)
+{
+    if (n < 2) return;
+    int h = n / 2;
+    msort(a, tmp, h, pos, axis);
+    msort(a + h, tmp, n - h, pos, axis);
+    int i = 0, j = h, o = 0;
+    while (i < h && j < n) {
+        float ka = axis ? pos[a[i]].y : pos[a[i]].x;
+        float kb = axis ? pos[a[j]].y : pos[a[j]].x;
+        if (kb < ka) tmp[o++] = a[j++];
+        else tmp[o++] = a[i++];
+    }
+    while (i < h) tmp[o++] = a[i++];
+    while (j < n) tmp[o++] = a[j++];
+    memcpy(a, tmp, sizeof(int) * (size_t)n);
+}
+
+/* KDTree::ConstructRecursive (KDTree.cpp:59-83) */
+static void kd_rec(og_kdtree* t, int index, int lo, int hi, int depth, int* ids, int* tmp)
+{
+    if (lo >= hi) return;
+    msort(ids + lo, tmp, hi - lo, t->sort_pos, depth % 2);
+    int mid = lo + (hi - 1 - lo) / 2;
+    t->tree[index] = ids[mid];
+    kd_rec(t, index * 2 + 1, lo, mid, depth + 1, ids, tmp);
+    kd_rec(t, index * 2 + 2, mid + 1, hi, depth + 1, ids, tmp);
+}
+
+/* KDTree::Construct (KDTree.cpp:22-57) */
+void og_kdtree_build(og_kdtree* t, const og_state* s)
+{
+    int size = s->num_agents;
+    if (size == 0) return; /* the reference keeps the previous tree */
+    if (t->idx_cap < size) {
+        free(t->idx);
+        t->idx = (int*)malloc(sizeof(int) * (size_t)size * 2);
+        t->idx_cap = size;
+    }
+    int c = 0;
+    for (int i = 0; i <= s->last_idx; i++)
+        if (s->active[i]) t->idx[c++] = i;
+    t->max_depth = (int)ceil(log2((double)size + 1.0) - 1.0);
+    int tsize = (int)pow(2.0, (double)(t->max_depth + 1)) - 1;
+    if (t->tree_cap < tsize) {
+        free(t->tree);
+        t->tree = (int*)malloc(sizeof(int) * (size_t)tsize);
+        t->tree_cap = tsize;
+    }
+    t->tree_size = tsize;
+    for (int i = 0; i < tsize; i++) t->tree[i] = -1;
+    t->sort_pos = s->pos;
+    kd_rec(t, 0, 0, size, 0, t->idx, t->idx + t->idx_cap);
+}
+
+/* KDTree::KNearestAgents_R (KDTree.cpp:98-202), quirks included */
+static void kd_knn_rec(og_kdtree* t, const og_v2* pos, og_v2 target, int cur, int k, int* kfound, int depth)
+{
+    if (depth > t->max_depth) return;
+    if (t->tree[cur] == -1) return;
+    og_v2 cp = pos[t->tree[cur]];
+    float dx = cp.x - target.x, dy = cp.y - target.y;
+    float d = dx * dx + dy * dy;
+    int* ni = t->cache;
+    float* nd = t->dist;
+    if (*kfound < k && d > OG_EPS) {
+        ni[*kfound] = t->tree[cur];
+        nd[*kfound] = d;
+        (*kfound)++;
+        if (*kfound == k) {
+            float largest = d;
+            int li = k - 1;
+            for (int i = 0; i < k - 1; i++)
+                if (nd[i] > largest) { largest = nd[i]; li = i; }
+            nd[0] = largest;
+            ni[0] = ni[li];
+            nd[li] = d;
+            ni[li] = t->tree[cur];
+        }
+    } else {
+        *kfound = k;
+        if (d < nd[0] && d > OG_EPS) {
+            nd[0] = d;
+            ni[0] = t->tree[cur];
+            float largest = d;
+            int li = 0;
+            for (int i = 1; i < k; i++)
+                if (nd[i] > largest) { largest = nd[i]; li = i; }
+            nd[0] = largest;
+            ni[0] = ni[li];
+            nd[li] = d;
+            ni[li] = t->tree[cur];
+        }
+    }
+    float cv = depth % 2 == 0 ? cp.x : cp.y;
+    float tv = depth % 2 == 0 ? target.x : target.y;
+    if (tv < cv) {
+        kd_knn_rec(t, pos, target, cur * 2 + 1, k, kfound, depth + 1);
+        float db = tv - cv;
+        if (db * db < nd[k - 1]) kd_knn_rec(t, pos, target, cur * 2 + 2, k, kfound, depth + 1);
+    } else {
+        kd_knn_rec(t, pos, target, cur * 2 + 2, k, kfound, depth + 1);
+        float db = tv - cv;
+        if (db * db < nd[k - 1]) kd_knn_rec(t, pos, target, cur * 2 + 1, k, kfound, depth + 1);
+    }
+}
+
+/* KDTree::KNearestAgents (KDTree.cpp:85-96): returns kFound, list in the cache */
+int og_kdtree_query(og_kdtree* t, const og_state* s, int agent, int* out_ids)
+{
+    int k = t->k;
+    for (int i = 0; i < k; i++) t->dist[i] = FLT_MAX;
+    int kfound = 0;
+    kd_knn_rec(t, s->pos, s->pos[agent], 0, k, &kfound, 0);
+    if (out_ids)
+        for (int i = 0; i < k; i++) out_ids[i] = t->cache[i];
+    return kfound;
+}
+
+/* ---------------------------------------------------------------------------
+ * Simulator::FindNearestObstacles (ECMAgentSimulator/Simulator.cpp:259-292)
+ * ------------------------------------------------------------------------- */
+int og_find_obstacles(const og_obstacles* o, og_v2 pos, float range_sq, int* out, int cap, int libm)
+{
+    int n = 0;
+    for (int i = 0; i < o->n_verts; i++) {
+        og_v2 a = o->p[i];
+        og_v2 b = o->p[o->next[i]];
+        /* LineLeftDistance (UtilityFunctions.cpp:28-31): Det(v1 - p, v2 - v1) */
+        float sld = vdet(vsub(a, pos), vsub(b, a));
+        float num = libm ? powf(sld, 2.0f) : sld * sld;
+        float sq = num / vsqdist(a, b);
+        if (sq < range_sq) {
+            if (sld < 0.0f) {
+                og_v2 c = closest_on_segment(pos, a, b);
+                if (vsqdist(c, pos) < range_sq) {
+                    if (n < cap) out[n] = i;
+                    n++;
+                }
+            }
+        }
+    }
+    return n;
+}
+
+/* ---------------------------------------------------------------------------
+ * ORCA::GenerateConstraints (ECMAgentSimulator/ORCA.cpp:60-424)
+ * A constraint is stored as 4 floats: point.x, point.y, normal.x, normal.y
+ * (Constraint::Init, ORCA.h:29-47; slope/intercepts are unused by the LP).
+ * ------------------------------------------------------------------------- */
+static inline int push_con(float* c, int n, int cap, og_v2 p, og_v2 nrm)
+{
+    if (n < cap) {
+        c[4 * n + 0] = p.x;
+        c[4 * n + 1] = p.y;
+        c[4 * n + 2] = nrm.x;
+        c[4 * n + 3] = nrm.y;
+    }
+    return n + 1;
+}
+
+int og_generate_constraints(const og_obstacles* o, const og_state* s, const og_params* p, int agent,
+                            const int* nbrs, int n_nbrs, const int* obst, int n_obst_cand,
+                            float* cons, int cap, int* out_n_obst)
+{
+    og_v2 position = s->pos[agent];
+    og_v2 velocity = s->vel[agent];
+    float clr = s->clear[agent];
+    int n = 0;
+    const og_v2 zero = v2(0.0f, 0.0f);
+    const float inf = INFINITY;
+
+    for (int i = 0; i < n_obst_cand; i++) {
+        int L = obst[i];
+        int R = o->next[L];
+        og_v2 rp1 = vsub(o->p[L], position);
+        og_v2 rp2 = vsub(o->p[R], position);
+        og_v2 seg = vsub(o->p[R], o->p[L]);
+        const float sparam = vdot(vmul(rp1, -1.0f), seg) / vlen2(seg);
+        const float distSqLine = vlen2(vsub(vmul(rp1, -1.0f), vmul(seg, sparam)));
+        const float distSq1 = vlen2(rp1);
+        const float distSq2 = vlen2(rp2);
+        seg = vnormalize(seg);
+        const float radiusSq = clr * clr;
+
+        if (sparam < 0.0f && distSq1 <= radiusSq) { /* ORCA.cpp:92-105 */
+            if (o->convex[L]) n = push_con(cons, n, cap, zero, vnormalized(vmul(rp1, -1.0f)));
+            continue;
+        } else if (sparam > 1.0f && distSq2 <= radiusSq) { /* ORCA.cpp:108-121 */
+            og_v2 rnd = vnormalize(vsub(o->p[o->next[R]], o->p[R]));
+            if (o->convex[R] && vdet(rp2, rnd) >= 0.0f)
+                n = push_con(cons, n, cap, zero, vnormalized(vmul(rp2, -1.0f)));
+            continue;
+        } else if (sparam >= 0.0f && sparam < 1.0f && distSqLine <= radiusSq) { /* ORCA.cpp:124-135 */
+            n = push_con(cons, n, cap, zero, vright(seg));
+            continue;
+        }
+
+        og_v2 leftLeg, rightLeg;
+        if (sparam < 0.0f && distSqLine <= radiusSq) { /* ORCA.cpp:146-169 */
+            if (!o->convex[L]) continue;
+            R = L;
+            const float leg1 = sqrtf(distSq1 - radiusSq);
+            leftLeg = vdiv(v2(rp1.x * leg1 - rp1.y * clr, rp1.x * clr + rp1.y * leg1), distSq1);
+            rightLeg = vdiv(v2(rp1.x * leg1 + rp1.y * clr, -rp1.x * clr + rp1.y * leg1), distSq1);
+        } else if (sparam > 1.0f && distSqLine <= radiusSq) { /* ORCA.cpp:171-183 */
+            if (!o->convex[R]) continue;
+            L = R;
+            const float leg2 = sqrtf(distSq2 - radiusSq);
+            leftLeg = vdiv(v2(rp2.x * leg2 - rp2.y * clr, rp2.x * clr + rp2.y * leg2), distSq2);
+            rightLeg = vdiv(v2(rp2.x * leg2 + rp2.y * clr, -rp2.x * clr + rp2.y * leg2), distSq2);
+        } else { /* ORCA.cpp:186-212 */
+            if (o->convex[L]) {
+                const float leg1 = sqrtf(distSq1 - radiusSq);
+                leftLeg = vdiv(v2(rp1.x * leg1 - rp1.y * clr, rp1.x * clr + rp1.y * leg1), distSq1);
+            } else {
+                leftLeg = vmul(seg, -1.0f);
+            }
+            if (o->convex[R]) {
+                const float leg2 = sqrtf(distSq2 - radiusSq);
+                rightLeg = vdiv(v2(rp2.x * leg2 + rp2.y * clr, -rp2.x * clr + rp2.y * leg2), distSq2);
+            } else {
+                rightLeg = seg;
+            }
+        }
+
+        /* foreign legs, ORCA.cpp:218-239 */
+        int leftNeighbor = o->prev[L];
+        int isLeftForeign = 0, isRightForeign = 0;
+        og_v2 lnd = vnormalize(vsub(o->p[L], o->p[leftNeighbor]));
+        if (o->convex[L] && vdet(leftLeg, vmul(lnd, -1.0f)) >= 0.0f) {
+            leftLeg = vmul(lnd, -1.0f);
+            isLeftForeign = 1;
+        }
+        og_v2 rnd = vnormalize(vsub(o->p[o->next[R]], o->p[R]));
+        if (o->convex[R] && vdet(rightLeg, rnd) <= 0.0f) {
+            rightLeg = rnd;
+            isRightForeign = 1;
+        }
+
+        /* cut-off, ORCA.cpp:241-332 */
+        float invT = 1.0f / p->tau_obst;
+        const og_v2 leftCutoff = vmul(vsub(o->p[L], position), invT);
+        const og_v2 rightCutoff = vmul(vsub(o->p[R], position), invT);
+        const og_v2 cutoffVec = vsub(rightCutoff, leftCutoff);
+        const float t = (L == R ? 0.5f : vdot(vsub(velocity, leftCutoff), cutoffVec) / vlen2(cutoffVec));
+        const float tLeft = vdot(vsub(velocity, leftCutoff), leftLeg);
+        const float tRight = vdot(vsub(velocity, rightCutoff), rightLeg);
+
+        if ((t < 0.0f && tLeft < 0.0f) || (L == R && tLeft < 0.0f && tRight < 0.0f)) {
+            og_v2 unitW = vnormalized(vsub(velocity, leftCutoff));
+            og_v2 pc = vadd(leftCutoff, vmul(vmul(unitW, invT), clr));
+            n = push_con(cons, n, cap, pc, unitW);
+            continue;
+        } else if (t > 1.0f && tRight < 0.0f) {
+            og_v2 unitW = vnormalized(vsub(velocity, rightCutoff));
+            og_v2 pc = vadd(rightCutoff, vmul(vmul(unitW, invT), clr));
+            n = push_con(cons, n, cap, pc, unitW);
+            continue;
+        }
+
+        const float distSqCutoff = ((t < 0.0f || t > 1.0f || L == R) ? inf
+                                    : vlen2(vsub(velocity, vadd(leftCutoff, vmul(cutoffVec, t)))));
+        const float distSqLeft = ((tLeft < 0.0f) ? inf : vlen2(vsub(velocity, vadd(leftCutoff, vmul(leftLeg, tLeft)))));
+        const float distSqRight = ((tRight < 0.0f) ? inf : vlen2(vsub(velocity, vadd(rightCutoff, vmul(rightLeg, tRight)))));
+
+        if (distSqCutoff <= distSqLeft && distSqCutoff <= distSqRight) {
+            og_v2 normal = vleft(vmul(seg, -1.0f));
+            og_v2 pc = vadd(leftCutoff, vmul(vmul(normal, invT), clr));
+            n = push_con(cons, n, cap, pc, normal);
+            continue;
+        } else if (distSqLeft <= distSqRight) {
+            if (isLeftForeign) continue;
+            og_v2 normal = vleft(leftLeg);
+            og_v2 pc = vadd(leftCutoff, vmul(vmul(normal, clr), invT));
+            n = push_con(cons, n, cap, pc, normal);
+            continue;
+        } else {
+            if (isRightForeign) continue;
+            og_v2 normal = vright(rightLeg);
+            og_v2 pc = vadd(rightCutoff, vmul(vmul(normal, clr), invT));
+            n = push_con(cons, n, cap, pc, normal);
+            continue;
+        }
+    }
+    *out_n_obst = n;
+
+    /* agent constraints, ORCA.cpp:339-423 */
+    const float ta = p->tau_agent;
+    for (int i = 0; i < n_nbrs; i++) {
+        int nb = nbrs[i];
+        og_v2 np = s->pos[nb];
+        og_v2 nv = s->vel[nb];
+        float nc = s->clear[nb];
+        og_v2 VOPos = v2((np.x - position.x) / ta, (np.y - position.y) / ta);
+        float VOPosLength = vlen(VOPos);
+        float combinedRadius = nc + clr;
+        float VORadius = combinedRadius / ta;
+        og_v2 relVel = v2(velocity.x - nv.x, velocity.y - nv.y);
+        og_v2 relPos = v2(np.x - position.x, np.y - position.y);
+        float relPosLength = vlen(relPos);
+
+        if (relPosLength < combinedRadius) { /* ORCA.cpp:356-372 */
+            og_v2 w = vsub(relVel, vdiv(relPos, p->dt));
+            float wLength = vlen(w);
+            og_v2 unitW = vdiv(w, wLength);
+            og_v2 U = vmul(unitW, (combinedRadius / p->dt - wLength));
+            n = push_con(cons, n, cap, vadd(velocity, vmul(U, 0.5f)), unitW);
+            continue;
+        }
+
+        float tanAngleFactor = VORadius / VOPosLength;
+        float tanHalfAngle = p->libm ? atanf(tanAngleFactor) : ecmg_atanf(tanAngleFactor);
+        og_v2 VOLeftLeg = rotate(VOPos, tanHalfAngle, p->libm);
+        og_v2 VORightLeg = rotate(VOPos, -tanHalfAngle, p->libm);
+        float sqDistFromCircleCentre = vsqdist(VOPos, relVel);
+        og_v2 bse = vsub(VOLeftLeg, VOPos), chk = vsub(relVel, VOPos);
+        int liesBelow = bse.x * chk.y - bse.y * chk.x > 0; /* IsLeftOfVector */
+
+        if (liesBelow) {
+            float distToEdge = VORadius - sqrtf(sqDistFromCircleCentre);
+            og_v2 lineNormal = vnormalize(vsub(relVel, VOPos));
+            og_v2 pointOnLine = vadd(velocity, vmul(vmul(lineNormal, distToEdge), 0.5f));
+            n = push_con(cons, n, cap, pointOnLine, lineNormal);
+        } else {
+            og_v2 leftPerp = vdiv(vleft(VOPos), VOPosLength);
+            int closerToLeft = vdot(leftPerp, relVel) >= 0;
+            if (closerToLeft) {
+                og_v2 lln = vnormalized(VOLeftLeg);
+                float len = vdot(relVel, lln); /* GetClosestPointOnLineThroughOrigin */
+                og_v2 U = vsub(vmul(lln, len), relVel);
+                n = push_con(cons, n, cap, vadd(velocity, vmul(U, 0.5f)), vleft(lln));
+            } else {
+                og_v2 rln = vnormalized(VORightLeg);
+                float len = vdot(relVel, rln);
+                og_v2 U = vsub(vmul(rln, len), relVel);
+                n = push_con(cons, n, cap, vadd(velocity, vmul(U, 0.5f)), vright(rln));
+            }
+        }
+    }
+    return n;
+}
+
+/* ---------------------------------------------------------------------------
+ * ORCA::RandomizedLP (ECMAgentSimulator/ORCA.cpp:428-587)
+ * ------------------------------------------------------------------------- */
+int og_lp(const float* cons, int n, og_v2 opt, float maxSpeed, int useDirOpt, og_v2* out)
+{
+    if (useDirOpt) {
+        *out = vmul(opt, maxSpeed);
+    } else if (vlen(opt) > maxSpeed) {
+        *out = vmul(vnormalized(opt), maxSpeed);
+    } else {
+        *out = opt;
+    }
+    if (n == 0) return n;
+
+    for (int i = 0; i < n; i++) {
+        og_v2 P = v2(cons[4 * i], cons[4 * i + 1]);
+        og_v2 N = v2(cons[4 * i + 2], cons[4 * i + 3]);
+        /* Constraint::Contains (ORCA.h:49-60): Det(Right(N), P - out) <= 0 */
+        if (vdet(vright(N), vsub(P, *out)) <= 0.0f) continue;
+
+        og_v2 dir = vright(N);
+        float dirPointDot = vdot(dir, P);
+        float discriminant = dirPointDot * dirPointDot + maxSpeed * maxSpeed - vdot(P, P);
+        if (discriminant <= 0.0f) return i;
+
+        float sq = sqrtf(discriminant);
+        float left = -dirPointDot - sq;
+        float right = -dirPointDot + sq;
+        for (int j = 0; j < i; j++) {
+            og_v2 Pj = v2(cons[4 * j], cons[4 * j + 1]);
+            og_v2 Nj = v2(cons[4 * j + 2], cons[4 * j + 3]);
+            float den = vdet(vright(N), vright(Nj));
+            float num = vdet(vright(Nj), vsub(P, Pj));
+            if (fabsf(den) <= OG_EPS) {
+                if (num < 0.0f) return i;
+                continue;
+            }
+            const float t = num / den;
+            if (den >= 0.0f) right = (t < right) ? t : right; /* std::min(right, t) */
+            else left = (left < t) ? t : left;                 /* std::max(left, t)  */
+            if (left > right) return i;
+        }
+        if (useDirOpt) {
+            if (vdot(opt, vright(N)) > 0) *out = vadd(P, vmul(vright(N), right));
+            else *out = vadd(P, vmul(vright(N), left));
+        } else {
+            float t = vdot(vright(N), vsub(opt, P));
+            if (t < left) *out = vadd(P, vmul(vright(N), left));
+            else if (t > right) *out = vadd(P, vmul(vright(N), right));
+            else *out = vadd(P, vmul(vright(N), t));
+        }
+    }
+    return n;
+}
+
+/* ---------------------------------------------------------------------------
+ * ORCA::RandomizedLP3D (ECMAgentSimulator/ORCA.cpp:592-669)
+ * ------------------------------------------------------------------------- */
+void og_lp3d(const float* cons, int n, int nObst, float maxSpeed, int failed, og_v2* out)
+{
+    float maxPen = 0.0f;
+    float* proj = (float*)malloc(sizeof(float) * 4 * (size_t)(n + 1));
+    for (int i = failed; i < n; i++) {
+        og_v2 Pi = v2(cons[4 * i], cons[4 * i + 1]);
+        og_v2 Ni = v2(cons[4 * i + 2], cons[4 * i + 3]);
+        og_v2 dir = vright(Ni);
+        if (vdet(dir, vsub(Pi, *out)) <= maxPen) continue;
+
+        int m = 0;
+        for (int k = 0; k < nObst; k++, m++) memcpy(proj + 4 * m, cons + 4 * k, sizeof(float) * 4);
+        for (int j = nObst; j < i; j++) {
+            og_v2 Pj = v2(cons[4 * j], cons[4 * j + 1]);
+            og_v2 Nj = v2(cons[4 * j + 2], cons[4 * j + 3]);
+            float det = vdet(vright(Ni), vright(Nj));
+            og_v2 newP;
+            if (fabsf(det) <= OG_EPS) {
+                if (vdot(Ni, Nj) > 0) continue;
+                newP = vmul(vadd(Pi, Pj), 0.5f);
+            } else {
+                float t = vdet(vright(Nj), vsub(Pi, Pj)) / det;
+                newP = vadd(Pi, vmul(vright(Ni), t));
+            }
+            og_v2 nn = vnormalized(vsub(Nj, Ni));
+            proj[4 * m + 0] = newP.x;
+            proj[4 * m + 1] = newP.y;
+            proj[4 * m + 2] = nn.x;
+            proj[4 * m + 3] = nn.y;
+            m++;
+        }
+        og_v2 temp = *out;
+        if (og_lp(proj, m, Ni, maxSpeed, 1, out) < m) *out = temp;
+        maxPen = vdet(dir, vsub(Pi, *out));
+    }
+    free(proj);
+}
+
+/* ORCA::GetVelocity (ECMAgentSimulator/ORCA.cpp:14-57), neighbours given */
+int og_orca_velocity(const og_obstacles* o, const og_state* s, const og_params* p,
+                     int agent, const int* nbrs, int n_nbrs, og_v2 pref_vel,
+                     og_v2* out_vel, int* out_n_obst, int* out_fail)
+{
+    float maxSpeed = p->max_speed > 0.0f ? p->max_speed : s->pref_speed[agent];
+    float range = p->tau_obst * maxSpeed + s->clear[agent];
+    int cap_o = 64;
+    int* ob = (int*)malloc(sizeof(int) * (size_t)cap_o);
+    int no = og_find_obstacles(o, s->pos[agent], range * range, ob, cap_o, p->libm);
+    if (no > cap_o) {
+        free(ob);
+        cap_o = no;
+        ob = (int*)malloc(sizeof(int) * (size_t)cap_o);
+        no = og_find_obstacles(o, s->pos[agent], range * range, ob, cap_o, p->libm);
+    }
+    int cap = no + n_nbrs + 1;
+    float* cons = (float*)malloc(sizeof(float) * 4 * (size_t)cap);
+    int nob = 0;
+    int m = og_generate_constraints(o, s, p, agent, nbrs, n_nbrs, ob, no, cons, cap, &nob);
+    int failed = og_lp(cons, m, pref_vel, maxSpeed, 0, out_vel);
+    if (failed < m) og_lp3d(cons, m, nob, maxSpeed, failed, out_vel);
+    if (out_n_obst) *out_n_obst = nob;
+    if (out_fail) *out_fail = failed;
+    free(cons);
+    free(ob);
+    return m;
+}
+
+/* ---------------------------------------------------------------------------
+ * ECM queries
+ * ------------------------------------------------------------------------- */
+
+/* MathUtility::Contains(Point, vector<Segment>) (UtilityFunctions.cpp:54-86) */
+static int contains_poly(og_v2 p, const og_v2* q, int nq)
+{
+    int inside = 0;
+    for (int s = 0; s < nq; s++) {
+        og_v2 a = q[s], b = q[(s + 1) % nq];
+        if (vapprox(p, a)) return 0;
+        if (vapprox(p, b)) return 0;
+        if (p.y > fminf(a.y, b.y)) {
+            if (p.y < fmaxf(a.y, b.y)) {
+                if (p.x < fmaxf(a.x, b.x)) {
+                    float xi = (p.y - a.y) * (b.x - a.x) / (b.y - a.y) + a.x;
+                    if (a.x == b.x || p.x < xi) inside = !inside;
+                }
+            }
+        }
+    }
+    return inside;
+}
+
+/* cell c of ECMCellCollection::Construct (ECMCellCollection.cpp:10-49):
+   cell 2e = left, 2e+1 = right; polygon of PointLocationQueryLinear
+   (ECMCellCollection.cpp:67-80): [v(he1.target), b.p0, b.p1, v(he0.target)] */
+static void cell_quad(const og_ecm* e, int c, og_v2* q)
+{
+    int ed = c >> 1;
+    const int h0 = 2 * ed, h1 = 2 * ed + 1;
+    og_v2 b0, b1;
+    if ((c & 1) == 0) { b0 = e->he_left[h0]; b1 = e->he_right[h1]; }
+    else { b0 = e->he_right[h0]; b1 = e->he_left[h1]; }
+    q[0] = e->v_pos[e->he_target[h1]];
+    q[1] = b0;
+    q[2] = b1;
+    q[3] = e->v_pos[e->he_target[h0]];
+}
+
+/* ECMCellCollection::PointLocationQueryLinear (ECMCellCollection.cpp:57-90) */
+int og_point_location(const og_ecm* e, og_v2 p)
+{
+    og_v2 q[4];
+    for (int c = 0; c < 2 * e->n_edges; c++) {
+        cell_quad(e, c, q);
+        if (contains_poly(p, q, 4)) return c;
+    }
+    return -1;
+}
+
+/* MathUtility::GetRayToLineSegmentIntersection (UtilityFunctions.cpp:323-349) */
+static int ray_segment(og_v2 o, og_v2 d, og_v2 p1, og_v2 p2, og_v2* out)
+{
+    og_v2 v1 = vsub(o, p1);
+    og_v2 v2_ = vsub(p2, p1);
+    og_v2 v3 = v2(-d.y, d.x);
+    float dot = vdot(v2_, v3);
+    if (fabsf(dot) < 0.000001) return 0;
+    float t1 = vdet(v2_, v1) / dot; /* Cross(v2, v1) */
+    float t2 = vdot(v1, v3) / dot;
+    if (t1 >= 0.0 && (t2 >= 0.0 && t2 <= 1.0)) {
+        out->x = o.x + d.x * t1;
+        out->y = o.y + d.y * t1;
+        return 1;
+    }
+    return 0;
+}
+
+/* ECM::RetractPoint (ECMGenerator/ECM.cpp:20-96) */
+int og_retract(const og_ecm* e, og_v2 loc, og_v2* out, int* out_edge)
+{
+    int c = og_point_location(e, loc);
+    if (c < 0) return 0;
+    int ed = c >> 1;
+    const int h0 = 2 * ed, h1 = 2 * ed + 1;
+    int ip1 = e->he_target[h1], ip2 = e->he_target[h0];
+    og_v2 p1 = e->v_pos[ip1], p2 = e->v_pos[ip2];
+    int toP2 = e->he_target[h0] == e->v_idx[ip2] ? 0 : 1;
+    int toP1 = (toP2 + 1) % 2;
+    og_v2 o1, o2, rd;
+    /* IsLeftOfSegment (UtilityFunctions.cpp:193-196) */
+    int left = (p2.x - p1.x) * (loc.y - p1.y) - (p2.y - p1.y) * (loc.x - p1.x) > 0;
+    if (left) {
+        o1 = e->he_left[2 * ed + toP2];
+        o2 = e->he_right[2 * ed + toP1];
+        if (vapprox(o1, o2)) rd = vadd(vsub(p1, o1), vsub(p2, o1));
+        else { og_v2 v = vsub(o2, o1); rd = v2(v.y, -v.x); }
+        rd = vnormalize(rd);
+    } else {
+        o1 = e->he_right[2 * ed + toP2];
+        o2 = e->he_left[2 * ed + toP1];
+        if (vapprox(o1, o2)) rd = vadd(vsub(p1, o1), vsub(p2, o1));
+        else { og_v2 v = vsub(o2, o1); rd = v2(-v.y, v.x); }
+        rd = vnormalize(rd);
+    }
+    if (out_edge) *out_edge = ed;
+    return ray_segment(loc, rd, p1, p2, out);
+}
+
+/* IRMPathFollower::FindAttractionPoint (ECMAgentSimulator/IRMPathFollower.cpp:14-115)
+   *out is only written on the paths where the reference writes outPoint. */
+int og_irm(const og_ecm* e, og_v2 pos, const og_v2* path, int n, og_v2* out)
+{
+    og_v2 r;
+    int ed;
+    if (!og_retract(e, pos, &r, &ed)) return 0;
+    og_v2 oa = e->he_left[2 * ed];
+    og_v2 ob = e->he_right[2 * ed + 1];
+    og_v2 co = closest_on_segment(r, oa, ob);
+    float clearance = vlen(vsub(r, co));
+    float rcs = clearance * clearance;
+    og_v2 goal = path[n - 1];
+    og_v2 ptg = vsub(goal, r);
+    if (vlen2(ptg) < rcs) { *out = goal; return 1; }
+    int success = 0;
+    for (int i = 0; i < n - 1; i++) {
+        og_v2 p1 = vsub(path[i], r);
+        og_v2 p2 = vsub(path[i + 1], r);
+        og_v2 ed2 = vsub(p2, p1);
+        float els = vlen2(ed2);
+        float det = vdet(p1, p2);
+        float disc = rcs * els - det * det;
+        if (disc < OG_EPS) continue;
+        success = 1;
+        int dySign = ed2.y < 0.0f ? -1 : 1;
+        float sd = sqrtf(disc);
+        og_v2 i1 = v2((det * ed2.y + (float)dySign * ed2.x * sd) / els, (-det * ed2.x + fabsf(ed2.y) * sd) / els);
+        og_v2 i2 = v2((det * ed2.y - (float)dySign * ed2.x * sd) / els, (-det * ed2.x - fabsf(ed2.y) * sd) / els);
+        og_v2 g1 = vadd(p1, r), g2 = vadd(p2, r);
+        og_v2 gi1 = vadd(i1, r), gi2 = vadd(i2, r);
+        og_v2 edge = vsub(g2, g1);
+        float t1 = vdot(vsub(gi1, g1), edge) / els;
+        float t2 = vdot(vsub(gi2, g1), edge) / els;
+        float maxT = -1.0f;
+        if (t1 >= 0.0f && t1 <= 1.0f) { *out = gi1; maxT = t1; }
+        if (t2 >= 0.0f && t2 <= 1.0f) {
+            if (t2 > maxT) *out = gi2;
+        }
+    }
+    return success;
+}
+
+/* ---------------------------------------------------------------------------
+ * Simulator::Update (ECMAgentSimulator/Simulator.cpp:314-323)
+ * ------------------------------------------------------------------------- */
+typedef struct {
+    const og_obstacles* o;
+    const og_state* s;
+    const og_params* p;
+    const unsigned char* alive;   /* active after the attraction stage */
+    const og_state* snap;         /* neighbour set: active at tick start */
+    og_v2* vorca;
+    og_tick_out* out;
+    int lo, hi;
+    int n_lp3d;
+} og_job;
+
+static void orca_range(og_job* j)
+{
+    const og_params* p = j->p;
+    int k = p->k;
+    int* ids = (int*)malloc(sizeof(int) * (size_t)(k > 0 ? k : 1));
+    float* d2 = (float*)malloc(sizeof(float) * (size_t)(k > 0 ? k : 1));
+    float r2 = p->neighbor_dist * p->neighbor_dist;
+    for (int i = j->lo; i < j->hi; i++) {
+        if (!j->alive[i]) continue;
+        int nn = og_knn_exact(j->snap, i, k, r2, ids, d2);
+        int nob = 0, fail = 0;
+        og_v2 v;
+        int m = og_orca_velocity(j->o, j->s, p, i, ids, nn, j->s->pref_vel[i], &v, &nob, &fail);
+        j->vorca[i] = v;
+        if (fail < m) j->n_lp3d++;
+        og_tick_out* out = j->out;
+        if (out) {
+            if (out->nbr_ids) {
+                for (int q = 0; q < k; q++) out->nbr_ids[(size_t)i * k + q] = q < nn ? ids[q] : -1;
+            }
+            if (out->nbr_count) out->nbr_count[i] = nn;
+            if (out->n_constraints) out->n_constraints[i] = m;
+            if (out->n_obst_constraints) out->n_obst_constraints[i] = nob;
+            if (out->lp_fail) out->lp_fail[i] = fail;
+        }
+    }
+    free(ids);
+    free(d2);
+}
+
+static void* orca_thread(void* arg)
+{
+    orca_range((og_job*)arg);
+    return NULL;
+}
+
+int og_tick(const og_obstacles* o, const og_ecm* e, og_state* s, const og_params* p,
+            og_kdtree* kd, og_tick_out* out)
+{
+    /* UpdateMaxAgentIndex (Simulator.cpp:481-492) */
+    int empty = 0;
+    for (int i = s->last_idx; i >= 0; i--) {
+        if (s->active[i]) break;
+        empty++;
+    }
+    s->last_idx = s->last_idx - empty;
+    int last = s->last_idx;
+    int n = s->n_slots;
+
+    /* tick-start snapshot: the neighbour structure is built before any agent
+       is destroyed (Simulator.cpp:319 before 320) */
+    unsigned char* act0 = (unsigned char*)malloc((size_t)(n > 0 ? n : 1));
+    memcpy(act0, s->active, (size_t)n);
+    og_state snap = *s;
+    snap.active = act0;
+    if (p->knn_mode == 1 && kd) og_kdtree_build(kd, s);
+
+    if (out) { out->n_destroyed = 0; out->n_replan = 0; out->n_lp3d = 0; }
+
+    /* UpdateAttractionPointSystem (Simulator.cpp:538-590) */
+    const float delSq = p->delete_radius * p->delete_radius;
+    const float arrSq = p->arrival_radius * p->arrival_radius;
+    for (int i = 0; i <= last; i++) {
+        if (!s->active[i]) continue;
+        const og_v2* path = s->path_xy + s->path_off[i];
+        int np = s->path_len[i];
+        og_v2 pos = s->pos[i];
+        og_v2 g = path[np - 1];
+        float dx = pos.x - g.x, dy = pos.y - g.y; /* SquareDistance(x0,y0,x1,y1) */
+        float dist = dx * dx + dy * dy;
+        if (dist < arrSq) {
+            s->attr[i] = g;
+            if (dist < delSq) { /* DestroyAgent (Simulator.cpp:202-208) */
+                s->num_agents--;
+                s->active[i] = 0;
+                if (out) {
+                    if (out->destroyed) out->destroyed[out->n_destroyed] = i;
+                    out->n_destroyed++;
+                }
+            }
+        } else {
+            og_v2 ap = v2(0.0f, 0.0f); /* Point attractionPoint; */
+            if (og_irm(e, pos, path, np, &ap)) {
+                s->attr[i] = ap;
+            } else if (out) {
+                if (out->replan) out->replan[out->n_replan] = i;
+                if (out->replan_pos) out->replan_pos[out->n_replan] = pos;
+                out->n_replan++;
+            }
+        }
+    }
+
+    /* ApplySteeringForce (Simulator.cpp:638-657) */
+    for (int i = 0; i <= last; i++) {
+        if (!s->active[i]) continue;
+        og_v2 d = vsub(s->attr[i], s->pos[i]);
+        d = vnormalize(d);
+        d = vmul(d, s->pref_speed[i]);
+        s->pref_vel[i] = d;
+    }
+
+    /* ApplyObstacleAvoidanceForce (Simulator.cpp:659-686) */
+    og_v2* vorca = (og_v2*)malloc(sizeof(og_v2) * (size_t)(n > 0 ? n : 1));
+    int n_lp3d = 0;
+    if (p->knn_mode == 1) {
+        int k = p->k;
+        int* ids = (int*)malloc(sizeof(int) * (size_t)k);
+        for (int i = 0; i <= last; i++) {
+            if (!s->active[i]) continue;
+            int nn = og_kdtree_query(kd, &snap, i, ids);
+            int nob = 0, fail = 0;
+            og_v2 v;
+            int m = og_orca_velocity(o, s, p, i, ids, nn, s->pref_vel[i], &v, &nob, &fail);
+            vorca[i] = v;
+            if (fail < m) n_lp3d++;
+            if (out) {
+                if (out->nbr_ids)
+                    for (int q = 0; q < k; q++) out->nbr_ids[(size_t)i * k + q] = q < nn ? ids[q] : -1;
+                if (out->nbr_count) out->nbr_count[i] = nn;
+                if (out->n_constraints) out->n_constraints[i] = m;
+                if (out->n_obst_constraints) out->n_obst_constraints[i] = nob;
+                if (out->lp_fail) out->lp_fail[i] = fail;
+            }
+        }
+        free(ids);
+    } else {
+        int th = p->threads > 1 ? p->threads : 1;
+        og_job* jobs = (og_job*)calloc((size_t)th, sizeof(og_job));
+        pthread_t* tid = (pthread_t*)calloc((size_t)th, sizeof(pthread_t));
+        int span = (last + 1 + th - 1) / th;
+        for (int t = 0; t < th; t++) {
+            jobs[t].o = o; jobs[t].s = s; jobs[t].p = p; jobs[t].alive = s->active;
+            jobs[t].snap = &snap; jobs[t].vorca = vorca; jobs[t].out = out;
+            jobs[t].lo = t * span;
+            jobs[t].hi = (t + 1) * span < last + 1 ? (t + 1) * span : last + 1;
+            if (th > 1) pthread_create(&tid[t], NULL, orca_thread, &jobs[t]);
+            else orca_range(&jobs[t]);
+        }
+        for (int t = 0; t < th; t++) {
+            if (th > 1) pthread_join(tid[t], NULL);
+            n_lp3d += jobs[t].n_lp3d;
+        }
+        free(jobs);
+        free(tid);
+    }
+    if (out) {
+        out->n_lp3d = n_lp3d;
+        if (out->v_orca)
+            for (int i = 0; i <= last; i++)
+                if (s->active[i]) out->v_orca[i] = vorca[i];
+    }
+
+    /* UpdateVelocitySystem (Simulator.cpp:619-635): force = vOrca - v
+       (Simulator.cpp:676-677), v += F * (1/m) * dt */
+    const float massRecip = 1.0f / p->mass;
+    for (int i = 0; i <= last; i++) {
+        if (!s->active[i]) continue;
+        float fx = vorca[i].x - s->vel[i].x;
+        float fy = vorca[i].y - s->vel[i].y;
+        s->vel[i].x += fx * massRecip * p->dt;
+        s->vel[i].y += fy * massRecip * p->dt;
+    }
+    /* UpdatePositionSystem (Simulator.cpp:592-606) */
+    for (int i = 0; i <= last; i++) {
+        if (!s->active[i]) continue;
+        s->pos[i].x += (s->vel[i].x * p->dt);
+        s->pos[i].y += (s->vel[i].y * p->dt);
+    }
+    free(vorca);
+    free(act0);
+    return 0;
+}

@@ -1,0 +1,140 @@
+/*
+ * ecmg_oracle.h -- CPU oracle for the per-tick crowd update.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * simulator's tick (ECMAgentSimulator/Simulator.cpp:314-323 and everything it
+ * calls on the hot path), used by tests/, by __graft_entry__.smoke() and by the
+ * cpu_baseline leg of bench.py as the checker.  The product library never links
+ * or calls it.
+ *
+ * Parity is pinned: tests/test_oracle_vs_reference.py runs this file next to
+ * the reference's own sources (compiled by oracle/Makefile into oracle/_ref)
+ * and requires bit-identical results when both use the host libm, and
+ * tests/golden/ holds fixtures produced by the reference itself.
+ *
+ * Floating point: every expression keeps the reference's operand order; the
+ * file is compiled with -ffp-contract=off so nothing is fused.  og_params.libm
+ * selects the transcendental source: 1 = the host libm (atanf/sinf/cosf/powf,
+ * as the reference), 0 = the deterministic ecmg_tmath.h routines that the CUDA
+ * kernels also use (and x*x for powf(x, 2)).
+ */
+#ifndef ECMG_ORACLE_H
+#define ECMG_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct { float x, y; } og_v2;
+
+/* Static obstacles, flattened in the reference's global order
+   (Environment::GetObstacles() obstacle by obstacle, vertex by vertex). */
+typedef struct {
+    int n_verts;
+    const og_v2* p;              /* ObstacleVertex::p                         */
+    const int* next;             /* ObstacleVertex::nextObstacle (index)      */
+    const int* prev;             /* ObstacleVertex::prevObstacle (index)      */
+    const unsigned char* convex; /* ObstacleVertex::isConvex                  */
+} og_obstacles;
+
+/* ECM graph (ECMGenerator/ECM.h:20-50); half-edge h of edge e is 2e+h. */
+typedef struct {
+    int n_vertices;
+    const og_v2* v_pos;     /* ECMVertex::position       */
+    const float* v_clear;   /* ECMVertex::clearance      */
+    const int* v_idx;       /* ECMVertex::idx            */
+    const int* v_halfedge;  /* ECMVertex::half_edge_idx  */
+    int n_edges;
+    const int* he_target;   /* [2E] ECMHalfEdge::v_target_idx */
+    const int* he_next;     /* [2E] ECMHalfEdge::next_idx     */
+    const og_v2* he_left;   /* [2E] ECMHalfEdge::closest_left */
+    const og_v2* he_right;  /* [2E] ECMHalfEdge::closest_right */
+} og_ecm;
+
+typedef struct {
+    float dt;               /* Simulator::m_SimStepTime                      */
+    float tau_agent;        /* ORCA::m_lookAheadAgent                        */
+    float tau_obst;         /* ORCA::m_lookAheadObstacle                     */
+    float neighbor_dist;    /* kNN cut-off radius (exact-kNN mode only)      */
+    float max_speed;        /* <= 0: LP radius = preferred speed (Simulator.cpp:671) */
+    float mass;             /* Simulator.cpp:622                             */
+    float arrival_radius;   /* Simulator.cpp:543                             */
+    float delete_radius;    /* Simulator.cpp:542                             */
+    int k;                  /* ORCA(numNeighbors)                            */
+    int knn_mode;           /* 0 = exact kNN (d2,id) within neighbor_dist; 1 = kd-tree as the reference */
+    int libm;               /* 1 = host libm transcendentals; 0 = ecmg_tmath.h */
+    int threads;            /* >1: split the per-agent stages over threads (exact-kNN mode only) */
+} og_params;
+
+/* Slot-indexed agent state (Simulator component arrays). */
+typedef struct {
+    int n_slots;
+    int last_idx;           /* Simulator::m_LastEntityIdx */
+    int num_agents;         /* Simulator::m_NumEntities   */
+    og_v2* pos;
+    og_v2* vel;
+    og_v2* attr;            /* attraction points          */
+    og_v2* pref_vel;
+    float* clear;
+    float* pref_speed;
+    unsigned char* active;
+    int* path_off;          /* path CSR: agent i owns path_xy[path_off[i] .. +path_len[i]) */
+    int* path_len;
+    const og_v2* path_xy;
+} og_state;
+
+/* Optional per-tick outputs; any pointer may be NULL. */
+typedef struct {
+    int* destroyed;         /* slots destroyed this tick, in slot order      */
+    int n_destroyed;
+    int* replan;            /* slots whose IRM query failed, in slot order    */
+    og_v2* replan_pos;      /* position used for the replan                   */
+    int n_replan;
+    int* nbr_ids;           /* [n_slots * k] neighbour list per slot (-1 pad)  */
+    int* nbr_count;         /* [n_slots]                                      */
+    og_v2* v_orca;          /* [n_slots] LP result                            */
+    int* n_constraints;     /* [n_slots]                                      */
+    int* n_obst_constraints;/* [n_slots]                                      */
+    int* lp_fail;           /* [n_slots] failed index of the 2D LP (== n if none) */
+    int n_lp3d;             /* agents that needed the 3D LP                   */
+} og_tick_out;
+
+/* kd-tree state of the reference (KDTree.h:57-80) plus ORCA's neighbour cache
+   (ORCA.h:100), which the reference carries across agents and ticks. */
+typedef struct og_kdtree og_kdtree;
+
+og_kdtree* og_kdtree_create(int k);
+void og_kdtree_destroy(og_kdtree* t);
+void og_kdtree_build(og_kdtree* t, const og_state* s);
+int og_kdtree_query(og_kdtree* t, const og_state* s, int agent, int* out_ids);
+
+/* exact k nearest (d2, id) with EPSILON < d2 < r2; returns the count */
+int og_knn_exact(const og_state* s, int agent, int k, float r2, int* out_ids, float* out_d2);
+
+int og_find_obstacles(const og_obstacles* o, og_v2 pos, float range_sq, int* out, int cap, int libm);
+
+/* ORCA constraints + LP + LP3D for one agent with the given neighbour list.
+   Returns the number of constraints. */
+int og_orca_velocity(const og_obstacles* o, const og_state* s, const og_params* p,
+                     int agent, const int* nbrs, int n_nbrs, og_v2 pref_vel,
+                     og_v2* out_vel, int* out_n_obst, int* out_fail);
+
+/* half-plane LP of ORCA.cpp:428-587; constraints as (point, normal) quadruples */
+int og_lp(const float* cons, int n, og_v2 opt, float max_speed, int use_dir_opt, og_v2* out);
+void og_lp3d(const float* cons, int n, int n_obst, float max_speed, int failed, og_v2* out);
+int og_generate_constraints(const og_obstacles* o, const og_state* s, const og_params* p, int agent,
+                            const int* nbrs, int n_nbrs, const int* obst, int n_obst_cand,
+                            float* cons_out, int cap, int* out_n_obst);
+
+int og_point_location(const og_ecm* e, og_v2 p);
+int og_retract(const og_ecm* e, og_v2 p, og_v2* out, int* out_edge);
+int og_irm(const og_ecm* e, og_v2 pos, const og_v2* path, int n, og_v2* out);
+
+/* One Simulator::Update.  kd may be NULL unless p->knn_mode == 1. */
+int og_tick(const og_obstacles* o, const og_ecm* e, og_state* s, const og_params* p,
+            og_kdtree* kd, og_tick_out* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
