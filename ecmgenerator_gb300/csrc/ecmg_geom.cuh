@@ -1,0 +1,592 @@
+/*
+ * ecmg_geom.cuh -- per-agent geometry of the crowd tick, compiled for the
+ * device (tick kernels) and for the host (planner, setup).
+ *
+ * Every function restates one reference function with the same sequence of
+ * binary32 operations, so that the tick computes what the reference computes
+ * on the same inputs; the source location is given above each function.
+ * Translation units that include this header are built without fused
+ * multiply-add (-fmad=false for nvcc, -ffp-contract=off for g++).
+ */
+#ifndef ECMG_GEOM_CUH
+#define ECMG_GEOM_CUH
+
+#include "ecmg_tmath.h"
+
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define EG_HD __host__ __device__ __forceinline__
+#define EG_NI static __host__ __device__ __noinline__
+#else
+#include <cmath>
+#define EG_HD inline
+#define EG_NI inline
+#ifndef __align__
+#define __align__(n) __attribute__((aligned(n)))
+#endif
+#endif
+
+namespace ecmg {
+
+constexpr float kEps = 0.0001f; /* Utility::EPSILON, ECMGenerator/Configuration.h:14 */
+
+struct __align__(8) V2 {
+    float x, y;
+};
+
+EG_HD V2 mk(float x, float y) { V2 r; r.x = x; r.y = y; return r; }
+/* Vec2/Point operators, ECMGenerator/ECMDataTypes.h:20-98 */
+EG_HD V2 operator+(V2 a, V2 b) { return mk(a.x + b.x, a.y + b.y); }
+EG_HD V2 operator-(V2 a, V2 b) { return mk(a.x - b.x, a.y - b.y); }
+EG_HD V2 operator*(V2 a, float s) { return mk(a.x * s, a.y * s); }
+EG_HD V2 operator/(V2 a, float s) { return mk(a.x / s, a.y / s); }
+/* MathUtility, ECMGenerator/UtilityFunctions.cpp:170-262 */
+EG_HD float dot(V2 a, V2 b) { return a.x * b.x + a.y * b.y; }
+EG_HD float det(V2 a, V2 b) { return a.x * b.y - a.y * b.x; }
+EG_HD float len2(V2 a) { return a.x * a.x + a.y * a.y; }
+EG_HD float len(V2 a) { return sqrtf(a.x * a.x + a.y * a.y); }
+EG_HD V2 right(V2 a) { return mk(a.y, -a.x); }
+EG_HD V2 left(V2 a) { return mk(-a.y, a.x); }
+/* Vec2::Normalize (ECMDataTypes.h:45-52) */
+EG_HD V2 normalize(V2 a)
+{
+    float l = len(a);
+    if (l == 0.0f) return a;
+    a.x /= l;
+    a.y /= l;
+    return a;
+}
+/* Vec2::Normalized (ECMDataTypes.h:54-60); zero vector -> (0,0) */
+EG_HD V2 normalized(V2 a)
+{
+    float l = len(a);
+    if (l == 0.0f) return mk(0.0f, 0.0f);
+    return mk(a.x / l, a.y / l);
+}
+/* Point::Approximate (ECMDataTypes.cpp:97-100) */
+EG_HD bool approx(V2 p, V2 a)
+{
+    return p.x < (a.x + kEps) && p.x > (a.x - kEps) && p.y < (a.y + kEps) && p.y > (a.y - kEps);
+}
+/* MathUtility::SquareDistance(Point, Point) (UtilityFunctions.cpp:32-39) */
+EG_HD float sqdist(V2 p1, V2 p2)
+{
+    float dx = p2.x - p1.x, dy = p2.y - p1.y;
+    return dx * dx + dy * dy;
+}
+/* MathUtility::GetClosestPointOnSegment (UtilityFunctions.cpp:287-306) */
+EG_HD V2 closest_on_segment(V2 point, V2 s1, V2 s2)
+{
+    if (approx(s1, s2)) return s1;
+    V2 seg = s2 - s1;
+    V2 pts = point - s1;
+    float tsq = sqdist(s1, s2);
+    float d = (pts.x * seg.x + pts.y * seg.y) / tsq;
+    if (d > 1.0f) d = 1.0f;
+    if (d < 0.0f) d = 0.0f;
+    return mk(s1.x + d * seg.x, s1.y + d * seg.y);
+}
+/* MathUtility::RotateVector (UtilityFunctions.cpp:233-242) with the
+   deterministic sin/cos of ecmg_tmath.h */
+EG_HD V2 rotate(V2 v, float rad)
+{
+    float sn, cs;
+    ecmg_sincosf(rad, &sn, &cs);
+    return mk(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
+}
+
+/* ------------------------------------------------------------------------
+ * ECM (ECMGenerator/ECM.h), flattened.  Cell c: edge c>>1, left (even) or
+ * right (odd) side (ECMCellCollection::Construct, ECMCellCollection.cpp:10-49).
+ * ---------------------------------------------------------------------- */
+struct EcmView {
+    const V2* v_pos;
+    const int* v_idx;
+    const int* he_target;
+    const V2* he_left;
+    const V2* he_right;
+    int n_edges;
+    /* point-location grid over the cell quads: cell g lists, in ascending
+       order, every ECM cell whose bounding box (grown by a margin) meets g */
+    float gx0, gy0, ginv;
+    int gw, gh;
+    const int* g_start;   /* gw*gh + 1 */
+    const int* g_items;
+    /* sorted distinct y of all quad corners: a query whose y equals one of
+       them falls back to the linear scan (the ray-cast test can then report
+       a hit left of the quad's bounding box) */
+    const float* special_y;
+    int n_special;
+};
+
+/* quad of PointLocationQueryLinear (ECMCellCollection.cpp:67-80):
+   [v(he1.target), boundary.p0, boundary.p1, v(he0.target)] */
+EG_HD void cell_quad(const EcmView& e, int c, V2* q)
+{
+    int ed = c >> 1;
+    int h0 = 2 * ed, h1 = 2 * ed + 1;
+    V2 b0, b1;
+    if ((c & 1) == 0) { b0 = e.he_left[h0]; b1 = e.he_right[h1]; }
+    else { b0 = e.he_right[h0]; b1 = e.he_left[h1]; }
+    q[0] = e.v_pos[e.he_target[h1]];
+    q[1] = b0;
+    q[2] = b1;
+    q[3] = e.v_pos[e.he_target[h0]];
+}
+
+/* MathUtility::Contains(Point, vector<Segment>) (UtilityFunctions.cpp:54-86) */
+EG_HD bool contains_quad(V2 p, const V2* q)
+{
+    bool inside = false;
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+        V2 a = q[s], b = q[(s + 1) & 3];
+        if (approx(p, a)) return false;
+        if (approx(p, b)) return false;
+        if (p.y > fminf(a.y, b.y)) {
+            if (p.y < fmaxf(a.y, b.y)) {
+                if (p.x < fmaxf(a.x, b.x)) {
+                    float xi = (p.y - a.y) * (b.x - a.x) / (b.y - a.y) + a.x;
+                    if (a.x == b.x || p.x < xi) inside = !inside;
+                }
+            }
+        }
+    }
+    return inside;
+}
+
+EG_HD bool is_special_y(const EcmView& e, float y)
+{
+    int lo = 0, hi = e.n_special;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        float v = e.special_y[mid];
+        if (v < y) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo < e.n_special && e.special_y[lo] == y;
+}
+
+/* ECMCellCollection::PointLocationQueryLinear (ECMCellCollection.cpp:57-90):
+   the first cell, in cell order, whose quad contains p.  The grid returns the
+   same cell: every quad that can contain p is listed in p's grid cell, and
+   the list is scanned in ascending cell order. */
+EG_NI int point_location(const EcmView& e, V2 p)
+{
+    V2 q[4];
+    if (e.n_special > 0 && is_special_y(e, p.y)) {
+        for (int c = 0; c < 2 * e.n_edges; c++) {
+            cell_quad(e, c, q);
+            if (contains_quad(p, q)) return c;
+        }
+        return -1;
+    }
+    float fx = (p.x - e.gx0) * e.ginv, fy = (p.y - e.gy0) * e.ginv;
+    if (!(fx >= 0.0f && fy >= 0.0f && fx < (float)e.gw && fy < (float)e.gh)) return -1;
+    int g = (int)fy * e.gw + (int)fx;
+    int b = e.g_start[g], en = e.g_start[g + 1];
+    for (int i = b; i < en; i++) {
+        int c = e.g_items[i];
+        cell_quad(e, c, q);
+        if (contains_quad(p, q)) return c;
+    }
+    return -1;
+}
+
+/* MathUtility::GetRayToLineSegmentIntersection (UtilityFunctions.cpp:323-349) */
+EG_HD bool ray_segment(V2 o, V2 d, V2 p1, V2 p2, V2* out)
+{
+    V2 v1 = o - p1;
+    V2 v2 = p2 - p1;
+    V2 v3 = mk(-d.y, d.x);
+    float dt = dot(v2, v3);
+    if ((double)fabsf(dt) < 0.000001) return false;
+    float t1 = det(v2, v1) / dt;
+    float t2 = dot(v1, v3) / dt;
+    if (t1 >= 0.0f && (t2 >= 0.0f && t2 <= 1.0f)) {
+        out->x = o.x + d.x * t1;
+        out->y = o.y + d.y * t1;
+        return true;
+    }
+    return false;
+}
+
+/* ECM::RetractPoint (ECMGenerator/ECM.cpp:20-96) */
+EG_HD bool retract(const EcmView& e, V2 loc, V2* out, int* out_edge)
+{
+    int c = point_location(e, loc);
+    if (c < 0) return false;
+    int ed = c >> 1;
+    int ip1 = e.he_target[2 * ed + 1], ip2 = e.he_target[2 * ed];
+    V2 p1 = e.v_pos[ip1], p2 = e.v_pos[ip2];
+    int toP2 = e.he_target[2 * ed] == e.v_idx[ip2] ? 0 : 1;
+    int toP1 = (toP2 + 1) % 2;
+    V2 o1, o2, rd;
+    bool isLeft = (p2.x - p1.x) * (loc.y - p1.y) - (p2.y - p1.y) * (loc.x - p1.x) > 0; /* IsLeftOfSegment */
+    if (isLeft) {
+        o1 = e.he_left[2 * ed + toP2];
+        o2 = e.he_right[2 * ed + toP1];
+        if (approx(o1, o2)) rd = (p1 - o1) + (p2 - o1);
+        else { V2 v = o2 - o1; rd = mk(v.y, -v.x); }
+    } else {
+        o1 = e.he_right[2 * ed + toP2];
+        o2 = e.he_left[2 * ed + toP1];
+        if (approx(o1, o2)) rd = (p1 - o1) + (p2 - o1);
+        else { V2 v = o2 - o1; rd = mk(-v.y, v.x); }
+    }
+    rd = normalize(rd);
+    *out_edge = ed;
+    return ray_segment(loc, rd, p1, p2, out);
+}
+
+/* IRMPathFollower::FindAttractionPoint (IRMPathFollower.cpp:14-115).
+   *out is written only where the reference writes outPoint. */
+EG_NI bool irm(const EcmView& e, V2 pos, const V2* path, int n, V2* out)
+{
+    V2 r;
+    int ed;
+    if (!retract(e, pos, &r, &ed)) return false;
+    V2 co = closest_on_segment(r, e.he_left[2 * ed], e.he_right[2 * ed + 1]);
+    float clr = len(r - co);
+    float rcs = clr * clr;
+    V2 goal = path[n - 1];
+    if (len2(goal - r) < rcs) { *out = goal; return true; }
+    bool success = false;
+    for (int i = 0; i < n - 1; i++) {
+        V2 p1 = path[i] - r;
+        V2 p2 = path[i + 1] - r;
+        V2 ed2 = p2 - p1;
+        float els = len2(ed2);
+        float dd = det(p1, p2);
+        float disc = rcs * els - dd * dd;
+        if (disc < kEps) continue;
+        success = true;
+        float dySign = ed2.y < 0.0f ? -1.0f : 1.0f;
+        float sd = sqrtf(disc);
+        V2 i1 = mk((dd * ed2.y + dySign * ed2.x * sd) / els, (-dd * ed2.x + fabsf(ed2.y) * sd) / els);
+        V2 i2 = mk((dd * ed2.y - dySign * ed2.x * sd) / els, (-dd * ed2.x - fabsf(ed2.y) * sd) / els);
+        V2 g1 = p1 + r, g2 = p2 + r;
+        V2 gi1 = i1 + r, gi2 = i2 + r;
+        V2 edge = g2 - g1;
+        float t1 = dot(gi1 - g1, edge) / els;
+        float t2 = dot(gi2 - g1, edge) / els;
+        float maxT = -1.0f;
+        if (t1 >= 0.0f && t1 <= 1.0f) { *out = gi1; maxT = t1; }
+        if (t2 >= 0.0f && t2 <= 1.0f) {
+            if (t2 > maxT) *out = gi2;
+        }
+    }
+    return success;
+}
+
+/* ------------------------------------------------------------------------
+ * Obstacles
+ * ---------------------------------------------------------------------- */
+struct ObstView {
+    const V2* p;
+    const int* next;
+    const int* prev;
+    const unsigned char* convex;
+    int n_verts;
+    /* candidate grid: cell g lists, ascending, every obstacle edge (vertex id)
+       within `reach` metres of the cell */
+    float gx0, gy0, ginv;
+    int gw, gh;
+    float reach;
+    const int* g_start;
+    const int* g_items;
+};
+
+/* one edge of Simulator::FindNearestObstacles (Simulator.cpp:268-290) */
+EG_HD bool obstacle_in_range(const ObstView& o, int i, V2 pos, float rangeSq)
+{
+    V2 a = o.p[i];
+    V2 b = o.p[o.next[i]];
+    float sld = det(a - pos, b - a); /* LineLeftDistance */
+    float sq = (sld * sld) / sqdist(a, b); /* std::powf(sld, 2.0f) */
+    if (sq < rangeSq) {
+        if (sld < 0.0f) {
+            V2 c = closest_on_segment(pos, a, b);
+            if (sqdist(c, pos) < rangeSq) return true;
+        }
+    }
+    return false;
+}
+
+/* ------------------------------------------------------------------------
+ * ORCA (ECMAgentSimulator/ORCA.cpp)
+ * ---------------------------------------------------------------------- */
+struct Con {
+    V2 p; /* Constraint::PointOnLine */
+    V2 n; /* Constraint::Normal      */
+};
+
+/* obstacle part of ORCA::GenerateConstraints (ORCA.cpp:70-333) for one
+   candidate edge L; returns true and fills *c when a constraint is emitted */
+EG_NI bool obstacle_constraint(const ObstView& o, int L, V2 position, V2 velocity, float clr,
+                               float tau_obst, Con* c)
+{
+    int R = o.next[L];
+    V2 pL = o.p[L], pR = o.p[R];
+    V2 rp1 = pL - position;
+    V2 rp2 = pR - position;
+    V2 seg = pR - pL;
+    const float s = dot(rp1 * -1.0f, seg) / len2(seg);
+    const float distSqLine = len2(rp1 * -1.0f - seg * s);
+    const float distSq1 = len2(rp1);
+    const float distSq2 = len2(rp2);
+    seg = normalize(seg);
+    const float radiusSq = clr * clr;
+    const V2 zero = mk(0.0f, 0.0f);
+    bool cL = o.convex[L] != 0, cR = o.convex[R] != 0;
+
+    if (s < 0.0f && distSq1 <= radiusSq) {
+        if (cL) { c->p = zero; c->n = normalized(rp1 * -1.0f); return true; }
+        return false;
+    } else if (s > 1.0f && distSq2 <= radiusSq) {
+        V2 rnd = normalize(o.p[o.next[R]] - pR);
+        if (cR && det(rp2, rnd) >= 0.0f) { c->p = zero; c->n = normalized(rp2 * -1.0f); return true; }
+        return false;
+    } else if (s >= 0.0f && s < 1.0f && distSqLine <= radiusSq) {
+        c->p = zero;
+        c->n = right(seg);
+        return true;
+    }
+
+    V2 leftLeg, rightLeg;
+    if (s < 0.0f && distSqLine <= radiusSq) {
+        if (!cL) return false;
+        R = L;
+        pR = pL;
+        cR = cL;
+        const float leg1 = sqrtf(distSq1 - radiusSq);
+        leftLeg = mk(rp1.x * leg1 - rp1.y * clr, rp1.x * clr + rp1.y * leg1) / distSq1;
+        rightLeg = mk(rp1.x * leg1 + rp1.y * clr, -rp1.x * clr + rp1.y * leg1) / distSq1;
+    } else if (s > 1.0f && distSqLine <= radiusSq) {
+        if (!cR) return false;
+        L = R;
+        pL = pR;
+        cL = cR;
+        const float leg2 = sqrtf(distSq2 - radiusSq);
+        leftLeg = mk(rp2.x * leg2 - rp2.y * clr, rp2.x * clr + rp2.y * leg2) / distSq2;
+        rightLeg = mk(rp2.x * leg2 + rp2.y * clr, -rp2.x * clr + rp2.y * leg2) / distSq2;
+    } else {
+        if (cL) {
+            const float leg1 = sqrtf(distSq1 - radiusSq);
+            leftLeg = mk(rp1.x * leg1 - rp1.y * clr, rp1.x * clr + rp1.y * leg1) / distSq1;
+        } else {
+            leftLeg = seg * -1.0f;
+        }
+        if (cR) {
+            const float leg2 = sqrtf(distSq2 - radiusSq);
+            rightLeg = mk(rp2.x * leg2 + rp2.y * clr, -rp2.x * clr + rp2.y * leg2) / distSq2;
+        } else {
+            rightLeg = seg;
+        }
+    }
+
+    bool isLeftForeign = false, isRightForeign = false;
+    V2 lnd = normalize(pL - o.p[o.prev[L]]);
+    if (cL && det(leftLeg, lnd * -1.0f) >= 0.0f) {
+        leftLeg = lnd * -1.0f;
+        isLeftForeign = true;
+    }
+    V2 rnd = normalize(o.p[o.next[R]] - pR);
+    if (cR && det(rightLeg, rnd) <= 0.0f) {
+        rightLeg = rnd;
+        isRightForeign = true;
+    }
+
+    float invT = 1.0f / tau_obst;
+    const V2 leftCutoff = (pL - position) * invT;
+    const V2 rightCutoff = (pR - position) * invT;
+    const V2 cutoffVec = rightCutoff - leftCutoff;
+    const bool same = (L == R);
+    const float t = (same ? 0.5f : dot(velocity - leftCutoff, cutoffVec) / len2(cutoffVec));
+    const float tLeft = dot(velocity - leftCutoff, leftLeg);
+    const float tRight = dot(velocity - rightCutoff, rightLeg);
+
+    if ((t < 0.0f && tLeft < 0.0f) || (same && tLeft < 0.0f && tRight < 0.0f)) {
+        V2 unitW = normalized(velocity - leftCutoff);
+        c->p = leftCutoff + (unitW * invT) * clr;
+        c->n = unitW;
+        return true;
+    } else if (t > 1.0f && tRight < 0.0f) {
+        V2 unitW = normalized(velocity - rightCutoff);
+        c->p = rightCutoff + (unitW * invT) * clr;
+        c->n = unitW;
+        return true;
+    }
+
+    const float inf = INFINITY;
+    const float distSqCutoff = ((t < 0.0f || t > 1.0f || same) ? inf : len2(velocity - (leftCutoff + cutoffVec * t)));
+    const float distSqLeft = ((tLeft < 0.0f) ? inf : len2(velocity - (leftCutoff + leftLeg * tLeft)));
+    const float distSqRight = ((tRight < 0.0f) ? inf : len2(velocity - (rightCutoff + rightLeg * tRight)));
+
+    if (distSqCutoff <= distSqLeft && distSqCutoff <= distSqRight) {
+        V2 normal = left(seg * -1.0f);
+        c->p = leftCutoff + (normal * invT) * clr;
+        c->n = normal;
+        return true;
+    } else if (distSqLeft <= distSqRight) {
+        if (isLeftForeign) return false;
+        V2 normal = left(leftLeg);
+        c->p = leftCutoff + (normal * clr) * invT;
+        c->n = normal;
+        return true;
+    } else {
+        if (isRightForeign) return false;
+        V2 normal = right(rightLeg);
+        c->p = rightCutoff + (normal * clr) * invT;
+        c->n = normal;
+        return true;
+    }
+}
+
+/* agent part of ORCA::GenerateConstraints (ORCA.cpp:339-423) for one neighbour */
+EG_HD Con agent_constraint(V2 position, V2 velocity, float clr, V2 np, V2 nv, float nclr, float tau, float dt)
+{
+    Con c;
+    V2 VOPos = mk((np.x - position.x) / tau, (np.y - position.y) / tau);
+    float VOPosLength = len(VOPos);
+    float combinedRadius = nclr + clr;
+    float VORadius = combinedRadius / tau;
+    V2 relVel = mk(velocity.x - nv.x, velocity.y - nv.y);
+    V2 relPos = mk(np.x - position.x, np.y - position.y);
+    float relPosLength = len(relPos);
+    if (relPosLength < combinedRadius) {
+        V2 w = relVel - relPos / dt;
+        float wLength = len(w);
+        V2 unitW = w / wLength;
+        V2 U = unitW * (combinedRadius / dt - wLength);
+        c.p = velocity + U * 0.5f;
+        c.n = unitW;
+        return c;
+    }
+    float tanAngleFactor = VORadius / VOPosLength;
+    float tanHalfAngle = ecmg_atanf(tanAngleFactor);
+    V2 VOLeftLeg = rotate(VOPos, tanHalfAngle);
+    V2 VORightLeg = rotate(VOPos, -tanHalfAngle);
+    float sqDistFromCircleCentre = sqdist(VOPos, relVel);
+    V2 bse = VOLeftLeg - VOPos, chk = relVel - VOPos;
+    bool liesBelow = bse.x * chk.y - bse.y * chk.x > 0; /* IsLeftOfVector */
+    if (liesBelow) {
+        float distToEdge = VORadius - sqrtf(sqDistFromCircleCentre);
+        V2 lineNormal = normalize(relVel - VOPos);
+        c.p = velocity + (lineNormal * distToEdge) * 0.5f;
+        c.n = lineNormal;
+    } else {
+        V2 leftPerp = left(VOPos) / VOPosLength;
+        if (dot(leftPerp, relVel) >= 0) {
+            V2 lln = normalized(VOLeftLeg);
+            float l = dot(relVel, lln); /* GetClosestPointOnLineThroughOrigin */
+            V2 U = (lln * l) - relVel;
+            c.p = velocity + U * 0.5f;
+            c.n = left(lln);
+        } else {
+            V2 rln = normalized(VORightLeg);
+            float l = dot(relVel, rln);
+            V2 U = (rln * l) - relVel;
+            c.p = velocity + U * 0.5f;
+            c.n = right(rln);
+        }
+    }
+    return c;
+}
+
+/* ORCA::RandomizedLP (ORCA.cpp:428-587).  The constraint at index i is
+   fetched through get(i) so that callers may keep constraints in registers,
+   shared or local memory. */
+template <class Get>
+EG_HD int lp2d(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2* out)
+{
+    if (useDirOpt) *out = opt * maxSpeed;
+    else if (len(opt) > maxSpeed) *out = normalized(opt) * maxSpeed;
+    else *out = opt;
+    if (n == 0) return n;
+    for (int i = 0; i < n; i++) {
+        Con h = get(i);
+        if (det(right(h.n), h.p - *out) <= 0.0f) continue; /* Constraint::Contains */
+        V2 dir = right(h.n);
+        float dirPointDot = dot(dir, h.p);
+        float disc = dirPointDot * dirPointDot + maxSpeed * maxSpeed - dot(h.p, h.p);
+        if (disc <= 0.0f) return i;
+        float sq = sqrtf(disc);
+        float lo = -dirPointDot - sq;
+        float hi = -dirPointDot + sq;
+        for (int j = 0; j < i; j++) {
+            Con g = get(j);
+            float den = det(right(h.n), right(g.n));
+            float num = det(right(g.n), h.p - g.p);
+            if (fabsf(den) <= kEps) {
+                if (num < 0.0f) return i;
+                continue;
+            }
+            const float t = num / den;
+            if (den >= 0.0f) hi = (t < hi) ? t : hi; /* std::min(right, t) */
+            else lo = (lo < t) ? t : lo;             /* std::max(left, t)  */
+            if (lo > hi) return i;
+        }
+        if (useDirOpt) {
+            if (dot(opt, right(h.n)) > 0) *out = h.p + right(h.n) * hi;
+            else *out = h.p + right(h.n) * lo;
+        } else {
+            float t = dot(right(h.n), opt - h.p);
+            if (t < lo) *out = h.p + right(h.n) * lo;
+            else if (t > hi) *out = h.p + right(h.n) * hi;
+            else *out = h.p + right(h.n) * t;
+        }
+    }
+    return n;
+}
+
+/* ORCA::RandomizedLP3D (ORCA.cpp:592-669).  proj must hold n constraints.
+   With fp64 the bisector lines are intersected in double precision (the
+   reference computes them in float). */
+template <class Get>
+EG_HD void lp3d(const Get& get, int n, int nObst, float maxSpeed, int failed, V2* out, Con* proj, bool fp64)
+{
+    float maxPen = 0.0f;
+    for (int i = failed; i < n; i++) {
+        Con ci = get(i);
+        V2 dir = right(ci.n);
+        if (det(dir, ci.p - *out) <= maxPen) continue;
+        int m = 0;
+        for (int q = 0; q < nObst; q++) proj[m++] = get(q);
+        for (int j = nObst; j < i; j++) {
+            Con cj = get(j);
+            float dt = det(right(ci.n), right(cj.n));
+            V2 np_;
+            if (fabsf(dt) <= kEps) {
+                if (dot(ci.n, cj.n) > 0) continue;
+                np_ = (ci.p + cj.p) * 0.5f;
+            } else if (!fp64) {
+                float t = det(right(cj.n), ci.p - cj.p) / dt;
+                np_ = ci.p + right(ci.n) * t;
+            } else {
+                double ax = (double)cj.n.y, ay = -(double)cj.n.x;             /* Right(cj.N) */
+                double bx = (double)ci.p.x - (double)cj.p.x, by = (double)ci.p.y - (double)cj.p.y;
+                double rx = (double)ci.n.y, ry = -(double)ci.n.x;             /* Right(ci.N) */
+                double dd = rx * ay - ry * ax;
+                double t = (ax * by - ay * bx) / dd;
+                np_ = mk((float)((double)ci.p.x + rx * t), (float)((double)ci.p.y + ry * t));
+            }
+            Con nc;
+            nc.p = np_;
+            nc.n = normalized(cj.n - ci.n);
+            proj[m++] = nc;
+        }
+        V2 temp = *out;
+        struct ProjGet {
+            const Con* c;
+            EG_HD Con operator()(int q) const { return c[q]; }
+        } pg{proj};
+        if (lp2d(pg, m, ci.n, maxSpeed, true, out) < m) *out = temp;
+        maxPen = det(dir, ci.p - *out);
+    }
+}
+
+} /* namespace ecmg */
+
+#endif

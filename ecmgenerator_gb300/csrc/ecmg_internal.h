@@ -1,0 +1,111 @@
+/*
+ * ecmg_internal.h -- device-side layout shared by the kernels and the host
+ * context (not part of the C ABI).
+ */
+#ifndef ECMG_INTERNAL_H
+#define ECMG_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include "ecmg_geom.cuh"
+
+namespace ecmg {
+
+/* Constraint capacity per agent: obstacle constraints + neighbours.  An agent
+   that would need more sets ECMG_DEV_ERR_CONSTRAINTS and is computed with the
+   first kMaxCons constraints only; the tick then returns ECMG_ERR_BOUND. */
+constexpr int kMaxCons = 64;
+constexpr int kMaxK = 32;
+
+/* device counters (int[kCounters]) */
+enum {
+    C_DESTROYED = 0,
+    C_REPLAN = 1,
+    C_LP3D = 2,
+    C_ERROR = 3,       /* bitmask of ECMG_DEV_ERR_* */
+    C_PROCESSED = 4,   /* agents processed by the per-agent kernel */
+    C_WORK = 5,        /* work counter of the persistent agent kernel */
+    C_LAST = 6,        /* last slot index to scan (host-written before the tick) */
+    C_NSORTED = 7,     /* agents in the neighbour grid */
+    kCounters = 16
+};
+
+enum {
+    ECMG_DEV_ERR_CONSTRAINTS = 1,
+    ECMG_DEV_ERR_LIST = 2,
+};
+
+/* Uniform agent grid: cells [0, gw*gh) cover the scene rectangle; agents
+   outside it go to the overflow bucket gw*gh, which every query scans. */
+struct AgentGrid {
+    float x0, y0, cell, inv;
+    int gw, gh;
+    int ncells; /* gw*gh, overflow bucket index */
+};
+
+struct TickArgs {
+    /* slot-indexed state */
+    V2* pos;
+    V2* vel;
+    V2* attr;
+    V2* pref_vel;
+    const float* clear;
+    const float* speed;
+    unsigned char* active;
+    const int* path_off;
+    const int* path_len;
+    const V2* path_xy;
+    /* tick-start snapshot in grid order */
+    const int* s_slot;
+    const V2* s_pos;
+    const V2* s_vel;
+    const float* s_clear;
+    const int* cell_start; /* ncells + 2 */
+    AgentGrid grid;
+    ObstView ob;
+    EcmView ecm;
+    /* parameters */
+    float dt, tau_a, tau_o, rnb, rnb2, max_speed, mass_recip, arr_sq, del_sq;
+    int k;
+    int lp3d_fp64;
+    /* outputs */
+    int* counters;
+    int* destroyed_list;
+    int* replan_list;
+    V2* replan_pos;
+    int list_cap;
+    /* recording (may be null) */
+    int* rec_nbr;
+    int* rec_cnt;
+    V2* rec_vorca;
+    int* rec_fail;
+    int* rec_ncons;
+    int* rec_nobst;
+};
+
+struct BinArgs {
+    const V2* pos;
+    const float* clear;
+    const V2* vel;
+    const unsigned char* active;
+    int* key;        /* slot -> bucket */
+    int* rank;       /* slot -> rank inside the bucket */
+    int* cell_count; /* ncells + 1 buckets (+1 sentinel) */
+    int* s_slot;
+    V2* s_pos;
+    V2* s_vel;
+    float* s_clear;
+    const int* cell_start;
+    int* counters;
+    AgentGrid grid;
+};
+
+/* kernels.cu */
+cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int scan_blocks,
+                        int block, int sms, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1);
+cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k, float r, AgentGrid g,
+                       int* key, int* rank, int* cell_count, int* cell_start, int* s_slot, V2* s_pos,
+                       int* scan_tmp, int scan_blocks, int* out_ids, int* out_cnt, cudaStream_t s);
+int scan_tmp_ints(int n);
+
+}  // namespace ecmg
+#endif

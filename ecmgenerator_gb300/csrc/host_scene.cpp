@@ -1,0 +1,370 @@
+/*
+ * host_scene.cpp -- host side of the static scene: obstacle rings, ECM
+ * point-location grid, obstacle candidate grid and the path planner.
+ * Compiled with -ffp-contract=off so that the shared geometry in
+ * ecmg_geom.cuh rounds as on the device.
+ */
+#include "host_scene.h"
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+#include <queue>
+
+namespace ecmg {
+
+EcmView HostScene::ecm_view() const
+{
+    EcmView e{};
+    e.v_pos = v_pos.data();
+    e.v_idx = v_idx.data();
+    e.he_target = he_target.data();
+    e.he_left = he_left.data();
+    e.he_right = he_right.data();
+    e.n_edges = (int)(he_target.size() / 2);
+    e.gx0 = ecm_grid.x0;
+    e.gy0 = ecm_grid.y0;
+    e.ginv = ecm_grid.inv;
+    e.gw = ecm_grid.gw;
+    e.gh = ecm_grid.gh;
+    e.g_start = ecm_grid.start.data();
+    e.g_items = ecm_grid.items.data();
+    e.special_y = special_y.data();
+    e.n_special = (int)special_y.size();
+    return e;
+}
+
+ObstView HostScene::obst_view(const GridCSR* g) const
+{
+    ObstView o{};
+    o.p = ob_p.data();
+    o.next = ob_next.data();
+    o.prev = ob_prev.data();
+    o.convex = ob_convex.data();
+    o.n_verts = (int)ob_p.size();
+    if (g && g->gw > 0) {
+        o.gx0 = g->x0;
+        o.gy0 = g->y0;
+        o.ginv = g->inv;
+        o.gw = g->gw;
+        o.gh = g->gh;
+        o.reach = g->reach;
+        o.g_start = g->start.data();
+        o.g_items = g->items.data();
+    }
+    return o;
+}
+
+void set_obstacles(HostScene& s, int n_obst, const int* off, const float* xy)
+{
+    int nv = n_obst > 0 ? off[n_obst] : 0;
+    s.ob_p.resize(nv);
+    s.ob_next.resize(nv);
+    s.ob_prev.resize(nv);
+    s.ob_convex.resize(nv);
+    s.ob_ring_off.assign(off, off + n_obst + 1);
+    for (int i = 0; i < nv; i++) s.ob_p[i] = mk(xy[2 * i], xy[2 * i + 1]);
+    for (int o = 0; o < n_obst; o++) {
+        int a = off[o], n = off[o + 1] - a;
+        for (int i = 0; i < n; i++) {
+            int g = a + i;
+            /* Obstacle::Initialize: i == 0 links to verts[n-1] and verts[1] */
+            s.ob_prev[g] = a + (i == 0 ? n - 1 : i - 1);
+            s.ob_next[g] = a + (i == 0 ? 1 % n : (i + 1) % n);
+        }
+        for (int i = 0; i < n; i++) {
+            int g = a + i;
+            if (n == 2) { s.ob_convex[g] = 1; continue; }
+            V2 p = s.ob_p[g], pp = s.ob_p[s.ob_prev[g]], pn = s.ob_p[s.ob_next[g]];
+            s.ob_convex[g] = det(pp - pn, p - pp) >= 0.0f ? 1 : 0;
+        }
+    }
+}
+
+static void bbox_grow(float& x0, float& y0, float& x1, float& y1, V2 p)
+{
+    x0 = std::min(x0, p.x);
+    y0 = std::min(y0, p.y);
+    x1 = std::max(x1, p.x);
+    y1 = std::max(y1, p.y);
+}
+
+void build_ecm_grid(HostScene& s)
+{
+    int E = (int)(s.he_target.size() / 2);
+    int C = 2 * E;
+    EcmView ev = s.ecm_view();
+    std::vector<V2> q(4 * (size_t)C);
+    float x0 = std::numeric_limits<float>::max(), y0 = x0, x1 = -x0, y1 = -x0;
+    std::vector<float> ys;
+    ys.reserve(4 * (size_t)C);
+    for (int c = 0; c < C; c++) {
+        cell_quad(ev, c, &q[4 * (size_t)c]);
+        for (int k = 0; k < 4; k++) {
+            bbox_grow(x0, y0, x1, y1, q[4 * (size_t)c + k]);
+            ys.push_back(q[4 * (size_t)c + k].y);
+        }
+    }
+    std::sort(ys.begin(), ys.end());
+    ys.erase(std::unique(ys.begin(), ys.end()), ys.end());
+    s.special_y = ys;
+    if (C == 0) {
+        s.ecm_grid = GridCSR();
+        s.ecm_grid.start.assign(2, 0);
+        s.ecm_grid.gw = s.ecm_grid.gh = 1;
+        return;
+    }
+    float maxc = std::max(std::max(std::fabs(x0), std::fabs(x1)), std::max(std::fabs(y0), std::fabs(y1)));
+    /* margin covers the rounding of the x-intersection in the ray-cast test and
+       of the query's cell index (coordinates stay far below 1e5) */
+    float margin = 0.01f + 1e-6f * maxc;
+    float area = (x1 - x0) * (y1 - y0);
+    float cell = std::sqrt(std::max(area, 1.0f) / (float)C) * 1.5f;
+    cell = std::min(std::max(cell, 0.5f), 64.0f);
+    GridCSR& g = s.ecm_grid;
+    g.x0 = x0 - 2 * margin;
+    g.y0 = y0 - 2 * margin;
+    g.cell = cell;
+    g.inv = 1.0f / cell;
+    g.gw = std::max(1, (int)std::ceil((x1 - g.x0 + 2 * margin) / cell) + 1);
+    g.gh = std::max(1, (int)std::ceil((y1 - g.y0 + 2 * margin) / cell) + 1);
+    size_t ng = (size_t)g.gw * g.gh;
+    std::vector<int> cnt(ng + 1, 0);
+    auto range = [&](int c, int& ix0, int& iy0, int& ix1, int& iy1) {
+        float a0 = std::numeric_limits<float>::max(), b0 = a0, a1 = -a0, b1 = -a0;
+        for (int k = 0; k < 4; k++) bbox_grow(a0, b0, a1, b1, q[4 * (size_t)c + k]);
+        ix0 = std::max(0, (int)std::floor((a0 - margin - g.x0) * g.inv));
+        iy0 = std::max(0, (int)std::floor((b0 - margin - g.y0) * g.inv));
+        ix1 = std::min(g.gw - 1, (int)std::floor((a1 + margin - g.x0) * g.inv));
+        iy1 = std::min(g.gh - 1, (int)std::floor((b1 + margin - g.y0) * g.inv));
+    };
+    for (int c = 0; c < C; c++) {
+        int ix0, iy0, ix1, iy1;
+        range(c, ix0, iy0, ix1, iy1);
+        for (int y = iy0; y <= iy1; y++)
+            for (int x = ix0; x <= ix1; x++) cnt[(size_t)y * g.gw + x]++;
+    }
+    g.start.assign(ng + 1, 0);
+    for (size_t i = 0; i < ng; i++) g.start[i + 1] = g.start[i] + cnt[i];
+    g.items.assign((size_t)g.start[ng], 0);
+    std::vector<int> cur(g.start.begin(), g.start.end() - 1);
+    for (int c = 0; c < C; c++) { /* ascending c -> ascending lists */
+        int ix0, iy0, ix1, iy1;
+        range(c, ix0, iy0, ix1, iy1);
+        for (int y = iy0; y <= iy1; y++)
+            for (int x = ix0; x <= ix1; x++) g.items[(size_t)cur[(size_t)y * g.gw + x]++] = c;
+    }
+}
+
+static double seg_rect_dist(V2 a, V2 b, double rx0, double ry0, double rx1, double ry1)
+{
+    /* distance between segment ab and an axis-aligned rectangle (double) */
+    auto inside = [&](double x, double y) { return x >= rx0 && x <= rx1 && y >= ry0 && y <= ry1; };
+    if (inside(a.x, a.y) || inside(b.x, b.y)) return 0.0;
+    auto pt_seg = [](double px, double py, double ax, double ay, double bx, double by) {
+        double dx = bx - ax, dy = by - ay, L = dx * dx + dy * dy;
+        double t = L > 0 ? ((px - ax) * dx + (py - ay) * dy) / L : 0.0;
+        t = std::min(1.0, std::max(0.0, t));
+        double qx = ax + t * dx - px, qy = ay + t * dy - py;
+        return std::sqrt(qx * qx + qy * qy);
+    };
+    auto seg_seg_cross = [](double ax, double ay, double bx, double by, double cx, double cy, double dx, double dy) {
+        auto orient = [](double px, double py, double qx, double qy, double rx, double ry) {
+            return (qx - px) * (ry - py) - (qy - py) * (rx - px);
+        };
+        double o1 = orient(ax, ay, bx, by, cx, cy), o2 = orient(ax, ay, bx, by, dx, dy);
+        double o3 = orient(cx, cy, dx, dy, ax, ay), o4 = orient(cx, cy, dx, dy, bx, by);
+        return ((o1 > 0) != (o2 > 0)) && ((o3 > 0) != (o4 > 0));
+    };
+    double cs[4][2] = {{rx0, ry0}, {rx1, ry0}, {rx1, ry1}, {rx0, ry1}};
+    double d = std::numeric_limits<double>::max();
+    for (int k = 0; k < 4; k++) {
+        const double* p = cs[k];
+        const double* q = cs[(k + 1) & 3];
+        if (seg_seg_cross(a.x, a.y, b.x, b.y, p[0], p[1], q[0], q[1])) return 0.0;
+        d = std::min(d, pt_seg(p[0], p[1], a.x, a.y, b.x, b.y));
+    }
+    d = std::min(d, pt_seg(a.x, a.y, rx0, ry0, rx1, ry0));
+    d = std::min(d, pt_seg(a.x, a.y, rx1, ry0, rx1, ry1));
+    d = std::min(d, pt_seg(a.x, a.y, rx1, ry1, rx0, ry1));
+    d = std::min(d, pt_seg(a.x, a.y, rx0, ry1, rx0, ry0));
+    d = std::min(d, pt_seg(b.x, b.y, rx0, ry0, rx1, ry0));
+    d = std::min(d, pt_seg(b.x, b.y, rx1, ry0, rx1, ry1));
+    d = std::min(d, pt_seg(b.x, b.y, rx1, ry1, rx0, ry1));
+    d = std::min(d, pt_seg(b.x, b.y, rx0, ry1, rx0, ry0));
+    return d;
+}
+
+void build_obst_grid(const HostScene& s, float reach, float cell, GridCSR& g)
+{
+    int nv = (int)s.ob_p.size();
+    float x0 = s.bx0, y0 = s.by0, x1 = s.bx1, y1 = s.by1;
+    for (int i = 0; i < nv; i++) bbox_grow(x0, y0, x1, y1, s.ob_p[i]);
+    float pad = reach + cell;
+    g.reach = reach;
+    g.cell = cell;
+    g.inv = 1.0f / cell;
+    g.x0 = x0 - pad;
+    g.y0 = y0 - pad;
+    g.gw = std::max(1, (int)std::ceil((x1 + pad - g.x0) / cell));
+    g.gh = std::max(1, (int)std::ceil((y1 + pad - g.y0) / cell));
+    size_t ng = (size_t)g.gw * g.gh;
+    const double margin = 0.05; /* float rounding of the exact in-range test */
+    std::vector<std::vector<int>> lists(ng);
+    for (int i = 0; i < nv; i++) { /* ascending vertex id -> ascending lists */
+        V2 a = s.ob_p[i], b = s.ob_p[s.ob_next[i]];
+        double r = (double)reach + margin;
+        int ix0 = std::max(0, (int)std::floor((std::min(a.x, b.x) - r - g.x0) / cell));
+        int iy0 = std::max(0, (int)std::floor((std::min(a.y, b.y) - r - g.y0) / cell));
+        int ix1 = std::min(g.gw - 1, (int)std::floor((std::max(a.x, b.x) + r - g.x0) / cell));
+        int iy1 = std::min(g.gh - 1, (int)std::floor((std::max(a.y, b.y) + r - g.y0) / cell));
+        for (int y = iy0; y <= iy1; y++)
+            for (int x = ix0; x <= ix1; x++) {
+                double rx0 = (double)g.x0 + (double)x * cell, ry0 = (double)g.y0 + (double)y * cell;
+                if (seg_rect_dist(a, b, rx0, ry0, rx0 + cell, ry0 + cell) <= r) lists[(size_t)y * g.gw + x].push_back(i);
+            }
+    }
+    g.start.assign(ng + 1, 0);
+    for (size_t i = 0; i < ng; i++) g.start[i + 1] = g.start[i] + (int)lists[i].size();
+    g.items.clear();
+    g.items.reserve((size_t)g.start[ng]);
+    for (auto& l : lists) g.items.insert(g.items.end(), l.begin(), l.end());
+}
+
+/* ---------------------------------------------------------------------- */
+static double pt_seg_d(V2 p, V2 a, V2 b)
+{
+    double dx = (double)b.x - a.x, dy = (double)b.y - a.y, L = dx * dx + dy * dy;
+    double t = L > 0 ? (((double)p.x - a.x) * dx + ((double)p.y - a.y) * dy) / L : 0.0;
+    t = std::min(1.0, std::max(0.0, t));
+    double qx = a.x + t * dx - p.x, qy = a.y + t * dy - p.y;
+    return std::sqrt(qx * qx + qy * qy);
+}
+
+static bool segs_cross(V2 a, V2 b, V2 c, V2 d)
+{
+    auto orient = [](V2 p, V2 q, V2 r) {
+        return ((double)q.x - p.x) * ((double)r.y - p.y) - ((double)q.y - p.y) * ((double)r.x - p.x);
+    };
+    double o1 = orient(a, b, c), o2 = orient(a, b, d), o3 = orient(c, d, a), o4 = orient(c, d, b);
+    return ((o1 > 0) != (o2 > 0)) && ((o3 > 0) != (o4 > 0));
+}
+
+/* straight piece a->b keeps `clr` from every obstacle edge near it */
+static bool clear_line(const HostScene& s, const GridCSR& g, V2 a, V2 b, double clr)
+{
+    if (g.gw == 0) return true;
+    double pad = clr + 0.01;
+    int ix0 = std::max(0, (int)std::floor((std::min(a.x, b.x) - pad - g.x0) * g.inv));
+    int iy0 = std::max(0, (int)std::floor((std::min(a.y, b.y) - pad - g.y0) * g.inv));
+    int ix1 = std::min(g.gw - 1, (int)std::floor((std::max(a.x, b.x) + pad - g.x0) * g.inv));
+    int iy1 = std::min(g.gh - 1, (int)std::floor((std::max(a.y, b.y) + pad - g.y0) * g.inv));
+    for (int y = iy0; y <= iy1; y++)
+        for (int x = ix0; x <= ix1; x++) {
+            size_t c = (size_t)y * g.gw + x;
+            for (int q = g.start[c]; q < g.start[c + 1]; q++) {
+                int i = g.items[(size_t)q];
+                V2 c0 = s.ob_p[i], c1 = s.ob_p[s.ob_next[i]];
+                if (segs_cross(a, b, c0, c1)) return false;
+                double d = std::min(std::min(pt_seg_d(a, c0, c1), pt_seg_d(b, c0, c1)),
+                                    std::min(pt_seg_d(c0, a, b), pt_seg_d(c1, a, b)));
+                if (d < clr) return false;
+            }
+        }
+    /* the walkable rectangle's border */
+    double lo = std::min(std::min(a.x - s.bx0, b.x - s.bx0), std::min(a.y - s.by0, b.y - s.by0));
+    double hi = std::min(std::min(s.bx1 - a.x, s.bx1 - b.x), std::min(s.by1 - a.y, s.by1 - b.y));
+    return std::min(lo, hi) >= clr;
+}
+
+bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float clearance,
+               std::vector<V2>& out, PlanScratch& scr)
+{
+    out.clear();
+    if (!s.has_ecm) return false;
+    EcmView ev = s.ecm_view();
+    V2 rs, rg;
+    int es, eg;
+    if (!retract(ev, start, &rs, &es)) return false;
+    if (!retract(ev, goal, &rg, &eg)) return false;
+    if (es == eg) { /* ECMPathPlanner.cpp:74-80 */
+        out.push_back(start);
+        out.push_back(goal);
+        return true;
+    }
+    int V = (int)s.v_pos.size();
+    if ((int)scr.g.size() != V) {
+        scr.g.assign(V, 0.0f);
+        scr.parent.assign(V, -1);
+        scr.stamp.assign(V, 0);
+        scr.closed.assign(V, 0);
+        scr.gen = 0;
+    }
+    int gen = ++scr.gen;
+    auto touch = [&](int v) {
+        if (scr.stamp[v] != gen) {
+            scr.stamp[v] = gen;
+            scr.g[v] = std::numeric_limits<float>::max();
+            scr.parent[v] = -1;
+            scr.closed[v] = 0;
+        }
+    };
+    auto dist = [](V2 a, V2 b) { return std::sqrt((a.x - b.x) * (a.x - b.x) + (a.y - b.y) * (a.y - b.y)); };
+    typedef std::pair<float, int> QE;
+    std::priority_queue<QE, std::vector<QE>, std::greater<QE>> open;
+    int sa = s.he_target[2 * es], sb = s.he_target[2 * es + 1];
+    int ga = s.he_target[2 * eg], gb = s.he_target[2 * eg + 1];
+    for (int v : {sa, sb}) {
+        touch(v);
+        float g0 = dist(start, s.v_pos[v]);
+        if (g0 < scr.g[v]) {
+            scr.g[v] = g0;
+            open.push(QE(g0 + dist(s.v_pos[v], goal), v));
+        }
+    }
+    int found = -1;
+    while (!open.empty()) {
+        QE top = open.top();
+        open.pop();
+        int v = top.second;
+        if (scr.closed[v]) continue;
+        scr.closed[v] = 1;
+        if (s.v_clear[v] < clearance) continue; /* AStar.cpp:103 */
+        if (v == ga || v == gb) { found = v; break; }
+        int h0 = s.v_halfedge[v];
+        if (h0 < 0) continue;
+        int h = h0, guard = 0;
+        do {
+            int w = s.he_target[h];
+            touch(w);
+            if (!scr.closed[w]) {
+                float ng = scr.g[v] + dist(s.v_pos[v], s.v_pos[w]);
+                if (ng < scr.g[w]) {
+                    scr.g[w] = ng;
+                    scr.parent[w] = v;
+                    open.push(QE(ng + dist(s.v_pos[w], goal), w));
+                }
+            }
+            h = s.he_next[h];
+        } while (h != h0 && ++guard < 1024);
+    }
+    if (found < 0) return false;
+    std::vector<V2> pts;
+    pts.push_back(goal);
+    for (int v = found; v >= 0; v = scr.parent[v]) pts.push_back(s.v_pos[v]);
+    pts.push_back(start);
+    std::reverse(pts.begin(), pts.end());
+    /* greedy shortening */
+    double clr = (double)clearance;
+    out.push_back(pts[0]);
+    size_t i = 0;
+    while (i + 1 < pts.size()) {
+        size_t j = i + 1;
+        while (j + 1 < pts.size() && clear_line(s, vis, pts[i], pts[j + 1], clr)) j++;
+        out.push_back(pts[j]);
+        i = j;
+    }
+    return true;
+}
+
+}  // namespace ecmg

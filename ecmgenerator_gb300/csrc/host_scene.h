@@ -1,0 +1,67 @@
+/*
+ * host_scene.h -- host copies of the static scene (obstacles, ECM), the
+ * acceleration grids built from them, and the host path planner.
+ */
+#ifndef ECMG_HOST_SCENE_H
+#define ECMG_HOST_SCENE_H
+
+#include <vector>
+#include "ecmg_geom.cuh"
+
+namespace ecmg {
+
+struct GridCSR {
+    float x0 = 0, y0 = 0, cell = 1, inv = 1;
+    int gw = 0, gh = 0;
+    float reach = 0;
+    std::vector<int> start; /* gw*gh + 1 */
+    std::vector<int> items;
+};
+
+struct HostScene {
+    /* obstacles, global (obstacle, vertex) order */
+    std::vector<V2> ob_p;
+    std::vector<int> ob_next, ob_prev;
+    std::vector<unsigned char> ob_convex;
+    std::vector<int> ob_ring_off;
+    /* ECM */
+    std::vector<V2> v_pos;
+    std::vector<float> v_clear;
+    std::vector<int> v_idx, v_halfedge, he_target, he_next;
+    std::vector<V2> he_left, he_right;
+    GridCSR ecm_grid;
+    std::vector<float> special_y;
+    /* scene rectangle (ECM and obstacle bounding box) */
+    float bx0 = 0, by0 = 0, bx1 = 0, by1 = 0;
+    bool has_ecm = false;
+
+    EcmView ecm_view() const;
+    ObstView obst_view(const GridCSR* g) const;
+};
+
+/* Obstacle::Initialize (ECMDataTypes.cpp:23-61): links and convexity */
+void set_obstacles(HostScene& s, int n_obst, const int* off, const float* xy);
+/* point-location grid + special y list over the ECM cell quads */
+void build_ecm_grid(HostScene& s);
+/* candidate lists: every obstacle edge within `reach` of each cell */
+void build_obst_grid(const HostScene& s, float reach, float cell, GridCSR& g);
+
+struct PlanScratch {
+    std::vector<float> g;
+    std::vector<int> parent;
+    std::vector<int> stamp;
+    std::vector<unsigned char> closed;
+    int gen = 0;
+};
+
+/* ECMPathPlanner::FindPath (ECMGenerator/ECMPathPlanner.cpp:22-136) as an
+   indicative route: locate and retract start and goal; same edge -> straight
+   line; otherwise A* over ECM vertices with the clearance filter of
+   AStar::FindPath (AStar.cpp:44-160), then the polyline start, vertices, goal
+   is shortened greedily wherever a straight piece keeps `clearance` from every
+   obstacle edge.  Returns false when no path exists. */
+bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float clearance,
+               std::vector<V2>& out, PlanScratch& scr);
+
+}  // namespace ecmg
+#endif

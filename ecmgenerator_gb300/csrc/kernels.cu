@@ -1,0 +1,465 @@
+/*
+ * kernels.cu -- the per-tick kernels.
+ *
+ * One tick (Simulator::Update, ECMAgentSimulator/Simulator.cpp:314-323) is
+ *   k_bin      bucket every active slot into the uniform agent grid
+ *   k_scan_*   exclusive scan of the bucket counts
+ *   k_scatter  tick-start snapshot of position/velocity/radius in grid order
+ *   k_agents   one thread per agent: attraction point (IRM), preferred
+ *              velocity, exact kNN on the grid, obstacle + agent ORCA
+ *              half-planes, 2D LP (+3D LP), velocity and position update
+ * The snapshot makes the tick Jacobi-exact: neighbours are read from the
+ * tick-start copy while each thread writes its own slot, which is what the
+ * reference's system order guarantees (velocities change only in
+ * UpdateVelocitySystem, after every agent's ORCA query).
+ *
+ * Built with -fmad=false: every float expression is the reference's sequence
+ * of separately rounded operations.
+ */
+#include "ecmg_internal.h"
+
+#include <stdint.h>
+
+namespace ecmg {
+
+/* ---------------------------------------------------------------------- */
+/* grid cell of a position; cells outside [0,gw)x[0,gh) -> overflow bucket  */
+__device__ __forceinline__ void cell_of(const AgentGrid& g, V2 p, int* cx, int* cy)
+{
+    float fx = (p.x - g.x0) * g.inv;
+    float fy = (p.y - g.y0) * g.inv;
+    fx = fminf(fmaxf(fx, -1.0e6f), 1.0e6f); /* NaN -> -1e6 (fmaxf drops NaN) */
+    fy = fminf(fmaxf(fy, -1.0e6f), 1.0e6f);
+    *cx = (int)floorf(fx);
+    *cy = (int)floorf(fy);
+}
+
+__device__ __forceinline__ int bucket_of(const AgentGrid& g, V2 p)
+{
+    int cx, cy;
+    cell_of(g, p, &cx, &cy);
+    if (cx < 0 || cy < 0 || cx >= g.gw || cy >= g.gh) return g.ncells;
+    return cy * g.gw + cx;
+}
+
+__global__ void k_bin(BinArgs a)
+{
+    int last = a.counters[C_LAST];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= last; i += gridDim.x * blockDim.x) {
+        if (!a.active[i]) continue;
+        int b = bucket_of(a.grid, a.pos[i]);
+        a.key[i] = b;
+        a.rank[i] = atomicAdd(&a.cell_count[b], 1);
+    }
+}
+
+__global__ void k_scatter(BinArgs a)
+{
+    int last = a.counters[C_LAST];
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.counters[C_NSORTED] = a.cell_start[a.grid.ncells + 1];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= last; i += gridDim.x * blockDim.x) {
+        if (!a.active[i]) continue;
+        int d = a.cell_start[a.key[i]] + a.rank[i];
+        a.s_slot[d] = i;
+        a.s_pos[d] = a.pos[i];
+        if (a.s_vel) a.s_vel[d] = a.vel[i];
+        if (a.s_clear) a.s_clear[d] = a.clear[i];
+    }
+}
+
+/* ---- exclusive scan of n ints (n <= 1024 * 1024 * 4 per pass) ------------ */
+constexpr int kScanBlock = 1024;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* sh, int* total)
+{
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int s = lane < (blockDim.x >> 5) ? sh[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        sh[lane] = s;
+    }
+    __syncthreads();
+    int incl = x + (w > 0 ? sh[w - 1] : 0);
+    *total = sh[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return incl - v;
+}
+
+__global__ void k_scan_local(const int* in, int* out, int* block_sums, int n)
+{
+    __shared__ int sh[32];
+    int i = blockIdx.x * kScanBlock + threadIdx.x;
+    int v = i < n ? in[i] : 0;
+    int tot;
+    int ex = block_exclusive_scan(v, sh, &tot);
+    if (i < n) out[i] = ex;
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_top(int* block_sums, int nb, int* out, int n)
+{
+    __shared__ int sh[32];
+    int carry = 0;
+    for (int base = 0; base < nb; base += kScanBlock) {
+        int i = base + threadIdx.x;
+        int v = i < nb ? block_sums[i] : 0;
+        int tot;
+        int ex = block_exclusive_scan(v, sh, &tot);
+        if (i < nb) block_sums[i] = ex + carry;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) out[n] = carry; /* total after the last element */
+}
+
+__global__ void k_scan_add(int* out, const int* block_sums, int n)
+{
+    int i = blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < n) out[i] += block_sums[blockIdx.x];
+}
+
+int scan_tmp_ints(int n) { return (n + kScanBlock - 1) / kScanBlock + 32; }
+
+/* out[0..n] = exclusive scan of in[0..n-1], out[n] = total */
+static cudaError_t scan(const int* in, int* out, int n, int* tmp, cudaStream_t s)
+{
+    int nb = (n + kScanBlock - 1) / kScanBlock;
+    k_scan_local<<<nb, kScanBlock, 0, s>>>(in, out, tmp, n);
+    k_scan_top<<<1, kScanBlock, 0, s>>>(tmp, nb, out, n);
+    k_scan_add<<<nb, kScanBlock, 0, s>>>(out, tmp, n);
+    return cudaGetLastError();
+}
+
+/* ---------------------------------------------------------------------- */
+/* exact kNN on the grid: the k smallest (d2, slot) with EPS < d2 < r^2.
+   keys: d2 bits (non-negative floats order as unsigned ints) : slot.       */
+template <int K>
+struct Knn {
+    unsigned long long key[K];
+    int ix[K]; /* grid-order index of the neighbour */
+    int cnt;
+    unsigned long long kth; /* key of the k-th entry once cnt == k */
+};
+
+template <int K>
+__device__ __forceinline__ void knn_consider(Knn<K>& s, int k, int j, V2 p, const V2* s_pos, const int* s_slot,
+                                             float r2)
+{
+    V2 q = s_pos[j];
+    float dx = q.x - p.x, dy = q.y - p.y;
+    float d2 = dx * dx + dy * dy; /* KDTree.cpp:107-108 */
+    if (!(d2 > kEps) || !(d2 < r2)) return;
+    unsigned hi = __float_as_uint(d2);
+    if (s.cnt == k && hi > (unsigned)(s.kth >> 32)) return;
+    unsigned long long kk = ((unsigned long long)hi << 32) | (unsigned)s_slot[j];
+    if (s.cnt == k && kk >= s.kth) return;
+    unsigned long long kth = s.kth;
+#pragma unroll
+    for (int q = K - 1; q >= 0; q--) {
+        unsigned long long nk;
+        int ni;
+        if (q > 0 && s.key[q - 1] > kk) { nk = s.key[q - 1]; ni = s.ix[q - 1]; }
+        else if (s.key[q] > kk) { nk = kk; ni = j; }
+        else { nk = s.key[q]; ni = s.ix[q]; }
+        s.key[q] = nk;
+        s.ix[q] = ni;
+        if (q == k - 1) kth = nk;
+    }
+    s.kth = kth;
+    if (s.cnt < k) s.cnt++;
+}
+
+template <int K>
+__device__ void knn_grid(Knn<K>& s, int k, V2 p, float rnb, float r2, const V2* s_pos, const int* s_slot,
+                         const int* cell_start, const AgentGrid& g)
+{
+#pragma unroll
+    for (int q = 0; q < K; q++) { s.key[q] = ~0ull; s.ix[q] = -1; }
+    s.cnt = 0;
+    s.kth = ~0ull;
+    /* agents outside the grid rectangle */
+    for (int j = cell_start[g.ncells], e = cell_start[g.ncells + 1]; j < e; j++)
+        knn_consider<K>(s, k, j, p, s_pos, s_slot, r2);
+    int cx, cy;
+    cell_of(g, p, &cx, &cy);
+    float x0 = g.x0 + (float)cx * g.cell, y0 = g.y0 + (float)cy * g.cell;
+    float m = fminf(fminf(p.x - x0, x0 + g.cell - p.x), fminf(p.y - y0, y0 + g.cell - p.y));
+    m = fmaxf(m, 0.0f);
+    int rmax = (int)ceilf(rnb * g.inv) + 2;
+    for (int R = 0; R <= rmax; R++) {
+        if (R >= 1) {
+            /* lower bound of the distance to any agent in ring R or beyond;
+               1 cm absorbs the rounding of the bucket assignment */
+            float lb = (float)(R - 1) * g.cell + m - 0.01f;
+            if (lb >= rnb) break;
+            if (s.cnt == k && lb > 0.0f && lb * lb > __uint_as_float((unsigned)(s.kth >> 32))) break;
+        }
+        int ylo = cy - R, yhi = cy + R;
+        for (int y = ylo; y <= yhi; y++) {
+            if (y < 0 || y >= g.gh) continue;
+            bool full = (y == ylo || y == yhi);
+            int xa = cx - R, xb = cx + R;
+            if (full) {
+                int a = max(xa, 0), b = min(xb, g.gw - 1);
+                if (a > b) continue;
+                int j0 = cell_start[y * g.gw + a], j1 = cell_start[y * g.gw + b + 1];
+                for (int j = j0; j < j1; j++) knn_consider<K>(s, k, j, p, s_pos, s_slot, r2);
+            } else {
+                if (xa >= 0 && xa < g.gw) {
+                    int c = y * g.gw + xa;
+                    for (int j = cell_start[c], e = cell_start[c + 1]; j < e; j++)
+                        knn_consider<K>(s, k, j, p, s_pos, s_slot, r2);
+                }
+                if (xb >= 0 && xb < g.gw && xb != xa) {
+                    int c = y * g.gw + xb;
+                    for (int j = cell_start[c], e = cell_start[c + 1]; j < e; j++)
+                        knn_consider<K>(s, k, j, p, s_pos, s_slot, r2);
+                }
+            }
+        }
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+struct LocalGet {
+    const Con* c;
+    __device__ Con operator()(int i) const { return c[i]; }
+};
+
+template <int K>
+__device__ void agent_tick(const TickArgs& a, int t)
+{
+    const int slot = a.s_slot[t];
+    const V2 pos = a.s_pos[t];
+    const V2 vel = a.s_vel[t];
+    const float clr = a.s_clear[t];
+
+    /* UpdateAttractionPointSystem (Simulator.cpp:538-590) */
+    const int off = a.path_off[slot], np = a.path_len[slot];
+    const V2* path = a.path_xy + off;
+    const V2 goal = path[np - 1];
+    float gdx = pos.x - goal.x, gdy = pos.y - goal.y;
+    float dist = gdx * gdx + gdy * gdy;
+    V2 attr;
+    if (dist < a.arr_sq) {
+        attr = goal;
+        a.attr[slot] = attr;
+        if (dist < a.del_sq) { /* DestroyAgent: skipped by every later system */
+            a.active[slot] = 0;
+            int q = atomicAdd(&a.counters[C_DESTROYED], 1);
+            if (q < a.list_cap) a.destroyed_list[q] = slot;
+            else atomicOr(&a.counters[C_ERROR], ECMG_DEV_ERR_LIST);
+            if (a.rec_cnt) a.rec_cnt[slot] = -1;
+            return;
+        }
+    } else {
+        V2 ap = mk(0.0f, 0.0f); /* Point attractionPoint; (0,0) */
+        if (irm(a.ecm, pos, path, np, &ap)) {
+            attr = ap;
+            a.attr[slot] = attr;
+        } else {
+            attr = a.attr[slot]; /* unchanged; the host re-plans before the next tick */
+            int q = atomicAdd(&a.counters[C_REPLAN], 1);
+            if (q < a.list_cap) { a.replan_list[q] = slot; a.replan_pos[q] = pos; }
+            else atomicOr(&a.counters[C_ERROR], ECMG_DEV_ERR_LIST);
+        }
+    }
+
+    /* ApplySteeringForce (Simulator.cpp:638-657) */
+    const float speed = a.speed[slot];
+    V2 pv = normalize(attr - pos) * speed;
+    a.pref_vel[slot] = pv;
+
+    /* ORCA::GetVelocity (ORCA.cpp:14-57) with maxSpeed = preferred speed
+       (Simulator.cpp:671) unless a global maximum is configured */
+    const float maxSpeed = a.max_speed > 0.0f ? a.max_speed : speed;
+    Knn<K> nn;
+    knn_grid<K>(nn, a.k, pos, a.rnb, a.rnb2, a.s_pos, a.s_slot, a.cell_start, a.grid);
+
+    Con cons[kMaxCons];
+    int m = 0;
+    bool overflow = false;
+    const float range = a.tau_o * maxSpeed + clr;
+    const float rsq = range * range;
+    {
+        const ObstView& o = a.ob;
+        int b = 0, e = 0;
+        const int* items = nullptr;
+        float fx = (pos.x - o.gx0) * o.ginv, fy = (pos.y - o.gy0) * o.ginv;
+        if (o.g_start && range <= o.reach && fx >= 0.0f && fy >= 0.0f && fx < (float)o.gw && fy < (float)o.gh) {
+            int g = (int)fy * o.gw + (int)fx;
+            b = o.g_start[g];
+            e = o.g_start[g + 1];
+            items = o.g_items;
+        } else {
+            e = o.n_verts; /* linear scan: the reference's own loop */
+        }
+        for (int q = b; q < e; q++) {
+            int L = items ? items[q] : q;
+            if (!obstacle_in_range(o, L, pos, rsq)) continue;
+            Con c;
+            if (obstacle_constraint(o, L, pos, vel, clr, a.tau_o, &c)) {
+                if (m < kMaxCons) cons[m++] = c;
+                else overflow = true;
+            }
+        }
+    }
+    const int nObst = m;
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        if (q < nn.cnt) {
+            int j = nn.ix[q];
+            Con c = agent_constraint(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt);
+            if (m < kMaxCons) cons[m++] = c;
+            else overflow = true;
+        }
+    }
+    if (overflow) atomicOr(&a.counters[C_ERROR], ECMG_DEV_ERR_CONSTRAINTS);
+
+    V2 v;
+    LocalGet get{cons};
+    int failed = lp2d(get, m, pv, maxSpeed, false, &v);
+    if (failed < m) {
+        Con proj[kMaxCons];
+        lp3d(get, m, nObst, maxSpeed, failed, &v, proj, a.lp3d_fp64 != 0);
+        atomicAdd(&a.counters[C_LP3D], 1);
+    }
+
+    /* force = vOrca - v (Simulator.cpp:676-677); UpdateVelocitySystem
+       (Simulator.cpp:619-635); UpdatePositionSystem (Simulator.cpp:592-606) */
+    float fx = v.x - vel.x, fy = v.y - vel.y;
+    V2 nv = mk(vel.x + fx * a.mass_recip * a.dt, vel.y + fy * a.mass_recip * a.dt);
+    V2 npos = mk(pos.x + (nv.x * a.dt), pos.y + (nv.y * a.dt));
+    a.vel[slot] = nv;
+    a.pos[slot] = npos;
+
+    if (a.rec_cnt) {
+        a.rec_cnt[slot] = nn.cnt;
+        for (int q = 0; q < a.k; q++) a.rec_nbr[slot * a.k + q] = -1;
+#pragma unroll
+        for (int q = 0; q < K; q++)
+            if (q < nn.cnt) a.rec_nbr[slot * a.k + q] = a.s_slot[nn.ix[q]];
+        a.rec_vorca[slot] = v;
+        a.rec_fail[slot] = failed;
+        a.rec_ncons[slot] = m;
+        a.rec_nobst[slot] = nObst;
+    }
+}
+
+/* persistent kernel: warps take 32 consecutive grid-order agents at a time */
+template <int K>
+__global__ void __launch_bounds__(128) k_agents(TickArgs a)
+{
+    const int n = a.counters[C_NSORTED];
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&a.counters[C_WORK], 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        int t = base + lane;
+        if (t < n) agent_tick<K>(a, t);
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(128) k_knn(const V2* s_pos, const int* s_slot, const int* cell_start,
+                                             AgentGrid g, int k, float rnb, float r2, const int* counters,
+                                             int* out_ids, int* out_cnt)
+{
+    const int n = counters[C_NSORTED];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        Knn<K> nn;
+        V2 p = s_pos[t];
+        knn_grid<K>(nn, k, p, rnb, r2, s_pos, s_slot, cell_start, g);
+        int slot = s_slot[t];
+        out_cnt[slot] = nn.cnt;
+#pragma unroll
+        for (int q = 0; q < K; q++)
+            if (q < k) out_ids[slot * k + q] = q < nn.cnt ? s_slot[nn.ix[q]] : -1;
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+static int grid_for(int n, int block, int sms, int per_sm)
+{
+    int g = (n + block - 1) / block;
+    int cap = sms * per_sm;
+    return g < 1 ? 1 : (g > cap ? cap : g);
+}
+
+cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int scan_blocks,
+                        int block, int sms, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1)
+{
+    (void)scan_blocks;
+    int nb = b.grid.ncells + 1;
+    cudaError_t e = cudaMemsetAsync(b.cell_count, 0, sizeof(int) * (size_t)(nb + 1), s);
+    if (e != cudaSuccess) return e;
+    int gb = grid_for(max_slots, 256, sms, 8);
+    k_bin<<<gb, 256, 0, s>>>(b);
+    e = scan(b.cell_count, (int*)b.cell_start, nb, scan_tmp, s);
+    if (e != cudaSuccess) return e;
+    k_scatter<<<gb, 256, 0, s>>>(b);
+    if (ev0) cudaEventRecord(ev0, s);
+    int ga = sms * 16; /* persistent: enough warps per SM to hide latency */
+    (void)block;
+    if (t.k <= 8) k_agents<8><<<ga, 128, 0, s>>>(t);
+    else if (t.k <= 16) k_agents<16><<<ga, 128, 0, s>>>(t);
+    else k_agents<32><<<ga, 128, 0, s>>>(t);
+    if (ev1) cudaEventRecord(ev1, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k, float r, AgentGrid g,
+                       int* key, int* rank, int* cell_count, int* cell_start, int* s_slot, V2* s_pos,
+                       int* scan_tmp, int scan_blocks, int* out_ids, int* out_cnt, cudaStream_t s)
+{
+    (void)scan_blocks;
+    /* the counters live behind the bucket counts: [nb+1 .. nb+1+kCounters) */
+    int nb = g.ncells + 1;
+    int* counters = cell_count + nb + 1;
+    cudaError_t e = cudaMemsetAsync(cell_count, 0, sizeof(int) * (size_t)(nb + 1 + kCounters), s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(out_cnt, 0, sizeof(int) * (size_t)n, s);
+    if (e != cudaSuccess) return e;
+    int last = n - 1;
+    e = cudaMemcpyAsync(counters + C_LAST, &last, sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    BinArgs b{};
+    b.pos = pos;
+    b.active = active;
+    b.key = key;
+    b.rank = rank;
+    b.cell_count = cell_count;
+    b.s_slot = s_slot;
+    b.s_pos = s_pos;
+    b.cell_start = cell_start;
+    b.counters = counters;
+    b.grid = g;
+    int gb = (n + 255) / 256;
+    if (gb < 1) gb = 1;
+    k_bin<<<gb, 256, 0, s>>>(b);
+    e = scan(cell_count, cell_start, nb, scan_tmp, s);
+    if (e != cudaSuccess) return e;
+    k_scatter<<<gb, 256, 0, s>>>(b);
+    int ga = (n + 127) / 128;
+    if (ga < 1) ga = 1;
+    float r2 = r * r;
+    if (k <= 8) k_knn<8><<<ga, 128, 0, s>>>(s_pos, s_slot, cell_start, g, k, r, r2, counters, out_ids, out_cnt);
+    else if (k <= 16) k_knn<16><<<ga, 128, 0, s>>>(s_pos, s_slot, cell_start, g, k, r, r2, counters, out_ids, out_cnt);
+    else k_knn<32><<<ga, 128, 0, s>>>(s_pos, s_slot, cell_start, g, k, r, r2, counters, out_ids, out_cnt);
+    return cudaGetLastError();
+}
+
+}  // namespace ecmg

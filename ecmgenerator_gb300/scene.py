@@ -222,6 +222,11 @@ def sample_free(rng, scene: Scene, n: int, radius: np.ndarray | float, bidx: Box
         py = rng.uniform(y0, y1, todo.size)
         clr = bidx.clearance(px, py, reach=rmax + margin + 1.0)
         good = clr >= rad[todo] + margin
+        if not no_overlap:
+            sel = todo[good]
+            out[sel, 0], out[sel, 1] = px[good], py[good]
+            done[sel] = True
+            continue
         for j in np.nonzero(good)[0]:
             i = int(todo[j])
             if no_overlap:

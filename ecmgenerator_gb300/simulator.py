@@ -1,0 +1,263 @@
+"""Python mirror of ``ECM::Simulation::Simulator`` (ECMAgentSimulator/Simulator.h:59-188)
+over the C ABI of libecmg.so.
+
+Method names follow the reference (snake_case); the tick runs on the GPU and
+nothing here computes simulation results on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import EcmgError, FIELD
+
+F32, I32, U8 = np.float32, np.int32, np.uint8
+
+
+def _a(x, dt):
+    return np.ascontiguousarray(x, dtype=dt)
+
+
+def _ptr(x):
+    return x.ctypes.data if x is not None else None
+
+
+class Planner:
+    """Host-only ECM planner (ecmg_planner_*); needs no GPU."""
+
+    def __init__(self, scene):
+        L = self.L = _lib.load()
+        self._keep, o, e = _scene_structs(scene)
+        h = C.c_void_p()
+        rc = L.ecmg_planner_create(C.byref(o), C.byref(e), C.byref(h))
+        if rc:
+            raise EcmgError(rc, "ecmg_planner_create failed")
+        self.h = h
+
+    def find_paths(self, starts, goals, clearances, threads=0, cap=1024):
+        starts, goals, clr = _a(starts, F32).reshape(-1, 2), _a(goals, F32).reshape(-1, 2), _a(clearances, F32)
+        n = starts.shape[0]
+        out = np.zeros((n, cap, 2), F32)
+        cnt = np.zeros(n, I32)
+        rc = self.L.ecmg_planner_find_paths(self.h, n, _ptr(starts), _ptr(goals), _ptr(clr), threads, cap, _ptr(out),
+                                            _ptr(cnt))
+        if rc:
+            raise EcmgError(rc, "ecmg_planner_find_paths failed")
+        return [out[i, :cnt[i]].copy() if cnt[i] > 0 else None for i in range(n)]
+
+    def locate(self, xy):
+        xy = _a(xy, F32).reshape(-1, 2)
+        out = np.zeros(xy.shape[0], I32)
+        rc = self.L.ecmg_planner_locate(self.h, xy.shape[0], _ptr(xy), _ptr(out))
+        if rc:
+            raise EcmgError(rc, "ecmg_planner_locate failed")
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ecmg_planner_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _scene_structs(scene):
+    e = scene.ecm
+    keep = [_a(scene.obst_off, I32), _a(scene.obst_xy, F32), _a(e.v_pos, F32), _a(e.v_clear, F32), _a(e.v_idx, I32),
+            _a(e.v_halfedge, I32), _a(e.he_target, I32), _a(e.he_next, I32), _a(e.he_left, F32),
+            _a(e.he_right, F32)]
+    o = _lib.Obstacles(scene.n_obstacles, _ptr(keep[0]), _ptr(keep[1]))
+    es = _lib.Ecm(e.n_vertices, _ptr(keep[2]), _ptr(keep[3]), _ptr(keep[4]), _ptr(keep[5]), e.n_edges,
+                  _ptr(keep[6]), _ptr(keep[7]), _ptr(keep[8]), _ptr(keep[9]))
+    return keep, o, es
+
+
+class Simulator:
+    """Simulator(ecm, planner, environment, maxAgents, simStepTime) on the GPU."""
+
+    def __init__(self, scene, max_agents: int, sim_step_time: float, *, max_neighbors: int = 5,
+                 tau_agent: float = 10.0, tau_obst: float = 10.0, neighbor_dist: float = 5.0,
+                 max_speed: float = 0.0, use_graph: bool = True, lp3d_fp64: bool = False, grid_cell: float = 0.0,
+                 mass: float = 0.8, arrival_radius: float = 20.0, delete_radius: float = 2.0):
+        self.L = _lib.load()
+        p = _lib.default_params(dt=sim_step_time, max_neighbors=max_neighbors, tau_agent=tau_agent,
+                                tau_obst=tau_obst, neighbor_dist=neighbor_dist, max_speed=max_speed,
+                                use_graph=int(use_graph), lp3d_fp64=int(lp3d_fp64), grid_cell=grid_cell, mass=mass,
+                                arrival_radius=arrival_radius, delete_radius=delete_radius)
+        self.params = p
+        h = C.c_void_p()
+        rc = self.L.ecmg_create(C.byref(p), int(max_agents), C.byref(h))
+        if rc:
+            raise EcmgError(rc, "ecmg_create failed (is a CUDA device visible?)")
+        self.h = h
+        self.max_agents = int(max_agents)
+        self.k = int(max_neighbors)
+        self.scene = scene
+        self._keep, o, e = _scene_structs(scene)
+        self._ck(self.L.ecmg_set_obstacles(self.h, C.byref(o)))
+        self._ck(self.L.ecmg_set_ecm(self.h, C.byref(e)))
+        self._plan_cb = None
+
+    # -- plumbing --------------------------------------------------------
+    def _ck(self, rc):
+        if rc:
+            msg = self.L.ecmg_last_error(self.h)
+            raise EcmgError(rc, msg.decode() if msg else "")
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ecmg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- Simulator API ---------------------------------------------------
+    def initialize(self):
+        """Simulator::Initialize (Simulator.cpp:21-60): storage is allocated by
+        the constructor; kept for API parity."""
+
+    def set_planner(self, fn):
+        """fn(sx, sy, gx, gy, clearance) -> (n,2) array or None."""
+        if fn is None:
+            self._plan_cb = None
+            self._ck(self.L.ecmg_set_planner(self.h, _lib.PLAN_FN(), None))
+            return
+
+        def cb(user, sx, sy, gx, gy, clr, out, cap):
+            p = fn(sx, sy, gx, gy, clr)
+            if p is None:
+                return -1
+            p = np.asarray(p, F32).reshape(-1, 2)[:cap]
+            for i in range(p.shape[0]):
+                out[2 * i] = float(p[i, 0])
+                out[2 * i + 1] = float(p[i, 1])
+            return int(p.shape[0])
+
+        self._plan_cb = _lib.PLAN_FN(cb)
+        self._ck(self.L.ecmg_set_planner(self.h, self._plan_cb, None))
+
+    def spawn_agent(self, start, goal, clearance: float, preferred_speed: float) -> int:
+        """Simulator::SpawnAgent; returns the slot or -1 (Simulator.cpp:168-200)."""
+        s = C.c_int(-1)
+        rc = self.L.ecmg_spawn_agent(self.h, float(start[0]), float(start[1]), float(goal[0]), float(goal[1]),
+                                     float(clearance), float(preferred_speed), C.byref(s))
+        if rc in (4, 6, 7):
+            return -1
+        self._ck(rc)
+        return s.value
+
+    def add_agents(self, pos, clearance, pref_speed, paths) -> np.ndarray:
+        pos = _a(pos, F32).reshape(-1, 2)
+        n = pos.shape[0]
+        clr, spd = _a(clearance, F32), _a(pref_speed, F32)
+        lens = np.array([len(p) for p in paths], I32)
+        offs = np.zeros(n, I32)
+        if n:
+            offs[1:] = np.cumsum(lens)[:-1]
+        xy = _a(np.concatenate([np.asarray(p, F32).reshape(-1, 2) for p in paths], 0), F32) if n else \
+            np.zeros((0, 2), F32)
+        out = np.zeros(n, I32)
+        self._ck(self.L.ecmg_add_agents(self.h, n, _ptr(pos), _ptr(clr), _ptr(spd), _ptr(offs), _ptr(lens),
+                                        _ptr(xy), _ptr(out)))
+        return out
+
+    def destroy_agent(self, idx: int):
+        self._ck(self.L.ecmg_destroy_agent(self.h, int(idx)))
+
+    def update(self, dt: float | None = None, ticks: int = 1) -> _lib.TickStats:
+        """Simulator::Update; like the reference, dt is ignored and the step
+        time given at construction is used (Simulator.cpp:313-323)."""
+        st = _lib.TickStats()
+        self._ck(self.L.ecmg_tick(self.h, int(ticks), C.byref(st)))
+        return st
+
+    def reset(self):
+        self._ck(self.L.ecmg_reset(self.h))
+
+    def set_path(self, idx: int, path):
+        p = _a(path, F32).reshape(-1, 2)
+        self._ck(self.L.ecmg_set_path(self.h, int(idx), _ptr(p), p.shape[0]))
+
+    def get_path(self, idx: int, cap: int = 4096) -> np.ndarray:
+        out = np.zeros((cap, 2), F32)
+        n = C.c_int()
+        self._ck(self.L.ecmg_get_path(self.h, int(idx), _ptr(out), cap, C.byref(n)))
+        return out[: min(n.value, cap)].copy()
+
+    def find_path(self, start, goal, clearance, cap=4096):
+        out = np.zeros((cap, 2), F32)
+        n = C.c_int()
+        rc = self.L.ecmg_find_path(self.h, float(start[0]), float(start[1]), float(goal[0]), float(goal[1]),
+                                   float(clearance), _ptr(out), cap, C.byref(n))
+        return None if rc else out[: min(n.value, cap)].copy()
+
+    # -- getters (Simulator.h:114-126) -------------------------------------
+    def _get(self, field, shape, dt):
+        out = np.zeros(shape, dt)
+        self._ck(self.L.ecmg_get_state(self.h, FIELD[field], _ptr(out)))
+        return out
+
+    def get_num_agents(self) -> int:
+        n = C.c_int()
+        self._ck(self.L.ecmg_get_counts(self.h, C.byref(n), None, None))
+        return n.value
+
+    def get_last_index(self) -> int:
+        n = C.c_int()
+        self._ck(self.L.ecmg_get_counts(self.h, None, C.byref(n), None))
+        return n.value
+
+    def get_position_data(self):
+        return self._get("position", (self.max_agents, 2), F32)
+
+    def get_velocity_data(self):
+        return self._get("velocity", (self.max_agents, 2), F32)
+
+    def get_preferred_velocity_data(self):
+        return self._get("pref_velocity", (self.max_agents, 2), F32)
+
+    def get_attraction_point_data(self):
+        return self._get("attraction", (self.max_agents, 2), F32)
+
+    def get_clearance_data(self):
+        return self._get("clearance", (self.max_agents,), F32)
+
+    def get_speed_data(self):
+        return self._get("speed", (self.max_agents,), F32)
+
+    def get_active_flags(self):
+        return self._get("active", (self.max_agents,), U8)
+
+    def set_state(self, field: str, arr):
+        dt = U8 if field == "active" else F32
+        arr = _a(arr, dt)
+        self._ck(self.L.ecmg_set_state(self.h, FIELD[field], _ptr(arr)))
+
+    # -- inspection --------------------------------------------------------
+    def set_record(self, on: bool = True):
+        self._ck(self.L.ecmg_set_record(self.h, int(on)))
+
+    def get_record(self) -> dict:
+        n, k = self.max_agents, self.k
+        d = dict(nbr_ids=np.zeros((n, k), I32), nbr_count=np.zeros(n, I32), v_orca=np.zeros((n, 2), F32),
+                 lp_fail=np.zeros(n, I32), n_constraints=np.zeros(n, I32), n_obst_constraints=np.zeros(n, I32))
+        self._ck(self.L.ecmg_get_record(self.h, _ptr(d["nbr_ids"]), _ptr(d["nbr_count"]), _ptr(d["v_orca"]),
+                                        _ptr(d["lp_fail"]), _ptr(d["n_constraints"]), _ptr(d["n_obst_constraints"])))
+        return d

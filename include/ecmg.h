@@ -1,0 +1,210 @@
+/*
+ * ecmg.h -- C ABI of the GB300 crowd-tick library (libecmg.so).
+ *
+ * The library replaces the per-tick update of the ECMGenerator crowd simulator,
+ * ECM::Simulation::Simulator (ECMAgentSimulator/Simulator.h:59-188): neighbour
+ * query, ORCA velocity selection, IRM path following and integration, executed
+ * as sm_103a kernels on one GPU with the agent state resident in device memory.
+ * Scene construction (obstacles, the Explicit Corridor Map) and path planning
+ * stay on the host.
+ *
+ * Conventions: every entry point returns an ecmg_status (0 = ECMG_OK).  Arrays
+ * are host arrays unless the name says "dev".  Slot indices are the reference's
+ * Entity ids: slots are handed out by a LIFO free-slot stack exactly like
+ * Simulator::m_freeEntitySpaces (Simulator.h:66-69, 167).  One context must not
+ * be used from two threads at once (the reference is single-threaded).
+ * ecmg_last_error() describes the most recent failure of a context.
+ */
+#ifndef ECMG_H
+#define ECMG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    ECMG_OK = 0,
+    ECMG_ERR_INVALID_ARG = 1,   /* bad pointer, size or value (NaN/inf input, empty path, ...) */
+    ECMG_ERR_CUDA = 2,          /* a CUDA runtime call failed                                   */
+    ECMG_ERR_BOUND = 3,         /* a device capacity or loop bound was exceeded (see last_error) */
+    ECMG_ERR_NO_SLOT = 4,       /* no free agent slot (SpawnAgent returns -1, Simulator.cpp:170) */
+    ECMG_ERR_STATE = 5,         /* call made in the wrong state (e.g. tick before set_ecm)     */
+    ECMG_ERR_INVALID_SPAWN = 6, /* spawn location occupied (ValidSpawnLocation, Simulator.cpp:295) */
+    ECMG_ERR_NO_PATH = 7,       /* the planner found no path                                    */
+    ECMG_ERR_NO_DEVICE = 8      /* no CUDA device                                               */
+} ecmg_status;
+
+typedef struct ecmg_ctx ecmg_ctx;
+
+/* Tick parameters.  ecmg_default_params() gives the reference's values:
+   ORCA(5) (Simulator.cpp:55), time horizons 10 s (ORCA.h:102-103), mass 0.8
+   (Simulator.cpp:622), arrival / delete radii 20 m / 2 m (Simulator.cpp:542-543).
+   max_speed <= 0 reproduces the reference, whose LP radius is each agent's
+   preferred speed (Simulator.cpp:671). */
+typedef struct {
+    float dt;              /* Simulator::m_SimStepTime (ctor argument)            */
+    float tau_agent;       /* ORCA::m_lookAheadAgent                              */
+    float tau_obst;        /* ORCA::m_lookAheadObstacle                           */
+    float neighbor_dist;   /* neighbour cut-off of the grid kNN (metres)          */
+    float max_speed;       /* <= 0: preferred speed per agent                     */
+    float mass;
+    float arrival_radius;
+    float delete_radius;
+    int max_neighbors;     /* ORCA(numNeighbors); 1..32                           */
+    int lp3d_fp64;         /* 1: build the 3D-LP projection lines in FP64         */
+    int use_graph;         /* 1: capture the tick as a CUDA graph                 */
+    int block_size;        /* 0: autotuned                                        */
+    float grid_cell;       /* agent grid cell (metres); 0: derived from density  */
+} ecmg_params;
+
+/* Per-tick counters (summed over the ticks of one ecmg_tick call). */
+typedef struct {
+    int ticks;
+    int active_agents;     /* after the last tick (Simulator::GetNumAgents)       */
+    int last_index;        /* Simulator::GetLastIndex after the last tick          */
+    long long agent_steps; /* sum over ticks of agents processed                  */
+    long long destroyed;   /* agents that reached their goal (DestroyAgent)       */
+    long long replans;     /* IRM failures handed to the host planner             */
+    long long replans_failed;
+    long long lp3d;        /* agents whose 2D LP was infeasible                   */
+    float device_ms;       /* device time of the ticks (CUDA events)              */
+    float agent_kernel_ms; /* device time of the per-agent kernel alone           */
+} ecmg_tick_stats;
+
+/* Static obstacles: n_obstacles rings, ring r = xy[2*ring_offsets[r] ..
+   2*ring_offsets[r+1]), counter-clockwise as Environment::AddObstacle expects
+   (Environment.cpp:199-229).  Convexity and prev/next links are derived as
+   Obstacle::Initialize does (ECMDataTypes.cpp:23-61). */
+typedef struct {
+    int n_obstacles;
+    const int* ring_offsets;  /* n_obstacles + 1 */
+    const float* xy;
+} ecmg_obstacles;
+
+/* Explicit Corridor Map in ECMGraph's layout (ECMGenerator/ECM.h:20-116):
+   vertex i = (v_pos[2i], v_pos[2i+1]); half-edge h of edge e has index 2e+h. */
+typedef struct {
+    int n_vertices;
+    const float* v_pos;       /* 2*V  ECMVertex::position        */
+    const float* v_clear;     /* V    ECMVertex::clearance       */
+    const int* v_idx;         /* V    ECMVertex::idx             */
+    const int* v_halfedge;    /* V    ECMVertex::half_edge_idx   */
+    int n_edges;
+    const int* he_target;     /* 2E   ECMHalfEdge::v_target_idx  */
+    const int* he_next;       /* 2E   ECMHalfEdge::next_idx      */
+    const float* he_left;     /* 4E   ECMHalfEdge::closest_left  */
+    const float* he_right;    /* 4E   ECMHalfEdge::closest_right */
+} ecmg_ecm;
+
+/* Host planner used for spawning and for re-planning after an IRM failure
+   (Simulator::UpdatePath, Simulator.cpp:97-124).  Write at most cap points
+   to out_xy and return their count, or a negative value for "no path". */
+typedef int (*ecmg_plan_fn)(void* user, float sx, float sy, float gx, float gy,
+                            float clearance, float* out_xy, int cap);
+
+enum {
+    ECMG_FIELD_POSITION = 0,       /* float[2*n]  GetPositionData           */
+    ECMG_FIELD_VELOCITY = 1,       /* float[2*n]  GetVelocityData           */
+    ECMG_FIELD_PREF_VELOCITY = 2,  /* float[2*n]  GetPreferredVelocityData  */
+    ECMG_FIELD_ATTRACTION = 3,     /* float[2*n]  GetAttractionPointData    */
+    ECMG_FIELD_CLEARANCE = 4,      /* float[n]    GetClearanceData          */
+    ECMG_FIELD_SPEED = 5,          /* float[n]    preferred speed           */
+    ECMG_FIELD_ACTIVE = 6          /* uint8[n]    GetActiveFlags            */
+};
+
+/* defaults as listed above; dt = 0.1 (ECMApplication/main.cpp:53) */
+void ecmg_default_params(ecmg_params* p);
+
+/* Simulator(ecm, planner, env, maxAgents, simStepTime) + Initialize()
+   (Simulator.h:63-74, Simulator.cpp:21-60); device 0 of the process. */
+ecmg_status ecmg_create(const ecmg_params* p, int max_agents, ecmg_ctx** out);
+/* ~Simulator / ClearSimulator (Simulator.cpp:62-95) */
+ecmg_status ecmg_destroy(ecmg_ctx* ctx);
+const char* ecmg_last_error(const ecmg_ctx* ctx);
+ecmg_status ecmg_get_params(const ecmg_ctx* ctx, ecmg_params* out);
+
+/* Environment::GetObstacles (Environment.h:55), read by FindNearestObstacles */
+ecmg_status ecmg_set_obstacles(ecmg_ctx* ctx, const ecmg_obstacles* o);
+/* the ECM the Simulator and its planner hold (Simulator.h:154-155) */
+ecmg_status ecmg_set_ecm(ecmg_ctx* ctx, const ecmg_ecm* e);
+/* replaces the built-in A* planner (NULL restores it) */
+ecmg_status ecmg_set_planner(ecmg_ctx* ctx, ecmg_plan_fn fn, void* user);
+
+/* Simulator::SpawnAgent (Simulator.cpp:168-200): ValidSpawnLocation, then a
+   planned path.  *out_slot = slot, or -1 with ECMG_ERR_NO_SLOT /
+   ECMG_ERR_INVALID_SPAWN / ECMG_ERR_NO_PATH. */
+ecmg_status ecmg_spawn_agent(ecmg_ctx* ctx, float sx, float sy, float gx, float gy,
+                             float clearance, float pref_speed, int* out_slot);
+/* Bulk spawn with caller-supplied paths (agent i's path is
+   path_xy[2*path_off[i] .. 2*(path_off[i]+path_len[i]))); no spawn-location
+   check.  out_slots may be NULL. */
+ecmg_status ecmg_add_agents(ecmg_ctx* ctx, int n, const float* pos, const float* clearance,
+                            const float* pref_speed, const int* path_off, const int* path_len,
+                            const float* path_xy, int* out_slots);
+/* Simulator::DestroyAgent (Simulator.cpp:202-208) */
+ecmg_status ecmg_destroy_agent(ecmg_ctx* ctx, int slot);
+/* Simulator::Reset (Simulator.cpp:325-333) */
+ecmg_status ecmg_reset(ecmg_ctx* ctx);
+/* replace one agent's path (Simulator::UpdatePath with a given polyline) */
+ecmg_status ecmg_set_path(ecmg_ctx* ctx, int slot, const float* xy, int n);
+/* plan with the context's planner (ECMPathPlanner::FindPath) */
+ecmg_status ecmg_find_path(ecmg_ctx* ctx, float sx, float sy, float gx, float gy, float clearance,
+                           float* out_xy, int cap, int* out_n);
+/* Host-only planner over a scene (needs no GPU): the same planner the context
+   uses, for scene set-up and batch planning on `threads` host threads.
+   out_xy holds cap_per_path points per request; out_n[i] is the point count,
+   -1 when no path exists, -2 when the path has more than cap_per_path points. */
+typedef struct ecmg_planner ecmg_planner;
+ecmg_status ecmg_planner_create(const ecmg_obstacles* o, const ecmg_ecm* e, ecmg_planner** out);
+ecmg_status ecmg_planner_destroy(ecmg_planner* p);
+ecmg_status ecmg_planner_find_paths(ecmg_planner* p, int n, const float* starts, const float* goals,
+                                    const float* clearances, int threads, int cap_per_path,
+                                    float* out_xy, int* out_n);
+/* ECMGraph::FindCell for n points: cell index (2*edge + side) or -1 */
+ecmg_status ecmg_planner_locate(ecmg_planner* p, int n, const float* xy, int* out_cell);
+
+/* n_ticks x Simulator::Update (Simulator.cpp:314-323).  Re-planning requests
+   raised by a tick are served on the host before the next tick starts. */
+ecmg_status ecmg_tick(ecmg_ctx* ctx, int n_ticks, ecmg_tick_stats* stats);
+
+/* Getters of Simulator.h:114-126, copied to caller memory (n_slots entries) */
+ecmg_status ecmg_get_state(ecmg_ctx* ctx, int field, void* host_dst);
+/* Overwrite slot-indexed state from the host (float[2*n] for the 2-vectors);
+   used to start a tick from a given state. */
+ecmg_status ecmg_set_state(ecmg_ctx* ctx, int field, const void* host_src);
+ecmg_status ecmg_get_counts(const ecmg_ctx* ctx, int* num_agents, int* last_index, int* max_agents);
+ecmg_status ecmg_get_path(ecmg_ctx* ctx, int slot, float* out_xy, int cap, int* out_n);
+
+/* Record per-agent results of the following ticks for inspection:
+   neighbour list (slot ids, -1 padded, max_neighbors per slot), LP result,
+   failed index of the 2D LP (== n_constraints when feasible), constraint
+   counts.  Recording costs bandwidth; it is off by default. */
+ecmg_status ecmg_set_record(ecmg_ctx* ctx, int on);
+ecmg_status ecmg_get_record(ecmg_ctx* ctx, int* nbr_ids, int* nbr_count, float* v_orca,
+                            int* lp_fail, int* n_constraints, int* n_obst_constraints);
+
+/* the cudaStream_t the context launches on (for callers that record CUDA
+   events or order their own work around the tick) */
+void* ecmg_stream(const ecmg_ctx* ctx);
+
+/* Kernel launch list of the last tick (names in launch order); returns the
+   number of kernels per tick. */
+int ecmg_kernels_per_tick(const ecmg_ctx* ctx);
+
+/* Stand-alone exact kNN on device arrays: for each of n agents at dev_pos
+   (float2) with dev_active != 0, the k nearest other active agents with
+   1e-4 < d^2 < radius^2, ordered by (d^2, index) -- the neighbour definition
+   of the tick.  dev_scratch must hold ecmg_knn_scratch_bytes(n, ...) bytes;
+   stream is a cudaStream_t (NULL = legacy default stream). */
+size_t ecmg_knn_scratch_bytes(int n, float min_x, float min_y, float max_x, float max_y, float cell);
+ecmg_status ecmg_knn(const float* dev_pos, const unsigned char* dev_active, int n, int k, float radius,
+                     float min_x, float min_y, float max_x, float max_y, float cell,
+                     int* dev_out_ids, int* dev_out_count, void* dev_scratch, size_t scratch_bytes,
+                     void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ECMG_H */

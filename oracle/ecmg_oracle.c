@@ -5,6 +5,7 @@
  * the file:line it follows.  Operand order of every float expression is the
  * reference's; build with -ffp-contract=off.
  */
+#define _POSIX_C_SOURCE 200809L
 #include "ecmg_oracle.h"
 #include "../ecmgenerator_gb300/csrc/ecmg_tmath.h"
 
@@ -952,3 +953,96 @@ int og_tick(const og_obstacles* o, const og_ecm* e, og_state* s, const og_params
     free(act0);
     return 0;
 }
+
+/* ---------------------------------------------------------------------------
+ * CPU-baseline timing (see ecmg_oracle.h)
+ * ------------------------------------------------------------------------- */
+#include <time.h>
+
+static double og_now(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+typedef struct {
+    const og_obstacles* o;
+    const og_ecm* e;
+    const og_state* s;
+    const og_params* p;
+    og_kdtree kd; /* shares the tree, owns its neighbour cache */
+    const int* sample;
+    int lo, hi;
+    double sink;
+} og_sjob;
+
+static void* sample_thread(void* arg)
+{
+    og_sjob* j = (og_sjob*)arg;
+    const og_state* s = j->s;
+    const og_params* p = j->p;
+    int k = p->k;
+    int* ids = (int*)malloc(sizeof(int) * (size_t)k);
+    const float arrSq = p->arrival_radius * p->arrival_radius;
+    for (int q = j->lo; q < j->hi; q++) {
+        int i = j->sample[q];
+        const og_v2* path = s->path_xy + s->path_off[i];
+        int np = s->path_len[i];
+        og_v2 pos = s->pos[i];
+        og_v2 g = path[np - 1];
+        float dx = pos.x - g.x, dy = pos.y - g.y;
+        og_v2 attr = s->attr[i];
+        if (dx * dx + dy * dy < arrSq) attr = g;
+        else {
+            og_v2 ap = v2(0.0f, 0.0f);
+            if (og_irm(j->e, pos, path, np, &ap)) attr = ap;
+        }
+        og_v2 pv = vmul(vnormalize(vsub(attr, pos)), s->pref_speed[i]);
+        int nn = og_kdtree_query(&j->kd, s, i, ids);
+        og_v2 v;
+        int nob, fail;
+        og_orca_velocity(j->o, s, p, i, ids, nn, pv, &v, &nob, &fail);
+        j->sink += v.x + v.y;
+    }
+    free(ids);
+    return NULL;
+}
+
+int og_time_sample(const og_obstacles* o, const og_ecm* e, const og_state* s, const og_params* p,
+                   const int* sample, int n_sample, int threads, double* t_build, double* t_agents)
+{
+    og_kdtree* kd = og_kdtree_create(p->k);
+    double t0 = og_now();
+    og_kdtree_build(kd, s);
+    double t1 = og_now();
+    int th = threads > 1 ? threads : 1;
+    og_sjob* jobs = (og_sjob*)calloc((size_t)th, sizeof(og_sjob));
+    pthread_t* tid = (pthread_t*)calloc((size_t)th, sizeof(pthread_t));
+    int span = (n_sample + th - 1) / th;
+    for (int t = 0; t < th; t++) {
+        jobs[t].o = o; jobs[t].e = e; jobs[t].s = s; jobs[t].p = p;
+        jobs[t].kd = *kd;
+        jobs[t].kd.cache = (int*)calloc((size_t)p->k, sizeof(int));
+        jobs[t].kd.dist = (float*)malloc(sizeof(float) * (size_t)p->k);
+        jobs[t].sample = sample;
+        jobs[t].lo = t * span < n_sample ? t * span : n_sample;
+        jobs[t].hi = (t + 1) * span < n_sample ? (t + 1) * span : n_sample;
+    }
+    double t2 = og_now();
+    for (int t = 1; t < th; t++) pthread_create(&tid[t], NULL, sample_thread, &jobs[t]);
+    sample_thread(&jobs[0]);
+    for (int t = 1; t < th; t++) pthread_join(tid[t], NULL);
+    double t3 = og_now();
+    for (int t = 0; t < th; t++) { free(jobs[t].kd.cache); free(jobs[t].kd.dist); }
+    free(jobs);
+    free(tid);
+    og_kdtree_destroy(kd);
+    if (t_build) *t_build = t1 - t0;
+    if (t_agents) *t_agents = t3 - t2;
+    return 0;
+}
+
+/* the shared transcendentals, exported for their accuracy tests */
+float og_test_atanf(float x) { return ecmg_atanf(x); }
+void og_test_sincosf(float a, float* s, float* c) { ecmg_sincosf(a, s, c); }

@@ -134,6 +134,15 @@ int og_irm(const og_ecm* e, og_v2 pos, const og_v2* path, int n, og_v2* out);
 int og_tick(const og_obstacles* o, const og_ecm* e, og_state* s, const og_params* p,
             og_kdtree* kd, og_tick_out* out);
 
+/* CPU-baseline timing on a bounded sample: builds the reference kd-tree over
+   every active agent (timed as *t_build) and runs the per-agent stages of the
+   tick -- IRM attraction point with the linear point location, steering,
+   kd-tree kNN, obstacle scan, constraints, LP and LP3D -- for the n_sample
+   listed agents on `threads` host threads (timed as *t_agents, seconds).
+   State is not modified. */
+int og_time_sample(const og_obstacles* o, const og_ecm* e, const og_state* s, const og_params* p,
+                   const int* sample, int n_sample, int threads, double* t_build, double* t_agents);
+
 #ifdef __cplusplus
 }
 #endif

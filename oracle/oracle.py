@@ -200,6 +200,19 @@ class Port:
     def kdtree(self, k):
         return self.lib.og_kdtree_create(k)
 
+    def time_sample(self, obst_s, ecm_s, st, params, sample, threads=1):
+        """Seconds spent building the kd-tree and running the per-agent tick
+        stages for ``sample`` (see og_time_sample)."""
+        L = self.lib
+        L.og_time_sample.argtypes = [C.POINTER(Obst), C.POINTER(EcmS), C.POINTER(State), C.POINTER(Params),
+                                     C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        sample = np.ascontiguousarray(sample, I32)
+        s = self.state(st)
+        tb, ta = C.c_double(), C.c_double()
+        L.og_time_sample(C.byref(obst_s), C.byref(ecm_s), C.byref(s), C.byref(params), _addr(sample),
+                         int(sample.shape[0]), int(threads), C.byref(tb), C.byref(ta))
+        return tb.value, ta.value
+
 
 class Ref:
     """The reference's own simulator, driven through ref_harness.cpp."""
