@@ -183,6 +183,7 @@ def run_ours(args):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     steps = 0
     agent_ms = 0.0
+    tot = dict(lp3d=0, replans=0, replans_failed=0, destroyed=0, device_ms=0.0)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -196,6 +197,11 @@ def run_ours(args):
                 ev[i][1].record(stream)
             steps += s.agent_steps
             agent_ms += s.agent_kernel_ms
+            tot["lp3d"] += s.lp3d
+            tot["replans"] += s.replans
+            tot["replans_failed"] += s.replans_failed
+            tot["destroyed"] += s.destroyed
+            tot["device_ms"] += s.device_ms
         torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in ev)
     if world > 1:
@@ -225,7 +231,7 @@ def run_ours(args):
     except OSError:
         pass
     hbm = peaks.get("hbm_gbs") or 6800.0
-    achieved = ALG_BYTES_PER_AGENT * (steps / max(args.steps, 1)) / (kern_ms / 1e3) / 1e9
+    achieved = ALG_BYTES_PER_AGENT * (steps / max(args.steps, 1)) / (kern_ms / 1e3) / 1e9 if kern_ms > 0 else 0.0
     traffic = None
     tf = os.path.join(HERE, "profiles", "k_agents_traffic.json")
     if os.path.exists(tf):
@@ -251,6 +257,10 @@ def run_ours(args):
         "gpu_launches": 6 * args.steps,
         "clocks": clk.summary(),
         "tick_ms_device": ms / args.steps,
+        "tick_stats": {"lp3d_per_tick": tot["lp3d"] / args.steps, "replans_per_tick": tot["replans"] / args.steps,
+                       "replans_failed_per_tick": tot["replans_failed"] / args.steps,
+                       "destroyed_per_tick": tot["destroyed"] / args.steps,
+                       "graph_ms_per_tick": tot["device_ms"] / args.steps},
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(scene, st, k, threads=1, budget_s=args.cpu_budget)

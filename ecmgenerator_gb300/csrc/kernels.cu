@@ -188,16 +188,16 @@ __device__ void knn_grid(Knn<K>& s, int k, V2 p, float rnb, float r2, const V2* 
     for (int q = 0; q < K; q++) { s.key[q] = ~0ull; s.ix[q] = -1; }
     s.cnt = 0;
     s.kth = ~0ull;
-    /* agents outside the grid rectangle */
-    for (int j = cell_start[g.ncells], e = cell_start[g.ncells + 1]; j < e; j++)
-        knn_consider<K>(s, k, j, p, s_pos, s_slot, r2);
     int cx, cy;
     cell_of(g, p, &cx, &cy);
     float x0 = g.x0 + (float)cx * g.cell, y0 = g.y0 + (float)cy * g.cell;
     float m = fminf(fminf(p.x - x0, x0 + g.cell - p.x), fminf(p.y - y0, y0 + g.cell - p.y));
     m = fmaxf(m, 0.0f);
-    int rmax = (int)ceilf(rnb * g.inv) + 2;
-    for (int R = 0; R <= rmax; R++) {
+    const int rmax = (int)ceilf(rnb * g.inv) + 2;
+    /* ring R = -1 is the overflow bucket (agents outside the grid rectangle);
+       ring R >= 0 are the cells at Chebyshev distance R.  Every candidate range
+       funnels into one loop so that the insertion code exists once. */
+    for (int R = -1; R <= rmax; R++) {
         if (R >= 1) {
             /* lower bound of the distance to any agent in ring R or beyond;
                1 cm absorbs the rounding of the bucket assignment */
@@ -205,27 +205,26 @@ __device__ void knn_grid(Knn<K>& s, int k, V2 p, float rnb, float r2, const V2* 
             if (lb >= rnb) break;
             if (s.cnt == k && lb > 0.0f && lb * lb > __uint_as_float((unsigned)(s.kth >> 32))) break;
         }
-        int ylo = cy - R, yhi = cy + R;
+        const int ylo = R < 0 ? 0 : cy - R, yhi = R < 0 ? 0 : cy + R;
         for (int y = ylo; y <= yhi; y++) {
-            if (y < 0 || y >= g.gh) continue;
-            bool full = (y == ylo || y == yhi);
-            int xa = cx - R, xb = cx + R;
-            if (full) {
-                int a = max(xa, 0), b = min(xb, g.gw - 1);
-                if (a > b) continue;
-                int j0 = cell_start[y * g.gw + a], j1 = cell_start[y * g.gw + b + 1];
+            for (int side = 0; side < 2; side++) {
+                int j0 = 0, j1 = 0;
+                if (R < 0) {
+                    if (side == 0) { j0 = cell_start[g.ncells]; j1 = cell_start[g.ncells + 1]; }
+                } else if (y >= 0 && y < g.gh) {
+                    const int xa = cx - R, xb = cx + R;
+                    if (y == ylo || y == yhi) {
+                        int a = max(xa, 0), b = min(xb, g.gw - 1);
+                        if (side == 0 && a <= b) { j0 = cell_start[y * g.gw + a]; j1 = cell_start[y * g.gw + b + 1]; }
+                    } else {
+                        int x = side == 0 ? xa : xb;
+                        if (x >= 0 && x < g.gw && (side == 0 || xb != xa)) {
+                            j0 = cell_start[y * g.gw + x];
+                            j1 = cell_start[y * g.gw + x + 1];
+                        }
+                    }
+                }
                 for (int j = j0; j < j1; j++) knn_consider<K>(s, k, j, p, s_pos, s_slot, r2);
-            } else {
-                if (xa >= 0 && xa < g.gw) {
-                    int c = y * g.gw + xa;
-                    for (int j = cell_start[c], e = cell_start[c + 1]; j < e; j++)
-                        knn_consider<K>(s, k, j, p, s_pos, s_slot, r2);
-                }
-                if (xb >= 0 && xb < g.gw && xb != xa) {
-                    int c = y * g.gw + xb;
-                    for (int j = cell_start[c], e = cell_start[c + 1]; j < e; j++)
-                        knn_consider<K>(s, k, j, p, s_pos, s_slot, r2);
-                }
             }
         }
     }
@@ -236,6 +235,22 @@ struct LocalGet {
     const Con* c;
     __device__ Con operator()(int i) const { return c[i]; }
 };
+
+/* out-of-line copies keep the per-agent kernel small enough for the
+   instruction cache: each is called from a loop or a rare branch */
+__device__ __noinline__ Con agent_constraint_ni(V2 position, V2 velocity, float clr, V2 np, V2 nv, float nclr,
+                                                float tau, float dt)
+{
+    return agent_constraint(position, velocity, clr, np, nv, nclr, tau, dt);
+}
+
+__device__ __noinline__ void lp3d_local(const Con* cons, int m, int nObst, float maxSpeed, int failed, V2* v,
+                                        bool fp64)
+{
+    Con proj[kMaxCons];
+    LocalGet get{cons};
+    lp3d(get, m, nObst, maxSpeed, failed, v, proj, fp64);
+}
 
 template <int K>
 __device__ void agent_tick(const TickArgs& a, int t)
@@ -316,14 +331,14 @@ __device__ void agent_tick(const TickArgs& a, int t)
         }
     }
     const int nObst = m;
+    int nb[K];
 #pragma unroll
-    for (int q = 0; q < K; q++) {
-        if (q < nn.cnt) {
-            int j = nn.ix[q];
-            Con c = agent_constraint(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt);
-            if (m < kMaxCons) cons[m++] = c;
-            else overflow = true;
-        }
+    for (int q = 0; q < K; q++) nb[q] = nn.ix[q];
+    for (int q = 0; q < nn.cnt; q++) {
+        int j = nb[q];
+        Con c = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt);
+        if (m < kMaxCons) cons[m++] = c;
+        else overflow = true;
     }
     if (overflow) atomicOr(&a.counters[C_ERROR], ECMG_DEV_ERR_CONSTRAINTS);
 
@@ -331,8 +346,7 @@ __device__ void agent_tick(const TickArgs& a, int t)
     LocalGet get{cons};
     int failed = lp2d(get, m, pv, maxSpeed, false, &v);
     if (failed < m) {
-        Con proj[kMaxCons];
-        lp3d(get, m, nObst, maxSpeed, failed, &v, proj, a.lp3d_fp64 != 0);
+        lp3d_local(cons, m, nObst, maxSpeed, failed, &v, a.lp3d_fp64 != 0);
         atomicAdd(&a.counters[C_LP3D], 1);
     }
 
@@ -402,6 +416,9 @@ static int grid_for(int n, int block, int sms, int per_sm)
 cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int scan_blocks,
                         int block, int sms, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1)
 {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cap);
+    const unsigned evflags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
     (void)scan_blocks;
     int nb = b.grid.ncells + 1;
     cudaError_t e = cudaMemsetAsync(b.cell_count, 0, sizeof(int) * (size_t)(nb + 1), s);
@@ -411,13 +428,14 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
     e = scan(b.cell_count, (int*)b.cell_start, nb, scan_tmp, s);
     if (e != cudaSuccess) return e;
     k_scatter<<<gb, 256, 0, s>>>(b);
-    if (ev0) cudaEventRecord(ev0, s);
+    /* external event nodes when captured, so that the kernel can be timed */
+    if (ev0) cudaEventRecordWithFlags(ev0, s, evflags);
     int ga = sms * 16; /* persistent: enough warps per SM to hide latency */
     (void)block;
     if (t.k <= 8) k_agents<8><<<ga, 128, 0, s>>>(t);
     else if (t.k <= 16) k_agents<16><<<ga, 128, 0, s>>>(t);
     else k_agents<32><<<ga, 128, 0, s>>>(t);
-    if (ev1) cudaEventRecord(ev1, s);
+    if (ev1) cudaEventRecordWithFlags(ev1, s, evflags);
     return cudaGetLastError();
 }
 
