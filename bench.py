@@ -132,6 +132,21 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def reduce_over_ranks(ms, steps, world, device):
+    """Whole-job numbers of independent replicas: the slowest rank's time and
+    the sum of the agent-steps every rank processed."""
+    if world <= 1:
+        return ms, float(steps)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms, float(steps)], dtype=torch.float64, device=device)
+    tmax = t.clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(tmax[0]), float(t[1])
+
+
 def cpu_baseline(scene, st, k, threads, budget_s=12.0):
     """The C oracle (reference algorithm: kd-tree kNN, linear point location,
     ORCA, LP/LP3D) on a random sample of the same workload's agents; the
@@ -204,14 +219,7 @@ def run_ours(args):
             tot["device_ms"] += s.device_ms
         torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in ev)
-    if world > 1:
-        t = torch.tensor([ms, float(steps)], device="cuda")
-        tmax = t.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        ms_all, steps_all = float(tmax[0]), float(t[1])
-    else:
-        ms_all, steps_all = ms, float(steps)
+    ms_all, steps_all = reduce_over_ranks(ms, steps, world, "cuda")
     value = steps_all / (ms_all / 1e3)
     # e2e through the public API: update + positions/velocities back to host
     e2e_steps = 0
