@@ -110,6 +110,8 @@ def load(build_if_missing: bool = False):
         "ecmg_get_record": (C.c_int, [vp, vp, vp, vp, vp, vp, vp]),
         "ecmg_kernels_per_tick": (C.c_int, [vp]),
         "ecmg_stream": (vp, [vp]),
+        "ecmg_knn_noalloc": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
+                                       C.c_float, C.c_float, vp, vp, vp]),
         "ecmg_knn_scratch_bytes": (C.c_size_t, [C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float]),
         "ecmg_knn": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                                C.c_float, vp, vp, vp, C.c_size_t, vp]),

@@ -204,6 +204,21 @@ ecmg_status ecmg_knn(const float* dev_pos, const unsigned char* dev_active, int 
                      int* dev_out_ids, int* dev_out_count, void* dev_scratch, size_t scratch_bytes,
                      void* stream);
 
+/* ecmg_knn without caller scratch.  No counterpart in the reference: it is
+   for callers that may not allocate device memory at query time (a real-time
+   frame loop, where cudaMalloc would synchronise the device, or a plug-in
+   whose host application owns the allocator).  Scratch is a fixed device
+   array of ECMG_KNN_STATIC_SCRATCH_BYTES held by every GPU that loads the
+   library until the process exits; a query needing more
+   (ecmg_knn_scratch_bytes > the limit) returns ECMG_ERR_BOUND.  The first call
+   on a device resolves the array's device address -- make it before any
+   stream capture.  Calls share the array: overlapping calls on one device
+   race.  Allocates nothing. */
+#define ECMG_KNN_STATIC_SCRATCH_BYTES (16u * 1024u * 1024u)
+ecmg_status ecmg_knn_noalloc(const float* dev_pos, const unsigned char* dev_active, int n, int k, float radius,
+                             float min_x, float min_y, float max_x, float max_y, float cell,
+                             int* dev_out_ids, int* dev_out_count, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

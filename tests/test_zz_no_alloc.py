@@ -1,0 +1,52 @@
+"""ecmg_knn_noalloc, the kNN entry point that allocates nothing (its scratch
+is a fixed device array): for callers that may not allocate device memory
+while they run the query, e.g. a real-time frame loop or a plug-in whose host
+application owns the allocator.  Two calls in a row must give what ecmg_knn
+gives with caller-provided scratch, so the shared array's leftover contents
+from one call cannot leak into the next.  This file is collected last."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_knn_noalloc_matches_knn_twice(lib):
+    import torch
+
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(4)
+    n, k, r = 20000, 16, 3.0
+    box = (0.0, 0.0, 60.0, 60.0)
+    cell = 1.0
+    need = lib.ecmg_knn_scratch_bytes(n, *box, cell)
+    assert 0 < need <= 16 * 1024 * 1024
+    scratch = torch.empty(need, dtype=torch.uint8, device=dev)
+    for call in range(2):
+        pos = torch.from_numpy(rng.uniform(0, 60, (n, 2)).astype(np.float32)).to(dev)
+        act = torch.from_numpy((rng.uniform(0, 1, n) < (0.9 if call == 0 else 0.6)).astype(np.uint8)).to(dev)
+        ref_ids = torch.full((n, k), -5, dtype=torch.int32, device=dev)
+        ref_cnt = torch.zeros(n, dtype=torch.int32, device=dev)
+        assert lib.ecmg_knn(pos.data_ptr(), act.data_ptr(), n, k, r, *box, cell, ref_ids.data_ptr(),
+                            ref_cnt.data_ptr(), scratch.data_ptr(), need, None) == 0
+        ids = torch.full((n, k), -9, dtype=torch.int32, device=dev)
+        cnt = torch.full((n,), -9, dtype=torch.int32, device=dev)
+        assert lib.ecmg_knn_noalloc(pos.data_ptr(), act.data_ptr(), n, k, r, *box, cell, ids.data_ptr(),
+                                    cnt.data_ptr(), None) == 0
+        torch.cuda.synchronize()
+        live = act.cpu().numpy() == 1
+        assert np.array_equal(cnt.cpu().numpy(), ref_cnt.cpu().numpy())
+        assert np.array_equal(ids.cpu().numpy()[live], ref_ids.cpu().numpy()[live])
+
+
+def test_knn_noalloc_rejects_oversize(lib):
+    import torch
+
+    dev = torch.device("cuda:0")
+    n = 4_000_000  # needs more than the 16 MiB array
+    pos = torch.zeros((16, 2), dtype=torch.float32, device=dev)
+    act = torch.zeros(16, dtype=torch.uint8, device=dev)
+    out = torch.zeros(16, dtype=torch.int32, device=dev)
+    assert lib.ecmg_knn_scratch_bytes(n, 0.0, 0.0, 100.0, 100.0, 1.0) > 16 * 1024 * 1024
+    rc = lib.ecmg_knn_noalloc(pos.data_ptr(), act.data_ptr(), n, 4, 1.0, 0.0, 0.0, 100.0, 100.0, 1.0,
+                              out.data_ptr(), out.data_ptr(), None)
+    assert rc == 3  # ECMG_ERR_BOUND, before any device work
