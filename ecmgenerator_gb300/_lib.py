@@ -37,7 +37,12 @@ class TickStats(C.Structure):
     _fields_ = [("ticks", C.c_int), ("active_agents", C.c_int), ("last_index", C.c_int),
                 ("agent_steps", C.c_longlong), ("destroyed", C.c_longlong), ("replans", C.c_longlong),
                 ("replans_failed", C.c_longlong), ("lp3d", C.c_longlong), ("device_ms", C.c_float),
-                ("agent_kernel_ms", C.c_float)]
+                ("agent_kernel_ms", C.c_float), ("host_ms", C.c_float)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("block_size", C.c_int), ("agents_per_warp_grab", C.c_int), ("grid_cell_scale", C.c_float),
+                ("best_tick_ms", C.c_float), ("trials", C.c_int)]
 
 
 class Obstacles(C.Structure):
@@ -110,6 +115,14 @@ def load(build_if_missing: bool = False):
         "ecmg_get_record": (C.c_int, [vp, vp, vp, vp, vp, vp, vp]),
         "ecmg_kernels_per_tick": (C.c_int, [vp]),
         "ecmg_stream": (vp, [vp]),
+        "ecmg_create_batch": (C.c_int, [C.POINTER(Params), C.c_int, vp, C.POINTER(vp)]),
+        "ecmg_scene_count": (C.c_int, [vp]),
+        "ecmg_scene_set_obstacles": (C.c_int, [vp, C.c_int, C.POINTER(Obstacles)]),
+        "ecmg_scene_set_ecm": (C.c_int, [vp, C.c_int, C.POINTER(Ecm)]),
+        "ecmg_scene_add_agents": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, vp]),
+        "ecmg_scene_counts": (C.c_int, [vp, C.c_int, ip, ip, ip, ip]),
+        "ecmg_set_launch": (C.c_int, [vp, C.c_int, C.c_int, C.c_float]),
+        "ecmg_autotune": (C.c_int, [vp, C.c_int, C.POINTER(TuneResult)]),
         "ecmg_knn_noalloc": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
                                        C.c_float, C.c_float, vp, vp, vp]),
         "ecmg_knn_scratch_bytes": (C.c_size_t, [C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float]),

@@ -1,16 +1,26 @@
 /*
- * ctx.cu -- the C ABI of include/ecmg.h: context, device buffers, agent pool,
- * tick loop (optionally captured as a CUDA graph) and host re-planning.
+ * ctx.cu -- the simulation context of include/ecmg.h: device buffers, agent
+ * pool, one or many independent scenes, the tick loop (optionally captured as
+ * a CUDA graph), host re-planning and the launch-configuration autotuner.
+ *
+ * A context holds n_scenes independent scenes (the reference runs one
+ * Simulator per Environment).  Scene s owns the slot range
+ * [slot_base_s, slot_base_s + cap_s), its own LIFO free-slot stack
+ * (Simulator.h:66-69, 167), obstacles, ECM, planner and agent grid.  All
+ * scenes advance in one launch sequence per tick; the per-agent kernel is
+ * persistent and load-balances work across scenes of uneven size.
  */
 #include "../../include/ecmg.h"
 #include "ecmg_internal.h"
 #include "host_scene.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -42,6 +52,35 @@ struct DBuf {
     }
 };
 
+struct SceneState {
+    HostScene hs;
+    bool has_obst = false;
+    GridCSR ob_grid;  /* device candidate grid */
+    GridCSR vis_grid; /* planner visibility grid */
+    float ob_reach_needed = 0.0f;
+    bool ob_dirty = true;
+    AgentGrid grid{};
+    bool grid_ready = false;
+    int grid_agents = 0;
+    int bucket_base = 0;
+    DBuf<V2> d_ob_p, d_v_pos, d_he_left, d_he_right;
+    DBuf<int> d_ob_next, d_ob_prev, d_v_idx, d_he_target, d_ob_gstart, d_ob_gitems, d_ecm_gstart, d_ecm_gitems;
+    DBuf<unsigned char> d_ob_convex;
+    DBuf<float> d_special_y;
+    int slot_base = 0, slot_cap = 0;
+    std::vector<int> free_stack; /* back() = top */
+    int num_agents = 0;
+    int last_idx = -1; /* Simulator::m_LastEntityIdx as a global slot index */
+
+    void free_all()
+    {
+        d_ob_p.free_(); d_v_pos.free_(); d_he_left.free_(); d_he_right.free_();
+        d_ob_next.free_(); d_ob_prev.free_(); d_v_idx.free_(); d_he_target.free_();
+        d_ob_gstart.free_(); d_ob_gitems.free_(); d_ecm_gstart.free_(); d_ecm_gitems.free_();
+        d_ob_convex.free_(); d_special_y.free_();
+    }
+};
+
 }  // namespace
 
 struct ecmg_ctx {
@@ -51,46 +90,40 @@ struct ecmg_ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr, ev_a0 = nullptr, ev_a1 = nullptr;
     int sms = 1;
+    /* launch configuration (autotuned) */
+    int block = 128;
+    int tile = 32;
+    float cell_scale = 0.4f;
 
     /* host mirrors (Simulator bookkeeping, Simulator.h:164-171) */
     std::vector<unsigned char> active;
     std::vector<float> clear, speed;
     std::vector<std::vector<V2>> paths;
-    std::vector<int> free_stack; /* back() = top */
+    std::vector<int> slot_scene;
+    std::vector<std::unique_ptr<SceneState>> scenes;
     int num_agents = 0;
-    int last_idx = -1;
 
     /* device agent state */
     DBuf<V2> pos, vel, attr, pref_vel, replan_pos;
     DBuf<float> d_clear, d_speed;
     DBuf<unsigned char> d_active;
-    DBuf<int> path_off, path_len, key, rank, destroyed_list, replan_list;
+    DBuf<int> path_off, path_len, key, rank, destroyed_list, replan_list, d_slot_scene, nbr, ncnt;
     DBuf<V2> path_xy;
     size_t path_used = 0;
     /* snapshot */
     DBuf<int> s_slot;
     DBuf<V2> s_pos, s_vel;
     DBuf<float> s_clear;
-    /* grid */
-    AgentGrid grid{};
-    bool grid_ready = false;
-    int grid_agents = 0;
+    /* buckets of all scenes */
+    int total_buckets = 0;
+    bool table_dirty = true;
+    DBuf<SceneDev> d_scenes;
     DBuf<int> cell_count, cell_start, scan_tmp, counters;
-    /* scene */
-    HostScene scene;
-    bool has_obst = false;
-    GridCSR ob_grid;     /* device candidate grid */
-    GridCSR vis_grid;    /* planner visibility grid */
-    float ob_reach_needed = 0.0f;
-    bool ob_dirty = true;
-    DBuf<V2> d_ob_p, d_v_pos, d_he_left, d_he_right;
-    DBuf<int> d_ob_next, d_ob_prev, d_v_idx, d_he_target, d_ob_gstart, d_ob_gitems, d_ecm_gstart, d_ecm_gitems;
-    DBuf<unsigned char> d_ob_convex;
-    DBuf<float> d_special_y;
     /* planner */
     ecmg_plan_fn plan_fn = nullptr;
     void* plan_user = nullptr;
     PlanScratch scratch;
+    bool replan_enabled = true;
     /* recording */
     bool record = false;
     DBuf<int> rec_nbr, rec_cnt, rec_fail, rec_ncons, rec_nobst;
@@ -100,6 +133,14 @@ struct ecmg_ctx {
     /* graph */
     cudaGraphExec_t graph = nullptr;
     bool graph_dirty = true;
+    int graph_last = -2; /* last slot the captured launch sizes cover */
+
+    int global_last() const
+    {
+        int m = -1;
+        for (auto& s : scenes) m = std::max(m, s->last_idx);
+        return m;
+    }
 };
 
 static ecmg_status fail(ecmg_ctx* c, ecmg_status s, const char* fmt, ...)
@@ -164,14 +205,22 @@ static ecmg_status check_params(ecmg_ctx* c, const ecmg_params* p)
     if (!(p->mass > 0.0f)) return fail(c, ECMG_ERR_INVALID_ARG, "mass must be > 0");
     if (!std::isfinite(p->max_speed)) return fail(c, ECMG_ERR_INVALID_ARG, "max_speed must be finite");
     if (p->grid_cell < 0.0f || !std::isfinite(p->grid_cell)) return fail(c, ECMG_ERR_INVALID_ARG, "grid_cell must be >= 0");
+    if (p->block_size != 0 && p->block_size != 64 && p->block_size != 128 && p->block_size != 256)
+        return fail(c, ECMG_ERR_INVALID_ARG, "block_size must be 0, 64, 128 or 256");
     return ECMG_OK;
 }
 
-ecmg_status ecmg_create(const ecmg_params* p, int max_agents, ecmg_ctx** out)
+ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max_agents_per_scene, ecmg_ctx** out)
 {
     if (!out) return ECMG_ERR_INVALID_ARG;
     *out = nullptr;
-    if (max_agents < 1) return ECMG_ERR_INVALID_ARG;
+    if (n_scenes < 1 || !max_agents_per_scene) return ECMG_ERR_INVALID_ARG;
+    long long total = 0;
+    for (int s = 0; s < n_scenes; s++) {
+        if (max_agents_per_scene[s] < 1) return ECMG_ERR_INVALID_ARG;
+        total += max_agents_per_scene[s];
+    }
+    if (total > (1ll << 30)) return ECMG_ERR_INVALID_ARG;
     ecmg_params prm;
     if (p) prm = *p;
     else ecmg_default_params(&prm);
@@ -184,7 +233,8 @@ ecmg_status ecmg_create(const ecmg_params* p, int max_agents, ecmg_ctx** out)
     ecmg_status st = check_params(c, &prm);
     if (st != ECMG_OK) { delete c; return st; }
     c->prm = prm;
-    c->max_agents = max_agents;
+    if (prm.block_size) c->block = prm.block_size;
+    c->max_agents = (int)total;
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
@@ -194,12 +244,15 @@ ecmg_status ecmg_create(const ecmg_params* p, int max_agents, ecmg_ctx** out)
     CKC(cudaEventCreate(&c->ev_t1));
     CKC(cudaEventCreate(&c->ev_a0));
     CKC(cudaEventCreate(&c->ev_a1));
-    size_t N = (size_t)max_agents;
+    size_t N = (size_t)total;
     CKC(c->pos.alloc(N)); CKC(c->vel.alloc(N)); CKC(c->attr.alloc(N)); CKC(c->pref_vel.alloc(N));
     CKC(c->d_clear.alloc(N)); CKC(c->d_speed.alloc(N)); CKC(c->d_active.alloc(N));
     CKC(c->path_off.alloc(N)); CKC(c->path_len.alloc(N)); CKC(c->key.alloc(N)); CKC(c->rank.alloc(N));
     CKC(c->destroyed_list.alloc(N)); CKC(c->replan_list.alloc(N)); CKC(c->replan_pos.alloc(N));
     CKC(c->s_slot.alloc(N)); CKC(c->s_pos.alloc(N)); CKC(c->s_vel.alloc(N)); CKC(c->s_clear.alloc(N));
+    CKC(c->d_slot_scene.alloc(N));
+    CKC(c->nbr.alloc(N * (size_t)prm.max_neighbors));
+    CKC(c->ncnt.alloc(N));
     CKC(c->counters.alloc(kCounters));
     CKC(c->path_xy.alloc(std::max<size_t>(1024, 4 * N)));
     CKC(cudaMemset(c->pos.p, 0, sizeof(V2) * N)); CKC(cudaMemset(c->vel.p, 0, sizeof(V2) * N));
@@ -207,15 +260,35 @@ ecmg_status ecmg_create(const ecmg_params* p, int max_agents, ecmg_ctx** out)
     CKC(cudaMemset(c->d_active.p, 0, N)); CKC(cudaMemset(c->path_len.p, 0, sizeof(int) * N));
     CKC(cudaMemset(c->path_off.p, 0, sizeof(int) * N));
     CKC(cudaHostAlloc((void**)&c->h_counters, sizeof(int) * 2 * kCounters, cudaHostAllocDefault));
-#undef CKC
     c->active.assign(N, 0);
     c->clear.assign(N, 0.0f);
     c->speed.assign(N, 0.0f);
     c->paths.assign(N, {});
-    c->free_stack.reserve(N);
-    for (int i = max_agents - 1; i >= 0; i--) c->free_stack.push_back(i); /* Simulator.h:66-69 */
+    c->slot_scene.assign(N, 0);
+    int base = 0;
+    for (int s = 0; s < n_scenes; s++) {
+        auto sc = std::make_unique<SceneState>();
+        sc->slot_base = base;
+        sc->slot_cap = max_agents_per_scene[s];
+        sc->last_idx = base - 1;
+        sc->free_stack.reserve(sc->slot_cap);
+        for (int i = base + sc->slot_cap - 1; i >= base; i--) sc->free_stack.push_back(i); /* Simulator.h:66-69 */
+        for (int i = base; i < base + sc->slot_cap; i++) c->slot_scene[i] = s;
+        base += sc->slot_cap;
+        c->scenes.push_back(std::move(sc));
+    }
+    CKC(cudaMemcpy(c->d_slot_scene.p, c->slot_scene.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+#undef CKC
     *out = c;
     return ECMG_OK;
+}
+
+ecmg_status ecmg_create(const ecmg_params* p, int max_agents, ecmg_ctx** out)
+{
+    if (!out) return ECMG_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (max_agents < 1) return ECMG_ERR_INVALID_ARG;
+    return ecmg_create_batch(p, 1, &max_agents, out);
 }
 
 ecmg_status ecmg_destroy(ecmg_ctx* c)
@@ -224,20 +297,18 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->graph) cudaGraphExecDestroy(c->graph);
     DBuf<V2>* v2s[] = {&c->pos, &c->vel, &c->attr, &c->pref_vel, &c->replan_pos, &c->path_xy, &c->s_pos, &c->s_vel,
-                       &c->d_ob_p, &c->d_v_pos, &c->d_he_left, &c->d_he_right, &c->rec_vorca};
+                       &c->rec_vorca};
     for (auto* b : v2s) b->free_();
     DBuf<int>* is[] = {&c->path_off, &c->path_len, &c->key, &c->rank, &c->destroyed_list, &c->replan_list,
-                       &c->s_slot, &c->cell_count, &c->cell_start, &c->scan_tmp, &c->counters, &c->d_ob_next,
-                       &c->d_ob_prev, &c->d_v_idx, &c->d_he_target, &c->d_ob_gstart, &c->d_ob_gitems,
-                       &c->d_ecm_gstart, &c->d_ecm_gitems, &c->rec_nbr, &c->rec_cnt, &c->rec_fail,
-                       &c->rec_ncons, &c->rec_nobst};
+                       &c->d_slot_scene, &c->nbr, &c->ncnt, &c->s_slot, &c->cell_count, &c->cell_start, &c->scan_tmp, &c->counters,
+                       &c->rec_nbr, &c->rec_cnt, &c->rec_fail, &c->rec_ncons, &c->rec_nobst};
     for (auto* b : is) b->free_();
     c->d_clear.free_();
     c->d_speed.free_();
     c->s_clear.free_();
-    c->d_special_y.free_();
     c->d_active.free_();
-    c->d_ob_convex.free_();
+    c->d_scenes.free_();
+    for (auto& s : c->scenes) s->free_all();
     if (c->h_counters) cudaFreeHost(c->h_counters);
     if (c->ev_t0) cudaEventDestroy(c->ev_t0);
     if (c->ev_t1) cudaEventDestroy(c->ev_t1);
@@ -248,9 +319,9 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
     return ECMG_OK;
 }
 
-static void scene_bbox(ecmg_ctx* c)
+static void scene_bbox(SceneState& sc)
 {
-    HostScene& s = c->scene;
+    HostScene& s = sc.hs;
     float x0 = 1e30f, y0 = 1e30f, x1 = -1e30f, y1 = -1e30f;
     auto grow = [&](V2 p) {
         x0 = std::min(x0, p.x); y0 = std::min(y0, p.y);
@@ -264,9 +335,16 @@ static void scene_bbox(ecmg_ctx* c)
     s.bx0 = x0; s.by0 = y0; s.bx1 = x1; s.by1 = y1;
 }
 
-ecmg_status ecmg_set_obstacles(ecmg_ctx* c, const ecmg_obstacles* o)
+static SceneState* scene_at(ecmg_ctx* c, int scene)
 {
-    if (!c || !o) return fail(c, ECMG_ERR_INVALID_ARG, "null argument");
+    if (!c || scene < 0 || scene >= (int)c->scenes.size()) return nullptr;
+    return c->scenes[scene].get();
+}
+
+ecmg_status ecmg_scene_set_obstacles(ecmg_ctx* c, int scene, const ecmg_obstacles* o)
+{
+    SceneState* sc = scene_at(c, scene);
+    if (!sc || !o) return fail(c, ECMG_ERR_INVALID_ARG, "null argument or bad scene");
     if (o->n_obstacles < 0 || (o->n_obstacles > 0 && (!o->ring_offsets || !o->xy)))
         return fail(c, ECMG_ERR_INVALID_ARG, "bad obstacle arrays");
     for (int r = 0; r < o->n_obstacles; r++)
@@ -275,31 +353,33 @@ ecmg_status ecmg_set_obstacles(ecmg_ctx* c, const ecmg_obstacles* o)
     int nv = o->n_obstacles > 0 ? o->ring_offsets[o->n_obstacles] : 0;
     for (int i = 0; i < nv; i++)
         if (!finite2(o->xy[2 * i], o->xy[2 * i + 1])) return fail(c, ECMG_ERR_INVALID_ARG, "non-finite obstacle vertex");
-    set_obstacles(c->scene, o->n_obstacles, o->ring_offsets, o->xy);
-    scene_bbox(c);
-    HostScene& s = c->scene;
+    set_obstacles(sc->hs, o->n_obstacles, o->ring_offsets, o->xy);
+    scene_bbox(*sc);
+    HostScene& s = sc->hs;
     size_t n = std::max<size_t>(1, s.ob_p.size());
-    CK(c->d_ob_p.alloc(n)); CK(c->d_ob_next.alloc(n)); CK(c->d_ob_prev.alloc(n)); CK(c->d_ob_convex.alloc(n));
+    CK(sc->d_ob_p.alloc(n)); CK(sc->d_ob_next.alloc(n)); CK(sc->d_ob_prev.alloc(n)); CK(sc->d_ob_convex.alloc(n));
     if (nv > 0) {
-        CK(cudaMemcpy(c->d_ob_p.p, s.ob_p.data(), sizeof(V2) * nv, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(c->d_ob_next.p, s.ob_next.data(), sizeof(int) * nv, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(c->d_ob_prev.p, s.ob_prev.data(), sizeof(int) * nv, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(c->d_ob_convex.p, s.ob_convex.data(), nv, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->d_ob_p.p, s.ob_p.data(), sizeof(V2) * nv, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->d_ob_next.p, s.ob_next.data(), sizeof(int) * nv, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->d_ob_prev.p, s.ob_prev.data(), sizeof(int) * nv, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->d_ob_convex.p, s.ob_convex.data(), nv, cudaMemcpyHostToDevice));
     }
-    build_obst_grid(s, 0.0f, 4.0f, c->vis_grid);
-    c->has_obst = true;
-    c->ob_dirty = true;
-    c->grid_ready = false;
+    build_obst_grid(s, 0.0f, 4.0f, sc->vis_grid);
+    sc->has_obst = true;
+    sc->ob_dirty = true;
+    sc->grid_ready = false;
+    c->table_dirty = true;
     c->graph_dirty = true;
     return ECMG_OK;
 }
 
-ecmg_status ecmg_set_ecm(ecmg_ctx* c, const ecmg_ecm* e)
+ecmg_status ecmg_scene_set_ecm(ecmg_ctx* c, int scene, const ecmg_ecm* e)
 {
-    if (!c || !e) return fail(c, ECMG_ERR_INVALID_ARG, "null argument");
+    SceneState* sc = scene_at(c, scene);
+    if (!sc || !e) return fail(c, ECMG_ERR_INVALID_ARG, "null argument or bad scene");
     if (e->n_vertices < 0 || e->n_edges < 0) return fail(c, ECMG_ERR_INVALID_ARG, "negative sizes");
     int V = e->n_vertices, E = e->n_edges;
-    HostScene& s = c->scene;
+    HostScene& s = sc->hs;
     s.v_pos.resize(V); s.v_clear.resize(V); s.v_idx.resize(V); s.v_halfedge.resize(V);
     s.he_target.resize(2 * (size_t)E); s.he_next.resize(2 * (size_t)E);
     s.he_left.resize(2 * (size_t)E); s.he_right.resize(2 * (size_t)E);
@@ -315,37 +395,43 @@ ecmg_status ecmg_set_ecm(ecmg_ctx* c, const ecmg_ecm* e)
         if (t < 0 || t >= V) return fail(c, ECMG_ERR_INVALID_ARG, "half-edge %d targets vertex %d of %d", h, t, V);
         s.he_target[h] = t;
         s.he_next[h] = e->he_next ? e->he_next[h] : -1;
+        if (!finite2(e->he_left[2 * h], e->he_left[2 * h + 1]) || !finite2(e->he_right[2 * h], e->he_right[2 * h + 1]))
+            return fail(c, ECMG_ERR_INVALID_ARG, "non-finite closest point");
         s.he_left[h] = mk(e->he_left[2 * h], e->he_left[2 * h + 1]);
         s.he_right[h] = mk(e->he_right[2 * h], e->he_right[2 * h + 1]);
     }
     s.has_ecm = true;
-    scene_bbox(c);
+    scene_bbox(*sc);
     build_ecm_grid(s);
-    if (c->has_obst) build_obst_grid(s, 0.0f, 4.0f, c->vis_grid);
+    if (sc->has_obst) build_obst_grid(s, 0.0f, 4.0f, sc->vis_grid);
     size_t nV = std::max<size_t>(1, V), nH = std::max<size_t>(1, 2 * (size_t)E);
-    CK(c->d_v_pos.alloc(nV)); CK(c->d_v_idx.alloc(nV)); CK(c->d_he_target.alloc(nH));
-    CK(c->d_he_left.alloc(nH)); CK(c->d_he_right.alloc(nH));
-    CK(c->d_ecm_gstart.alloc(s.ecm_grid.start.size()));
-    CK(c->d_ecm_gitems.alloc(std::max<size_t>(1, s.ecm_grid.items.size())));
-    CK(c->d_special_y.alloc(std::max<size_t>(1, s.special_y.size())));
+    CK(sc->d_v_pos.alloc(nV)); CK(sc->d_v_idx.alloc(nV)); CK(sc->d_he_target.alloc(nH));
+    CK(sc->d_he_left.alloc(nH)); CK(sc->d_he_right.alloc(nH));
+    CK(sc->d_ecm_gstart.alloc(s.ecm_grid.start.size()));
+    CK(sc->d_ecm_gitems.alloc(std::max<size_t>(1, s.ecm_grid.items.size())));
+    CK(sc->d_special_y.alloc(std::max<size_t>(1, s.special_y.size())));
     if (V) {
-        CK(cudaMemcpy(c->d_v_pos.p, s.v_pos.data(), sizeof(V2) * V, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(c->d_v_idx.p, s.v_idx.data(), sizeof(int) * V, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->d_v_pos.p, s.v_pos.data(), sizeof(V2) * V, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->d_v_idx.p, s.v_idx.data(), sizeof(int) * V, cudaMemcpyHostToDevice));
     }
     if (E) {
-        CK(cudaMemcpy(c->d_he_target.p, s.he_target.data(), sizeof(int) * 2 * E, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(c->d_he_left.p, s.he_left.data(), sizeof(V2) * 2 * E, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(c->d_he_right.p, s.he_right.data(), sizeof(V2) * 2 * E, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->d_he_target.p, s.he_target.data(), sizeof(int) * 2 * E, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->d_he_left.p, s.he_left.data(), sizeof(V2) * 2 * E, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->d_he_right.p, s.he_right.data(), sizeof(V2) * 2 * E, cudaMemcpyHostToDevice));
     }
-    CK(cudaMemcpy(c->d_ecm_gstart.p, s.ecm_grid.start.data(), sizeof(int) * s.ecm_grid.start.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(sc->d_ecm_gstart.p, s.ecm_grid.start.data(), sizeof(int) * s.ecm_grid.start.size(), cudaMemcpyHostToDevice));
     if (!s.ecm_grid.items.empty())
-        CK(cudaMemcpy(c->d_ecm_gitems.p, s.ecm_grid.items.data(), sizeof(int) * s.ecm_grid.items.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(sc->d_ecm_gitems.p, s.ecm_grid.items.data(), sizeof(int) * s.ecm_grid.items.size(), cudaMemcpyHostToDevice));
     if (!s.special_y.empty())
-        CK(cudaMemcpy(c->d_special_y.p, s.special_y.data(), sizeof(float) * s.special_y.size(), cudaMemcpyHostToDevice));
-    c->grid_ready = false;
+        CK(cudaMemcpy(sc->d_special_y.p, s.special_y.data(), sizeof(float) * s.special_y.size(), cudaMemcpyHostToDevice));
+    sc->grid_ready = false;
+    c->table_dirty = true;
     c->graph_dirty = true;
     return ECMG_OK;
 }
+
+ecmg_status ecmg_set_obstacles(ecmg_ctx* c, const ecmg_obstacles* o) { return ecmg_scene_set_obstacles(c, 0, o); }
+ecmg_status ecmg_set_ecm(ecmg_ctx* c, const ecmg_ecm* e) { return ecmg_scene_set_ecm(c, 0, e); }
 
 ecmg_status ecmg_set_planner(ecmg_ctx* c, ecmg_plan_fn fn, void* user)
 {
@@ -391,23 +477,26 @@ static ecmg_status upload_path(ecmg_ctx* c, int slot)
     return ECMG_OK;
 }
 
-static void note_range(ecmg_ctx* c, float clearance, float speed)
+static void note_range(ecmg_ctx* c, SceneState* sc, float clearance, float speed)
 {
     float ms = c->prm.max_speed > 0.0f ? c->prm.max_speed : speed;
     float r = c->prm.tau_obst * ms + clearance;
-    if (r > c->ob_reach_needed) {
-        c->ob_reach_needed = r;
-        if (r > c->ob_grid.reach) c->ob_dirty = true;
+    if (r > sc->ob_reach_needed) {
+        sc->ob_reach_needed = r;
+        if (r > sc->ob_grid.reach) sc->ob_dirty = true;
     }
 }
 
-ecmg_status ecmg_add_agents(ecmg_ctx* c, int n, const float* pos, const float* clearance, const float* pref_speed,
-                            const int* path_off, const int* path_len, const float* path_xy, int* out_slots)
+ecmg_status ecmg_scene_add_agents(ecmg_ctx* c, int scene, int n, const float* pos, const float* clearance,
+                                  const float* pref_speed, const int* path_off, const int* path_len,
+                                  const float* path_xy, int* out_slots)
 {
-    if (!c) return ECMG_ERR_INVALID_ARG;
+    SceneState* sc = scene_at(c, scene);
+    if (!sc) return fail(c, ECMG_ERR_INVALID_ARG, "bad scene");
     if (n < 0 || (n > 0 && (!pos || !clearance || !pref_speed || !path_off || !path_len || !path_xy)))
         return fail(c, ECMG_ERR_INVALID_ARG, "null or negative argument");
-    if ((size_t)n > c->free_stack.size()) return fail(c, ECMG_ERR_NO_SLOT, "%d agents requested, %zu slots free", n, c->free_stack.size());
+    if ((size_t)n > sc->free_stack.size())
+        return fail(c, ECMG_ERR_NO_SLOT, "%d agents requested, %zu slots free", n, sc->free_stack.size());
     for (int i = 0; i < n; i++) {
         if (!finite2(pos[2 * i], pos[2 * i + 1]) || !std::isfinite(clearance[i]) || !std::isfinite(pref_speed[i]))
             return fail(c, ECMG_ERR_INVALID_ARG, "agent %d: non-finite input", i);
@@ -420,20 +509,20 @@ ecmg_status ecmg_add_agents(ecmg_ctx* c, int n, const float* pos, const float* c
     }
     std::vector<int> slots(n);
     for (int i = 0; i < n; i++) {
-        int idx = c->free_stack.back();
-        c->free_stack.pop_back();
+        int idx = sc->free_stack.back();
+        sc->free_stack.pop_back();
         slots[i] = idx;
+        sc->num_agents++;
         c->num_agents++;
-        c->last_idx = std::max(c->last_idx, idx);
+        sc->last_idx = std::max(sc->last_idx, idx);
         c->active[idx] = 1;
         c->clear[idx] = clearance[i];
         c->speed[idx] = pref_speed[i];
         c->paths[idx].assign((const V2*)(path_xy + 2 * (size_t)path_off[i]),
                              (const V2*)(path_xy + 2 * (size_t)(path_off[i] + path_len[i])));
-        note_range(c, clearance[i], pref_speed[i]);
+        note_range(c, sc, clearance[i], pref_speed[i]);
     }
     /* contiguous runs of slots are uploaded in one copy each */
-    std::vector<V2> zero(1, mk(0, 0));
     for (int i = 0; i < n;) {
         int j = i;
         while (j + 1 < n && slots[j + 1] == slots[j] + 1) j++;
@@ -476,11 +565,20 @@ ecmg_status ecmg_add_agents(ecmg_ctx* c, int n, const float* pos, const float* c
         }
     }
     if (out_slots) std::memcpy(out_slots, slots.data(), sizeof(int) * n);
-    if (c->grid_agents == 0 || c->num_agents > 2 * c->grid_agents) c->grid_ready = false;
+    if (sc->grid_agents == 0 || sc->num_agents > 2 * sc->grid_agents) {
+        sc->grid_ready = false;
+        c->table_dirty = true;
+    }
     return ECMG_OK;
 }
 
-static ecmg_status plan(ecmg_ctx* c, V2 s, V2 g, float clr, std::vector<V2>& out)
+ecmg_status ecmg_add_agents(ecmg_ctx* c, int n, const float* pos, const float* clearance, const float* pref_speed,
+                            const int* path_off, const int* path_len, const float* path_xy, int* out_slots)
+{
+    return ecmg_scene_add_agents(c, 0, n, pos, clearance, pref_speed, path_off, path_len, path_xy, out_slots);
+}
+
+static ecmg_status plan(ecmg_ctx* c, SceneState* sc, V2 s, V2 g, float clr, std::vector<V2>& out, PlanScratch& scr)
 {
     out.clear();
     if (c->plan_fn) {
@@ -491,8 +589,8 @@ static ecmg_status plan(ecmg_ctx* c, V2 s, V2 g, float clr, std::vector<V2>& out
         for (int i = 0; i < n; i++) out.push_back(mk(buf[2 * i], buf[2 * i + 1]));
         return n > 0 ? ECMG_OK : ECMG_ERR_NO_PATH;
     }
-    if (!c->scene.has_ecm) return ECMG_ERR_STATE;
-    return plan_path(c->scene, c->vis_grid, s, g, clr, out, c->scratch) ? ECMG_OK : ECMG_ERR_NO_PATH;
+    if (!sc->hs.has_ecm) return ECMG_ERR_STATE;
+    return plan_path(sc->hs, sc->vis_grid, s, g, clr, out, scr) ? ECMG_OK : ECMG_ERR_NO_PATH;
 }
 
 ecmg_status ecmg_find_path(ecmg_ctx* c, float sx, float sy, float gx, float gy, float clearance, float* out_xy,
@@ -500,114 +598,24 @@ ecmg_status ecmg_find_path(ecmg_ctx* c, float sx, float sy, float gx, float gy, 
 {
     if (!c || !out_n || (cap > 0 && !out_xy)) return ECMG_ERR_INVALID_ARG;
     std::vector<V2> p;
-    ecmg_status st = plan(c, mk(sx, sy), mk(gx, gy), clearance, p);
+    ecmg_status st = plan(c, c->scenes[0].get(), mk(sx, sy), mk(gx, gy), clearance, p, c->scratch);
     *out_n = st == ECMG_OK ? (int)p.size() : -1;
     for (int i = 0; i < (int)p.size() && i < cap; i++) { out_xy[2 * i] = p[i].x; out_xy[2 * i + 1] = p[i].y; }
     return st;
 }
 
-struct ecmg_planner {
-    HostScene scene;
-    GridCSR vis;
-};
-
-ecmg_status ecmg_planner_create(const ecmg_obstacles* o, const ecmg_ecm* e, ecmg_planner** out)
-{
-    if (!o || !e || !out) return ECMG_ERR_INVALID_ARG;
-    *out = nullptr;
-    if (o->n_obstacles < 0 || e->n_vertices < 0 || e->n_edges < 0) return ECMG_ERR_INVALID_ARG;
-    for (int r = 0; r < o->n_obstacles; r++)
-        if (o->ring_offsets[r + 1] - o->ring_offsets[r] < 2) return ECMG_ERR_INVALID_ARG;
-    for (int h = 0; h < 2 * e->n_edges; h++)
-        if (e->he_target[h] < 0 || e->he_target[h] >= e->n_vertices) return ECMG_ERR_INVALID_ARG;
-    ecmg_planner* p = new ecmg_planner();
-    HostScene& s = p->scene;
-    set_obstacles(s, o->n_obstacles, o->ring_offsets, o->xy);
-    int V = e->n_vertices, E = e->n_edges;
-    s.v_pos.resize(V); s.v_clear.resize(V); s.v_idx.resize(V); s.v_halfedge.resize(V);
-    s.he_target.assign(e->he_target, e->he_target + 2 * (size_t)E);
-    s.he_next.assign(e->he_next, e->he_next + 2 * (size_t)E);
-    s.he_left.resize(2 * (size_t)E); s.he_right.resize(2 * (size_t)E);
-    for (int i = 0; i < V; i++) {
-        s.v_pos[i] = mk(e->v_pos[2 * i], e->v_pos[2 * i + 1]);
-        s.v_clear[i] = e->v_clear[i];
-        s.v_idx[i] = e->v_idx ? e->v_idx[i] : i;
-        s.v_halfedge[i] = e->v_halfedge[i];
-    }
-    for (int h = 0; h < 2 * E; h++) {
-        s.he_left[h] = mk(e->he_left[2 * h], e->he_left[2 * h + 1]);
-        s.he_right[h] = mk(e->he_right[2 * h], e->he_right[2 * h + 1]);
-    }
-    s.has_ecm = true;
-    float x0 = 1e30f, y0 = 1e30f, x1 = -1e30f, y1 = -1e30f;
-    auto grow = [&](V2 q) { x0 = std::min(x0, q.x); y0 = std::min(y0, q.y); x1 = std::max(x1, q.x); y1 = std::max(y1, q.y); };
-    for (auto& q : s.ob_p) grow(q);
-    for (auto& q : s.v_pos) grow(q);
-    for (auto& q : s.he_left) grow(q);
-    for (auto& q : s.he_right) grow(q);
-    if (x0 > x1) { x0 = y0 = 0; x1 = y1 = 1; }
-    s.bx0 = x0; s.by0 = y0; s.bx1 = x1; s.by1 = y1;
-    build_ecm_grid(s);
-    build_obst_grid(s, 0.0f, 4.0f, p->vis);
-    *out = p;
-    return ECMG_OK;
-}
-
-ecmg_status ecmg_planner_destroy(ecmg_planner* p)
-{
-    if (!p) return ECMG_ERR_INVALID_ARG;
-    delete p;
-    return ECMG_OK;
-}
-
-ecmg_status ecmg_planner_find_paths(ecmg_planner* pl, int n, const float* starts, const float* goals,
-                                    const float* clearances, int threads, int cap, float* out_xy, int* out_n)
-{
-    if (!pl || n < 0 || cap < 1 || (n > 0 && (!starts || !goals || !clearances || !out_xy || !out_n)))
-        return ECMG_ERR_INVALID_ARG;
-    if (threads < 1) threads = (int)std::max(1u, std::thread::hardware_concurrency());
-    threads = std::min(threads, std::max(1, n));
-    auto work = [&](int t) {
-        PlanScratch scr;
-        std::vector<V2> p;
-        for (int i = t; i < n; i += threads) {
-            bool ok = plan_path(pl->scene, pl->vis, mk(starts[2 * i], starts[2 * i + 1]),
-                                mk(goals[2 * i], goals[2 * i + 1]), clearances[i], p, scr);
-            if (!ok) { out_n[i] = -1; continue; }
-            if ((int)p.size() > cap) { out_n[i] = -2; continue; }
-            out_n[i] = (int)p.size();
-            for (size_t q = 0; q < p.size(); q++) {
-                out_xy[2 * ((size_t)i * cap + q)] = p[q].x;
-                out_xy[2 * ((size_t)i * cap + q) + 1] = p[q].y;
-            }
-        }
-    };
-    std::vector<std::thread> th;
-    for (int t = 1; t < threads; t++) th.emplace_back(work, t);
-    work(0);
-    for (auto& x : th) x.join();
-    return ECMG_OK;
-}
-
-ecmg_status ecmg_planner_locate(ecmg_planner* pl, int n, const float* xy, int* out)
-{
-    if (!pl || n < 0 || (n > 0 && (!xy || !out))) return ECMG_ERR_INVALID_ARG;
-    EcmView ev = pl->scene.ecm_view();
-    for (int i = 0; i < n; i++) out[i] = point_location(ev, mk(xy[2 * i], xy[2 * i + 1]));
-    return ECMG_OK;
-}
-
 /* Simulator::ValidSpawnLocation (Simulator.cpp:295-311) on the device state */
-static ecmg_status valid_spawn(ecmg_ctx* c, V2 loc, float clearance, bool* ok)
+static ecmg_status valid_spawn(ecmg_ctx* c, SceneState* sc, V2 loc, float clearance, bool* ok)
 {
     *ok = true;
-    if (c->last_idx < 0) return ECMG_OK;
-    std::vector<V2> p((size_t)c->last_idx + 1);
+    if (sc->last_idx < sc->slot_base) return ECMG_OK;
+    int b = sc->slot_base, n = sc->last_idx - b + 1;
+    std::vector<V2> p((size_t)n);
     CK(cudaStreamSynchronize(c->stream));
-    CK(cudaMemcpy(p.data(), c->pos.p, sizeof(V2) * p.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(p.data(), c->pos.p + b, sizeof(V2) * p.size(), cudaMemcpyDeviceToHost));
     float cs = clearance * clearance;
-    for (int i = 0; i <= c->last_idx; i++) {
-        if (!c->active[i]) continue;
+    for (int i = 0; i < n; i++) {
+        if (!c->active[b + i]) continue;
         float dx = loc.x - p[i].x, dy = loc.y - p[i].y;
         if (dx * dx + dy * dy < cs) { *ok = false; return ECMG_OK; }
     }
@@ -619,30 +627,33 @@ ecmg_status ecmg_spawn_agent(ecmg_ctx* c, float sx, float sy, float gx, float gy
 {
     if (!c || !out_slot) return ECMG_ERR_INVALID_ARG;
     *out_slot = -1;
+    SceneState* sc = c->scenes[0].get();
     if (!finite2(sx, sy) || !finite2(gx, gy) || !std::isfinite(clearance) || !std::isfinite(pref_speed))
         return fail(c, ECMG_ERR_INVALID_ARG, "non-finite spawn argument");
-    if (c->free_stack.empty()) return fail(c, ECMG_ERR_NO_SLOT, "no free slot");
+    if (sc->free_stack.empty()) return fail(c, ECMG_ERR_NO_SLOT, "no free slot");
     bool ok;
-    ecmg_status st = valid_spawn(c, mk(sx, sy), clearance, &ok);
+    ecmg_status st = valid_spawn(c, sc, mk(sx, sy), clearance, &ok);
     if (st != ECMG_OK) return st;
     if (!ok) return fail(c, ECMG_ERR_INVALID_SPAWN, "spawn location occupied");
     std::vector<V2> p;
-    st = plan(c, mk(sx, sy), mk(gx, gy), clearance, p);
+    st = plan(c, sc, mk(sx, sy), mk(gx, gy), clearance, p, c->scratch);
     if (st != ECMG_OK || p.empty()) return fail(c, ECMG_ERR_NO_PATH, "no path from (%g,%g) to (%g,%g)", sx, sy, gx, gy);
     std::vector<float> xy(2 * p.size());
     for (size_t i = 0; i < p.size(); i++) { xy[2 * i] = p[i].x; xy[2 * i + 1] = p[i].y; }
     int off = 0, len = (int)p.size();
     float pos[2] = {sx, sy};
-    return ecmg_add_agents(c, 1, pos, &clearance, &pref_speed, &off, &len, xy.data(), out_slot);
+    return ecmg_scene_add_agents(c, 0, 1, pos, &clearance, &pref_speed, &off, &len, xy.data(), out_slot);
 }
 
 ecmg_status ecmg_destroy_agent(ecmg_ctx* c, int slot)
 {
     if (!c || slot < 0 || slot >= c->max_agents) return fail(c, ECMG_ERR_INVALID_ARG, "bad slot");
     if (!c->active[slot]) return fail(c, ECMG_ERR_INVALID_ARG, "slot %d is not active", slot);
+    SceneState* sc = c->scenes[c->slot_scene[slot]].get();
+    sc->num_agents--;
     c->num_agents--;
     c->active[slot] = 0;
-    c->free_stack.push_back(slot);
+    sc->free_stack.push_back(slot);
     unsigned char z = 0;
     CK(cudaMemcpy(c->d_active.p + slot, &z, 1, cudaMemcpyHostToDevice));
     return ECMG_OK;
@@ -651,13 +662,18 @@ ecmg_status ecmg_destroy_agent(ecmg_ctx* c, int slot)
 ecmg_status ecmg_reset(ecmg_ctx* c)
 {
     if (!c) return ECMG_ERR_INVALID_ARG;
-    for (int i = 0; i <= c->last_idx; i++) /* Simulator.cpp:327-332 */
-        if (c->active[i]) {
-            c->num_agents--;
-            c->active[i] = 0;
-            c->free_stack.push_back(i);
-        }
-    if (c->last_idx >= 0) CK(cudaMemset(c->d_active.p, 0, (size_t)c->last_idx + 1));
+    for (auto& scp : c->scenes) { /* Simulator.cpp:327-332 */
+        SceneState* sc = scp.get();
+        for (int i = sc->slot_base; i <= sc->last_idx; i++)
+            if (c->active[i]) {
+                sc->num_agents--;
+                c->num_agents--;
+                c->active[i] = 0;
+                sc->free_stack.push_back(i);
+            }
+    }
+    int last = c->global_last();
+    if (last >= 0) CK(cudaMemset(c->d_active.p, 0, (size_t)last + 1));
     return ECMG_OK;
 }
 
@@ -682,42 +698,90 @@ ecmg_status ecmg_get_path(ecmg_ctx* c, int slot, float* out_xy, int cap, int* ou
 /* ---------------------------------------------------------------------- */
 static ecmg_status ensure_grids(ecmg_ctx* c)
 {
-    HostScene& s = c->scene;
-    if (c->ob_dirty) {
-        float reach = std::max(c->ob_reach_needed, 1.0f) * 1.05f + 0.1f;
-        build_obst_grid(s, reach, std::max(2.0f, std::min(reach, 8.0f)), c->ob_grid);
-        CK(c->d_ob_gstart.alloc(c->ob_grid.start.size()));
-        CK(c->d_ob_gitems.alloc(std::max<size_t>(1, c->ob_grid.items.size())));
-        CK(cudaMemcpy(c->d_ob_gstart.p, c->ob_grid.start.data(), sizeof(int) * c->ob_grid.start.size(), cudaMemcpyHostToDevice));
-        if (!c->ob_grid.items.empty())
-            CK(cudaMemcpy(c->d_ob_gitems.p, c->ob_grid.items.data(), sizeof(int) * c->ob_grid.items.size(), cudaMemcpyHostToDevice));
-        c->ob_dirty = false;
-        c->graph_dirty = true;
-    }
-    if (!c->grid_ready) {
-        float w = std::max(1.0f, s.bx1 - s.bx0), h = std::max(1.0f, s.by1 - s.by0);
-        float cell = c->prm.grid_cell;
-        if (!(cell > 0.0f)) {
-            float dens = (float)std::max(1, c->num_agents) / (w * h);
-            cell = std::sqrt((float)c->prm.max_neighbors / dens) * 0.6f;
-            cell = std::min(std::max(cell, 0.5f), std::max(0.5f, c->prm.neighbor_dist));
+    for (auto& scp : c->scenes) {
+        SceneState* sc = scp.get();
+        HostScene& s = sc->hs;
+        if (sc->ob_dirty) {
+            float reach = std::max(sc->ob_reach_needed, 1.0f) * 1.05f + 0.1f;
+            build_obst_grid(s, reach, std::max(2.0f, std::min(reach, 8.0f)), sc->ob_grid);
+            CK(sc->d_ob_gstart.alloc(sc->ob_grid.start.size()));
+            CK(sc->d_ob_gitems.alloc(std::max<size_t>(1, sc->ob_grid.items.size())));
+            CK(cudaMemcpy(sc->d_ob_gstart.p, sc->ob_grid.start.data(), sizeof(int) * sc->ob_grid.start.size(),
+                          cudaMemcpyHostToDevice));
+            if (!sc->ob_grid.items.empty())
+                CK(cudaMemcpy(sc->d_ob_gitems.p, sc->ob_grid.items.data(), sizeof(int) * sc->ob_grid.items.size(),
+                              cudaMemcpyHostToDevice));
+            sc->ob_dirty = false;
+            c->table_dirty = true;
         }
-        /* at most 32M cells */
-        while ((double)(w / cell + 3) * (double)(h / cell + 3) > 32.0e6) cell *= 1.5f;
-        AgentGrid g;
-        g.cell = cell;
-        g.inv = 1.0f / cell;
-        g.x0 = s.bx0 - cell;
-        g.y0 = s.by0 - cell;
-        g.gw = (int)std::ceil(w / cell) + 3;
-        g.gh = (int)std::ceil(h / cell) + 3;
-        g.ncells = g.gw * g.gh;
-        c->grid = g;
-        CK(c->cell_count.alloc((size_t)g.ncells + 2 + kCounters));
-        CK(c->cell_start.alloc((size_t)g.ncells + 2));
-        CK(c->scan_tmp.alloc((size_t)scan_tmp_ints(g.ncells + 1)));
-        c->grid_ready = true;
-        c->grid_agents = std::max(1, c->num_agents);
+        if (!sc->grid_ready) {
+            float w = std::max(1.0f, s.bx1 - s.bx0), h = std::max(1.0f, s.by1 - s.by0);
+            float cell = c->prm.grid_cell;
+            if (!(cell > 0.0f)) {
+                float dens = (float)std::max(1, sc->num_agents) / (w * h);
+                cell = std::sqrt((float)c->prm.max_neighbors / dens) * c->cell_scale;
+                cell = std::min(std::max(cell, 0.3f), std::max(0.3f, c->prm.neighbor_dist));
+            }
+            while ((double)(w / cell + 3) * (double)(h / cell + 3) > 32.0e6) cell *= 1.5f; /* <= 32M cells */
+            AgentGrid g;
+            g.cell = cell;
+            g.inv = 1.0f / cell;
+            g.x0 = s.bx0 - cell;
+            g.y0 = s.by0 - cell;
+            g.gw = (int)std::ceil(w / cell) + 3;
+            g.gh = (int)std::ceil(h / cell) + 3;
+            g.ncells = g.gw * g.gh;
+            sc->grid = g;
+            sc->grid_ready = true;
+            sc->grid_agents = std::max(1, sc->num_agents);
+            c->table_dirty = true;
+        }
+    }
+    if (c->table_dirty) {
+        int base = 0;
+        std::vector<SceneDev> tab(c->scenes.size());
+        for (size_t i = 0; i < c->scenes.size(); i++) {
+            SceneState* sc = c->scenes[i].get();
+            HostScene& s = sc->hs;
+            sc->bucket_base = base;
+            base += sc->grid.ncells + 1;
+            SceneDev& d = tab[i];
+            d = SceneDev{};
+            d.grid = sc->grid;
+            d.bucket_base = sc->bucket_base;
+            ObstView& o = d.ob;
+            o.p = sc->d_ob_p.p;
+            o.next = sc->d_ob_next.p;
+            o.prev = sc->d_ob_prev.p;
+            o.convex = sc->d_ob_convex.p;
+            o.n_verts = sc->has_obst ? (int)s.ob_p.size() : 0;
+            if (sc->ob_grid.gw > 0) {
+                o.gx0 = sc->ob_grid.x0; o.gy0 = sc->ob_grid.y0; o.ginv = sc->ob_grid.inv;
+                o.gw = sc->ob_grid.gw; o.gh = sc->ob_grid.gh; o.reach = sc->ob_grid.reach;
+                o.g_start = sc->d_ob_gstart.p;
+                o.g_items = sc->d_ob_gitems.p;
+            }
+            EcmView& e = d.ecm;
+            e.v_pos = sc->d_v_pos.p;
+            e.v_idx = sc->d_v_idx.p;
+            e.he_target = sc->d_he_target.p;
+            e.he_left = sc->d_he_left.p;
+            e.he_right = sc->d_he_right.p;
+            e.n_edges = (int)(s.he_target.size() / 2);
+            e.gx0 = s.ecm_grid.x0; e.gy0 = s.ecm_grid.y0; e.ginv = s.ecm_grid.inv;
+            e.gw = s.ecm_grid.gw; e.gh = s.ecm_grid.gh;
+            e.g_start = sc->d_ecm_gstart.p;
+            e.g_items = sc->d_ecm_gitems.p;
+            e.special_y = sc->d_special_y.p;
+            e.n_special = (int)s.special_y.size();
+        }
+        c->total_buckets = base;
+        CK(c->d_scenes.alloc(tab.size()));
+        CK(cudaMemcpy(c->d_scenes.p, tab.data(), sizeof(SceneDev) * tab.size(), cudaMemcpyHostToDevice));
+        CK(c->cell_count.alloc((size_t)base + 2));
+        CK(c->cell_start.alloc((size_t)base + 2));
+        CK(c->scan_tmp.alloc((size_t)scan_tmp_ints(base)));
+        c->table_dirty = false;
         c->graph_dirty = true;
     }
     if (c->record) {
@@ -745,7 +809,9 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t)
     b.s_clear = c->s_clear.p;
     b.cell_start = c->cell_start.p;
     b.counters = c->counters.p;
-    b.grid = c->grid;
+    b.scenes = c->d_scenes.p;
+    b.slot_scene = c->scenes.size() > 1 ? c->d_slot_scene.p : nullptr;
+    b.total_buckets = c->total_buckets;
 
     t = TickArgs{};
     t.pos = c->pos.p;
@@ -763,35 +829,11 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t)
     t.s_vel = c->s_vel.p;
     t.s_clear = c->s_clear.p;
     t.cell_start = c->cell_start.p;
-    t.grid = c->grid;
-    HostScene& s = c->scene;
-    ObstView o{};
-    o.p = c->d_ob_p.p;
-    o.next = c->d_ob_next.p;
-    o.prev = c->d_ob_prev.p;
-    o.convex = c->d_ob_convex.p;
-    o.n_verts = c->has_obst ? (int)s.ob_p.size() : 0;
-    if (c->ob_grid.gw > 0) {
-        o.gx0 = c->ob_grid.x0; o.gy0 = c->ob_grid.y0; o.ginv = c->ob_grid.inv;
-        o.gw = c->ob_grid.gw; o.gh = c->ob_grid.gh; o.reach = c->ob_grid.reach;
-        o.g_start = c->d_ob_gstart.p;
-        o.g_items = c->d_ob_gitems.p;
-    }
-    t.ob = o;
-    EcmView e{};
-    e.v_pos = c->d_v_pos.p;
-    e.v_idx = c->d_v_idx.p;
-    e.he_target = c->d_he_target.p;
-    e.he_left = c->d_he_left.p;
-    e.he_right = c->d_he_right.p;
-    e.n_edges = (int)(s.he_target.size() / 2);
-    e.gx0 = s.ecm_grid.x0; e.gy0 = s.ecm_grid.y0; e.ginv = s.ecm_grid.inv;
-    e.gw = s.ecm_grid.gw; e.gh = s.ecm_grid.gh;
-    e.g_start = c->d_ecm_gstart.p;
-    e.g_items = c->d_ecm_gitems.p;
-    e.special_y = c->d_special_y.p;
-    e.n_special = (int)s.special_y.size();
-    t.ecm = e;
+    t.nbr = c->nbr.p;
+    t.ncnt = c->ncnt.p;
+    t.scenes = c->d_scenes.p;
+    t.slot_scene = b.slot_scene;
+    t.tile = c->tile;
     const ecmg_params& p = c->prm;
     t.dt = p.dt;
     t.tau_a = p.tau_agent;
@@ -820,7 +862,7 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t)
 }
 
 /* the device work of one tick: counters in, kernels, counters out */
-static cudaError_t enqueue_tick(ecmg_ctx* c)
+static cudaError_t enqueue_tick(ecmg_ctx* c, int launch_slots)
 {
     BinArgs b;
     TickArgs t;
@@ -828,7 +870,7 @@ static cudaError_t enqueue_tick(ecmg_ctx* c)
     cudaGetLastError(); /* launch errors below must not be confused with older ones */
     cudaError_t e = cudaMemcpyAsync(c->counters.p, c->h_counters, sizeof(int) * kCounters, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return e;
-    e = launch_tick(b, t, c->max_agents, c->scan_tmp.p, 0, c->prm.block_size, c->sms, c->stream, c->ev_a0, c->ev_a1);
+    e = launch_tick(b, t, launch_slots, c->scan_tmp.p, c->block, c->sms, c->stream, c->ev_a0, c->ev_a1);
     if (e != cudaSuccess) return e;
     return cudaMemcpyAsync(c->h_counters + kCounters, c->counters.p, sizeof(int) * kCounters, cudaMemcpyDeviceToHost,
                            c->stream);
@@ -839,37 +881,39 @@ void* ecmg_stream(const ecmg_ctx* c) { return c ? (void*)c->stream : nullptr; }
 int ecmg_kernels_per_tick(const ecmg_ctx* c)
 {
     (void)c;
-    return 6; /* k_bin, k_scan_local, k_scan_top, k_scan_add, k_scatter, k_agents */
+    return 7; /* k_bin, k_scan_local, k_scan_top, k_scan_add, k_scatter, k_neighbors, k_agents */
 }
 
-ecmg_status ecmg_tick(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
+static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
 {
-    if (!c || n_ticks < 0) return ECMG_ERR_INVALID_ARG;
-    if (!c->scene.has_ecm) return fail(c, ECMG_ERR_STATE, "ecmg_set_ecm must be called before ecmg_tick");
+    for (auto& scp : c->scenes)
+        if (!scp->hs.has_ecm) return fail(c, ECMG_ERR_STATE, "every scene needs an ECM before ecmg_tick");
     ecmg_tick_stats st{};
     ecmg_status result = ECMG_OK;
     for (int tk = 0; tk < n_ticks; tk++) {
-        /* UpdateMaxAgentIndex (Simulator.cpp:481-492) */
-        int empty = 0;
-        for (int i = c->last_idx; i >= 0; i--) {
-            if (c->active[i]) break;
-            empty++;
+        auto hs = std::chrono::steady_clock::now();
+        /* UpdateMaxAgentIndex (Simulator.cpp:481-492), per scene */
+        for (auto& scp : c->scenes) {
+            SceneState* sc = scp.get();
+            while (sc->last_idx >= sc->slot_base && !c->active[sc->last_idx]) sc->last_idx--;
         }
-        c->last_idx -= empty;
         st.ticks++;
-        if (c->last_idx < 0) continue;
+        int last = c->global_last();
+        if (last < 0) continue;
         ecmg_status gs = ensure_grids(c);
         if (gs != ECMG_OK) return gs;
         std::memset(c->h_counters, 0, sizeof(int) * kCounters);
-        c->h_counters[C_LAST] = c->last_idx;
+        c->h_counters[C_LAST] = last;
+        st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - hs).count();
         CK(cudaEventRecord(c->ev_t0, c->stream));
         if (c->prm.use_graph) {
+            /* the graph bakes in launch sizes covering slots [0, max_agents) */
             if (c->graph_dirty || !c->graph) {
                 if (c->graph) cudaGraphExecDestroy(c->graph);
                 c->graph = nullptr;
                 cudaGraph_t g;
                 CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-                cudaError_t e = enqueue_tick(c);
+                cudaError_t e = enqueue_tick(c, c->max_agents);
                 cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
                 if (e != cudaSuccess) return fail(c, ECMG_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
                 if (e2 != cudaSuccess) return fail(c, ECMG_ERR_CUDA, "end capture: %s", cudaGetErrorString(e2));
@@ -879,10 +923,11 @@ ecmg_status ecmg_tick(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             }
             CK(cudaGraphLaunch(c->graph, c->stream));
         } else {
-            CK(enqueue_tick(c));
+            CK(enqueue_tick(c, last + 1));
         }
         CK(cudaEventRecord(c->ev_t1, c->stream));
         CK(cudaStreamSynchronize(c->stream));
+        auto h0 = std::chrono::steady_clock::now();
         float ms = 0, ams = 0;
         if (cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1) != cudaSuccess) ms = 0;
         if (cudaEventElapsedTime(&ams, c->ev_a0, c->ev_a1) != cudaSuccess) ams = 0;
@@ -897,7 +942,7 @@ ecmg_status ecmg_tick(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         st.replans += nr;
         if (out[C_ERROR]) {
             result = fail(c, ECMG_ERR_BOUND, "device bound exceeded (flags 0x%x): %s", out[C_ERROR],
-                          (out[C_ERROR] & ECMG_DEV_ERR_CONSTRAINTS) ? "more than 64 half-planes for one agent"
+                          (out[C_ERROR] & ECMG_DEV_ERR_CONSTRAINTS) ? "more than 24 obstacle half-planes for one agent"
                                                                     : "event list overflow");
         }
         if (nd > 0) {
@@ -905,12 +950,14 @@ ecmg_status ecmg_tick(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             CK(cudaMemcpy(d.data(), c->destroyed_list.p, sizeof(int) * d.size(), cudaMemcpyDeviceToHost));
             std::sort(d.begin(), d.end()); /* DestroyAgent order: slot order of the loop */
             for (int s : d) {
+                SceneState* sc = c->scenes[c->slot_scene[s]].get();
+                sc->num_agents--;
                 c->num_agents--;
                 c->active[s] = 0;
-                c->free_stack.push_back(s);
+                sc->free_stack.push_back(s);
             }
         }
-        if (nr > 0) {
+        if (nr > 0 && c->replan_enabled) {
             int m = std::min(nr, c->max_agents);
             std::vector<int> r(m);
             std::vector<V2> rp(m);
@@ -919,27 +966,159 @@ ecmg_status ecmg_tick(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             std::vector<int> order(m);
             for (int i = 0; i < m; i++) order[i] = i;
             std::sort(order.begin(), order.end(), [&](int a, int b) { return r[a] < r[b]; });
-            std::vector<V2> p;
-            for (int q : order) {
-                int s = r[q];
-                V2 goal = c->paths[s].back();
-                /* Simulator::UpdatePath (Simulator.cpp:97-124) from the tick-start position.
-                   When no path is found the agent keeps its previous path (the
-                   reference would keep an empty one and index path.x[-1]). */
-                if (plan(c, rp[q], goal, c->clear[s], p) == ECMG_OK && !p.empty()) {
-                    c->paths[s] = p;
-                    ecmg_status ps = upload_path(c, s);
+            /* Simulator::UpdatePath (Simulator.cpp:97-124) from the tick-start
+               position, served in slot order.  When no path is found the agent
+               keeps its previous path (the reference would keep an empty one and
+               index path.x[-1]).  The built-in planner is re-entrant, so large
+               batches are planned on several host threads. */
+            std::vector<std::vector<V2>> res(m);
+            std::vector<char> ok(m, 0);
+            auto serve = [&](int t, int nt) {
+                PlanScratch scr;
+                for (int i = t; i < m; i += nt) {
+                    int q = order[i], sl = r[q];
+                    SceneState* sc = c->scenes[c->slot_scene[sl]].get();
+                    V2 goal = c->paths[sl].back();
+                    ok[i] = plan(c, sc, rp[q], goal, c->clear[sl], res[i], scr) == ECMG_OK && !res[i].empty();
+                }
+            };
+            int nt = c->plan_fn ? 1 : std::min(16, std::max(1, m / 32));
+            nt = std::min<int>(nt, (int)std::max(1u, std::thread::hardware_concurrency()));
+            if (nt > 1) {
+                std::vector<std::thread> th;
+                for (int t = 1; t < nt; t++) th.emplace_back(serve, t, nt);
+                serve(0, nt);
+                for (auto& x : th) x.join();
+            } else {
+                serve(0, 1);
+            }
+            for (int i = 0; i < m; i++) {
+                int sl = r[order[i]];
+                if (ok[i]) {
+                    c->paths[sl] = res[i];
+                    ecmg_status ps = upload_path(c, sl);
                     if (ps != ECMG_OK) return ps;
                 } else {
                     st.replans_failed++;
                 }
             }
         }
+        st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - h0).count();
     }
     st.active_agents = c->num_agents;
-    st.last_index = c->last_idx;
+    st.last_index = c->global_last();
     if (stats) *stats = st;
     return result;
+}
+
+ecmg_status ecmg_tick(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
+{
+    if (!c || n_ticks < 0) return ECMG_ERR_INVALID_ARG;
+    return run_ticks(c, n_ticks, stats);
+}
+
+/* ---------------------------------------------------------------------- */
+/* Autotuner: times whole ticks for each launch configuration on copies of
+   the current state (the state is restored after every trial; trial ticks
+   serve no re-plans) and keeps the fastest. */
+ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* out)
+{
+    if (!c || ticks_per_trial < 1) return ECMG_ERR_INVALID_ARG;
+    if (c->num_agents == 0) return fail(c, ECMG_ERR_STATE, "autotune needs agents");
+    size_t N = (size_t)c->max_agents;
+    DBuf<V2> sp, sv, sa, spv;
+    DBuf<unsigned char> sact;
+    CK(sp.alloc(N)); CK(sv.alloc(N)); CK(sa.alloc(N)); CK(spv.alloc(N)); CK(sact.alloc(N));
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(sp.p, c->pos.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(sv.p, c->vel.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(sa.p, c->attr.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(spv.p, c->pref_vel.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(sact.p, c->d_active.p, N, cudaMemcpyDeviceToDevice));
+    std::vector<unsigned char> act = c->active;
+    std::vector<std::vector<int>> stacks;
+    std::vector<int> nums, lasts;
+    for (auto& s : c->scenes) { stacks.push_back(s->free_stack); nums.push_back(s->num_agents); lasts.push_back(s->last_idx); }
+    int num = c->num_agents;
+    auto restore = [&]() -> ecmg_status {
+        CK(cudaMemcpy(c->pos.p, sp.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
+        CK(cudaMemcpy(c->vel.p, sv.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
+        CK(cudaMemcpy(c->attr.p, sa.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
+        CK(cudaMemcpy(c->pref_vel.p, spv.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
+        CK(cudaMemcpy(c->d_active.p, sact.p, N, cudaMemcpyDeviceToDevice));
+        c->active = act;
+        for (size_t i = 0; i < c->scenes.size(); i++) {
+            c->scenes[i]->free_stack = stacks[i];
+            c->scenes[i]->num_agents = nums[i];
+            c->scenes[i]->last_idx = lasts[i];
+        }
+        c->num_agents = num;
+        return ECMG_OK;
+    };
+    const int blocks[] = {64, 128, 256};
+    const int tiles[] = {32, 64, 128};
+    const float scales[] = {0.3f, 0.4f, 0.5f, 0.6f, 0.8f};
+    int bb = c->block, bt = c->tile;
+    float bs = c->cell_scale, best = 1e30f;
+    const bool fixed_cell = c->prm.grid_cell > 0.0f;
+    c->replan_enabled = false;
+    int trials = 0;
+    for (float sc : scales) {
+        if (fixed_cell && sc != scales[0]) break;
+        c->cell_scale = sc;
+        for (auto& s : c->scenes) s->grid_ready = false;
+        for (int b : blocks) {
+            if (c->prm.block_size && b != c->prm.block_size) continue;
+            for (int t : tiles) {
+                c->block = b;
+                c->tile = t;
+                c->graph_dirty = true;
+                ecmg_tick_stats ts{};
+                ecmg_status st = run_ticks(c, 1, &ts); /* warm-up and graph capture */
+                if (st == ECMG_OK) st = run_ticks(c, ticks_per_trial, &ts);
+                ecmg_status rs = restore();
+                if (st != ECMG_OK || rs != ECMG_OK) {
+                    c->replan_enabled = true;
+                    return st != ECMG_OK ? st : rs;
+                }
+                trials++;
+                float ms = ts.device_ms / (float)ticks_per_trial;
+                if (ms < best) { best = ms; bb = b; bt = t; bs = sc; }
+            }
+        }
+    }
+    c->replan_enabled = true;
+    c->block = bb;
+    c->tile = bt;
+    c->cell_scale = bs;
+    for (auto& s : c->scenes) s->grid_ready = false;
+    c->graph_dirty = true;
+    sp.free_(); sv.free_(); sa.free_(); spv.free_(); sact.free_();
+    if (out) {
+        out->block_size = bb;
+        out->agents_per_warp_grab = bt;
+        out->grid_cell_scale = bs;
+        out->best_tick_ms = best;
+        out->trials = trials;
+    }
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_set_launch(ecmg_ctx* c, int block_size, int agents_per_warp_grab, float grid_cell_scale)
+{
+    if (!c) return ECMG_ERR_INVALID_ARG;
+    if (block_size != 64 && block_size != 128 && block_size != 256) return fail(c, ECMG_ERR_INVALID_ARG, "block size");
+    if (agents_per_warp_grab < 32 || agents_per_warp_grab % 32 || agents_per_warp_grab > 1024)
+        return fail(c, ECMG_ERR_INVALID_ARG, "agents per warp grab must be a multiple of 32 in [32, 1024]");
+    if (!(grid_cell_scale > 0.0f) || !std::isfinite(grid_cell_scale)) return fail(c, ECMG_ERR_INVALID_ARG, "grid scale");
+    c->block = block_size;
+    c->tile = agents_per_warp_grab;
+    if (grid_cell_scale != c->cell_scale) {
+        c->cell_scale = grid_cell_scale;
+        for (auto& s : c->scenes) s->grid_ready = false;
+    }
+    c->graph_dirty = true;
+    return ECMG_OK;
 }
 
 ecmg_status ecmg_get_state(ecmg_ctx* c, int field, void* dst)
@@ -973,12 +1152,14 @@ ecmg_status ecmg_set_state(ecmg_ctx* c, int field, const void* src)
     case ECMG_FIELD_CLEARANCE:
         std::memcpy(c->clear.data(), src, sizeof(float) * N);
         CK(cudaMemcpy(c->d_clear.p, src, sizeof(float) * N, cudaMemcpyHostToDevice));
-        for (size_t i = 0; i < N; i++) if (c->active[i]) note_range(c, c->clear[i], c->speed[i]);
+        for (size_t i = 0; i < N; i++)
+            if (c->active[i]) note_range(c, c->scenes[c->slot_scene[i]].get(), c->clear[i], c->speed[i]);
         break;
     case ECMG_FIELD_SPEED:
         std::memcpy(c->speed.data(), src, sizeof(float) * N);
         CK(cudaMemcpy(c->d_speed.p, src, sizeof(float) * N, cudaMemcpyHostToDevice));
-        for (size_t i = 0; i < N; i++) if (c->active[i]) note_range(c, c->clear[i], c->speed[i]);
+        for (size_t i = 0; i < N; i++)
+            if (c->active[i]) note_range(c, c->scenes[c->slot_scene[i]].get(), c->clear[i], c->speed[i]);
         break;
     default: return fail(c, ECMG_ERR_INVALID_ARG, "field %d cannot be set", field);
     }
@@ -989,10 +1170,24 @@ ecmg_status ecmg_get_counts(const ecmg_ctx* c, int* num_agents, int* last_index,
 {
     if (!c) return ECMG_ERR_INVALID_ARG;
     if (num_agents) *num_agents = c->num_agents;
-    if (last_index) *last_index = c->last_idx;
+    if (last_index) *last_index = c->global_last();
     if (max_agents) *max_agents = c->max_agents;
     return ECMG_OK;
 }
+
+ecmg_status ecmg_scene_counts(const ecmg_ctx* c, int scene, int* num_agents, int* last_index, int* slot_base,
+                              int* slot_count)
+{
+    if (!c || scene < 0 || scene >= (int)c->scenes.size()) return ECMG_ERR_INVALID_ARG;
+    const SceneState* sc = c->scenes[scene].get();
+    if (num_agents) *num_agents = sc->num_agents;
+    if (last_index) *last_index = sc->last_idx;
+    if (slot_base) *slot_base = sc->slot_base;
+    if (slot_count) *slot_count = sc->slot_cap;
+    return ECMG_OK;
+}
+
+int ecmg_scene_count(const ecmg_ctx* c) { return c ? (int)c->scenes.size() : 0; }
 
 ecmg_status ecmg_set_record(ecmg_ctx* c, int on)
 {
@@ -1016,61 +1211,6 @@ ecmg_status ecmg_get_record(ecmg_ctx* c, int* nbr_ids, int* nbr_count, float* v_
     if (n_cons) CK(cudaMemcpy(n_cons, c->rec_ncons.p, sizeof(int) * N, cudaMemcpyDeviceToHost));
     if (n_obst) CK(cudaMemcpy(n_obst, c->rec_nobst.p, sizeof(int) * N, cudaMemcpyDeviceToHost));
     return ECMG_OK;
-}
-
-/* ---------------------------------------------------------------------- */
-static AgentGrid knn_grid_of(float x0, float y0, float x1, float y1, float cell)
-{
-    AgentGrid g;
-    g.cell = cell;
-    g.inv = 1.0f / cell;
-    g.x0 = x0 - cell;
-    g.y0 = y0 - cell;
-    g.gw = (int)std::ceil(std::max(0.0f, x1 - x0) / cell) + 3;
-    g.gh = (int)std::ceil(std::max(0.0f, y1 - y0) / cell) + 3;
-    g.ncells = g.gw * g.gh;
-    return g;
-}
-
-static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
-
-size_t ecmg_knn_scratch_bytes(int n, float min_x, float min_y, float max_x, float max_y, float cell)
-{
-    if (n < 0 || !(cell > 0.0f) || !(max_x >= min_x) || !(max_y >= min_y)) return 0;
-    AgentGrid g = knn_grid_of(min_x, min_y, max_x, max_y, cell);
-    size_t nb = (size_t)g.ncells + 1;
-    size_t b = 0;
-    b += align256(sizeof(int) * (size_t)std::max(1, n)) * 3; /* key, rank, s_slot */
-    b += align256(sizeof(V2) * (size_t)std::max(1, n));      /* s_pos */
-    b += align256(sizeof(int) * (nb + 1 + kCounters));      /* cell_count + counters */
-    b += align256(sizeof(int) * (nb + 1));                  /* cell_start */
-    b += align256(sizeof(int) * (size_t)scan_tmp_ints((int)nb));
-    return b;
-}
-
-ecmg_status ecmg_knn(const float* dev_pos, const unsigned char* dev_active, int n, int k, float radius, float min_x,
-                     float min_y, float max_x, float max_y, float cell, int* dev_out_ids, int* dev_out_count,
-                     void* dev_scratch, size_t scratch_bytes, void* stream)
-{
-    if (n < 0 || k < 1 || k > kMaxK || !(radius > 0.0f) || !(cell > 0.0f)) return ECMG_ERR_INVALID_ARG;
-    if (n == 0) return ECMG_OK;
-    if (!dev_pos || !dev_active || !dev_out_ids || !dev_out_count || !dev_scratch) return ECMG_ERR_INVALID_ARG;
-    size_t need = ecmg_knn_scratch_bytes(n, min_x, min_y, max_x, max_y, cell);
-    if (need == 0 || scratch_bytes < need) return ECMG_ERR_INVALID_ARG;
-    AgentGrid g = knn_grid_of(min_x, min_y, max_x, max_y, cell);
-    size_t nb = (size_t)g.ncells + 1;
-    char* p = (char*)dev_scratch;
-    auto take = [&](size_t bytes) { char* r = p; p += align256(bytes); return r; };
-    int* key = (int*)take(sizeof(int) * n);
-    int* rank = (int*)take(sizeof(int) * n);
-    int* s_slot = (int*)take(sizeof(int) * n);
-    V2* s_pos = (V2*)take(sizeof(V2) * n);
-    int* cell_count = (int*)take(sizeof(int) * (nb + 1 + kCounters));
-    int* cell_start = (int*)take(sizeof(int) * (nb + 1));
-    int* scan_tmp = (int*)take(sizeof(int) * (size_t)scan_tmp_ints((int)nb));
-    cudaError_t e = launch_knn((const V2*)dev_pos, dev_active, n, k, radius, g, key, rank, cell_count, cell_start,
-                               s_slot, s_pos, scan_tmp, 0, dev_out_ids, dev_out_count, (cudaStream_t)stream);
-    return e == cudaSuccess ? ECMG_OK : ECMG_ERR_CUDA;
 }
 
 }  // extern "C"

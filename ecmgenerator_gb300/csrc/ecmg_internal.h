@@ -10,10 +10,11 @@
 
 namespace ecmg {
 
-/* Constraint capacity per agent: obstacle constraints + neighbours.  An agent
-   that would need more sets ECMG_DEV_ERR_CONSTRAINTS and is computed with the
-   first kMaxCons constraints only; the tick then returns ECMG_ERR_BOUND. */
-constexpr int kMaxCons = 64;
+/* Constraint capacity per agent: the k neighbour half-planes plus
+   kMaxObstCons obstacle half-planes.  An agent that would need more obstacle
+   half-planes sets ECMG_DEV_ERR_CONSTRAINTS and is computed with the first
+   kMaxObstCons only; the tick then returns ECMG_ERR_BOUND. */
+constexpr int kMaxObstCons = 24;
 constexpr int kMaxK = 32;
 
 /* device counters (int[kCounters]) */
@@ -42,6 +43,16 @@ struct AgentGrid {
     int ncells; /* gw*gh, overflow bucket index */
 };
 
+/* One independent scene of a batch: its agent grid, the first of its
+   buckets in the global bucket array, and its static obstacle / ECM views
+   (indices inside a view are local to the scene). */
+struct SceneDev {
+    AgentGrid grid;
+    int bucket_base;
+    ObstView ob;
+    EcmView ecm;
+};
+
 struct TickArgs {
     /* slot-indexed state */
     V2* pos;
@@ -59,10 +70,12 @@ struct TickArgs {
     const V2* s_pos;
     const V2* s_vel;
     const float* s_clear;
-    const int* cell_start; /* ncells + 2 */
-    AgentGrid grid;
-    ObstView ob;
-    EcmView ecm;
+    const int* cell_start; /* total buckets + 1 */
+    int* nbr;              /* [n * k] neighbours of grid-order agent t, as grid-order indices */
+    int* ncnt;             /* [n] neighbour count */
+    const SceneDev* scenes;
+    const int* slot_scene; /* slot -> scene (null: one scene) */
+    int tile;              /* agents a warp takes per work grab (multiple of 32) */
     /* parameters */
     float dt, tau_a, tau_o, rnb, rnb2, max_speed, mass_recip, arr_sq, del_sq;
     int k;
@@ -96,12 +109,15 @@ struct BinArgs {
     float* s_clear;
     const int* cell_start;
     int* counters;
-    AgentGrid grid;
+    AgentGrid grid;           /* used when scenes is null */
+    const SceneDev* scenes;   /* batch: per-scene grid and bucket base */
+    const int* slot_scene;
+    int total_buckets;        /* sum over scenes of (cells + overflow) */
 };
 
 /* kernels.cu */
-cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int scan_blocks,
-                        int block, int sms, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1);
+cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int block, int sms,
+                        cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1);
 cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k, float r, AgentGrid g,
                        int* key, int* rank, int* cell_count, int* cell_start, int* s_slot, V2* s_pos,
                        int* scan_tmp, int scan_blocks, int* out_ids, int* out_cnt, cudaStream_t s);

@@ -47,7 +47,13 @@ __global__ void k_bin(BinArgs a)
     int last = a.counters[C_LAST];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= last; i += gridDim.x * blockDim.x) {
         if (!a.active[i]) continue;
-        int b = bucket_of(a.grid, a.pos[i]);
+        int b;
+        if (a.scenes) {
+            const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[i] : 0];
+            b = sc.bucket_base + bucket_of(sc.grid, a.pos[i]);
+        } else {
+            b = bucket_of(a.grid, a.pos[i]);
+        }
         a.key[i] = b;
         a.rank[i] = atomicAdd(&a.cell_count[b], 1);
     }
@@ -56,7 +62,7 @@ __global__ void k_bin(BinArgs a)
 __global__ void k_scatter(BinArgs a)
 {
     int last = a.counters[C_LAST];
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.counters[C_NSORTED] = a.cell_start[a.grid.ncells + 1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.counters[C_NSORTED] = a.cell_start[a.total_buckets];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= last; i += gridDim.x * blockDim.x) {
         if (!a.active[i]) continue;
         int d = a.cell_start[a.key[i]] + a.rank[i];
@@ -244,10 +250,11 @@ __device__ __noinline__ Con agent_constraint_ni(V2 position, V2 velocity, float 
     return agent_constraint(position, velocity, clr, np, nv, nclr, tau, dt);
 }
 
+template <int MC>
 __device__ __noinline__ void lp3d_local(const Con* cons, int m, int nObst, float maxSpeed, int failed, V2* v,
                                         bool fp64)
 {
-    Con proj[kMaxCons];
+    Con proj[MC];
     LocalGet get{cons};
     lp3d(get, m, nObst, maxSpeed, failed, v, proj, fp64);
 }
@@ -259,6 +266,7 @@ __device__ void agent_tick(const TickArgs& a, int t)
     const V2 pos = a.s_pos[t];
     const V2 vel = a.s_vel[t];
     const float clr = a.s_clear[t];
+    const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
 
     /* UpdateAttractionPointSystem (Simulator.cpp:538-590) */
     const int off = a.path_off[slot], np = a.path_len[slot];
@@ -280,7 +288,7 @@ __device__ void agent_tick(const TickArgs& a, int t)
         }
     } else {
         V2 ap = mk(0.0f, 0.0f); /* Point attractionPoint; (0,0) */
-        if (irm(a.ecm, pos, path, np, &ap)) {
+        if (irm(sc.ecm, pos, path, np, &ap)) {
             attr = ap;
             a.attr[slot] = attr;
         } else {
@@ -299,16 +307,16 @@ __device__ void agent_tick(const TickArgs& a, int t)
     /* ORCA::GetVelocity (ORCA.cpp:14-57) with maxSpeed = preferred speed
        (Simulator.cpp:671) unless a global maximum is configured */
     const float maxSpeed = a.max_speed > 0.0f ? a.max_speed : speed;
-    Knn<K> nn;
-    knn_grid<K>(nn, a.k, pos, a.rnb, a.rnb2, a.s_pos, a.s_slot, a.cell_start, a.grid);
-
-    Con cons[kMaxCons];
+    const int ncnt = a.ncnt[t];
+    const int* nbr = a.nbr + (size_t)t * a.k;
+    constexpr int MC = K + kMaxObstCons; /* constraint capacity */
+    Con cons[MC];
     int m = 0;
     bool overflow = false;
     const float range = a.tau_o * maxSpeed + clr;
     const float rsq = range * range;
     {
-        const ObstView& o = a.ob;
+        const ObstView& o = sc.ob;
         int b = 0, e = 0;
         const int* items = nullptr;
         float fx = (pos.x - o.gx0) * o.ginv, fy = (pos.y - o.gy0) * o.ginv;
@@ -325,20 +333,15 @@ __device__ void agent_tick(const TickArgs& a, int t)
             if (!obstacle_in_range(o, L, pos, rsq)) continue;
             Con c;
             if (obstacle_constraint(o, L, pos, vel, clr, a.tau_o, &c)) {
-                if (m < kMaxCons) cons[m++] = c;
+                if (m < MC - K) cons[m++] = c;
                 else overflow = true;
             }
         }
     }
     const int nObst = m;
-    int nb[K];
-#pragma unroll
-    for (int q = 0; q < K; q++) nb[q] = nn.ix[q];
-    for (int q = 0; q < nn.cnt; q++) {
-        int j = nb[q];
-        Con c = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt);
-        if (m < kMaxCons) cons[m++] = c;
-        else overflow = true;
+    for (int q = 0; q < ncnt; q++) {
+        int j = nbr[q];
+        cons[m++] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt);
     }
     if (overflow) atomicOr(&a.counters[C_ERROR], ECMG_DEV_ERR_CONSTRAINTS);
 
@@ -346,7 +349,7 @@ __device__ void agent_tick(const TickArgs& a, int t)
     LocalGet get{cons};
     int failed = lp2d(get, m, pv, maxSpeed, false, &v);
     if (failed < m) {
-        lp3d_local(cons, m, nObst, maxSpeed, failed, &v, a.lp3d_fp64 != 0);
+        lp3d_local<MC>(cons, m, nObst, maxSpeed, failed, &v, a.lp3d_fp64 != 0);
         atomicAdd(&a.counters[C_LP3D], 1);
     }
 
@@ -359,11 +362,8 @@ __device__ void agent_tick(const TickArgs& a, int t)
     a.pos[slot] = npos;
 
     if (a.rec_cnt) {
-        a.rec_cnt[slot] = nn.cnt;
-        for (int q = 0; q < a.k; q++) a.rec_nbr[slot * a.k + q] = -1;
-#pragma unroll
-        for (int q = 0; q < K; q++)
-            if (q < nn.cnt) a.rec_nbr[slot * a.k + q] = a.s_slot[nn.ix[q]];
+        a.rec_cnt[slot] = ncnt;
+        for (int q = 0; q < a.k; q++) a.rec_nbr[slot * a.k + q] = q < ncnt ? a.s_slot[nbr[q]] : -1;
         a.rec_vorca[slot] = v;
         a.rec_fail[slot] = failed;
         a.rec_ncons[slot] = m;
@@ -371,19 +371,41 @@ __device__ void agent_tick(const TickArgs& a, int t)
     }
 }
 
-/* persistent kernel: warps take 32 consecutive grid-order agents at a time */
+/* neighbour lists of every grid-order agent of the tick (KNearestAgents,
+   KDTree.cpp:85-202, as the exact (d2, slot) query of the grid) */
 template <int K>
-__global__ void __launch_bounds__(128) k_agents(TickArgs a)
+__global__ void __launch_bounds__(128) k_neighbors(TickArgs a)
+{
+    const int n = a.counters[C_NSORTED];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int slot = a.s_slot[t];
+        const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
+        Knn<K> nn;
+        knn_grid<K>(nn, a.k, a.s_pos[t], a.rnb, a.rnb2, a.s_pos, a.s_slot, a.cell_start + sc.bucket_base, sc.grid);
+        a.ncnt[t] = nn.cnt;
+        int* o = a.nbr + (size_t)t * a.k;
+#pragma unroll
+        for (int q = 0; q < K; q++)
+            if (q < a.k) o[q] = nn.ix[q];
+    }
+}
+
+/* persistent kernel: a warp takes `tile` consecutive grid-order agents per
+   work grab (one atomic per grab) and runs them 32 at a time */
+template <int K>
+__global__ void __launch_bounds__(256) k_agents(TickArgs a)
 {
     const int n = a.counters[C_NSORTED];
     const int lane = threadIdx.x & 31;
     while (true) {
         int base = 0;
-        if (lane == 0) base = atomicAdd(&a.counters[C_WORK], 32);
+        if (lane == 0) base = atomicAdd(&a.counters[C_WORK], a.tile);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n) break;
-        int t = base + lane;
-        if (t < n) agent_tick<K>(a, t);
+        for (int o = 0; o < a.tile; o += 32) {
+            int t = base + o + lane;
+            if (t < n) agent_tick<K>(a, t);
+        }
     }
 }
 
@@ -413,14 +435,13 @@ static int grid_for(int n, int block, int sms, int per_sm)
     return g < 1 ? 1 : (g > cap ? cap : g);
 }
 
-cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int scan_blocks,
-                        int block, int sms, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1)
+cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int block, int sms,
+                        cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1)
 {
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(s, &cap);
     const unsigned evflags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
-    (void)scan_blocks;
-    int nb = b.grid.ncells + 1;
+    int nb = b.total_buckets;
     cudaError_t e = cudaMemsetAsync(b.cell_count, 0, sizeof(int) * (size_t)(nb + 1), s);
     if (e != cudaSuccess) return e;
     int gb = grid_for(max_slots, 256, sms, 8);
@@ -430,11 +451,22 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
     k_scatter<<<gb, 256, 0, s>>>(b);
     /* external event nodes when captured, so that the kernel can be timed */
     if (ev0) cudaEventRecordWithFlags(ev0, s, evflags);
-    int ga = sms * 16; /* persistent: enough warps per SM to hide latency */
-    (void)block;
-    if (t.k <= 8) k_agents<8><<<ga, 128, 0, s>>>(t);
-    else if (t.k <= 16) k_agents<16><<<ga, 128, 0, s>>>(t);
-    else k_agents<32><<<ga, 128, 0, s>>>(t);
+    if (block != 64 && block != 128 && block != 256) block = 128;
+    int gk = grid_for(max_slots, 128, sms, 16);
+    int per_sm = 1;
+    if (t.k <= 8) {
+        k_neighbors<8><<<gk, 128, 0, s>>>(t);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<8>, block, 0);
+        k_agents<8><<<sms * (per_sm > 0 ? per_sm : 1), block, 0, s>>>(t);
+    } else if (t.k <= 16) {
+        k_neighbors<16><<<gk, 128, 0, s>>>(t);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<16>, block, 0);
+        k_agents<16><<<sms * (per_sm > 0 ? per_sm : 1), block, 0, s>>>(t);
+    } else {
+        k_neighbors<32><<<gk, 128, 0, s>>>(t);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<32>, block, 0);
+        k_agents<32><<<sms * (per_sm > 0 ? per_sm : 1), block, 0, s>>>(t);
+    }
     if (ev1) cudaEventRecordWithFlags(ev1, s, evflags);
     return cudaGetLastError();
 }
@@ -465,6 +497,7 @@ cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k,
     b.cell_start = cell_start;
     b.counters = counters;
     b.grid = g;
+    b.total_buckets = nb;
     int gb = (n + 255) / 256;
     if (gb < 1) gb = 1;
     k_bin<<<gb, 256, 0, s>>>(b);

@@ -427,6 +427,33 @@ def build_ecm(scene: Scene, h: float = 0.2, tol: float = 0.3) -> Ecm:
     edges = [edges[i] for i in eorder]
     E = len(edges)
 
+    # A vertex where a corner's wedge meets the cell of one of that corner's
+    # own segments lies, in the exact diagram, on the segment's normal through
+    # the corner.  The sampled diagram puts it within ~h of that line; moving
+    # it onto the line makes the spoke to the corner perpendicular to the
+    # segment, so the corner triangle and the segment quad share one spoke and
+    # retraction rays (perpendicular to the segment) stay inside the quad.
+    vfeat: dict[int, set] = {}
+    for a_, b_, l_, r_ in edges:
+        for v_ in (a_, b_):
+            vfeat.setdefault(v_, set()).update((l_, r_))
+    for v_, fs in vfeat.items():
+        for f in fs:
+            if f < S:
+                continue
+            c = corner_pt[f - S]
+            for sg in fs:
+                if sg >= S or (seg_c0[sg] != f - S and seg_c1[sg] != f - S):
+                    continue
+                d = segs[sg, 2:4] - segs[sg, 0:2]
+                L2 = float(d @ d)
+                if L2 == 0.0:
+                    continue
+                t = float((vpos[v_] - c) @ d) / L2
+                if abs(t) * math.sqrt(L2) < 2.0 * h:
+                    vpos[v_] = vpos[v_] - t * d
+                break
+
     def feat_point(f, p):
         if f >= S:
             return corner_pt[f - S].copy()

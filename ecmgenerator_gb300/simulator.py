@@ -261,3 +261,64 @@ class Simulator:
         self._ck(self.L.ecmg_get_record(self.h, _ptr(d["nbr_ids"]), _ptr(d["nbr_count"]), _ptr(d["v_orca"]),
                                         _ptr(d["lp_fail"]), _ptr(d["n_constraints"]), _ptr(d["n_obst_constraints"])))
         return d
+
+
+class BatchSimulator(Simulator):
+    """Many independent scenes advanced by one launch sequence per tick
+    (ecmg_create_batch).  Scene s owns global slots
+    [slot_base(s), slot_base(s) + max_agents[s]); the getters return all slots."""
+
+    def __init__(self, scenes, max_agents_per_scene, sim_step_time: float, **kw):
+        self.L = _lib.load()
+        p = _lib.default_params(dt=sim_step_time)
+        for key, v in kw.items():
+            setattr(p, key, int(v) if key in ("use_graph", "lp3d_fp64", "max_neighbors", "block_size") else v)
+        self.params = p
+        caps = _a(max_agents_per_scene, I32)
+        h = C.c_void_p()
+        rc = self.L.ecmg_create_batch(C.byref(p), len(scenes), _ptr(caps), C.byref(h))
+        if rc:
+            raise EcmgError(rc, "ecmg_create_batch failed (is a CUDA device visible?)")
+        self.h = h
+        self.max_agents = int(caps.sum())
+        self.k = int(p.max_neighbors)
+        self.scenes = scenes
+        self._keep = []
+        for s, sc in enumerate(scenes):
+            keep, o, e = _scene_structs(sc)
+            self._keep.append(keep)
+            self._ck(self.L.ecmg_scene_set_obstacles(self.h, s, C.byref(o)))
+            self._ck(self.L.ecmg_scene_set_ecm(self.h, s, C.byref(e)))
+        self._plan_cb = None
+
+    def add_agents(self, pos, clearance, pref_speed, paths, scene: int = 0) -> np.ndarray:
+        pos = _a(pos, F32).reshape(-1, 2)
+        n = pos.shape[0]
+        clr, spd = _a(clearance, F32), _a(pref_speed, F32)
+        lens = np.array([len(p) for p in paths], I32)
+        offs = np.zeros(n, I32)
+        if n:
+            offs[1:] = np.cumsum(lens)[:-1]
+        xy = _a(np.concatenate([np.asarray(p, F32).reshape(-1, 2) for p in paths], 0), F32) if n else \
+            np.zeros((0, 2), F32)
+        out = np.zeros(n, I32)
+        self._ck(self.L.ecmg_scene_add_agents(self.h, int(scene), n, _ptr(pos), _ptr(clr), _ptr(spd), _ptr(offs),
+                                              _ptr(lens), _ptr(xy), _ptr(out)))
+        return out
+
+    def scene_counts(self, scene: int) -> dict:
+        v = [C.c_int() for _ in range(4)]
+        self._ck(self.L.ecmg_scene_counts(self.h, int(scene), *[C.byref(x) for x in v]))
+        return dict(num_agents=v[0].value, last_index=v[1].value, slot_base=v[2].value, slot_count=v[3].value)
+
+
+def autotune(sim: Simulator, ticks_per_trial: int = 2) -> dict:
+    """ecmg_autotune: pick block size, agents per warp grab and grid cell."""
+    r = _lib.TuneResult()
+    sim._ck(sim.L.ecmg_autotune(sim.h, int(ticks_per_trial), C.byref(r)))
+    return dict(block_size=r.block_size, agents_per_warp_grab=r.agents_per_warp_grab,
+                grid_cell_scale=r.grid_cell_scale, best_tick_ms=r.best_tick_ms, trials=r.trials)
+
+
+def set_launch(sim: Simulator, block_size: int, agents_per_warp_grab: int, grid_cell_scale: float):
+    sim._ck(sim.L.ecmg_set_launch(sim.h, int(block_size), int(agents_per_warp_grab), float(grid_cell_scale)))

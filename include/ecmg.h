@@ -70,7 +70,8 @@ typedef struct {
     long long replans_failed;
     long long lp3d;        /* agents whose 2D LP was infeasible                   */
     float device_ms;       /* device time of the ticks (CUDA events)              */
-    float agent_kernel_ms; /* device time of the per-agent kernel alone           */
+    float agent_kernel_ms; /* device time of the neighbour + per-agent kernels    */
+    float host_ms;         /* host time between ticks (bookkeeping, re-planning)  */
 } ecmg_tick_stats;
 
 /* Static obstacles: n_obstacles rings, ring r = xy[2*ring_offsets[r] ..
@@ -184,6 +185,39 @@ ecmg_status ecmg_get_path(ecmg_ctx* ctx, int slot, float* out_xy, int cap, int* 
 ecmg_status ecmg_set_record(ecmg_ctx* ctx, int on);
 ecmg_status ecmg_get_record(ecmg_ctx* ctx, int* nbr_ids, int* nbr_count, float* v_orca,
                             int* lp_fail, int* n_constraints, int* n_obst_constraints);
+
+/* ---- batches of independent scenes (one launch sequence per tick) ----------
+   Scene s owns the slot range [slot_base_s, slot_base_s + max_agents_s) with
+   its own free-slot stack, obstacles, ECM and planner; a scene is what one
+   reference Simulator + Environment hold.  ecmg_create(p, n, &ctx) is
+   ecmg_create_batch(p, 1, &n, &ctx); the single-scene calls act on scene 0. */
+ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max_agents_per_scene, ecmg_ctx** out);
+int ecmg_scene_count(const ecmg_ctx* ctx);
+ecmg_status ecmg_scene_set_obstacles(ecmg_ctx* ctx, int scene, const ecmg_obstacles* o);
+ecmg_status ecmg_scene_set_ecm(ecmg_ctx* ctx, int scene, const ecmg_ecm* e);
+ecmg_status ecmg_scene_add_agents(ecmg_ctx* ctx, int scene, int n, const float* pos, const float* clearance,
+                                  const float* pref_speed, const int* path_off, const int* path_len,
+                                  const float* path_xy, int* out_slots);
+ecmg_status ecmg_scene_counts(const ecmg_ctx* ctx, int scene, int* num_agents, int* last_index, int* slot_base,
+                              int* slot_count);
+
+/* ---- launch configuration ------------------------------------------------
+   The per-agent kernel is persistent: each warp takes agents_per_warp_grab
+   grid-order agents per atomic work grab.  The agent grid cell is
+   grid_cell_scale * sqrt(max_neighbors / agent density), unless
+   ecmg_params.grid_cell fixes it. */
+typedef struct {
+    int block_size;
+    int agents_per_warp_grab;
+    float grid_cell_scale;
+    float best_tick_ms;
+    int trials;
+} ecmg_tune_result;
+ecmg_status ecmg_set_launch(ecmg_ctx* ctx, int block_size, int agents_per_warp_grab, float grid_cell_scale);
+/* times ticks_per_trial ticks per configuration (block size x work grab x
+   grid cell) on a copy of the current state, restores the state after each
+   trial (no re-plans are served during trials) and keeps the fastest */
+ecmg_status ecmg_autotune(ecmg_ctx* ctx, int ticks_per_trial, ecmg_tune_result* out);
 
 /* the cudaStream_t the context launches on (for callers that record CUDA
    events or order their own work around the tick) */
