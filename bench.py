@@ -31,15 +31,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-WORKLOADS = {
-    "crossing_1m": dict(cfg="c3", agents=1_000_000, k=16),
-    "crossing_100k": dict(cfg="c3", agents=100_000, k=16),
-    "boxes_100k": dict(cfg="c2", agents=100_000, k=10),
-    "boxes_1k": dict(cfg="c1", agents=1_000, k=10),
-}
-ORCA = dict(tau_agent=2.0, tau_obst=2.0, neighbor_dist=5.0)
-DT = 1.0 / 60.0
-ALG_BYTES_PER_AGENT = 64  # algorithmic state traffic of the per-agent kernel
+from ecmgenerator_gb300.workloads import DT, ORCA, WORKLOADS  # noqa: E402
+
+# algorithmic state bytes per agent and tick: read pos 8, vel 8, radius 4, speed 4,
+# path cursor 4, attraction 8; write pos 8, vel 8, attraction 8, cursor 4
+ALG_BYTES_PER_AGENT = 64
 
 
 def log(*a):
@@ -54,28 +50,9 @@ def dist_env():
 
 
 def make_workload(name, seed):
-    from ecmgenerator_gb300 import agents as ag
-    from ecmgenerator_gb300.simulator import Planner
+    from ecmgenerator_gb300.workloads import make_workload as mk
 
-    w = WORKLOADS[name]
-    cfg = ag.scaled(w["cfg"], agents=w["agents"])
-    t0 = time.time()
-    scene = ag.build_scene(cfg, seed)
-    st = ag.spawn_agents(cfg, scene, seed)
-    pl = Planner(scene)
-    n = st.num_agents
-    paths = []
-    chunk = 100_000
-    for a in range(0, n, chunk):
-        b = min(n, a + chunk)
-        got = pl.find_paths(st.pos[a:b], st.goal[a:b], st.clear[a:b], threads=0, cap=64)
-        for i, p in enumerate(got):
-            if p is None:
-                p = np.stack([st.pos[a + i], st.goal[a + i]])
-            paths.append(np.asarray(p, np.float32))
-    st.set_paths(paths)
-    log(f"[bench] workload {name}: {n} agents, {scene.ecm.n_edges} ECM edges, setup {time.time() - t0:.1f}s")
-    return cfg, scene, st, paths, w["k"]
+    return mk(name, seed)
 
 
 class ClockSampler:
@@ -173,9 +150,65 @@ def cpu_baseline(scene, st, k, threads, budget_s=12.0):
             "ms_per_tick": tick_s * 1e3}
 
 
-def run_ours(args):
-    import ctypes as C
+def load_or_train_model(sim, args):
+    """The proposal network: committed weights when present, else trained
+    here on traces of this simulator's warm-up ticks (logged)."""
+    from ecmgenerator_gb300 import proposal as P
 
+    m = P.ProposalModel(seed=0)
+    path = args.proposal or os.path.join(HERE, "ecmgenerator_gb300", "data", "proposal.npy")
+    if os.path.exists(path):
+        m.load(path)
+        return m, {"weights": os.path.relpath(path, HERE)}
+    t0 = time.time()
+    x, y = P.collect_traces(sim, ticks=8)
+    loss, acc = m.train(x, y, steps=1500, batch=65536, lr=1e-3, seed=3)
+    info = {"weights": "trained in this run on traces of its own warm-up ticks", "rows": int(x.shape[0]),
+            "steps": 1500, "batch": 65536, "train_s": time.time() - t0, "loss": float(loss[-50:].mean()),
+            "acc": float(acc[-50:].mean()), "classes": P.class_histogram(y)}
+    log(f"[bench] trained proposal: {info}")
+    del x, y
+    return m, info
+
+
+class TickTimer:
+    """CUDA events on the library's stream around each tick, L2 flushed
+    (512 MB write, > 129 MB L2) before every timed tick."""
+
+    def __init__(self, sim, flush):
+        import torch
+
+        self.sim = sim
+        self.stream = torch.cuda.ExternalStream(sim.L.ecmg_stream(sim.h))
+        self.flush = flush
+        self.ev = []
+        self.steps = 0
+        self.agent_ms = 0.0
+        self.tot = dict(lp3d=0, replans=0, replans_failed=0, destroyed=0, device_ms=0.0, proposed=0, accepted=0,
+                        gated=0)
+
+    def tick(self):
+        import torch
+
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(self.stream):
+            self.flush.zero_()
+            e0.record(self.stream)
+        s = self.sim.update()
+        with torch.cuda.stream(self.stream):
+            e1.record(self.stream)
+        self.ev.append((e0, e1))
+        self.steps += s.agent_steps
+        self.agent_ms += s.agent_kernel_ms
+        for k in self.tot:
+            self.tot[k] += getattr(s, k)
+        return s
+
+    def ms(self):
+        return sum(a.elapsed_time(b) for a, b in self.ev)
+
+
+def run_ours(args):
     import torch
 
     rank, world, local = dist_env()
@@ -188,91 +221,118 @@ def run_ours(args):
 
     cfg, scene, st, paths, k = make_workload(args.workload, args.seed)
     n = st.num_agents
-    sim = Simulator(scene, n, DT, max_neighbors=k, **ORCA)
-    sim.add_agents(st.pos[:n], st.clear[:n], st.pref_speed[:n], paths)
-    stream = torch.cuda.ExternalStream(sim.L.ecmg_stream(sim.h))
+    # two simulators in the same state: the plain tick and the tick with the
+    # learned proposal (their trajectories are identical)
+    sims = []
+    for _ in range(2):
+        s_ = Simulator(scene, n, DT, max_neighbors=k, **ORCA)
+        s_.add_agents(st.pos[:n], st.clear[:n], st.pref_speed[:n], paths)
+        sims.append(s_)
+    plain, learned = sims
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     for _ in range(args.warmup):
-        sim.update()
+        plain.update()
+        learned.update()
+    model, model_info = load_or_train_model(learned, args) if not args.plain_only else (None, None)
+    if model is not None:
+        learned.set_proposal(model)
+        learned.update()  # capture of the learned graph
+        plain.update()
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    steps = 0
-    agent_ms = 0.0
-    tot = dict(lp3d=0, replans=0, replans_failed=0, destroyed=0, device_ms=0.0)
+    tp, tl = TickTimer(plain, flush), TickTimer(learned, flush)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for i in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()  # L2 flush (512 MB > 129 MB L2) before every timed tick
-                ev[i][0].record(stream)
-            s = sim.update()
-            with torch.cuda.stream(stream):
-                ev[i][1].record(stream)
-            steps += s.agent_steps
-            agent_ms += s.agent_kernel_ms
-            tot["lp3d"] += s.lp3d
-            tot["replans"] += s.replans
-            tot["replans_failed"] += s.replans_failed
-            tot["destroyed"] += s.destroyed
-            tot["device_ms"] += s.device_ms
+            tp.tick()
+            if model is not None:
+                tl.tick()
         torch.cuda.synchronize()
-    ms = sum(a.elapsed_time(b) for a, b in ev)
-    ms_all, steps_all = reduce_over_ranks(ms, steps, world, "cuda")
+    same = bool(np.array_equal(plain.get_position_data(), learned.get_position_data()))
+    main_t = tl if model is not None else tp
+    ms = main_t.ms()
+    ms_all, steps_all = reduce_over_ranks(ms, main_t.steps, world, "cuda")
     value = steps_all / (ms_all / 1e3)
+    p_ms_all, p_steps_all = reduce_over_ranks(tp.ms(), tp.steps, world, "cuda")
+    plain_value = p_steps_all / (p_ms_all / 1e3)
     # e2e through the public API: update + positions/velocities back to host
-    e2e_steps = 0
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        s = sim.update()
-        _ = sim.get_position_data()
-        _ = sim.get_velocity_data()
-        e2e_steps += s.agent_steps
-    t1 = time.perf_counter()
-    e2e = {"value": e2e_steps * max(world, 1) / (t1 - t0), "unit": "agent-steps/s", "h2d_bytes_per_step": 64,
-           "d2h_bytes_per_step": 16 * n + 64}
-    kern_ms = agent_ms / max(args.steps, 1)
+    e2e = {}
+    for name, sim in (("learned", learned), ("plain", plain)):
+        if name == "learned" and model is None:
+            continue
+        e2e_steps = 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s = sim.update()
+            _ = sim.get_position_data()
+            _ = sim.get_velocity_data()
+            e2e_steps += s.agent_steps
+        t1 = time.perf_counter()
+        e2e[name] = e2e_steps * max(world, 1) / (t1 - t0)
+    e2e_main = {"value": e2e["learned" if model is not None else "plain"], "unit": "agent-steps/s",
+                "h2d_bytes_per_step": 64, "d2h_bytes_per_step": 16 * n + 64,
+                "plain": e2e["plain"], "note": "wall clock of Simulator.update() + get_position_data() + "
+                "get_velocity_data() per tick; h2d = counters, d2h = positions and velocities + counters"}
+    kern_ms = main_t.agent_ms / max(args.steps, 1)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
     except OSError:
         pass
     hbm = peaks.get("hbm_gbs") or 6800.0
-    achieved = ALG_BYTES_PER_AGENT * (steps / max(args.steps, 1)) / (kern_ms / 1e3) / 1e9 if kern_ms > 0 else 0.0
+    per_tick = main_t.steps / max(args.steps, 1)
+    achieved = ALG_BYTES_PER_AGENT * per_tick / (kern_ms / 1e3) / 1e9 if kern_ms > 0 else 0.0
     traffic = None
     tf = os.path.join(HERE, "profiles", "k_agents_traffic.json")
     if os.path.exists(tf):
         try:
             t = json.load(open(tf)).get(args.workload)
             if t:
-                traffic = t["dram_bytes_per_agent"] * (steps / max(args.steps, 1))
+                traffic = t["dram_bytes_per_agent"] * per_tick
         except (OSError, ValueError, KeyError):
             traffic = None
+    T = main_t.tot
+    launches = plain.L.ecmg_kernels_per_tick(plain.h) * args.steps
+    if model is not None:
+        launches += learned.L.ecmg_kernels_per_tick(learned.h) * (args.steps - T["gated"]) + \
+            plain.L.ecmg_kernels_per_tick(plain.h) * T["gated"]
     out = {
-        "metric": "agent-steps/s (plain GPU ORCA tick)", "value": value, "unit": "agent-steps/s",
+        "metric": "agent-steps/s at 1M agents: learned-proposal vs plain GPU ORCA; ms/tick",
+        "value": value, "unit": "agent-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_all / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded scene, agents and paths)",
         "config": {"workload": args.workload, "agents": n, "max_neighbors": k, "neighbor_dist_m": 5.0,
-                   "time_horizon_s": 2.0, "dt_s": DT, "scene": cfg["cfg"] if "cfg" in cfg else args.workload,
+                   "time_horizon_s": 2.0, "dt_s": DT, "scene": f'{cfg["w"]:.0f}x{cfg["h"]:.0f} m, {cfg["boxes"]} boxes',
                    "l2": "flushed before every timed tick (512 MB write)", "parallelism": f"replicas x{world}",
-                   "seed": args.seed},
-        "e2e": e2e,
+                   "seed": args.seed, "mode": "learned proposal" if model is not None else "plain"},
+        "plain": {"value": plain_value, "ms_per_step": p_ms_all / args.steps,
+                  "lp3d_per_tick": tp.tot["lp3d"] / args.steps},
+        "learned_vs_plain": value / plain_value if model is not None else None,
+        "proposal": None if model is None else {
+            **model_info, "proposed_per_tick": T["proposed"] / args.steps,
+            "accepted_per_tick": T["accepted"] / args.steps,
+            "acceptance_rate": T["accepted"] / max(1, main_t.steps), "gated_ticks": T["gated"],
+            "trajectories_identical": same},
+        "e2e": e2e_main,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": "k_agents", "kernel_ms": kern_ms,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"},
-        "gpu_launches": 6 * args.steps,
+        "gpu_launches": launches,
         "clocks": clk.summary(),
-        "tick_ms_device": ms / args.steps,
-        "tick_stats": {"lp3d_per_tick": tot["lp3d"] / args.steps, "replans_per_tick": tot["replans"] / args.steps,
-                       "replans_failed_per_tick": tot["replans_failed"] / args.steps,
-                       "destroyed_per_tick": tot["destroyed"] / args.steps,
-                       "graph_ms_per_tick": tot["device_ms"] / args.steps},
+        "tick_stats": {"lp3d_per_tick": T["lp3d"] / args.steps, "replans_per_tick": T["replans"] / args.steps,
+                       "replans_failed_per_tick": T["replans_failed"] / args.steps,
+                       "destroyed_per_tick": T["destroyed"] / args.steps,
+                       "graph_ms_per_tick": T["device_ms"] / args.steps},
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(scene, st, k, threads=1, budget_s=args.cpu_budget)
-    sim.close()
+    for s_ in sims:
+        s_.close()
+    if model is not None:
+        model.close()
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -294,7 +354,7 @@ def run_reference(args):
     t1 = time.perf_counter()
     v = float(np.median([x["value"] for x in vals]))
     ms = 1e3 * st.num_agents / v
-    out = {"impl": "reference", "metric": "agent-steps/s (plain GPU ORCA tick)", "value": v, "unit": "agent-steps/s",
+    out = {"impl": "reference", "metric": "agent-steps/s at 1M agents: learned-proposal vs plain GPU ORCA; ms/tick", "value": v, "unit": "agent-steps/s",
            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene, agents and paths)",
            "config": {"workload": args.workload, "agents": st.num_agents, "max_neighbors": k, "seed": args.seed},
@@ -315,6 +375,8 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-only", action="store_true", help="time the plain tick only")
+    ap.add_argument("--proposal", default=None, help="proposal weights (.npy)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -37,7 +37,8 @@ class TickStats(C.Structure):
     _fields_ = [("ticks", C.c_int), ("active_agents", C.c_int), ("last_index", C.c_int),
                 ("agent_steps", C.c_longlong), ("destroyed", C.c_longlong), ("replans", C.c_longlong),
                 ("replans_failed", C.c_longlong), ("lp3d", C.c_longlong), ("device_ms", C.c_float),
-                ("agent_kernel_ms", C.c_float), ("host_ms", C.c_float)]
+                ("agent_kernel_ms", C.c_float), ("host_ms", C.c_float), ("proposed", C.c_longlong),
+                ("accepted", C.c_longlong), ("gated", C.c_longlong)]
 
 
 class TuneResult(C.Structure):
@@ -128,6 +129,19 @@ def load(build_if_missing: bool = False):
         "ecmg_knn_scratch_bytes": (C.c_size_t, [C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float]),
         "ecmg_knn": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                                C.c_float, vp, vp, vp, C.c_size_t, vp]),
+        "ecmg_mlp_create": (C.c_int, [C.c_ulonglong, C.POINTER(vp)]),
+        "ecmg_mlp_destroy": (C.c_int, [vp]),
+        "ecmg_mlp_param_count": (C.c_int, []),
+        "ecmg_mlp_get_params": (C.c_int, [vp, vp]),
+        "ecmg_mlp_set_params": (C.c_int, [vp, vp]),
+        "ecmg_mlp_loss_grad": (C.c_int, [vp, vp, vp, C.c_int, fp, vp]),
+        "ecmg_mlp_train": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_ulonglong, vp, vp]),
+        "ecmg_mlp_predict": (C.c_int, [vp, vp, C.c_int, vp]),
+        "ecmg_set_proposal": (C.c_int, [vp, vp]),
+        "ecmg_set_trace": (C.c_int, [vp, C.c_int]),
+        "ecmg_set_proposal_gate": (C.c_int, [vp, C.c_float, C.c_int]),
+        "ecmg_get_trace": (C.c_int, [vp, vp, vp, vp, C.c_int, ip]),
+        "ecmg_set_proposal_classes": (C.c_int, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

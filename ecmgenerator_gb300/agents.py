@@ -83,8 +83,8 @@ class Workload:
     meta: dict = field(default_factory=dict)
 
 
-# Workload definitions (sizes, distributions and ORCA settings of the
-# reference's configurations; see the design doc for the table).
+# Workload definitions: scene size, box count and side range, agent count,
+# neighbour count k, whether spawns may overlap, ECM sampling step.
 CONFIGS = {
     # 100x100 m, 40 boxes [2,8] m, 1k agents, k=10
     "c1": dict(w=100.0, h=100.0, boxes=40, side=(2.0, 8.0), agents=1000, k=10, overlap=False, h_ecm=0.1),

@@ -27,6 +27,13 @@
 
 using namespace ecmg;
 
+namespace ecmg {
+/* mlp.cu */
+cudaError_t mlp_infer(ecmg_mlp* mlp, const void* X, const int* n_dev, int n_max, unsigned char* cls, cudaStream_t s,
+                      int sms);
+cudaError_t mlp_pack(ecmg_mlp* mlp);
+}  // namespace ecmg
+
 namespace {
 
 template <class T>
@@ -128,10 +135,21 @@ struct ecmg_ctx {
     bool record = false;
     DBuf<int> rec_nbr, rec_cnt, rec_fail, rec_ncons, rec_nobst;
     DBuf<V2> rec_vorca;
+    /* learned proposal / trace */
+    ecmg_mlp* model = nullptr;
+    /* gating: a tick whose acceptance rate is below gate_min pauses the
+       model for gate_pause ticks (plain ticks), then it is tried again */
+    float gate_min = 0.1f;
+    int gate_pause = 64;
+    int gate_left = 0;
+    const unsigned char* cls_override = nullptr;
+    bool trace = false;
+    int trace_rows = 0;
+    DBuf<unsigned char> feat, cls, label;
     /* pinned staging */
     int* h_counters = nullptr; /* [2 * kCounters]: in, out */
     /* graph */
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr}; /* plain tick, tick with the proposal model */
     bool graph_dirty = true;
     int graph_last = -2; /* last slot the captured launch sizes cover */
 
@@ -295,7 +313,8 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
 {
     if (!c) return ECMG_ERR_INVALID_ARG;
     if (c->stream) cudaStreamSynchronize(c->stream);
-    if (c->graph) cudaGraphExecDestroy(c->graph);
+    for (auto& g : c->graph)
+        if (g) cudaGraphExecDestroy(g);
     DBuf<V2>* v2s[] = {&c->pos, &c->vel, &c->attr, &c->pref_vel, &c->replan_pos, &c->path_xy, &c->s_pos, &c->s_vel,
                        &c->rec_vorca};
     for (auto* b : v2s) b->free_();
@@ -307,6 +326,9 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
     c->d_speed.free_();
     c->s_clear.free_();
     c->d_active.free_();
+    c->feat.free_();
+    c->cls.free_();
+    c->label.free_();
     c->d_scenes.free_();
     for (auto& s : c->scenes) s->free_all();
     if (c->h_counters) cudaFreeHost(c->h_counters);
@@ -784,6 +806,12 @@ static ecmg_status ensure_grids(ecmg_ctx* c)
         c->table_dirty = false;
         c->graph_dirty = true;
     }
+    if (c->model || c->trace) {
+        size_t N = (size_t)c->max_agents;
+        CK(c->feat.alloc(N * kMlpIn * 2));
+        if (c->model) CK(c->cls.alloc(N));
+        if (c->trace) CK(c->label.alloc(N));
+    }
     if (c->record) {
         size_t N = (size_t)c->max_agents;
         int k = c->prm.max_neighbors;
@@ -793,7 +821,7 @@ static ecmg_status ensure_grids(ecmg_ctx* c)
     return ECMG_OK;
 }
 
-static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t)
+static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t, bool use_model)
 {
     b = BinArgs{};
     b.pos = c->pos.p;
@@ -851,6 +879,10 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t)
     t.replan_list = c->replan_list.p;
     t.replan_pos = c->replan_pos.p;
     t.list_cap = c->max_agents;
+    if (use_model || c->trace) t.feat = c->feat.p;
+    if (use_model) t.cls = c->cls.p;
+    t.cls_slot = c->cls_override;
+    if (c->trace) t.label = c->label.p;
     if (c->record) {
         t.rec_nbr = c->rec_nbr.p;
         t.rec_cnt = c->rec_cnt.p;
@@ -861,16 +893,37 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t)
     }
 }
 
+struct ProposeCall {
+    ecmg_mlp* model;
+    const void* feat;
+    const int* n_dev;
+    int n_max;
+    unsigned char* cls;
+    int sms;
+};
+
+static cudaError_t propose_cb(void* user, cudaStream_t s)
+{
+    const ProposeCall* pc = (const ProposeCall*)user;
+    return mlp_infer(pc->model, pc->feat, pc->n_dev, pc->n_max, pc->cls, s, pc->sms);
+}
+
 /* the device work of one tick: counters in, kernels, counters out */
-static cudaError_t enqueue_tick(ecmg_ctx* c, int launch_slots)
+static cudaError_t enqueue_tick(ecmg_ctx* c, int launch_slots, bool use_model)
 {
     BinArgs b;
     TickArgs t;
-    fill_args(c, b, t);
+    fill_args(c, b, t, use_model);
     cudaGetLastError(); /* launch errors below must not be confused with older ones */
     cudaError_t e = cudaMemcpyAsync(c->counters.p, c->h_counters, sizeof(int) * kCounters, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return e;
-    e = launch_tick(b, t, launch_slots, c->scan_tmp.p, c->block, c->sms, c->stream, c->ev_a0, c->ev_a1);
+    if (c->trace) {
+        e = cudaMemsetAsync(c->label.p, kClsOther, (size_t)launch_slots, c->stream);
+        if (e != cudaSuccess) return e;
+    }
+    ProposeCall pc{c->model, c->feat.p, c->counters.p + C_NSORTED, launch_slots, c->cls.p, c->sms};
+    e = launch_tick(b, t, launch_slots, c->scan_tmp.p, c->block, c->sms, c->stream, c->ev_a0, c->ev_a1,
+                    use_model ? propose_cb : nullptr, &pc);
     if (e != cudaSuccess) return e;
     return cudaMemcpyAsync(c->h_counters + kCounters, c->counters.p, sizeof(int) * kCounters, cudaMemcpyDeviceToHost,
                            c->stream);
@@ -880,8 +933,11 @@ void* ecmg_stream(const ecmg_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 int ecmg_kernels_per_tick(const ecmg_ctx* c)
 {
-    (void)c;
-    return 7; /* k_bin, k_scan_local, k_scan_top, k_scan_add, k_scatter, k_neighbors, k_agents */
+    /* k_bin, k_scan_local, k_scan_top, k_scan_add, k_scatter, k_attract,
+       k_neighbors, k_agents; k_features with a proposal model or a trace;
+       k_mlp_infer with a proposal model */
+    if (!c) return 8;
+    return 8 + ((c->model || c->trace) ? 1 : 0) + (c->model ? 1 : 0);
 }
 
 static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
@@ -890,6 +946,7 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         if (!scp->hs.has_ecm) return fail(c, ECMG_ERR_STATE, "every scene needs an ECM before ecmg_tick");
     ecmg_tick_stats st{};
     ecmg_status result = ECMG_OK;
+    if (c->model) CK(mlp_pack(c->model)); /* BF16 fragments of the current weights */
     for (int tk = 0; tk < n_ticks; tk++) {
         auto hs = std::chrono::steady_clock::now();
         /* UpdateMaxAgentIndex (Simulator.cpp:481-492), per scene */
@@ -905,25 +962,34 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         std::memset(c->h_counters, 0, sizeof(int) * kCounters);
         c->h_counters[C_LAST] = last;
         st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - hs).count();
+        const bool use_model = c->model && c->gate_left == 0;
+        if (c->model && !use_model) {
+            c->gate_left--;
+            st.gated++;
+        }
         CK(cudaEventRecord(c->ev_t0, c->stream));
         if (c->prm.use_graph) {
-            /* the graph bakes in launch sizes covering slots [0, max_agents) */
-            if (c->graph_dirty || !c->graph) {
-                if (c->graph) cudaGraphExecDestroy(c->graph);
-                c->graph = nullptr;
+            /* a graph bakes in launch sizes covering slots [0, max_agents) */
+            if (c->graph_dirty) {
+                for (auto& g : c->graph)
+                    if (g) cudaGraphExecDestroy(g);
+                c->graph[0] = c->graph[1] = nullptr;
+                c->graph_dirty = false;
+            }
+            cudaGraphExec_t& ge = c->graph[use_model ? 1 : 0];
+            if (!ge) {
                 cudaGraph_t g;
                 CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-                cudaError_t e = enqueue_tick(c, c->max_agents);
+                cudaError_t e = enqueue_tick(c, c->max_agents, use_model);
                 cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
                 if (e != cudaSuccess) return fail(c, ECMG_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
                 if (e2 != cudaSuccess) return fail(c, ECMG_ERR_CUDA, "end capture: %s", cudaGetErrorString(e2));
-                CK(cudaGraphInstantiate(&c->graph, g, 0));
+                CK(cudaGraphInstantiate(&ge, g, 0));
                 cudaGraphDestroy(g);
-                c->graph_dirty = false;
             }
-            CK(cudaGraphLaunch(c->graph, c->stream));
+            CK(cudaGraphLaunch(ge, c->stream));
         } else {
-            CK(enqueue_tick(c, last + 1));
+            CK(enqueue_tick(c, last + 1, use_model));
         }
         CK(cudaEventRecord(c->ev_t1, c->stream));
         CK(cudaStreamSynchronize(c->stream));
@@ -938,6 +1004,11 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         int nd = out[C_DESTROYED], nr = out[C_REPLAN];
         st.agent_steps += out[C_NSORTED];
         st.lp3d += out[C_LP3D];
+        st.proposed += out[C_PROPOSED];
+        st.accepted += out[C_ACCEPTED];
+        if (use_model && c->gate_min > 0.0f && (float)out[C_ACCEPTED] < c->gate_min * (float)out[C_NSORTED])
+            c->gate_left = c->gate_pause;
+        c->trace_rows = out[C_NSORTED];
         st.destroyed += nd;
         st.replans += nr;
         if (out[C_ERROR]) {
@@ -1194,6 +1265,61 @@ ecmg_status ecmg_set_record(ecmg_ctx* c, int on)
     if (!c) return ECMG_ERR_INVALID_ARG;
     c->record = on != 0;
     c->graph_dirty = true;
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_set_proposal(ecmg_ctx* c, ecmg_mlp* model)
+{
+    if (!c) return ECMG_ERR_INVALID_ARG;
+    if (model != c->model) {
+        c->model = model;
+        c->gate_left = 0;
+        c->graph_dirty = true;
+    }
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_set_proposal_gate(ecmg_ctx* c, float min_accept_rate, int pause_ticks)
+{
+    if (!c || !(min_accept_rate >= 0.0f && min_accept_rate <= 1.0f) || pause_ticks < 0) return ECMG_ERR_INVALID_ARG;
+    c->gate_min = min_accept_rate;
+    c->gate_pause = pause_ticks;
+    c->gate_left = 0;
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_set_trace(ecmg_ctx* c, int on)
+{
+    if (!c) return ECMG_ERR_INVALID_ARG;
+    if ((on != 0) != c->trace) {
+        c->trace = on != 0;
+        c->trace_rows = 0;
+        c->graph_dirty = true;
+    }
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_set_proposal_classes(ecmg_ctx* c, const unsigned char* dev_cls_by_slot)
+{
+    if (!c) return ECMG_ERR_INVALID_ARG;
+    if (dev_cls_by_slot != c->cls_override) {
+        c->cls_override = dev_cls_by_slot;
+        c->graph_dirty = true;
+    }
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_get_trace(ecmg_ctx* c, void* feat_dst, unsigned char* label_dst, int* slot_dst, int cap,
+                           int* n_rows)
+{
+    if (!c || cap < 0) return ECMG_ERR_INVALID_ARG;
+    if (!c->trace || !c->label.p) return fail(c, ECMG_ERR_STATE, "tracing is off");
+    CK(cudaStreamSynchronize(c->stream));
+    int n = std::min(cap, c->trace_rows);
+    if (n > 0 && feat_dst) CK(cudaMemcpy(feat_dst, c->feat.p, (size_t)n * kMlpIn * 2, cudaMemcpyDefault));
+    if (n > 0 && label_dst) CK(cudaMemcpy(label_dst, c->label.p, (size_t)n, cudaMemcpyDefault));
+    if (n > 0 && slot_dst) CK(cudaMemcpy(slot_dst, c->s_slot.p, sizeof(int) * n, cudaMemcpyDefault));
+    if (n_rows) *n_rows = n;
     return ECMG_OK;
 }
 

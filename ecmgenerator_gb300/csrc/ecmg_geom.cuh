@@ -495,11 +495,20 @@ EG_HD Con agent_constraint(V2 position, V2 velocity, float clr, V2 np, V2 nv, fl
     return c;
 }
 
+/* Which update produced an LP result: the last constraint whose line the
+   solution was moved onto (-1: none) and what fixed the position on it. */
+struct LpTrace {
+    int h = -1;
+    int src = 0; /* 0 projection of opt, 1 circle bound, 2 bound from constraint j */
+    int j = -1;
+};
+
 /* ORCA::RandomizedLP (ORCA.cpp:428-587).  The constraint at index i is
    fetched through get(i) so that callers may keep constraints in registers,
-   shared or local memory. */
-template <class Get>
-EG_HD int lp2d(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2* out)
+   shared or local memory.  With TRACE the last update is recorded in *tr
+   (bookkeeping only; the arithmetic is the same). */
+template <class Get, bool TRACE = false>
+EG_HD int lp2d(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2* out, LpTrace* tr = nullptr)
 {
     if (useDirOpt) *out = opt * maxSpeed;
     else if (len(opt) > maxSpeed) *out = normalized(opt) * maxSpeed;
@@ -515,6 +524,7 @@ EG_HD int lp2d(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2
         float sq = sqrtf(disc);
         float lo = -dirPointDot - sq;
         float hi = -dirPointDot + sq;
+        int lo_src = -1, hi_src = -1;
         for (int j = 0; j < i; j++) {
             Con g = get(j);
             float den = det(right(h.n), right(g.n));
@@ -524,8 +534,13 @@ EG_HD int lp2d(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2
                 continue;
             }
             const float t = num / den;
-            if (den >= 0.0f) hi = (t < hi) ? t : hi; /* std::min(right, t) */
-            else lo = (lo < t) ? t : lo;             /* std::max(left, t)  */
+            if (den >= 0.0f) { /* std::min(right, t) */
+                if (TRACE && t < hi) hi_src = j;
+                hi = (t < hi) ? t : hi;
+            } else { /* std::max(left, t) */
+                if (TRACE && lo < t) lo_src = j;
+                lo = (lo < t) ? t : lo;
+            }
             if (lo > hi) return i;
         }
         if (useDirOpt) {
@@ -533,9 +548,16 @@ EG_HD int lp2d(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2
             else *out = h.p + right(h.n) * lo;
         } else {
             float t = dot(right(h.n), opt - h.p);
-            if (t < lo) *out = h.p + right(h.n) * lo;
-            else if (t > hi) *out = h.p + right(h.n) * hi;
-            else *out = h.p + right(h.n) * t;
+            if (t < lo) {
+                *out = h.p + right(h.n) * lo;
+                if (TRACE) { tr->h = i; tr->src = lo_src < 0 ? 1 : 2; tr->j = lo_src; }
+            } else if (t > hi) {
+                *out = h.p + right(h.n) * hi;
+                if (TRACE) { tr->h = i; tr->src = hi_src < 0 ? 1 : 2; tr->j = hi_src; }
+            } else {
+                *out = h.p + right(h.n) * t;
+                if (TRACE) { tr->h = i; tr->src = 0; tr->j = -1; }
+            }
         }
     }
     return n;

@@ -17,6 +17,19 @@ namespace ecmg {
 constexpr int kMaxObstCons = 24;
 constexpr int kMaxK = 32;
 
+/* Learned active-set proposal (mlp.cu).  Features: 16 neighbours x 5 + 2,
+   zero-padded to kMlpIn.  Classes of an agent's 2D LP result, in terms of
+   its neighbour half-planes q (constraint index nObst + q):
+     kClsPref          no half-plane moved the initial velocity
+     kClsSingle + q    projection of the preferred velocity onto q
+     kClsPair + p      q_hi's line, bounded by q_lo's (q_lo < q_hi),
+                       p = q_hi * (q_hi - 1) / 2 + q_lo
+     kClsCircle + q    q's line, bounded by the speed circle
+     kClsOther         anything else (obstacle half-plane, neighbour >= 16,
+                       infeasible 2D LP) */
+constexpr int kMlpIn = 96, kMlpHid = 128, kMlpOut = 160, kMlpNbrs = 16;
+constexpr int kClsPref = 0, kClsSingle = 1, kClsPair = 17, kClsCircle = 137, kClsOther = 153;
+
 /* device counters (int[kCounters]) */
 enum {
     C_DESTROYED = 0,
@@ -27,6 +40,8 @@ enum {
     C_WORK = 5,        /* work counter of the persistent agent kernel */
     C_LAST = 6,        /* last slot index to scan (host-written before the tick) */
     C_NSORTED = 7,     /* agents in the neighbour grid */
+    C_PROPOSED = 8,    /* LPs that received a learned proposal */
+    C_ACCEPTED = 9,    /* proposals that passed the exact check */
     kCounters = 16
 };
 
@@ -73,6 +88,10 @@ struct TickArgs {
     const int* cell_start; /* total buckets + 1 */
     int* nbr;              /* [n * k] neighbours of grid-order agent t, as grid-order indices */
     int* ncnt;             /* [n] neighbour count */
+    void* feat;            /* [n, kMlpIn] bf16 proposal features (learned mode / tracing) */
+    const unsigned char* cls; /* [n] proposed class (null: plain LP) */
+    const unsigned char* cls_slot; /* [slots] proposed class by slot (overrides cls) */
+    unsigned char* label;  /* [n] class of the LP result (null: not traced) */
     const SceneDev* scenes;
     const int* slot_scene; /* slot -> scene (null: one scene) */
     int tile;              /* agents a warp takes per work grab (multiple of 32) */
@@ -115,9 +134,11 @@ struct BinArgs {
     int total_buckets;        /* sum over scenes of (cells + overflow) */
 };
 
-/* kernels.cu */
+/* kernels.cu; propose (may be null) runs between the feature kernel and the
+   per-agent kernel and fills TickArgs::cls */
+typedef cudaError_t (*ProposeFn)(void* user, cudaStream_t s);
 cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int block, int sms,
-                        cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1);
+                        cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1, ProposeFn propose, void* propose_user);
 cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k, float r, AgentGrid g,
                        int* key, int* rank, int* cell_count, int* cell_start, int* s_slot, V2* s_pos,
                        int* scan_tmp, int scan_blocks, int* out_ids, int* out_cnt, cudaStream_t s);

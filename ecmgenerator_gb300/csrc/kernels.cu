@@ -18,6 +18,7 @@
  */
 #include "ecmg_internal.h"
 
+#include <cuda_bf16.h>
 #include <stdint.h>
 
 namespace ecmg {
@@ -242,6 +243,132 @@ struct LocalGet {
     __device__ Con operator()(int i) const { return c[i]; }
 };
 
+/* adds the number of lanes with pred set to *ctr with one atomic per warp */
+__device__ __forceinline__ void warp_count(int* ctr, bool pred)
+{
+    unsigned m = __activemask();
+    unsigned b = __ballot_sync(m, pred);
+    if ((threadIdx.x & 31) == __ffs(m) - 1 && b) atomicAdd(ctr, __popc(b));
+}
+
+/* class of an LP result for the proposal's training labels (kCls*) */
+__device__ __forceinline__ int label_of(const LpTrace& tr, int failed, int m, int nObst)
+{
+    if (failed < m) return kClsOther;
+    if (tr.h < 0) return kClsPref;
+    int q = tr.h - nObst;
+    if (q < 0 || q >= kMlpNbrs) return kClsOther;
+    if (tr.src == 0) return kClsSingle + q;
+    if (tr.src == 1) return kClsCircle + q;
+    int qj = tr.j - nObst;
+    if (qj < 0) return kClsOther;
+    return kClsPair + q * (q - 1) / 2 + qj;
+}
+
+/* Exact check of a proposed active set.  Returns true only when the
+   incremental LP (lp2d, ORCA.cpp:428-587) provably ends with its last update
+   on the proposed half-plane h, fixed by the proposed bound; *out is then
+   computed with the LP's own final-step formula, so it is the LP's result.
+   Conditions: the bounds of h over every earlier half-plane and the speed
+   circle reproduce the proposed source; every later half-plane contains the
+   point (the LP's own test); the KKT multipliers of the proposed active set
+   are positive and every other earlier half-plane is slack, both by a margin,
+   so that the LP state before h violates h. */
+template <class Get>
+__device__ __noinline__ bool verify_proposal(const Get& get, int m, int nObst, int ncnt, V2 opt, float maxSpeed,
+                                             int cls, V2* out)
+{
+    const float margin = 1e-4f;
+    if (cls == kClsPref) {
+        V2 v0 = (len(opt) > maxSpeed) ? normalized(opt) * maxSpeed : opt;
+        for (int i = 0; i < m; i++) {
+            Con c = get(i);
+            if (det(right(c.n), c.p - v0) > 0.0f) return false;
+        }
+        *out = v0;
+        return true;
+    }
+    int q, qj = -1, kind; /* kind 0 single, 1 circle, 2 pair */
+    if (cls >= kClsSingle && cls < kClsPair) { q = cls - kClsSingle; kind = 0; }
+    else if (cls >= kClsCircle && cls < kClsOther) { q = cls - kClsCircle; kind = 1; }
+    else if (cls >= kClsPair && cls < kClsCircle) {
+        int p = cls - kClsPair;
+        q = 1;
+        while ((q + 1) * q / 2 <= p) q++; /* q*(q-1)/2 <= p < (q+1)*q/2 */
+        qj = p - q * (q - 1) / 2;
+        kind = 2;
+    } else return false;
+    if (q >= ncnt || q >= kMlpNbrs) return false;
+    const int h = nObst + q, jsrc = kind == 2 ? nObst + qj : -1;
+    if (h >= m) return false;
+    Con H = get(h);
+    V2 dir = right(H.n);
+    float dpd = dot(dir, H.p);
+    float disc = dpd * dpd + maxSpeed * maxSpeed - dot(H.p, H.p);
+    if (disc <= 0.0f) return false;
+    float sq = sqrtf(disc);
+    float lo = -dpd - sq, hi = -dpd + sq;
+    int lo_src = -1, hi_src = -1;
+    for (int j = 0; j < h; j++) {
+        Con G = get(j);
+        float den = det(right(H.n), right(G.n));
+        float num = det(right(G.n), H.p - G.p);
+        if (fabsf(den) <= kEps) {
+            if (num < 0.0f) return false;
+            continue;
+        }
+        const float t = num / den;
+        if (den >= 0.0f) {
+            if (t < hi) hi_src = j;
+            hi = (t < hi) ? t : hi;
+        } else {
+            if (lo < t) lo_src = j;
+            lo = (lo < t) ? t : lo;
+        }
+    }
+    if (lo > hi) return false;
+    float t = dot(dir, opt - H.p);
+    V2 v;
+    int src; /* -2 projection, -1 circle, else constraint index */
+    if (t < lo) { v = H.p + dir * lo; src = lo_src; }
+    else if (t > hi) { v = H.p + dir * hi; src = hi_src; }
+    else { v = H.p + dir * t; src = -2; }
+    if (kind == 0 && src != -2) return false;
+    if (kind == 1 && src != -1) return false;
+    if (kind == 2 && src != jsrc) return false;
+    for (int i = h + 1; i < m; i++) {
+        Con c = get(i);
+        if (det(right(c.n), c.p - v) > 0.0f) return false;
+    }
+    /* KKT of min |v - opt|^2 s.t. dot(N_i, v - P_i) >= 0, |v| <= maxSpeed */
+    V2 r = v - opt;
+    if (kind != 1) { /* the speed circle must be slack as well */
+        float rs = maxSpeed - margin;
+        if (!(rs > 0.0f && dot(v, v) < rs * rs)) return false;
+    }
+    if (kind == 0) {
+        if (!(dot(r, H.n) > margin)) return false;
+    } else if (kind == 2) {
+        Con G = get(jsrc);
+        float d2 = det(H.n, G.n);
+        float la = det(r, G.n) / d2, lb = det(H.n, r) / d2;
+        if (!(la > margin && lb > margin)) return false;
+    } else {
+        V2 nv = v * -1.0f;
+        float d2 = det(H.n, nv);
+        if (!(fabsf(d2) > kEps)) return false;
+        float la = det(r, nv) / d2, lb = det(H.n, r) / d2;
+        if (!(la > margin && lb > margin * maxSpeed)) return false;
+    }
+    for (int i = 0; i < h; i++) {
+        if (i == jsrc) continue;
+        Con c = get(i);
+        if (!(det(right(c.n), c.p - v) < -margin)) return false;
+    }
+    *out = v;
+    return true;
+}
+
 /* out-of-line copies keep the per-agent kernel small enough for the
    instruction cache: each is called from a loop or a rare branch */
 __device__ __noinline__ Con agent_constraint_ni(V2 position, V2 velocity, float clr, V2 np, V2 nv, float nclr,
@@ -259,13 +386,11 @@ __device__ __noinline__ void lp3d_local(const Con* cons, int m, int nObst, float
     lp3d(get, m, nObst, maxSpeed, failed, v, proj, fp64);
 }
 
-template <int K>
-__device__ void agent_tick(const TickArgs& a, int t)
+/* attraction point and preferred velocity of grid-order agent t */
+__device__ void attract_tick(const TickArgs& a, int t)
 {
     const int slot = a.s_slot[t];
     const V2 pos = a.s_pos[t];
-    const V2 vel = a.s_vel[t];
-    const float clr = a.s_clear[t];
     const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
 
     /* UpdateAttractionPointSystem (Simulator.cpp:538-590) */
@@ -303,6 +428,21 @@ __device__ void agent_tick(const TickArgs& a, int t)
     const float speed = a.speed[slot];
     V2 pv = normalize(attr - pos) * speed;
     a.pref_vel[slot] = pv;
+}
+
+/* ApplyObstacleAvoidanceForce + UpdateVelocitySystem + UpdatePositionSystem
+   of grid-order agent t (agents destroyed this tick are skipped) */
+template <int K>
+__device__ void orca_tick(const TickArgs& a, int t)
+{
+    const int slot = a.s_slot[t];
+    if (!a.active[slot]) return;
+    const V2 pos = a.s_pos[t];
+    const V2 vel = a.s_vel[t];
+    const float clr = a.s_clear[t];
+    const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
+    const float speed = a.speed[slot];
+    const V2 pv = a.pref_vel[slot];
 
     /* ORCA::GetVelocity (ORCA.cpp:14-57) with maxSpeed = preferred speed
        (Simulator.cpp:671) unless a global maximum is configured */
@@ -347,11 +487,29 @@ __device__ void agent_tick(const TickArgs& a, int t)
 
     V2 v;
     LocalGet get{cons};
-    int failed = lp2d(get, m, pv, maxSpeed, false, &v);
-    if (failed < m) {
-        lp3d_local<MC>(cons, m, nObst, maxSpeed, failed, &v, a.lp3d_fp64 != 0);
-        atomicAdd(&a.counters[C_LP3D], 1);
+    int failed = -1;
+    if (a.cls || a.cls_slot) { /* learned proposal: accepted only when the exact check passes */
+        const int c = a.cls_slot ? a.cls_slot[slot] : a.cls[t];
+        bool ok = c != kClsOther && verify_proposal(get, m, nObst, ncnt, pv, maxSpeed, c, &v);
+        if (ok) failed = m;
+        warp_count(&a.counters[C_PROPOSED], c != kClsOther);
+        warp_count(&a.counters[C_ACCEPTED], ok);
     }
+    bool need3d = false;
+    if (failed < 0) {
+        if (a.label) {
+            LpTrace tr;
+            failed = lp2d<LocalGet, true>(get, m, pv, maxSpeed, false, &v, &tr);
+            a.label[t] = (unsigned char)label_of(tr, failed, m, nObst);
+        } else {
+            failed = lp2d(get, m, pv, maxSpeed, false, &v);
+        }
+        if (failed < m) {
+            lp3d_local<MC>(cons, m, nObst, maxSpeed, failed, &v, a.lp3d_fp64 != 0);
+            need3d = true;
+        }
+    }
+    warp_count(&a.counters[C_LP3D], need3d);
 
     /* force = vOrca - v (Simulator.cpp:676-677); UpdateVelocitySystem
        (Simulator.cpp:619-635); UpdatePositionSystem (Simulator.cpp:592-606) */
@@ -390,6 +548,67 @@ __global__ void __launch_bounds__(128) k_neighbors(TickArgs a)
     }
 }
 
+/* UpdateAttractionPointSystem + ApplySteeringForce for every agent */
+__global__ void __launch_bounds__(128) k_attract(TickArgs a)
+{
+    const int n = a.counters[C_NSORTED];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) attract_tick(a, t);
+}
+
+/* proposal features of every grid-order agent (zeros for agents destroyed
+   this tick): 16 neighbours x (relative position / neighbour distance,
+   relative velocity / 2, radius sum), preferred velocity / LP radius */
+__global__ void __launch_bounds__(128) k_features(TickArgs a)
+{
+    const int n = a.counters[C_NSORTED];
+    __nv_bfloat16* F = (__nv_bfloat16*)a.feat;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        float f[kMlpIn];
+#pragma unroll
+        for (int i = 0; i < kMlpIn; i++) f[i] = 0.0f;
+        const int slot = a.s_slot[t];
+        if (a.active[slot]) {
+            const V2 pos = a.s_pos[t], vel = a.s_vel[t];
+            const float clr = a.s_clear[t];
+            const float speed = a.speed[slot];
+            const float maxSpeed = a.max_speed > 0.0f ? a.max_speed : speed;
+            const int ncnt = a.ncnt[t];
+            const int* nbr = a.nbr + (size_t)t * a.k;
+            const float inv_r = 1.0f / a.rnb;
+#pragma unroll
+            for (int q = 0; q < kMlpNbrs; q++) {
+                if (q < ncnt) {
+                    int j = nbr[q];
+                    V2 pj = a.s_pos[j], vj = a.s_vel[j];
+                    f[5 * q + 0] = (pj.x - pos.x) * inv_r;
+                    f[5 * q + 1] = (pj.y - pos.y) * inv_r;
+                    f[5 * q + 2] = (vel.x - vj.x) * 0.5f;
+                    f[5 * q + 3] = (vel.y - vj.y) * 0.5f;
+                    f[5 * q + 4] = a.s_clear[j] + clr;
+                }
+            }
+            V2 pv = a.pref_vel[slot];
+            float im = maxSpeed > 0.0f ? 1.0f / maxSpeed : 0.0f;
+            f[5 * kMlpNbrs] = pv.x * im;
+            f[5 * kMlpNbrs + 1] = pv.y * im;
+        }
+        uint4* row = reinterpret_cast<uint4*>(F + (size_t)t * kMlpIn);
+#pragma unroll
+        for (int c = 0; c < kMlpIn / 8; c++) {
+            __nv_bfloat162 h0 = __floats2bfloat162_rn(f[8 * c + 0], f[8 * c + 1]);
+            __nv_bfloat162 h1 = __floats2bfloat162_rn(f[8 * c + 2], f[8 * c + 3]);
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(f[8 * c + 4], f[8 * c + 5]);
+            __nv_bfloat162 h3 = __floats2bfloat162_rn(f[8 * c + 6], f[8 * c + 7]);
+            uint4 u;
+            u.x = *reinterpret_cast<unsigned*>(&h0);
+            u.y = *reinterpret_cast<unsigned*>(&h1);
+            u.z = *reinterpret_cast<unsigned*>(&h2);
+            u.w = *reinterpret_cast<unsigned*>(&h3);
+            row[c] = u;
+        }
+    }
+}
+
 /* persistent kernel: a warp takes `tile` consecutive grid-order agents per
    work grab (one atomic per grab) and runs them 32 at a time */
 template <int K>
@@ -404,7 +623,7 @@ __global__ void __launch_bounds__(256) k_agents(TickArgs a)
         if (base >= n) break;
         for (int o = 0; o < a.tile; o += 32) {
             int t = base + o + lane;
-            if (t < n) agent_tick<K>(a, t);
+            if (t < n) orca_tick<K>(a, t);
         }
     }
 }
@@ -436,7 +655,7 @@ static int grid_for(int n, int block, int sms, int per_sm)
 }
 
 cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int block, int sms,
-                        cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1)
+                        cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1, ProposeFn propose, void* propose_user)
 {
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(s, &cap);
@@ -454,16 +673,24 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
     if (block != 64 && block != 128 && block != 256) block = 128;
     int gk = grid_for(max_slots, 128, sms, 16);
     int per_sm = 1;
+    k_attract<<<gk, 128, 0, s>>>(t);
+    if (t.k <= 8) k_neighbors<8><<<gk, 128, 0, s>>>(t);
+    else if (t.k <= 16) k_neighbors<16><<<gk, 128, 0, s>>>(t);
+    else k_neighbors<32><<<gk, 128, 0, s>>>(t);
+    if (t.feat) {
+        k_features<<<gk, 128, 0, s>>>(t);
+        if (propose) {
+            cudaError_t e2 = propose(propose_user, s);
+            if (e2 != cudaSuccess) return e2;
+        }
+    }
     if (t.k <= 8) {
-        k_neighbors<8><<<gk, 128, 0, s>>>(t);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<8>, block, 0);
         k_agents<8><<<sms * (per_sm > 0 ? per_sm : 1), block, 0, s>>>(t);
     } else if (t.k <= 16) {
-        k_neighbors<16><<<gk, 128, 0, s>>>(t);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<16>, block, 0);
         k_agents<16><<<sms * (per_sm > 0 ? per_sm : 1), block, 0, s>>>(t);
     } else {
-        k_neighbors<32><<<gk, 128, 0, s>>>(t);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<32>, block, 0);
         k_agents<32><<<sms * (per_sm > 0 ? per_sm : 1), block, 0, s>>>(t);
     }

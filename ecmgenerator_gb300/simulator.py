@@ -263,6 +263,51 @@ class Simulator:
         return d
 
 
+    # -- learned active-set proposal ---------------------------------------
+    def set_proposal(self, model):
+        """model: proposal.ProposalModel or None (plain LP)"""
+        self._ck(self.L.ecmg_set_proposal(self.h, model.h if model is not None else None))
+        self._proposal = model
+
+    def set_proposal_gate(self, min_accept_rate: float = 0.1, pause_ticks: int = 64):
+        self._ck(self.L.ecmg_set_proposal_gate(self.h, float(min_accept_rate), int(pause_ticks)))
+
+    def set_proposal_classes(self, cls_by_slot):
+        """proposals per slot from a CUDA uint8 tensor (None: off)"""
+        ptr = None
+        if cls_by_slot is not None:
+            if not cls_by_slot.is_cuda or cls_by_slot.numel() < self.max_agents:
+                raise ValueError("expected a CUDA uint8 tensor with one class per slot")
+            ptr = cls_by_slot.data_ptr()
+        self._ck(self.L.ecmg_set_proposal_classes(self.h, ptr))
+        self._proposal_classes = cls_by_slot
+
+    def set_trace(self, on: bool = True):
+        self._ck(self.L.ecmg_set_trace(self.h, int(on)))
+
+    def get_trace(self, device: bool = False):
+        """(features bf16 [n, 96], labels uint8 [n], slots int32 [n]) of the
+        last tick in grid order: CUDA tensors with device=True, else numpy
+        (features as the raw bf16 bit patterns, uint16)"""
+        n = C.c_int()
+        self._ck(self.L.ecmg_get_trace(self.h, None, None, None, 0, C.byref(n)))
+        cap = self.max_agents
+        if device:
+            import torch
+            x = torch.empty((cap, 96), dtype=torch.bfloat16, device="cuda")
+            y = torch.empty(cap, dtype=torch.uint8, device="cuda")
+            sl = torch.empty(cap, dtype=torch.int32, device="cuda")
+            self._ck(self.L.ecmg_get_trace(self.h, x.data_ptr(), y.data_ptr(), sl.data_ptr(), cap, C.byref(n)))
+            m = n.value
+            return x[:m], y[:m], sl[:m]
+        x = np.zeros((cap, 96), np.uint16)
+        y = np.zeros(cap, U8)
+        sl = np.zeros(cap, I32)
+        self._ck(self.L.ecmg_get_trace(self.h, _ptr(x), _ptr(y), _ptr(sl), cap, C.byref(n)))
+        m = n.value
+        return x[:m], y[:m], sl[:m]
+
+
 class BatchSimulator(Simulator):
     """Many independent scenes advanced by one launch sequence per tick
     (ecmg_create_batch).  Scene s owns global slots

@@ -72,6 +72,9 @@ typedef struct {
     float device_ms;       /* device time of the ticks (CUDA events)              */
     float agent_kernel_ms; /* device time of the neighbour + per-agent kernels    */
     float host_ms;         /* host time between ticks (bookkeeping, re-planning)  */
+    long long proposed;    /* learned mode: LPs that received an active-set proposal */
+    long long accepted;    /* learned mode: proposals that passed the exact check     */
+    long long gated;       /* learned mode: ticks run without the model (gate closed) */
 } ecmg_tick_stats;
 
 /* Static obstacles: n_obstacles rings, ring r = xy[2*ring_offsets[r] ..
@@ -252,6 +255,61 @@ ecmg_status ecmg_knn(const float* dev_pos, const unsigned char* dev_active, int 
 ecmg_status ecmg_knn_noalloc(const float* dev_pos, const unsigned char* dev_active, int n, int k, float radius,
                              float min_x, float min_y, float max_x, float max_y, float cell,
                              int* dev_out_ids, int* dev_out_count, void* stream);
+
+/* ---- learned active-set proposal (no reference counterpart) --------------
+   A small MLP (96 inputs: 16 sorted neighbours x (relative position /
+   neighbor_dist, relative velocity / 2, radius sum) + preferred velocity /
+   LP radius, zero-padded; two hidden layers of 128 with GELU; 160 classes)
+   proposes which constraints bound the optimum of an agent's 2D LP
+   (ORCA.cpp:428-587): none, the projection onto neighbour q's half-plane,
+   q's line bounded by neighbour p's, or q's line bounded by the speed
+   circle.  The tick checks every proposal exactly (the proposed last update
+   of the incremental LP, containment by every later half-plane, KKT
+   multipliers and slack of the rest) and runs the full LP when the check
+   fails.  Inference runs in BF16 on the tensor cores with FP32 accumulation;
+   training (FP32 master weights, Adam) runs on the GPU in this library. */
+typedef struct ecmg_mlp ecmg_mlp;
+#define ECMG_MLP_IN 96
+#define ECMG_MLP_CLASSES 160
+ecmg_status ecmg_mlp_create(unsigned long long seed, ecmg_mlp** out);
+ecmg_status ecmg_mlp_destroy(ecmg_mlp* model);
+int ecmg_mlp_param_count(void);
+/* parameters as one float array: W1 [96x128] row-major, b1 [128],
+   W2 [128x128], b2 [128], W3 [128x160], b3 [160] */
+ecmg_status ecmg_mlp_get_params(ecmg_mlp* model, float* host_out);
+ecmg_status ecmg_mlp_set_params(ecmg_mlp* model, const float* host_in);
+/* mean softmax cross-entropy and its gradient (host float[param_count]) over
+   all n rows; dev_x: bf16 [n x 96], dev_y: class per row (device memory) */
+ecmg_status ecmg_mlp_loss_grad(ecmg_mlp* model, const void* dev_x, const unsigned char* dev_y, int n,
+                               float* loss, float* host_grad);
+/* `steps` Adam steps on minibatches of `batch` rows drawn with replacement
+   from the n rows (seeded); per-step loss / accuracy to host arrays if given */
+ecmg_status ecmg_mlp_train(ecmg_mlp* model, const void* dev_x, const unsigned char* dev_y, int n, int steps,
+                           int batch, float lr, unsigned long long seed, float* host_loss, float* host_acc);
+/* class of every row (argmax of the BF16 tensor-core forward) */
+ecmg_status ecmg_mlp_predict(ecmg_mlp* model, const void* dev_x, int n, unsigned char* dev_cls);
+
+/* Learned mode for a context: model != NULL turns it on (the context does
+   not own the model; keep it alive while it is set), NULL turns it off.
+   Results are those of the plain LP whether or not a proposal is accepted. */
+ecmg_status ecmg_set_proposal(ecmg_ctx* ctx, ecmg_mlp* model);
+/* Gate of the learned mode: a tick whose accepted proposals are fewer than
+   min_accept_rate x its agents runs the next pause_ticks ticks without the
+   model (no features, no inference), then tries it again.  Default 0.1 / 64;
+   min_accept_rate 0 keeps the model on every tick. */
+ecmg_status ecmg_set_proposal_gate(ecmg_ctx* ctx, float min_accept_rate, int pause_ticks);
+/* Trace mode: every tick also writes, for each agent in grid order, its
+   proposal features and the class of its plain LP result (training data). */
+ecmg_status ecmg_set_trace(ecmg_ctx* ctx, int on);
+/* the last tick's trace: rows of bf16 [96] features, class labels and the
+   agent slot of each row, copied to dst pointers in host or device memory
+   (any may be NULL; at most cap rows; *n_rows set) */
+ecmg_status ecmg_get_trace(ecmg_ctx* ctx, void* feat_dst, unsigned char* label_dst, int* slot_dst, int cap,
+                           int* n_rows);
+/* Proposals given per agent slot (device array of max_agents classes)
+   instead of by a model, e.g. the labels of a trace; NULL turns it off.
+   Exercises the exact check with known answers. */
+ecmg_status ecmg_set_proposal_classes(ecmg_ctx* ctx, const unsigned char* dev_cls_by_slot);
 
 #ifdef __cplusplus
 }
