@@ -171,6 +171,29 @@ def load_or_train_model(sim, args):
     return m, info
 
 
+def apply_launch(plain, learned, args):
+    """launch configuration of the per-agent kernel: autotuned on the plain
+    simulator's current state (restored afterwards), or fixed by --lp-mode"""
+    from ecmgenerator_gb300.simulator import autotune, set_launch, set_lp_mode
+
+    if args.lp_mode == "tune":
+        r = autotune(plain, ticks_per_trial=1)
+        log(f"[bench] autotune: {r}")
+        grab = r["agents_per_warp_grab"]
+        for s_ in (plain, learned):
+            if r["lp_mode"] == "warp":
+                set_launch(s_, 128, 32, r["grid_cell_scale"])
+                set_lp_mode(s_, "warp", grab)
+            else:
+                set_launch(s_, r["block_size"], grab, r["grid_cell_scale"])
+                set_lp_mode(s_, "thread", 1)
+        return r
+    grab = 4 if args.lp_mode == "warp" else 32
+    for s_ in (plain, learned):
+        set_lp_mode(s_, args.lp_mode, grab if args.lp_mode == "warp" else 1)
+    return {"lp_mode": args.lp_mode, "agents_per_warp_grab": grab}
+
+
 class TickTimer:
     """CUDA events on the library's stream around each tick, L2 flushed
     (512 MB write, > 129 MB L2) before every timed tick."""
@@ -230,6 +253,9 @@ def run_ours(args):
         sims.append(s_)
     plain, learned = sims
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    plain.update()
+    learned.update()
+    launch = apply_launch(plain, learned, args)
     for _ in range(args.warmup):
         plain.update()
         learned.update()
@@ -307,7 +333,8 @@ def run_ours(args):
         "config": {"workload": args.workload, "agents": n, "max_neighbors": k, "neighbor_dist_m": 5.0,
                    "time_horizon_s": 2.0, "dt_s": DT, "scene": f'{cfg["w"]:.0f}x{cfg["h"]:.0f} m, {cfg["boxes"]} boxes',
                    "l2": "flushed before every timed tick (512 MB write)", "parallelism": f"replicas x{world}",
-                   "seed": args.seed, "mode": "learned proposal" if model is not None else "plain"},
+                   "seed": args.seed, "mode": "learned proposal" if model is not None else "plain",
+                   "launch": launch},
         "plain": {"value": plain_value, "ms_per_step": p_ms_all / args.steps,
                   "lp3d_per_tick": tp.tot["lp3d"] / args.steps},
         "learned_vs_plain": value / plain_value if model is not None else None,
@@ -377,6 +404,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="time the plain tick only")
     ap.add_argument("--proposal", default=None, help="proposal weights (.npy)")
+    ap.add_argument("--lp-mode", default="tune", choices=["tune", "thread", "warp"],
+                    help="per-agent kernel layout (default: autotuned)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

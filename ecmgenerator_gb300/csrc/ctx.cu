@@ -101,6 +101,8 @@ struct ecmg_ctx {
     int block = 128;
     int tile = 32;
     float cell_scale = 0.4f;
+    int lp_mode = 0; /* 0: one thread per agent, 1: one warp per agent */
+    int wgrab = 4;   /* agents per work grab in warp mode */
 
     /* host mirrors (Simulator bookkeeping, Simulator.h:164-171) */
     std::vector<unsigned char> active;
@@ -861,7 +863,8 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t, bool use_model)
     t.ncnt = c->ncnt.p;
     t.scenes = c->d_scenes.p;
     t.slot_scene = b.slot_scene;
-    t.tile = c->tile;
+    t.tile = c->lp_mode ? c->wgrab : c->tile;
+    t.lp_mode = c->lp_mode;
     const ecmg_params& p = c->prm;
     t.dt = p.dt;
     t.tau_a = p.tau_agent;
@@ -1128,8 +1131,9 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
     };
     const int blocks[] = {64, 128, 256};
     const int tiles[] = {32, 64, 128};
+    const int wgrabs[] = {1, 2, 4, 8};
     const float scales[] = {0.3f, 0.4f, 0.5f, 0.6f, 0.8f};
-    int bb = c->block, bt = c->tile;
+    int bb = c->block, bt = c->tile, bmode = c->lp_mode, bw = c->wgrab;
     float bs = c->cell_scale, best = 1e30f;
     const bool fixed_cell = c->prm.grid_cell > 0.0f;
     c->replan_enabled = false;
@@ -1138,40 +1142,69 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
         if (fixed_cell && sc != scales[0]) break;
         c->cell_scale = sc;
         for (auto& s : c->scenes) s->grid_ready = false;
-        for (int b : blocks) {
-            if (c->prm.block_size && b != c->prm.block_size) continue;
-            for (int t : tiles) {
-                c->block = b;
-                c->tile = t;
-                c->graph_dirty = true;
-                ecmg_tick_stats ts{};
-                ecmg_status st = run_ticks(c, 1, &ts); /* warm-up and graph capture */
-                if (st == ECMG_OK) st = run_ticks(c, ticks_per_trial, &ts);
-                ecmg_status rs = restore();
-                if (st != ECMG_OK || rs != ECMG_OK) {
-                    c->replan_enabled = true;
-                    return st != ECMG_OK ? st : rs;
+        /* per-thread mode: block x work grab; warp mode: work grab */
+        for (int mode = 0; mode < 2; mode++) {
+            const int nb = mode ? 1 : 3, nt = 4;
+            for (int bi = 0; bi < nb; bi++) {
+                const int b = mode ? 256 : blocks[bi];
+                if (!mode && c->prm.block_size && b != c->prm.block_size) continue;
+                for (int ti = 0; ti < nt; ti++) {
+                    if (!mode && ti == 3) break;
+                    c->lp_mode = mode;
+                    if (mode) c->wgrab = wgrabs[ti];
+                    else {
+                        c->block = b;
+                        c->tile = tiles[ti];
+                    }
+                    c->graph_dirty = true;
+                    ecmg_tick_stats ts{};
+                    ecmg_status st = run_ticks(c, 1, &ts); /* warm-up and graph capture */
+                    if (st == ECMG_OK) st = run_ticks(c, ticks_per_trial, &ts);
+                    ecmg_status rs = restore();
+                    if (st != ECMG_OK || rs != ECMG_OK) {
+                        c->replan_enabled = true;
+                        return st != ECMG_OK ? st : rs;
+                    }
+                    trials++;
+                    float ms = ts.device_ms / (float)ticks_per_trial;
+                    if (ms < best) {
+                        best = ms;
+                        bmode = mode;
+                        bs = sc;
+                        if (mode) bw = c->wgrab;
+                        else { bb = c->block; bt = c->tile; }
+                    }
                 }
-                trials++;
-                float ms = ts.device_ms / (float)ticks_per_trial;
-                if (ms < best) { best = ms; bb = b; bt = t; bs = sc; }
             }
         }
     }
     c->replan_enabled = true;
     c->block = bb;
     c->tile = bt;
+    c->lp_mode = bmode;
+    c->wgrab = bw;
     c->cell_scale = bs;
     for (auto& s : c->scenes) s->grid_ready = false;
     c->graph_dirty = true;
     sp.free_(); sv.free_(); sa.free_(); spv.free_(); sact.free_();
     if (out) {
         out->block_size = bb;
-        out->agents_per_warp_grab = bt;
+        out->agents_per_warp_grab = bmode ? bw : bt;
+        out->lp_mode = bmode;
         out->grid_cell_scale = bs;
         out->best_tick_ms = best;
         out->trials = trials;
     }
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_set_lp_mode(ecmg_ctx* c, int mode, int agents_per_warp_grab)
+{
+    if (!c || (mode != ECMG_LP_THREAD && mode != ECMG_LP_WARP)) return ECMG_ERR_INVALID_ARG;
+    if (mode == ECMG_LP_WARP && (agents_per_warp_grab < 1 || agents_per_warp_grab > 64)) return ECMG_ERR_INVALID_ARG;
+    c->lp_mode = mode;
+    if (mode == ECMG_LP_WARP) c->wgrab = agents_per_warp_grab;
+    c->graph_dirty = true;
     return ECMG_OK;
 }
 

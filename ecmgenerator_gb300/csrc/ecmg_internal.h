@@ -94,7 +94,8 @@ struct TickArgs {
     unsigned char* label;  /* [n] class of the LP result (null: not traced) */
     const SceneDev* scenes;
     const int* slot_scene; /* slot -> scene (null: one scene) */
-    int tile;              /* agents a warp takes per work grab (multiple of 32) */
+    int tile;              /* agents a warp takes per work grab (per-thread mode: multiple of 32) */
+    int lp_mode;           /* 0: one thread per agent, 1: one warp per agent */
     /* parameters */
     float dt, tau_a, tau_o, rnb, rnb2, max_speed, mass_recip, arr_sq, del_sq;
     int k;

@@ -628,6 +628,387 @@ __global__ void __launch_bounds__(256) k_agents(TickArgs a)
     }
 }
 
+/* ------------------------------------------------------------------------
+ * Warp-cooperative per-agent step: one warp per agent.  The lanes build the
+ * obstacle and neighbour constraints in parallel and keep them in shared
+ * memory in the reference's order (ballot compaction preserves the candidate
+ * order).  The incremental LPs stay sequential over the constraint index i;
+ * the bounds of line i from the lines j < i are spread over the lanes and
+ * combined by min/max reductions that keep the first j on ties.  min/max are
+ * exact, the per-element arithmetic is the per-thread code's, and "some line
+ * is parallel and opposite" / "lo > hi" are order-free predicates, so the
+ * results equal the per-thread LP's bit for bit.
+ * ---------------------------------------------------------------------- */
+constexpr unsigned kFull = 0xffffffffu;
+
+struct SmemGet {
+    const Con* c;
+    __device__ Con operator()(int i) const { return c[i]; }
+};
+
+/* projected lines of RandomizedLP3D: the obstacle constraints, then the
+   bisectors */
+struct ProjGetW {
+    const Con* obs;
+    const Con* bis;
+    int nObst;
+    __device__ Con operator()(int i) const { return i < nObst ? obs[i] : bis[i - nObst]; }
+};
+
+/* lo/hi bounds on line h from the lines j < i (ORCA.cpp:461-497), lanes
+   taking j = lane, lane + 32, ...; false when a parallel line excludes h */
+template <class Get>
+__device__ __forceinline__ bool warp_bounds(const Get& get, const Con& h, int i, int lane, float* lo, float* hi,
+                                            int* lo_src, int* hi_src)
+{
+    float llo = -INFINITY, lhi = INFINITY;
+    int jlo = 0x7fffffff, jhi = 0x7fffffff;
+    bool bad = false;
+    const V2 rh = right(h.n);
+    for (int j = lane; j < i; j += 32) {
+        Con g = get(j);
+        float den = det(rh, right(g.n));
+        float num = det(right(g.n), h.p - g.p);
+        if (fabsf(den) <= kEps) {
+            if (num < 0.0f) bad = true;
+            continue;
+        }
+        const float t = num / den;
+        if (den >= 0.0f) {
+            if (t < lhi) { lhi = t; jhi = j; }
+        } else {
+            if (llo < t) { llo = t; jlo = j; }
+        }
+    }
+    if (__any_sync(kFull, bad)) return false;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        float v = __shfl_xor_sync(kFull, lhi, o);
+        int jj = __shfl_xor_sync(kFull, jhi, o);
+        if (v < lhi || (v == lhi && jj < jhi)) { lhi = v; jhi = jj; }
+        v = __shfl_xor_sync(kFull, llo, o);
+        jj = __shfl_xor_sync(kFull, jlo, o);
+        if (llo < v || (v == llo && jj < jlo)) { llo = v; jlo = jj; }
+    }
+    if (lhi < *hi) { *hi = lhi; *hi_src = jhi; }
+    if (*lo < llo) { *lo = llo; *lo_src = jlo; }
+    return true;
+}
+
+/* RandomizedLP (ORCA.cpp:428-587) for a whole warp; every lane returns the
+   same result */
+template <class Get, bool TRACE>
+__device__ int lp2d_warp(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2* out, LpTrace* tr,
+                         int lane)
+{
+    V2 v;
+    if (useDirOpt) v = opt * maxSpeed;
+    else if (len(opt) > maxSpeed) v = normalized(opt) * maxSpeed;
+    else v = opt;
+    for (int i = 0; i < n; i++) {
+        const Con h = get(i);
+        if (det(right(h.n), h.p - v) <= 0.0f) continue; /* Constraint::Contains */
+        const V2 dir = right(h.n);
+        const float dpd = dot(dir, h.p);
+        const float disc = dpd * dpd + maxSpeed * maxSpeed - dot(h.p, h.p);
+        if (disc <= 0.0f) { *out = v; return i; }
+        const float sq = sqrtf(disc);
+        float lo = -dpd - sq, hi = -dpd + sq;
+        int lo_src = -1, hi_src = -1;
+        if (!warp_bounds(get, h, i, lane, &lo, &hi, &lo_src, &hi_src) || lo > hi) { *out = v; return i; }
+        if (useDirOpt) {
+            if (dot(opt, dir) > 0) v = h.p + dir * hi;
+            else v = h.p + dir * lo;
+        } else {
+            const float t = dot(dir, opt - h.p);
+            if (t < lo) {
+                v = h.p + dir * lo;
+                if (TRACE) { tr->h = i; tr->src = lo_src < 0 ? 1 : 2; tr->j = lo_src; }
+            } else if (t > hi) {
+                v = h.p + dir * hi;
+                if (TRACE) { tr->h = i; tr->src = hi_src < 0 ? 1 : 2; tr->j = hi_src; }
+            } else {
+                v = h.p + dir * t;
+                if (TRACE) { tr->h = i; tr->src = 0; tr->j = -1; }
+            }
+        }
+    }
+    *out = v;
+    return n;
+}
+
+/* RandomizedLP3D (ORCA.cpp:592-669) for a whole warp: the bisectors of
+   line i are built by the lanes (compacted in j order), the projected LP is
+   lp2d_warp.  bis holds at least m - nObst lines. */
+__device__ __noinline__ void lp3d_warp(const Con* cons, Con* bis, int m, int nObst, float maxSpeed, int failed,
+                                       V2* vout, bool fp64, int lane)
+{
+    V2 v = *vout;
+    float maxPen = 0.0f;
+    for (int i = failed; i < m; i++) {
+        const Con ci = cons[i];
+        const V2 dir = right(ci.n);
+        if (det(dir, ci.p - v) <= maxPen) continue;
+        int cnt = 0;
+        for (int base = nObst; base < i; base += 32) {
+            const int j = base + lane;
+            bool keep = false;
+            Con nc;
+            if (j < i) {
+                const Con cj = cons[j];
+                const float dt = det(right(ci.n), right(cj.n));
+                if (fabsf(dt) <= kEps) {
+                    if (!(dot(ci.n, cj.n) > 0)) {
+                        nc.p = (ci.p + cj.p) * 0.5f;
+                        keep = true;
+                    }
+                } else if (!fp64) {
+                    const float t = det(right(cj.n), ci.p - cj.p) / dt;
+                    nc.p = ci.p + right(ci.n) * t;
+                    keep = true;
+                } else {
+                    double ax = (double)cj.n.y, ay = -(double)cj.n.x;
+                    double bx = (double)ci.p.x - (double)cj.p.x, by = (double)ci.p.y - (double)cj.p.y;
+                    double rx = (double)ci.n.y, ry = -(double)ci.n.x;
+                    double dd = rx * ay - ry * ax;
+                    double t = (ax * by - ay * bx) / dd;
+                    nc.p = mk((float)((double)ci.p.x + rx * t), (float)((double)ci.p.y + ry * t));
+                    keep = true;
+                }
+                if (keep) nc.n = normalized(cj.n - ci.n);
+            }
+            const unsigned b = __ballot_sync(kFull, keep);
+            if (keep) bis[cnt + __popc(b & ((1u << lane) - 1u))] = nc;
+            cnt += __popc(b);
+        }
+        __syncwarp();
+        const V2 temp = v;
+        ProjGetW pg{cons, bis, nObst};
+        if (lp2d_warp<ProjGetW, false>(pg, nObst + cnt, ci.n, maxSpeed, true, &v, nullptr, lane) < nObst + cnt)
+            v = temp;
+        maxPen = det(dir, ci.p - v);
+        __syncwarp(); /* bis is rewritten for the next line */
+    }
+    *vout = v;
+}
+
+/* verify_proposal for a whole warp (same conditions, lanes over the
+   constraints) */
+__device__ __noinline__ bool verify_proposal_warp(const Con* cons, int m, int nObst, int ncnt, V2 opt, float maxSpeed,
+                                                  int cls, V2* out, int lane)
+{
+    const float margin = 1e-4f;
+    SmemGet get{cons};
+    if (cls == kClsPref) {
+        V2 v0 = (len(opt) > maxSpeed) ? normalized(opt) * maxSpeed : opt;
+        bool bad = false;
+        for (int i = lane; i < m; i += 32) {
+            Con c = cons[i];
+            if (det(right(c.n), c.p - v0) > 0.0f) bad = true;
+        }
+        if (__any_sync(kFull, bad)) return false;
+        *out = v0;
+        return true;
+    }
+    int q, qj = -1, kind;
+    if (cls >= kClsSingle && cls < kClsPair) { q = cls - kClsSingle; kind = 0; }
+    else if (cls >= kClsCircle && cls < kClsOther) { q = cls - kClsCircle; kind = 1; }
+    else if (cls >= kClsPair && cls < kClsCircle) {
+        int p = cls - kClsPair;
+        q = 1;
+        while ((q + 1) * q / 2 <= p) q++;
+        qj = p - q * (q - 1) / 2;
+        kind = 2;
+    } else return false;
+    if (q >= ncnt || q >= kMlpNbrs) return false;
+    const int h = nObst + q, jsrc = kind == 2 ? nObst + qj : -1;
+    if (h >= m) return false;
+    const Con H = cons[h];
+    const V2 dir = right(H.n);
+    const float dpd = dot(dir, H.p);
+    const float disc = dpd * dpd + maxSpeed * maxSpeed - dot(H.p, H.p);
+    if (disc <= 0.0f) return false;
+    const float sq = sqrtf(disc);
+    float lo = -dpd - sq, hi = -dpd + sq;
+    int lo_src = -1, hi_src = -1;
+    if (!warp_bounds(get, H, h, lane, &lo, &hi, &lo_src, &hi_src) || lo > hi) return false;
+    const float t = dot(dir, opt - H.p);
+    V2 v;
+    int src;
+    if (t < lo) { v = H.p + dir * lo; src = lo_src; }
+    else if (t > hi) { v = H.p + dir * hi; src = hi_src; }
+    else { v = H.p + dir * t; src = -2; }
+    if (kind == 0 && src != -2) return false;
+    if (kind == 1 && src != -1) return false;
+    if (kind == 2 && src != jsrc) return false;
+    const V2 r = v - opt;
+    if (kind != 1) {
+        float rs = maxSpeed - margin;
+        if (!(rs > 0.0f && dot(v, v) < rs * rs)) return false;
+    }
+    if (kind == 0) {
+        if (!(dot(r, H.n) > margin)) return false;
+    } else if (kind == 2) {
+        const Con G = cons[jsrc];
+        float d2 = det(H.n, G.n);
+        float la = det(r, G.n) / d2, lb = det(H.n, r) / d2;
+        if (!(la > margin && lb > margin)) return false;
+    } else {
+        V2 nv = v * -1.0f;
+        float d2 = det(H.n, nv);
+        if (!(fabsf(d2) > kEps)) return false;
+        float la = det(r, nv) / d2, lb = det(H.n, r) / d2;
+        if (!(la > margin && lb > margin * maxSpeed)) return false;
+    }
+    bool bad = false;
+    for (int i = lane; i < m; i += 32) {
+        if (i == h || i == jsrc) continue;
+        const Con c = cons[i];
+        const float d = det(right(c.n), c.p - v);
+        if (i > h ? d > 0.0f : !(d < -margin)) bad = true;
+    }
+    if (__any_sync(kFull, bad)) return false;
+    *out = v;
+    return true;
+}
+
+struct WarpCounts {
+    int lp3d = 0, proposed = 0, accepted = 0;
+};
+
+/* orca_tick for grid-order agent t, one warp */
+template <int K>
+__device__ void orca_warp(const TickArgs& a, int t, int lane, Con* cons, Con* bis, WarpCounts& wc)
+{
+    constexpr int MC = K + kMaxObstCons;
+    const int slot = a.s_slot[t];
+    if (!a.active[slot]) return;
+    const V2 pos = a.s_pos[t];
+    const V2 vel = a.s_vel[t];
+    const float clr = a.s_clear[t];
+    const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
+    const float speed = a.speed[slot];
+    const V2 pv = a.pref_vel[slot];
+    const float maxSpeed = a.max_speed > 0.0f ? a.max_speed : speed;
+    const int ncnt = a.ncnt[t];
+    const int* nbr = a.nbr + (size_t)t * a.k;
+    int m = 0;
+    bool overflow = false;
+    const float range = a.tau_o * maxSpeed + clr;
+    const float rsq = range * range;
+    {
+        const ObstView& o = sc.ob;
+        int b = 0, e = 0;
+        const int* items = nullptr;
+        float fx = (pos.x - o.gx0) * o.ginv, fy = (pos.y - o.gy0) * o.ginv;
+        if (o.g_start && range <= o.reach && fx >= 0.0f && fy >= 0.0f && fx < (float)o.gw && fy < (float)o.gh) {
+            int g = (int)fy * o.gw + (int)fx;
+            b = o.g_start[g];
+            e = o.g_start[g + 1];
+            items = o.g_items;
+        } else {
+            e = o.n_verts;
+        }
+        for (int base = b; base < e; base += 32) {
+            const int q = base + lane;
+            bool emit = false;
+            Con c;
+            if (q < e) {
+                int L = items ? items[q] : q;
+                if (obstacle_in_range(o, L, pos, rsq)) emit = obstacle_constraint(o, L, pos, vel, clr, a.tau_o, &c);
+            }
+            const unsigned bal = __ballot_sync(kFull, emit);
+            if (emit) {
+                int at = m + __popc(bal & ((1u << lane) - 1u));
+                if (at < MC - K) cons[at] = c;
+                else overflow = true;
+            }
+            m += __popc(bal);
+        }
+        if (m > MC - K) m = MC - K;
+    }
+    overflow = __any_sync(kFull, overflow);
+    const int nObst = m;
+    if (lane < ncnt) {
+        const int j = nbr[lane];
+        cons[m + lane] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt);
+    }
+    m += ncnt;
+    __syncwarp();
+    if (overflow && lane == 0) atomicOr(&a.counters[C_ERROR], ECMG_DEV_ERR_CONSTRAINTS);
+
+    V2 v;
+    int failed = -1;
+    if (a.cls || a.cls_slot) {
+        const int c = a.cls_slot ? a.cls_slot[slot] : a.cls[t];
+        if (c != kClsOther) {
+            wc.proposed++;
+            if (verify_proposal_warp(cons, m, nObst, ncnt, pv, maxSpeed, c, &v, lane)) {
+                failed = m;
+                wc.accepted++;
+            }
+        }
+    }
+    if (failed < 0) {
+        SmemGet get{cons};
+        if (a.label) {
+            LpTrace tr;
+            failed = lp2d_warp<SmemGet, true>(get, m, pv, maxSpeed, false, &v, &tr, lane);
+            if (lane == 0) a.label[t] = (unsigned char)label_of(tr, failed, m, nObst);
+        } else {
+            failed = lp2d_warp<SmemGet, false>(get, m, pv, maxSpeed, false, &v, nullptr, lane);
+        }
+        if (failed < m) {
+            lp3d_warp(cons, bis, m, nObst, maxSpeed, failed, &v, a.lp3d_fp64 != 0, lane);
+            wc.lp3d++;
+        }
+    }
+
+    if (lane == 0) {
+        float fx = v.x - vel.x, fy = v.y - vel.y;
+        V2 nv = mk(vel.x + fx * a.mass_recip * a.dt, vel.y + fy * a.mass_recip * a.dt);
+        V2 npos = mk(pos.x + (nv.x * a.dt), pos.y + (nv.y * a.dt));
+        a.vel[slot] = nv;
+        a.pos[slot] = npos;
+        if (a.rec_cnt) {
+            a.rec_cnt[slot] = ncnt;
+            a.rec_vorca[slot] = v;
+            a.rec_fail[slot] = failed;
+            a.rec_ncons[slot] = m;
+            a.rec_nobst[slot] = nObst;
+        }
+    }
+    if (a.rec_cnt && lane < a.k) a.rec_nbr[slot * a.k + lane] = lane < ncnt ? a.s_slot[nbr[lane]] : -1;
+    __syncwarp(); /* cons and bis are reused by the warp's next agent */
+}
+
+/* persistent kernel, one warp per agent: a warp takes `tile` consecutive
+   grid-order agents per work grab */
+template <int K>
+__global__ void __launch_bounds__(256) k_agents_warp(TickArgs a)
+{
+    constexpr int MC = K + kMaxObstCons;
+    __shared__ Con s_cons[8][MC];
+    __shared__ Con s_bis[8][K];
+    const int n = a.counters[C_NSORTED];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int grab = a.tile > 0 ? a.tile : 1;
+    WarpCounts wc;
+    while (true) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&a.counters[C_WORK], grab);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= n) break;
+        const int end = min(n, base + grab);
+        for (int t = base; t < end; t++) orca_warp<K>(a, t, lane, s_cons[w], s_bis[w], wc);
+    }
+    if (lane == 0) {
+        if (wc.lp3d) atomicAdd(&a.counters[C_LP3D], wc.lp3d);
+        if (wc.proposed) atomicAdd(&a.counters[C_PROPOSED], wc.proposed);
+        if (wc.accepted) atomicAdd(&a.counters[C_ACCEPTED], wc.accepted);
+    }
+}
+
 template <int K>
 __global__ void __launch_bounds__(128) k_knn(const V2* s_pos, const int* s_slot, const int* cell_start,
                                              AgentGrid g, int k, float rnb, float r2, const int* counters,
@@ -684,7 +1065,18 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
             if (e2 != cudaSuccess) return e2;
         }
     }
-    if (t.k <= 8) {
+    if (t.lp_mode == 1) {
+        if (t.k <= 8) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_warp<8>, 256, 0);
+            k_agents_warp<8><<<sms * (per_sm > 0 ? per_sm : 1), 256, 0, s>>>(t);
+        } else if (t.k <= 16) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_warp<16>, 256, 0);
+            k_agents_warp<16><<<sms * (per_sm > 0 ? per_sm : 1), 256, 0, s>>>(t);
+        } else {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_warp<32>, 256, 0);
+            k_agents_warp<32><<<sms * (per_sm > 0 ? per_sm : 1), 256, 0, s>>>(t);
+        }
+    } else if (t.k <= 8) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<8>, block, 0);
         k_agents<8><<<sms * (per_sm > 0 ? per_sm : 1), block, 0, s>>>(t);
     } else if (t.k <= 16) {

@@ -362,8 +362,16 @@ def autotune(sim: Simulator, ticks_per_trial: int = 2) -> dict:
     r = _lib.TuneResult()
     sim._ck(sim.L.ecmg_autotune(sim.h, int(ticks_per_trial), C.byref(r)))
     return dict(block_size=r.block_size, agents_per_warp_grab=r.agents_per_warp_grab,
-                grid_cell_scale=r.grid_cell_scale, best_tick_ms=r.best_tick_ms, trials=r.trials)
+                grid_cell_scale=r.grid_cell_scale, best_tick_ms=r.best_tick_ms, trials=r.trials,
+                lp_mode=("warp" if r.lp_mode == 1 else "thread"))
 
 
 def set_launch(sim: Simulator, block_size: int, agents_per_warp_grab: int, grid_cell_scale: float):
     sim._ck(sim.L.ecmg_set_launch(sim.h, int(block_size), int(agents_per_warp_grab), float(grid_cell_scale)))
+
+
+def set_lp_mode(sim: Simulator, mode: str = "warp", agents_per_warp_grab: int = 4):
+    """per-agent kernel layout: "thread" (one thread per agent) or "warp"
+    (one warp per agent); results are identical"""
+    m = {"thread": 0, "warp": 1}[mode]
+    sim._ck(sim.L.ecmg_set_lp_mode(sim.h, m, int(agents_per_warp_grab)))

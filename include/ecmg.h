@@ -215,10 +215,19 @@ typedef struct {
     float grid_cell_scale;
     float best_tick_ms;
     int trials;
+    int lp_mode;             /* ECMG_LP_THREAD or ECMG_LP_WARP */
 } ecmg_tune_result;
 ecmg_status ecmg_set_launch(ecmg_ctx* ctx, int block_size, int agents_per_warp_grab, float grid_cell_scale);
-/* times ticks_per_trial ticks per configuration (block size x work grab x
-   grid cell) on a copy of the current state, restores the state after each
+/* Per-agent kernel layout.  ECMG_LP_THREAD: one thread per agent (work
+   grabs of agents_per_warp_grab from ecmg_set_launch).  ECMG_LP_WARP: one
+   warp per agent -- the lanes build the constraints in parallel and share
+   the inner loops of the LPs -- taking agents_per_warp_grab agents per work
+   grab (1..64).  Both give identical results. */
+#define ECMG_LP_THREAD 0
+#define ECMG_LP_WARP 1
+ecmg_status ecmg_set_lp_mode(ecmg_ctx* ctx, int mode, int agents_per_warp_grab);
+/* times ticks_per_trial ticks per configuration (per-agent kernel layout x
+   block size x work grab x grid cell) on a copy of the current state, restores the state after each
    trial (no re-plans are served during trials) and keeps the fastest */
 ecmg_status ecmg_autotune(ecmg_ctx* ctx, int ticks_per_trial, ecmg_tune_result* out);
 

@@ -152,20 +152,25 @@ def test_trace_features_match_tick_start_state(lib):
     sim.close()
 
 
-def _pair(n_agents=1000, ticks=30):
+def _pair(n_agents=1000, ticks=30, mode=None):
     """two simulators in the same state (the tick is deterministic)"""
+    from ecmgenerator_gb300.simulator import set_lp_mode
+
     a, b = _c1_sim(n_agents), _c1_sim(n_agents)
+    if mode:
+        set_lp_mode(b, mode, 2)
     a.update(ticks=ticks)
     b.update(ticks=ticks)
     assert np.array_equal(a.get_position_data(), b.get_position_data())
     return a, b
 
 
-def test_true_classes_as_proposals_are_accepted_and_exact(lib):
+@pytest.mark.parametrize("mode", ["thread", "warp"])
+def test_true_classes_as_proposals_are_accepted_and_exact(lib, mode):
     torch = _torch()
     from ecmgenerator_gb300 import proposal as P
 
-    a, b = _pair()
+    a, b = _pair(mode=mode)
     accepted = proposed = 0
     for t in range(10):
         a.set_trace(True)
@@ -186,10 +191,11 @@ def test_true_classes_as_proposals_are_accepted_and_exact(lib):
     b.close()
 
 
-def test_wrong_proposals_are_rejected_and_results_unchanged(lib):
+@pytest.mark.parametrize("mode", ["thread", "warp"])
+def test_wrong_proposals_are_rejected_and_results_unchanged(lib, mode):
     torch = _torch()
 
-    a, b = _pair()
+    a, b = _pair(mode=mode)
     g = torch.Generator(device="cuda").manual_seed(3)
     for t in range(10):
         a.update()

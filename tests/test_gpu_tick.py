@@ -9,11 +9,13 @@ pytestmark = pytest.mark.gpu
 ORCA = dict(tau_agent=2.0, tau_obst=2.0, neighbor_dist=5.0)
 
 
-def _pair(scene, st, paths, k, n_slots=None, **kw):
-    from ecmgenerator_gb300.simulator import Simulator
+def _pair(scene, st, paths, k, n_slots=None, lp_mode=None, grab=4, **kw):
+    from ecmgenerator_gb300.simulator import Simulator, set_lp_mode
 
     n = st.num_agents
     sim = Simulator(scene, n_slots or st.n_slots, 1.0 / 60.0, max_neighbors=k, **ORCA, **kw)
+    if lp_mode:
+        set_lp_mode(sim, lp_mode, grab)
     sim.set_record(True)
     sim.add_agents(st.pos[:n], st.clear[:n], st.pref_speed[:n], paths[:n])
     return sim
@@ -69,6 +71,34 @@ def test_tick_bitexact_no_graph(port, c1_small):
 def test_tick_bitexact_k(port, c1_small, k):
     scene, st, paths = c1_small
     _run(port, scene, st, paths, ticks=4, k=k)
+
+
+def test_tick_bitexact_warp_layout(port, c1_small):
+    """one warp per agent: the same bits as the per-thread kernel and the oracle"""
+    scene, st, paths = c1_small
+    _run(port, scene, st, paths, ticks=40, k=10, lp_mode="warp", grab=3)
+
+
+@pytest.mark.parametrize("k", [1, 16, 32])
+def test_tick_bitexact_warp_k(port, c1_small, k):
+    scene, st, paths = c1_small
+    _run(port, scene, st, paths, ticks=4, k=k, lp_mode="warp", grab=1)
+
+
+def test_tick_bitexact_warp_dense(port):
+    """overlapping crowd (infeasible 2D LPs, RandomizedLP3D for most agents)"""
+    from ecmgenerator_gb300 import agents as ag
+    from ecmgenerator_gb300.simulator import Planner
+
+    cfg = ag.scaled("c3", agents=3000, w=60.0, h=60.0, boxes=8, bands=4.0)
+    scene = ag.build_scene(cfg, 3)
+    st = ag.spawn_agents(cfg, scene, 3)
+    paths = Planner(scene).find_paths(st.pos, st.goal, st.clear)
+    paths = [p if p is not None else np.stack([st.pos[i], st.goal[i]]) for i, p in enumerate(paths)]
+    st.set_paths(paths)
+    for mode in ("thread", "warp"):
+        ev = _run(port, scene, st, paths, ticks=6, k=16, lp_mode=mode)
+        assert ev > 1000
 
 
 def test_knn_standalone(lib, c1_small):
