@@ -74,6 +74,7 @@ struct SceneState {
     DBuf<int> d_ob_next, d_ob_prev, d_v_idx, d_he_target, d_ob_gstart, d_ob_gitems, d_ecm_gstart, d_ecm_gitems;
     DBuf<unsigned char> d_ob_convex;
     DBuf<float> d_special_y;
+    DBuf<int> d_sp_start, d_sp_items;
     int slot_base = 0, slot_cap = 0;
     std::vector<int> free_stack; /* back() = top */
     int num_agents = 0;
@@ -84,7 +85,7 @@ struct SceneState {
         d_ob_p.free_(); d_v_pos.free_(); d_he_left.free_(); d_he_right.free_();
         d_ob_next.free_(); d_ob_prev.free_(); d_v_idx.free_(); d_he_target.free_();
         d_ob_gstart.free_(); d_ob_gitems.free_(); d_ecm_gstart.free_(); d_ecm_gitems.free_();
-        d_ob_convex.free_(); d_special_y.free_();
+        d_ob_convex.free_(); d_special_y.free_(); d_sp_start.free_(); d_sp_items.free_();
     }
 };
 
@@ -434,6 +435,12 @@ ecmg_status ecmg_scene_set_ecm(ecmg_ctx* c, int scene, const ecmg_ecm* e)
     CK(sc->d_ecm_gstart.alloc(s.ecm_grid.start.size()));
     CK(sc->d_ecm_gitems.alloc(std::max<size_t>(1, s.ecm_grid.items.size())));
     CK(sc->d_special_y.alloc(std::max<size_t>(1, s.special_y.size())));
+    CK(sc->d_sp_start.alloc(std::max<size_t>(1, s.sp_start.size())));
+    CK(sc->d_sp_items.alloc(std::max<size_t>(1, s.sp_items.size())));
+    if (!s.sp_start.empty())
+        CK(cudaMemcpy(sc->d_sp_start.p, s.sp_start.data(), sizeof(int) * s.sp_start.size(), cudaMemcpyHostToDevice));
+    if (!s.sp_items.empty())
+        CK(cudaMemcpy(sc->d_sp_items.p, s.sp_items.data(), sizeof(int) * s.sp_items.size(), cudaMemcpyHostToDevice));
     if (V) {
         CK(cudaMemcpy(sc->d_v_pos.p, s.v_pos.data(), sizeof(V2) * V, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(sc->d_v_idx.p, s.v_idx.data(), sizeof(int) * V, cudaMemcpyHostToDevice));
@@ -798,6 +805,8 @@ static ecmg_status ensure_grids(ecmg_ctx* c)
             e.g_items = sc->d_ecm_gitems.p;
             e.special_y = sc->d_special_y.p;
             e.n_special = (int)s.special_y.size();
+            e.sp_start = sc->d_sp_start.p;
+            e.sp_items = sc->d_sp_items.p;
         }
         c->total_buckets = base;
         CK(c->d_scenes.alloc(tab.size()));

@@ -113,11 +113,14 @@ struct EcmView {
     int gw, gh;
     const int* g_start;   /* gw*gh + 1 */
     const int* g_items;
-    /* sorted distinct y of all quad corners: a query whose y equals one of
-       them falls back to the linear scan (the ray-cast test can then report
-       a hit left of the quad's bounding box) */
+    /* sorted distinct y of all quad corners.  At such a height the ray-cast
+       test can report a hit left of a quad's bounding box, but only for the
+       quads with a corner at that height: sp_items[sp_start[s] ..
+       sp_start[s+1]) lists them (ascending) for special_y[s]. */
     const float* special_y;
     int n_special;
+    const int* sp_start;
+    const int* sp_items;
 };
 
 /* quad of PointLocationQueryLinear (ECMCellCollection.cpp:67-80):
@@ -156,7 +159,8 @@ EG_HD bool contains_quad(V2 p, const V2* q)
     return inside;
 }
 
-EG_HD bool is_special_y(const EcmView& e, float y)
+/* index s with special_y[s] == y, or -1 */
+EG_HD int special_index(const EcmView& e, float y)
 {
     int lo = 0, hi = e.n_special;
     while (lo < hi) {
@@ -165,33 +169,37 @@ EG_HD bool is_special_y(const EcmView& e, float y)
         if (v < y) lo = mid + 1;
         else hi = mid;
     }
-    return lo < e.n_special && e.special_y[lo] == y;
+    return (lo < e.n_special && e.special_y[lo] == y) ? lo : -1;
 }
 
 /* ECMCellCollection::PointLocationQueryLinear (ECMCellCollection.cpp:57-90):
-   the first cell, in cell order, whose quad contains p.  The grid returns the
-   same cell: every quad that can contain p is listed in p's grid cell, and
-   the list is scanned in ascending cell order. */
+   the first cell, in cell order, whose quad contains p.  Every quad that can
+   contain p is listed in p's grid cell or, when p.y is the height of a quad
+   corner, in that height's list; both lists are ascending, so the smaller of
+   their first hits is the linear scan's first hit. */
 EG_NI int point_location(const EcmView& e, V2 p)
 {
     V2 q[4];
-    if (e.n_special > 0 && is_special_y(e, p.y)) {
-        for (int c = 0; c < 2 * e.n_edges; c++) {
+    int best = -1;
+    const int s = e.n_special > 0 ? special_index(e, p.y) : -1;
+    if (s >= 0) {
+        for (int i = e.sp_start[s], en = e.sp_start[s + 1]; i < en; i++) {
+            int c = e.sp_items[i];
             cell_quad(e, c, q);
-            if (contains_quad(p, q)) return c;
+            if (contains_quad(p, q)) { best = c; break; }
         }
-        return -1;
     }
     float fx = (p.x - e.gx0) * e.ginv, fy = (p.y - e.gy0) * e.ginv;
-    if (!(fx >= 0.0f && fy >= 0.0f && fx < (float)e.gw && fy < (float)e.gh)) return -1;
+    if (!(fx >= 0.0f && fy >= 0.0f && fx < (float)e.gw && fy < (float)e.gh)) return best;
     int g = (int)fy * e.gw + (int)fx;
     int b = e.g_start[g], en = e.g_start[g + 1];
     for (int i = b; i < en; i++) {
         int c = e.g_items[i];
+        if (best >= 0 && c >= best) break;
         cell_quad(e, c, q);
         if (contains_quad(p, q)) return c;
     }
-    return -1;
+    return best;
 }
 
 /* MathUtility::GetRayToLineSegmentIntersection (UtilityFunctions.cpp:323-349) */
@@ -563,9 +571,19 @@ EG_HD int lp2d(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2
     return n;
 }
 
-/* ORCA::RandomizedLP3D (ORCA.cpp:592-669).  proj must hold n constraints.
-   With fp64 the bisector lines are intersected in double precision (the
-   reference computes them in float). */
+/* the projected lines of RandomizedLP3D: the obstacle constraints (read in
+   place), then the bisectors in proj */
+template <class Get>
+struct Lp3dProj {
+    const Get* get;
+    const Con* proj;
+    int nObst;
+    EG_HD Con operator()(int q) const { return q < nObst ? (*get)(q) : proj[q - nObst]; }
+};
+
+/* ORCA::RandomizedLP3D (ORCA.cpp:592-669).  proj must hold n - nObst
+   constraints.  With fp64 the bisector lines are intersected in double
+   precision (the reference computes them in float). */
 template <class Get>
 EG_HD void lp3d(const Get& get, int n, int nObst, float maxSpeed, int failed, V2* out, Con* proj, bool fp64)
 {
@@ -575,7 +593,6 @@ EG_HD void lp3d(const Get& get, int n, int nObst, float maxSpeed, int failed, V2
         V2 dir = right(ci.n);
         if (det(dir, ci.p - *out) <= maxPen) continue;
         int m = 0;
-        for (int q = 0; q < nObst; q++) proj[m++] = get(q);
         for (int j = nObst; j < i; j++) {
             Con cj = get(j);
             float dt = det(right(ci.n), right(cj.n));
@@ -600,11 +617,8 @@ EG_HD void lp3d(const Get& get, int n, int nObst, float maxSpeed, int failed, V2
             proj[m++] = nc;
         }
         V2 temp = *out;
-        struct ProjGet {
-            const Con* c;
-            EG_HD Con operator()(int q) const { return c[q]; }
-        } pg{proj};
-        if (lp2d(pg, m, ci.n, maxSpeed, true, out) < m) *out = temp;
+        Lp3dProj<Get> pg{&get, proj, nObst};
+        if (lp2d(pg, nObst + m, ci.n, maxSpeed, true, out) < nObst + m) *out = temp;
         maxPen = det(dir, ci.p - *out);
     }
 }

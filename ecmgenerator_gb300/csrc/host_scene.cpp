@@ -31,6 +31,8 @@ EcmView HostScene::ecm_view() const
     e.g_items = ecm_grid.items.data();
     e.special_y = special_y.data();
     e.n_special = (int)special_y.size();
+    e.sp_start = sp_start.data();
+    e.sp_items = sp_items.data();
     return e;
 }
 
@@ -108,6 +110,30 @@ void build_ecm_grid(HostScene& s)
     std::sort(ys.begin(), ys.end());
     ys.erase(std::unique(ys.begin(), ys.end()), ys.end());
     s.special_y = ys;
+    /* per special height, the quads with a corner there (ascending) */
+    {
+        std::vector<int> cnt(ys.size() + 1, 0);
+        std::vector<int> idx(4 * (size_t)C);
+        for (int c = 0; c < C; c++) {
+            for (int k = 0; k < 4; k++) {
+                float y = q[4 * (size_t)c + k].y;
+                int si = (int)(std::lower_bound(ys.begin(), ys.end(), y) - ys.begin());
+                bool dup = false;
+                for (int k2 = 0; k2 < k; k2++) dup |= idx[4 * (size_t)c + k2] == si;
+                idx[4 * (size_t)c + k] = dup ? -1 : si;
+                if (!dup) cnt[si + 1]++;
+            }
+        }
+        for (size_t i = 1; i < cnt.size(); i++) cnt[i] += cnt[i - 1];
+        s.sp_start = cnt;
+        s.sp_items.assign(std::max(1, cnt.back()), 0);
+        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+        for (int c = 0; c < C; c++)
+            for (int k = 0; k < 4; k++) {
+                int si = idx[4 * (size_t)c + k];
+                if (si >= 0) s.sp_items[fill[si]++] = c;
+            }
+    }
     if (C == 0) {
         s.ecm_grid = GridCSR();
         s.ecm_grid.start.assign(2, 0);

@@ -31,6 +31,7 @@ struct HostScene {
     std::vector<V2> he_left, he_right;
     GridCSR ecm_grid;
     std::vector<float> special_y;
+    std::vector<int> sp_start, sp_items; /* quads with a corner at special_y[s] */
     /* scene rectangle (ECM and obstacle bounding box) */
     float bx0 = 0, by0 = 0, bx1 = 0, by1 = 0;
     bool has_ecm = false;

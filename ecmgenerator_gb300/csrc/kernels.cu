@@ -381,7 +381,7 @@ template <int MC>
 __device__ __noinline__ void lp3d_local(const Con* cons, int m, int nObst, float maxSpeed, int failed, V2* v,
                                         bool fp64)
 {
-    Con proj[MC];
+    Con proj[MC - kMaxObstCons]; /* bisectors: at most the neighbour constraints */
     LocalGet get{cons};
     lp3d(get, m, nObst, maxSpeed, failed, v, proj, fp64);
 }

@@ -53,10 +53,19 @@ def test_planner_host_only(c1_small, port):
     pl = Planner(scene)
     rng = np.random.default_rng(1)
     q = rng.uniform(-3, 103, (3000, 2)).astype(np.float32)
-    q[:100, 1] = scene.ecm.v_pos[:100, 1]  # exact vertex heights take the linear fallback
+    q[:100, 1] = scene.ecm.v_pos[:100, 1]  # exact vertex heights
+    # every quad-corner height (vertices and boundary closest points), with x
+    # far outside the quads too: the ray-cast test's hits left of a quad
+    ys = np.concatenate([np.asarray(scene.ecm.v_pos).reshape(-1, 2)[:, 1],
+                         np.asarray(scene.ecm.he_left).reshape(-1, 2)[:, 1],
+                         np.asarray(scene.ecm.he_right).reshape(-1, 2)[:, 1]]).astype(np.float32)
+    q2 = np.stack([rng.uniform(-60, 160, 4000), rng.choice(ys, 4000)], 1).astype(np.float32)
+    q = np.concatenate([q, q2])
     E = port.ecm(scene.ecm)
     want = np.array([port.point_location(E, float(x), float(y)) for x, y in q])
-    assert np.array_equal(pl.locate(q), want)
+    got = pl.locate(q)
+    assert np.array_equal(got, want)
+    assert (want[3000:] >= 0).sum() > 1000
     ok = [p for p in paths if p is not None]
     assert len(ok) == len(paths)
     n_ok = sum(1 for i in range(st.num_agents) if np.allclose(paths[i][0], st.pos[i]) and np.allclose(paths[i][-1], st.goal[i]))
