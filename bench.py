@@ -150,9 +150,10 @@ def cpu_baseline(scene, st, k, threads, budget_s=12.0):
             "ms_per_tick": tick_s * 1e3}
 
 
-def load_or_train_model(sim, args):
+def load_or_train_model(plain, learned, args):
     """The proposal network: committed weights when present, else trained
-    here on traces of this simulator's warm-up ticks (logged)."""
+    here on traces of 8 plain ticks (both simulators advance by 8 ticks, so
+    they stay in the same state)."""
     from ecmgenerator_gb300 import proposal as P
 
     m = P.ProposalModel(seed=0)
@@ -161,7 +162,8 @@ def load_or_train_model(sim, args):
         m.load(path)
         return m, {"weights": os.path.relpath(path, HERE)}
     t0 = time.time()
-    x, y = P.collect_traces(sim, ticks=8)
+    x, y = P.collect_traces(plain, ticks=8)
+    learned.update(ticks=8)
     loss, acc = m.train(x, y, steps=1500, batch=65536, lr=1e-3, seed=3)
     info = {"weights": "trained in this run on traces of its own warm-up ticks", "rows": int(x.shape[0]),
             "steps": 1500, "batch": 65536, "train_s": time.time() - t0, "loss": float(loss[-50:].mean()),
@@ -259,7 +261,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         plain.update()
         learned.update()
-    model, model_info = load_or_train_model(learned, args) if not args.plain_only else (None, None)
+    model, model_info = load_or_train_model(plain, learned, args) if not args.plain_only else (None, None)
     if model is not None:
         learned.set_proposal(model)
         learned.update()  # capture of the learned graph

@@ -467,6 +467,7 @@ ecmg_status ecmg_set_ecm(ecmg_ctx* c, const ecmg_ecm* e) { return ecmg_scene_set
 ecmg_status ecmg_set_planner(ecmg_ctx* c, ecmg_plan_fn fn, void* user)
 {
     if (!c) return ECMG_ERR_INVALID_ARG;
+    if ((fn == nullptr) != (c->plan_fn == nullptr)) c->graph_dirty = true; /* TickArgs::replan_dev_fail */
     c->plan_fn = fn;
     c->plan_user = user;
     return ECMG_OK;
@@ -886,6 +887,7 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t, bool use_model)
     t.del_sq = p.delete_radius * p.delete_radius;
     t.k = p.max_neighbors;
     t.lp3d_fp64 = p.lp3d_fp64;
+    t.replan_dev_fail = c->plan_fn == nullptr ? 1 : 0;
     t.counters = c->counters.p;
     t.destroyed_list = c->destroyed_list.p;
     t.replan_list = c->replan_list.p;
@@ -1014,6 +1016,8 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         st.agent_kernel_ms += ams;
         const int* out = c->h_counters + kCounters;
         int nd = out[C_DESTROYED], nr = out[C_REPLAN];
+        st.replans += out[C_REPLAN_DEV];
+        st.replans_failed += out[C_REPLAN_DEV];
         st.agent_steps += out[C_NSORTED];
         st.lp3d += out[C_LP3D];
         st.proposed += out[C_PROPOSED];

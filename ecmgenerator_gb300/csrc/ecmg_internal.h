@@ -42,6 +42,7 @@ enum {
     C_NSORTED = 7,     /* agents in the neighbour grid */
     C_PROPOSED = 8,    /* LPs that received a learned proposal */
     C_ACCEPTED = 9,    /* proposals that passed the exact check */
+    C_REPLAN_DEV = 10, /* re-plans that fail at the start retraction (not listed) */
     kCounters = 16
 };
 
@@ -100,6 +101,7 @@ struct TickArgs {
     float dt, tau_a, tau_o, rnb, rnb2, max_speed, mass_recip, arr_sq, del_sq;
     int k;
     int lp3d_fp64;
+    int replan_dev_fail;   /* built-in planner: settle unretractable re-plans on the device */
     /* outputs */
     int* counters;
     int* destroyed_list;

@@ -150,13 +150,15 @@ static cudaError_t scan(const int* in, int* out, int n, int* tmp, cudaStream_t s
 
 /* ---------------------------------------------------------------------- */
 /* exact kNN on the grid: the k smallest (d2, slot) with EPS < d2 < r^2.
-   keys: d2 bits (non-negative floats order as unsigned ints) : slot.       */
+   keys: d2 bits (non-negative floats order as unsigned ints) : slot.
+   The list holds the k nearest in key[K-k .. K-1], ascending; key[0 .. K-k)
+   hold 0 (below every real key, as d2 > EPS) and never move, unfilled
+   entries hold ~0 (above every real key), so the k-th key is key[K-1]. */
 template <int K>
 struct Knn {
     unsigned long long key[K];
     int ix[K]; /* grid-order index of the neighbour */
     int cnt;
-    unsigned long long kth; /* key of the k-th entry once cnt == k */
 };
 
 template <int K>
@@ -168,10 +170,10 @@ __device__ __forceinline__ void knn_consider(Knn<K>& s, int k, int j, V2 p, cons
     float d2 = dx * dx + dy * dy; /* KDTree.cpp:107-108 */
     if (!(d2 > kEps) || !(d2 < r2)) return;
     unsigned hi = __float_as_uint(d2);
-    if (s.cnt == k && hi > (unsigned)(s.kth >> 32)) return;
+    if (hi > (unsigned)(s.key[K - 1] >> 32)) return;
     unsigned long long kk = ((unsigned long long)hi << 32) | (unsigned)s_slot[j];
-    if (s.cnt == k && kk >= s.kth) return;
-    unsigned long long kth = s.kth;
+    if (kk >= s.key[K - 1]) return;
+    /* drop key[K-1], shift the larger entries up, place kk */
 #pragma unroll
     for (int q = K - 1; q >= 0; q--) {
         unsigned long long nk;
@@ -181,9 +183,7 @@ __device__ __forceinline__ void knn_consider(Knn<K>& s, int k, int j, V2 p, cons
         else { nk = s.key[q]; ni = s.ix[q]; }
         s.key[q] = nk;
         s.ix[q] = ni;
-        if (q == k - 1) kth = nk;
     }
-    s.kth = kth;
     if (s.cnt < k) s.cnt++;
 }
 
@@ -192,9 +192,8 @@ __device__ void knn_grid(Knn<K>& s, int k, V2 p, float rnb, float r2, const V2* 
                          const int* cell_start, const AgentGrid& g)
 {
 #pragma unroll
-    for (int q = 0; q < K; q++) { s.key[q] = ~0ull; s.ix[q] = -1; }
+    for (int q = 0; q < K; q++) { s.key[q] = q < K - k ? 0ull : ~0ull; s.ix[q] = -1; }
     s.cnt = 0;
-    s.kth = ~0ull;
     int cx, cy;
     cell_of(g, p, &cx, &cy);
     float x0 = g.x0 + (float)cx * g.cell, y0 = g.y0 + (float)cy * g.cell;
@@ -210,10 +209,20 @@ __device__ void knn_grid(Knn<K>& s, int k, V2 p, float rnb, float r2, const V2* 
                1 cm absorbs the rounding of the bucket assignment */
             float lb = (float)(R - 1) * g.cell + m - 0.01f;
             if (lb >= rnb) break;
-            if (s.cnt == k && lb > 0.0f && lb * lb > __uint_as_float((unsigned)(s.kth >> 32))) break;
+            if (s.cnt == k && lb > 0.0f && lb * lb > __uint_as_float((unsigned)(s.key[K - 1] >> 32))) break;
         }
         const int ylo = R < 0 ? 0 : cy - R, yhi = R < 0 ? 0 : cy + R;
         for (int y = ylo; y <= yhi; y++) {
+            /* cells whose distance from p (less 1 cm for the rounding of the
+               bucket assignment) exceeds the current k-th distance, or the
+               neighbour distance, cannot hold an accepted candidate */
+            const float kd2 = s.cnt == k ? __uint_as_float((unsigned)(s.key[K - 1] >> 32)) : r2;
+            float dy = 0.0f;
+            if (R >= 0) {
+                const float ry0 = g.y0 + (float)y * g.cell;
+                dy = fmaxf(fmaxf(ry0 - p.y, p.y - (ry0 + g.cell)) - 0.01f, 0.0f);
+                if (dy * dy > kd2) continue;
+            }
             for (int side = 0; side < 2; side++) {
                 int j0 = 0, j1 = 0;
                 if (R < 0) {
@@ -221,13 +230,20 @@ __device__ void knn_grid(Knn<K>& s, int k, V2 p, float rnb, float r2, const V2* 
                 } else if (y >= 0 && y < g.gh) {
                     const int xa = cx - R, xb = cx + R;
                     if (y == ylo || y == yhi) {
-                        int a = max(xa, 0), b = min(xb, g.gw - 1);
+                        const float dxm = sqrtf(kd2 - dy * dy) + 0.01f;
+                        const int xl = (int)floorf(fmaxf((p.x - dxm - g.x0) * g.inv, -1.0e6f));
+                        const int xr = (int)floorf(fminf((p.x + dxm - g.x0) * g.inv, 1.0e6f));
+                        int a = max(max(xa, 0), xl), b = min(min(xb, g.gw - 1), xr);
                         if (side == 0 && a <= b) { j0 = cell_start[y * g.gw + a]; j1 = cell_start[y * g.gw + b + 1]; }
                     } else {
                         int x = side == 0 ? xa : xb;
                         if (x >= 0 && x < g.gw && (side == 0 || xb != xa)) {
-                            j0 = cell_start[y * g.gw + x];
-                            j1 = cell_start[y * g.gw + x + 1];
+                            const float rx0 = g.x0 + (float)x * g.cell;
+                            const float dx = fmaxf(fmaxf(rx0 - p.x, p.x - (rx0 + g.cell)) - 0.01f, 0.0f);
+                            if (!(dx * dx + dy * dy > kd2)) {
+                                j0 = cell_start[y * g.gw + x];
+                                j1 = cell_start[y * g.gw + x + 1];
+                            }
                         }
                     }
                 }
@@ -413,9 +429,16 @@ __device__ void attract_tick(const TickArgs& a, int t)
         }
     } else {
         V2 ap = mk(0.0f, 0.0f); /* Point attractionPoint; (0,0) */
-        if (irm(sc.ecm, pos, path, np, &ap)) {
+        bool no_retract = false;
+        if (irm(sc.ecm, pos, path, np, &ap, &no_retract)) {
             attr = ap;
             a.attr[slot] = attr;
+        } else if (no_retract && a.replan_dev_fail) {
+            /* the built-in planner starts by retracting this same position
+               with the same point location, so its re-plan fails: the agent
+               keeps its path and attraction point without a host round trip */
+            attr = a.attr[slot];
+            atomicAdd(&a.counters[C_REPLAN_DEV], 1);
         } else {
             attr = a.attr[slot]; /* unchanged; the host re-plans before the next tick */
             int q = atomicAdd(&a.counters[C_REPLAN], 1);
@@ -543,8 +566,10 @@ __global__ void __launch_bounds__(128) k_neighbors(TickArgs a)
         a.ncnt[t] = nn.cnt;
         int* o = a.nbr + (size_t)t * a.k;
 #pragma unroll
-        for (int q = 0; q < K; q++)
-            if (q < a.k) o[q] = nn.ix[q];
+        for (int q2 = 0; q2 < K; q2++) {
+            const int q = q2 - (K - a.k);
+            if (q >= 0) o[q] = nn.ix[q2];
+        }
     }
 }
 
@@ -1022,8 +1047,10 @@ __global__ void __launch_bounds__(128) k_knn(const V2* s_pos, const int* s_slot,
         int slot = s_slot[t];
         out_cnt[slot] = nn.cnt;
 #pragma unroll
-        for (int q = 0; q < K; q++)
-            if (q < k) out_ids[slot * k + q] = q < nn.cnt ? s_slot[nn.ix[q]] : -1;
+        for (int q2 = 0; q2 < K; q2++) {
+            const int q = q2 - (K - k);
+            if (q >= 0) out_ids[slot * k + q] = q < nn.cnt ? s_slot[nn.ix[q2]] : -1;
+        }
     }
 }
 
