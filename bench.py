@@ -209,8 +209,8 @@ class TickTimer:
         self.ev = []
         self.steps = 0
         self.agent_ms = 0.0
-        self.tot = dict(lp3d=0, replans=0, replans_failed=0, destroyed=0, device_ms=0.0, proposed=0, accepted=0,
-                        gated=0)
+        self.tot = dict(lp3d=0, replans=0, replans_failed=0, destroyed=0, device_ms=0.0, host_ms=0.0, proposed=0,
+                        accepted=0, gated=0)
 
     def tick(self):
         import torch
@@ -294,15 +294,16 @@ def run_ours(args):
         t0 = time.perf_counter()
         for _ in range(args.steps):
             s = sim.update()
-            _ = sim.get_position_data()
-            _ = sim.get_velocity_data()
+            _ = sim.view("position")  # ecmg_host_view: the reference's getters (raw host pointers)
+            _ = sim.view("velocity")
             e2e_steps += s.agent_steps
         t1 = time.perf_counter()
         e2e[name] = e2e_steps * max(world, 1) / (t1 - t0)
     e2e_main = {"value": e2e["learned" if model is not None else "plain"], "unit": "agent-steps/s",
                 "h2d_bytes_per_step": 64, "d2h_bytes_per_step": 16 * n + 64,
-                "plain": e2e["plain"], "note": "wall clock of Simulator.update() + get_position_data() + "
-                "get_velocity_data() per tick; h2d = counters, d2h = positions and velocities + counters"}
+                "plain": e2e["plain"], "note": "wall clock of Simulator.update() + the position and velocity getters "
+                "(ecmg_host_view: device -> page-locked host copy) per tick; h2d = counters, d2h = positions and "
+                "velocities + counters"}
     kern_ms = main_t.agent_ms / max(args.steps, 1)
     peaks = {}
     try:
@@ -354,7 +355,8 @@ def run_ours(args):
         "tick_stats": {"lp3d_per_tick": T["lp3d"] / args.steps, "replans_per_tick": T["replans"] / args.steps,
                        "replans_failed_per_tick": T["replans_failed"] / args.steps,
                        "destroyed_per_tick": T["destroyed"] / args.steps,
-                       "graph_ms_per_tick": T["device_ms"] / args.steps},
+                       "graph_ms_per_tick": T["device_ms"] / args.steps,
+                       "host_ms_per_tick": T["host_ms"] / args.steps},
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(scene, st, k, threads=1, budget_s=args.cpu_budget)

@@ -134,6 +134,10 @@ struct ecmg_ctx {
     void* plan_user = nullptr;
     PlanScratch scratch;
     bool replan_enabled = true;
+    /* per slot: the start edge from which the built-in planner's search
+       failed for the slot's current goal and clearance (-1: none) */
+    std::vector<int> fail_edge;
+    DBuf<int> d_fail_edge;
     /* recording */
     bool record = false;
     DBuf<int> rec_nbr, rec_cnt, rec_fail, rec_ncons, rec_nobst;
@@ -151,6 +155,7 @@ struct ecmg_ctx {
     DBuf<unsigned char> feat, cls, label;
     /* pinned staging */
     int* h_counters = nullptr; /* [2 * kCounters]: in, out */
+    void* hview[4] = {nullptr, nullptr, nullptr, nullptr}; /* ecmg_host_view of the float2 fields */
     /* graph */
     cudaGraphExec_t graph[2] = {nullptr, nullptr}; /* plain tick, tick with the proposal model */
     bool graph_dirty = true;
@@ -274,6 +279,8 @@ ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max
     CKC(c->d_slot_scene.alloc(N));
     CKC(c->nbr.alloc(N * (size_t)prm.max_neighbors));
     CKC(c->ncnt.alloc(N));
+    CKC(c->d_fail_edge.alloc(N));
+    CKC(cudaMemset(c->d_fail_edge.p, 0xff, sizeof(int) * N)); /* -1 */
     CKC(c->counters.alloc(kCounters));
     CKC(c->path_xy.alloc(std::max<size_t>(1024, 4 * N)));
     CKC(cudaMemset(c->pos.p, 0, sizeof(V2) * N)); CKC(cudaMemset(c->vel.p, 0, sizeof(V2) * N));
@@ -285,6 +292,7 @@ ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max
     c->clear.assign(N, 0.0f);
     c->speed.assign(N, 0.0f);
     c->paths.assign(N, {});
+    c->fail_edge.assign(N, -1);
     c->slot_scene.assign(N, 0);
     int base = 0;
     for (int s = 0; s < n_scenes; s++) {
@@ -322,7 +330,7 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
                        &c->rec_vorca};
     for (auto* b : v2s) b->free_();
     DBuf<int>* is[] = {&c->path_off, &c->path_len, &c->key, &c->rank, &c->destroyed_list, &c->replan_list,
-                       &c->d_slot_scene, &c->nbr, &c->ncnt, &c->s_slot, &c->cell_count, &c->cell_start, &c->scan_tmp, &c->counters,
+                       &c->d_slot_scene, &c->nbr, &c->ncnt, &c->d_fail_edge, &c->s_slot, &c->cell_count, &c->cell_start, &c->scan_tmp, &c->counters,
                        &c->rec_nbr, &c->rec_cnt, &c->rec_fail, &c->rec_ncons, &c->rec_nobst};
     for (auto* b : is) b->free_();
     c->d_clear.free_();
@@ -335,6 +343,8 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
     c->d_scenes.free_();
     for (auto& s : c->scenes) s->free_all();
     if (c->h_counters) cudaFreeHost(c->h_counters);
+    for (void* h : c->hview)
+        if (h) cudaFreeHost(h);
     if (c->ev_t0) cudaEventDestroy(c->ev_t0);
     if (c->ev_t1) cudaEventDestroy(c->ev_t1);
     if (c->ev_a0) cudaEventDestroy(c->ev_a0);
@@ -473,8 +483,22 @@ ecmg_status ecmg_set_planner(ecmg_ctx* c, ecmg_plan_fn fn, void* user)
     return ECMG_OK;
 }
 
+/* forgets a slot's failed-search edge (its path, goal or clearance changed) */
+static ecmg_status clear_fail_edge(ecmg_ctx* c, int slot)
+{
+    if (c->fail_edge[slot] < 0) return ECMG_OK;
+    c->fail_edge[slot] = -1;
+    const int none = -1;
+    CK(cudaMemcpy(c->d_fail_edge.p + slot, &none, sizeof(int), cudaMemcpyHostToDevice));
+    return ECMG_OK;
+}
+
 static ecmg_status upload_path(ecmg_ctx* c, int slot)
 {
+    {
+        ecmg_status fs = clear_fail_edge(c, slot);
+        if (fs != ECMG_OK) return fs;
+    }
     const std::vector<V2>& p = c->paths[slot];
     size_t n = p.size();
     if (c->path_used + n > c->path_xy.n) {
@@ -553,6 +577,8 @@ ecmg_status ecmg_scene_add_agents(ecmg_ctx* c, int scene, int n, const float* po
         c->paths[idx].assign((const V2*)(path_xy + 2 * (size_t)path_off[i]),
                              (const V2*)(path_xy + 2 * (size_t)(path_off[i] + path_len[i])));
         note_range(c, sc, clearance[i], pref_speed[i]);
+        ecmg_status fs = clear_fail_edge(c, idx);
+        if (fs != ECMG_OK) return fs;
     }
     /* contiguous runs of slots are uploaded in one copy each */
     for (int i = 0; i < n;) {
@@ -610,9 +636,11 @@ ecmg_status ecmg_add_agents(ecmg_ctx* c, int n, const float* pos, const float* c
     return ecmg_scene_add_agents(c, 0, n, pos, clearance, pref_speed, path_off, path_len, path_xy, out_slots);
 }
 
-static ecmg_status plan(ecmg_ctx* c, SceneState* sc, V2 s, V2 g, float clr, std::vector<V2>& out, PlanScratch& scr)
+static ecmg_status plan(ecmg_ctx* c, SceneState* sc, V2 s, V2 g, float clr, std::vector<V2>& out, PlanScratch& scr,
+                        int* astar_fail_edge = nullptr)
 {
     out.clear();
+    if (astar_fail_edge) *astar_fail_edge = -1;
     if (c->plan_fn) {
         std::vector<float> buf(2 * 4096);
         int n = c->plan_fn(c->plan_user, s.x, s.y, g.x, g.y, clr, buf.data(), 4096);
@@ -622,7 +650,7 @@ static ecmg_status plan(ecmg_ctx* c, SceneState* sc, V2 s, V2 g, float clr, std:
         return n > 0 ? ECMG_OK : ECMG_ERR_NO_PATH;
     }
     if (!sc->hs.has_ecm) return ECMG_ERR_STATE;
-    return plan_path(sc->hs, sc->vis_grid, s, g, clr, out, scr) ? ECMG_OK : ECMG_ERR_NO_PATH;
+    return plan_path(sc->hs, sc->vis_grid, s, g, clr, out, scr, astar_fail_edge) ? ECMG_OK : ECMG_ERR_NO_PATH;
 }
 
 ecmg_status ecmg_find_path(ecmg_ctx* c, float sx, float sy, float gx, float gy, float clearance, float* out_xy,
@@ -888,6 +916,7 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t, bool use_model)
     t.k = p.max_neighbors;
     t.lp3d_fp64 = p.lp3d_fp64;
     t.replan_dev_fail = c->plan_fn == nullptr ? 1 : 0;
+    t.fail_edge = c->d_fail_edge.p;
     t.counters = c->counters.p;
     t.destroyed_list = c->destroyed_list.p;
     t.replan_list = c->replan_list.p;
@@ -1060,13 +1089,14 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
                batches are planned on several host threads. */
             std::vector<std::vector<V2>> res(m);
             std::vector<char> ok(m, 0);
+            std::vector<int> fe(m, -1);
             auto serve = [&](int t, int nt) {
                 PlanScratch scr;
                 for (int i = t; i < m; i += nt) {
                     int q = order[i], sl = r[q];
                     SceneState* sc = c->scenes[c->slot_scene[sl]].get();
                     V2 goal = c->paths[sl].back();
-                    ok[i] = plan(c, sc, rp[q], goal, c->clear[sl], res[i], scr) == ECMG_OK && !res[i].empty();
+                    ok[i] = plan(c, sc, rp[q], goal, c->clear[sl], res[i], scr, &fe[i]) == ECMG_OK && !res[i].empty();
                 }
             };
             int nt = c->plan_fn ? 1 : std::min(16, std::max(1, m / 32));
@@ -1087,6 +1117,10 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
                     if (ps != ECMG_OK) return ps;
                 } else {
                     st.replans_failed++;
+                    if (fe[i] >= 0 && c->fail_edge[sl] != fe[i]) {
+                        c->fail_edge[sl] = fe[i];
+                        CK(cudaMemcpy(c->d_fail_edge.p + sl, &fe[i], sizeof(int), cudaMemcpyHostToDevice));
+                    }
                 }
             }
         }
@@ -1254,6 +1288,32 @@ ecmg_status ecmg_get_state(ecmg_ctx* c, int field, void* dst)
     default: return fail(c, ECMG_ERR_INVALID_ARG, "unknown field %d", field);
     }
     return ECMG_OK;
+}
+
+ecmg_status ecmg_host_view(ecmg_ctx* c, int field, const void** out)
+{
+    if (!c || !out) return ECMG_ERR_INVALID_ARG;
+    size_t N = (size_t)c->max_agents;
+    switch (field) {
+    case ECMG_FIELD_CLEARANCE: *out = c->clear.data(); return ECMG_OK;
+    case ECMG_FIELD_SPEED: *out = c->speed.data(); return ECMG_OK;
+    case ECMG_FIELD_ACTIVE: *out = c->active.data(); return ECMG_OK;
+    case ECMG_FIELD_POSITION:
+    case ECMG_FIELD_VELOCITY:
+    case ECMG_FIELD_PREF_VELOCITY:
+    case ECMG_FIELD_ATTRACTION: {
+        void*& h = c->hview[field];
+        if (!h) CK(cudaHostAlloc(&h, sizeof(V2) * N, cudaHostAllocDefault));
+        const V2* src = field == ECMG_FIELD_POSITION ? c->pos.p
+                        : field == ECMG_FIELD_VELOCITY ? c->vel.p
+                        : field == ECMG_FIELD_PREF_VELOCITY ? c->pref_vel.p : c->attr.p;
+        CK(cudaMemcpyAsync(h, src, sizeof(V2) * N, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        *out = h;
+        return ECMG_OK;
+    }
+    default: return fail(c, ECMG_ERR_INVALID_ARG, "unknown field %d", field);
+    }
 }
 
 ecmg_status ecmg_set_state(ecmg_ctx* c, int field, const void* src)

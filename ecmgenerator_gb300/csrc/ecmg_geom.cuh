@@ -251,7 +251,8 @@ EG_HD bool retract(const EcmView& e, V2 loc, V2* out, int* out_edge)
 /* IRMPathFollower::FindAttractionPoint (IRMPathFollower.cpp:14-115).
    *out is written only where the reference writes outPoint; *no_retract is
    set when the failure is the retraction of pos itself. */
-EG_NI bool irm(const EcmView& e, V2 pos, const V2* path, int n, V2* out, bool* no_retract = nullptr)
+EG_NI bool irm(const EcmView& e, V2 pos, const V2* path, int n, V2* out, bool* no_retract = nullptr,
+               int* edge = nullptr)
 {
     V2 r;
     int ed;
@@ -259,6 +260,7 @@ EG_NI bool irm(const EcmView& e, V2 pos, const V2* path, int n, V2* out, bool* n
         if (no_retract) *no_retract = true;
         return false;
     }
+    if (edge) *edge = ed;
     V2 co = closest_on_segment(r, e.he_left[2 * ed], e.he_right[2 * ed + 1]);
     float clr = len(r - co);
     float rcs = clr * clr;

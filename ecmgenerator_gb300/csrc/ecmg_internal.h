@@ -101,7 +101,8 @@ struct TickArgs {
     float dt, tau_a, tau_o, rnb, rnb2, max_speed, mass_recip, arr_sq, del_sq;
     int k;
     int lp3d_fp64;
-    int replan_dev_fail;   /* built-in planner: settle unretractable re-plans on the device */
+    int replan_dev_fail;   /* built-in planner: settle known-failing re-plans on the device */
+    const int* fail_edge;  /* slot -> ECM edge from which its re-plan search failed (-1: none) */
     /* outputs */
     int* counters;
     int* destroyed_list;

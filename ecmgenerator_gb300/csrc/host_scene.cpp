@@ -304,9 +304,10 @@ static bool clear_line(const HostScene& s, const GridCSR& g, V2 a, V2 b, double 
 }
 
 bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float clearance,
-               std::vector<V2>& out, PlanScratch& scr)
+               std::vector<V2>& out, PlanScratch& scr, int* astar_fail_edge)
 {
     out.clear();
+    if (astar_fail_edge) *astar_fail_edge = -1;
     if (!s.has_ecm) return false;
     EcmView ev = s.ecm_view();
     V2 rs, rg;
@@ -374,7 +375,10 @@ bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float 
             h = s.he_next[h];
         } while (h != h0 && ++guard < 1024);
     }
-    if (found < 0) return false;
+    if (found < 0) {
+        if (astar_fail_edge) *astar_fail_edge = es;
+        return false;
+    }
     std::vector<V2> pts;
     pts.push_back(goal);
     for (int v = found; v >= 0; v = scr.parent[v]) pts.push_back(s.v_pos[v]);

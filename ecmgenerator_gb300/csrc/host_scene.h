@@ -61,8 +61,11 @@ struct PlanScratch {
    AStar::FindPath (AStar.cpp:44-160), then the polyline start, vertices, goal
    is shortened greedily wherever a straight piece keeps `clearance` from every
    obstacle edge.  Returns false when no path exists. */
+/* *astar_fail_edge (optional) is set to the start's ECM edge when the search
+   itself fails (a property of that edge, the goal and the clearance only),
+   else to -1 */
 bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float clearance,
-               std::vector<V2>& out, PlanScratch& scr);
+               std::vector<V2>& out, PlanScratch& scr, int* astar_fail_edge = nullptr);
 
 }  // namespace ecmg
 #endif

@@ -430,13 +430,17 @@ __device__ void attract_tick(const TickArgs& a, int t)
     } else {
         V2 ap = mk(0.0f, 0.0f); /* Point attractionPoint; (0,0) */
         bool no_retract = false;
-        if (irm(sc.ecm, pos, path, np, &ap, &no_retract)) {
+        int red = -1;
+        if (irm(sc.ecm, pos, path, np, &ap, &no_retract, &red)) {
             attr = ap;
             a.attr[slot] = attr;
-        } else if (no_retract && a.replan_dev_fail) {
+        } else if (a.replan_dev_fail && (no_retract || (red >= 0 && a.fail_edge[slot] == red))) {
             /* the built-in planner starts by retracting this same position
-               with the same point location, so its re-plan fails: the agent
-               keeps its path and attraction point without a host round trip */
+               with the same point location; it fails there, or its search
+               already failed from this ECM edge for this goal and clearance
+               (a property of the edge only).  Either way the re-plan fails:
+               the agent keeps its path and attraction point without a host
+               round trip. */
             attr = a.attr[slot];
             atomicAdd(&a.counters[C_REPLAN_DEV], 1);
         } else {

@@ -214,6 +214,23 @@ class Simulator:
         self._ck(self.L.ecmg_get_state(self.h, FIELD[field], _ptr(out)))
         return out
 
+    def view(self, field: str):
+        """Read-only numpy view of the library's host copy of a field
+        (ecmg_host_view), as the reference's getters return pointers into the
+        Simulator's arrays: refreshed by this call, overwritten by the next
+        view of the same field."""
+        p = C.c_void_p()
+        self._ck(self.L.ecmg_host_view(self.h, FIELD[field], C.byref(p)))
+        n = self.max_agents
+        if field == "active":
+            arr = np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_uint8)), shape=(n,))
+        elif field in ("clearance", "speed"):
+            arr = np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_float)), shape=(n,))
+        else:
+            arr = np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_float)), shape=(n, 2))
+        arr.flags.writeable = False
+        return arr
+
     def get_num_agents(self) -> int:
         n = C.c_int()
         self._ck(self.L.ecmg_get_counts(self.h, C.byref(n), None, None))

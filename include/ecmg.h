@@ -175,6 +175,11 @@ ecmg_status ecmg_tick(ecmg_ctx* ctx, int n_ticks, ecmg_tick_stats* stats);
 
 /* Getters of Simulator.h:114-126, copied to caller memory (n_slots entries) */
 ecmg_status ecmg_get_state(ecmg_ctx* ctx, int field, void* host_dst);
+/* The getters as the reference has them: a pointer to library-owned host
+   memory (page-locked for the device fields, refreshed from the device by
+   this call).  The pointer stays valid until ecmg_destroy; its contents are
+   those of this call until the next ecmg_host_view of the same field. */
+ecmg_status ecmg_host_view(ecmg_ctx* ctx, int field, const void** out);
 /* Overwrite slot-indexed state from the host (float[2*n] for the 2-vectors);
    used to start a tick from a given state. */
 ecmg_status ecmg_set_state(ecmg_ctx* ctx, int field, const void* host_src);

@@ -55,13 +55,6 @@ public:
         check(ecmg_create(&p, maxAgents, &m_Ctx), "ecmg_create");
         check(ecmg_set_obstacles(m_Ctx, &obstacles), "ecmg_set_obstacles");
         check(ecmg_set_ecm(m_Ctx, &ecm), "ecmg_set_ecm");
-        m_Pos.resize(maxAgents);
-        m_Vel.resize(maxAgents);
-        m_PrefVel.resize(maxAgents);
-        m_Attr.resize(maxAgents);
-        m_Clear.resize(maxAgents);
-        m_Speed.resize(maxAgents);
-        m_Active.resize(maxAgents);
     }
     ~Simulator()
     {
@@ -79,24 +72,24 @@ public:
         ecmg_status s = ecmg_spawn_agent(m_Ctx, start.x, start.y, goal.x, goal.y, clearance, preferredSpeed, &slot);
         if (s == ECMG_ERR_NO_SLOT || s == ECMG_ERR_INVALID_SPAWN || s == ECMG_ERR_NO_PATH) return -1;
         check(s, "ecmg_spawn_agent");
-        m_Dirty = true;
+        m_Dirty = 0x7fu;
         return slot;
     }
     void DestroyAgent(int idx)
     {
         check(ecmg_destroy_agent(m_Ctx, idx), "ecmg_destroy_agent");
-        m_Dirty = true;
+        m_Dirty = 0x7fu;
     }
     /* like the reference, the argument is ignored in favour of the step time */
     void Update(float /*dt*/)
     {
         check(ecmg_tick(m_Ctx, 1, &m_Stats), "ecmg_tick");
-        m_Dirty = true;
+        m_Dirty = 0x7fu;
     }
     void Reset()
     {
         check(ecmg_reset(m_Ctx), "ecmg_reset");
-        m_Dirty = true;
+        m_Dirty = 0x7fu;
     }
     void SetPlanner(ecmg_plan_fn fn, void* user) { check(ecmg_set_planner(m_Ctx, fn, user), "ecmg_set_planner"); }
 
@@ -112,13 +105,18 @@ public:
         ecmg_get_counts(m_Ctx, nullptr, &n, nullptr);
         return n;
     }
-    PositionComponent* GetPositionData() { sync(); return m_Pos.data(); }
-    VelocityComponent* GetVelocityData() { sync(); return m_Vel.data(); }
-    VelocityComponent* GetPreferredVelocityData() { sync(); return m_PrefVel.data(); }
-    PositionComponent* GetAttractionPointData() { sync(); return m_Attr.data(); }
-    ClearanceComponent* GetClearanceData() { sync(); return m_Clear.data(); }
-    SpeedComponent* GetSpeedData() { sync(); return m_Speed.data(); }
-    bool* GetActiveFlags() { sync(); return reinterpret_cast<bool*>(m_Active.data()); }
+    /* raw host pointers as the reference returns them: library-owned host
+       copies, refreshed on the first call after the state changed */
+    PositionComponent* GetPositionData() { return static_cast<PositionComponent*>(view(ECMG_FIELD_POSITION)); }
+    VelocityComponent* GetVelocityData() { return static_cast<VelocityComponent*>(view(ECMG_FIELD_VELOCITY)); }
+    VelocityComponent* GetPreferredVelocityData()
+    {
+        return static_cast<VelocityComponent*>(view(ECMG_FIELD_PREF_VELOCITY));
+    }
+    PositionComponent* GetAttractionPointData() { return static_cast<PositionComponent*>(view(ECMG_FIELD_ATTRACTION)); }
+    ClearanceComponent* GetClearanceData() { return static_cast<ClearanceComponent*>(view(ECMG_FIELD_CLEARANCE)); }
+    SpeedComponent* GetSpeedData() { return static_cast<SpeedComponent*>(view(ECMG_FIELD_SPEED)); }
+    bool* GetActiveFlags() { return static_cast<bool*>(view(ECMG_FIELD_ACTIVE)); }
     float GetSimulationStepTime() const
     {
         ecmg_params p;
@@ -134,28 +132,22 @@ private:
         if (s != ECMG_OK)
             throw std::runtime_error(std::string(what) + ": " + (m_Ctx ? ecmg_last_error(m_Ctx) : "no context"));
     }
-    void sync()
+    void* view(int field)
     {
-        if (!m_Dirty) return;
-        check(ecmg_get_state(m_Ctx, ECMG_FIELD_POSITION, m_Pos.data()), "get position");
-        check(ecmg_get_state(m_Ctx, ECMG_FIELD_VELOCITY, m_Vel.data()), "get velocity");
-        check(ecmg_get_state(m_Ctx, ECMG_FIELD_PREF_VELOCITY, m_PrefVel.data()), "get preferred velocity");
-        check(ecmg_get_state(m_Ctx, ECMG_FIELD_ATTRACTION, m_Attr.data()), "get attraction");
-        check(ecmg_get_state(m_Ctx, ECMG_FIELD_CLEARANCE, m_Clear.data()), "get clearance");
-        check(ecmg_get_state(m_Ctx, ECMG_FIELD_SPEED, m_Speed.data()), "get speed");
-        check(ecmg_get_state(m_Ctx, ECMG_FIELD_ACTIVE, m_Active.data()), "get active");
-        m_Dirty = false;
+        if (m_Dirty & (1u << field)) {
+            const void* p = nullptr;
+            check(ecmg_host_view(m_Ctx, field, &p), "ecmg_host_view");
+            m_View[field] = const_cast<void*>(p);
+            m_Dirty &= ~(1u << field);
+        }
+        return m_View[field];
     }
 
     ecmg_ctx* m_Ctx = nullptr;
     int m_Max;
-    bool m_Dirty = true;
+    unsigned m_Dirty = 0x7fu; /* one bit per ECMG_FIELD_* */
+    void* m_View[7] = {};
     ecmg_tick_stats m_Stats{};
-    std::vector<PositionComponent> m_Pos, m_Attr;
-    std::vector<VelocityComponent> m_Vel, m_PrefVel;
-    std::vector<ClearanceComponent> m_Clear;
-    std::vector<SpeedComponent> m_Speed;
-    std::vector<std::uint8_t> m_Active;
 };
 
 }  // namespace ecmg

@@ -133,3 +133,27 @@ def test_knn_standalone(lib, c1_small):
     torch.cuda.synchronize()
     got = out.cpu().numpy()
     assert np.array_equal(got, want)
+
+
+def test_host_view_matches_getters(c1_small, lib):
+    """ecmg_host_view: library-owned host copies, the reference's raw-pointer getters"""
+    from ecmgenerator_gb300.simulator import Simulator
+
+    scene, st, paths = c1_small
+    sim = Simulator(scene, st.n_slots, 1.0 / 60.0, max_neighbors=10, **ORCA)
+    sim.add_agents(st.pos, st.clear, st.pref_speed, paths)
+    sim.update(ticks=3)
+    v1 = sim.view("position")
+    assert np.array_equal(v1, sim.get_position_data())
+    p1 = v1.__array_interface__["data"][0]
+    sim.update()
+    v2 = sim.view("position")
+    assert v2.__array_interface__["data"][0] == p1  # same host array, refreshed
+    assert np.array_equal(v2, sim.get_position_data())
+    for f, g in (("velocity", sim.get_velocity_data), ("pref_velocity", sim.get_preferred_velocity_data),
+                 ("attraction", sim.get_attraction_point_data), ("clearance", sim.get_clearance_data),
+                 ("speed", sim.get_speed_data), ("active", sim.get_active_flags)):
+        assert np.array_equal(sim.view(f), g()), f
+    with pytest.raises(ValueError):
+        v2[0, 0] = 1.0  # read-only
+    sim.close()
