@@ -209,8 +209,8 @@ class TickTimer:
         self.ev = []
         self.steps = 0
         self.agent_ms = 0.0
-        self.tot = dict(lp3d=0, replans=0, replans_failed=0, destroyed=0, device_ms=0.0, host_ms=0.0, proposed=0,
-                        accepted=0, gated=0)
+        self.tot = dict(lp3d=0, replans=0, replans_failed=0, replans_host=0, destroyed=0, device_ms=0.0, host_ms=0.0,
+                        proposed=0, accepted=0, gated=0)
 
     def tick(self):
         import torch
@@ -272,9 +272,12 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
+        # K plain ticks, then the learned simulator's K ticks from the same
+        # state (blocks, so that neither sim's timing sees the other's work)
         for i in range(args.steps):
             tp.tick()
-            if model is not None:
+        if model is not None:
+            for i in range(args.steps):
                 tl.tick()
         torch.cuda.synchronize()
     same = bool(np.array_equal(plain.get_position_data(), learned.get_position_data()))
@@ -354,6 +357,7 @@ def run_ours(args):
         "clocks": clk.summary(),
         "tick_stats": {"lp3d_per_tick": T["lp3d"] / args.steps, "replans_per_tick": T["replans"] / args.steps,
                        "replans_failed_per_tick": T["replans_failed"] / args.steps,
+                       "replans_host_per_tick": T["replans_host"] / args.steps,
                        "destroyed_per_tick": T["destroyed"] / args.steps,
                        "graph_ms_per_tick": T["device_ms"] / args.steps,
                        "host_ms_per_tick": T["host_ms"] / args.steps},

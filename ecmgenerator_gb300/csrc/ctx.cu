@@ -899,6 +899,8 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t, bool use_model)
     t.cell_start = c->cell_start.p;
     t.nbr = c->nbr.p;
     t.ncnt = c->ncnt.p;
+    t.slot_bucket = c->key.p;
+    t.slot_rank = c->rank.p;
     t.scenes = c->d_scenes.p;
     t.slot_scene = b.slot_scene;
     t.tile = c->lp_mode ? c->wgrab : c->tile;
@@ -1056,6 +1058,7 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         c->trace_rows = out[C_NSORTED];
         st.destroyed += nd;
         st.replans += nr;
+        st.replans_host += nr;
         if (out[C_ERROR]) {
             result = fail(c, ECMG_ERR_BOUND, "device bound exceeded (flags 0x%x): %s", out[C_ERROR],
                           (out[C_ERROR] & ECMG_DEV_ERR_CONSTRAINTS) ? "more than 24 obstacle half-planes for one agent"

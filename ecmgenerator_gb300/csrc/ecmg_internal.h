@@ -89,6 +89,8 @@ struct TickArgs {
     const int* cell_start; /* total buckets + 1 */
     int* nbr;              /* [n * k] neighbours of grid-order agent t, as grid-order indices */
     int* ncnt;             /* [n] neighbour count */
+    const int* slot_bucket; /* slot -> bucket of this tick's binning */
+    const int* slot_rank;   /* slot -> rank inside its bucket */
     void* feat;            /* [n, kMlpIn] bf16 proposal features (learned mode / tracing) */
     const unsigned char* cls; /* [n] proposed class (null: plain LP) */
     const unsigned char* cls_slot; /* [slots] proposed class by slot (overrides cls) */

@@ -153,11 +153,12 @@ static cudaError_t scan(const int* in, int* out, int n, int* tmp, cudaStream_t s
    keys: d2 bits (non-negative floats order as unsigned ints) : slot.
    The list holds the k nearest in key[K-k .. K-1], ascending; key[0 .. K-k)
    hold 0 (below every real key, as d2 > EPS) and never move, unfilled
-   entries hold ~0 (above every real key), so the k-th key is key[K-1]. */
+   entries hold ~0 (above every real key), so the k-th key is key[K-1].  The
+   slot in the low half of a key identifies the neighbour; its grid-order
+   index is recovered once at the end (bucket start + rank of the slot). */
 template <int K>
 struct Knn {
     unsigned long long key[K];
-    int ix[K]; /* grid-order index of the neighbour */
     int cnt;
 };
 
@@ -177,12 +178,10 @@ __device__ __forceinline__ void knn_consider(Knn<K>& s, int k, int j, V2 p, cons
 #pragma unroll
     for (int q = K - 1; q >= 0; q--) {
         unsigned long long nk;
-        int ni;
-        if (q > 0 && s.key[q - 1] > kk) { nk = s.key[q - 1]; ni = s.ix[q - 1]; }
-        else if (s.key[q] > kk) { nk = kk; ni = j; }
-        else { nk = s.key[q]; ni = s.ix[q]; }
+        if (q > 0 && s.key[q - 1] > kk) nk = s.key[q - 1];
+        else if (s.key[q] > kk) nk = kk;
+        else nk = s.key[q];
         s.key[q] = nk;
-        s.ix[q] = ni;
     }
     if (s.cnt < k) s.cnt++;
 }
@@ -192,7 +191,7 @@ __device__ void knn_grid(Knn<K>& s, int k, V2 p, float rnb, float r2, const V2* 
                          const int* cell_start, const AgentGrid& g)
 {
 #pragma unroll
-    for (int q = 0; q < K; q++) { s.key[q] = q < K - k ? 0ull : ~0ull; s.ix[q] = -1; }
+    for (int q = 0; q < K; q++) s.key[q] = q < K - k ? 0ull : ~0ull;
     s.cnt = 0;
     int cx, cy;
     cell_of(g, p, &cx, &cy);
@@ -572,7 +571,10 @@ __global__ void __launch_bounds__(128) k_neighbors(TickArgs a)
 #pragma unroll
         for (int q2 = 0; q2 < K; q2++) {
             const int q = q2 - (K - a.k);
-            if (q >= 0) o[q] = nn.ix[q2];
+            if (q >= 0) {
+                const int sl = (int)(unsigned)nn.key[q2];
+                o[q] = q < nn.cnt ? a.cell_start[a.slot_bucket[sl]] + a.slot_rank[sl] : -1;
+            }
         }
     }
 }
@@ -1053,7 +1055,7 @@ __global__ void __launch_bounds__(128) k_knn(const V2* s_pos, const int* s_slot,
 #pragma unroll
         for (int q2 = 0; q2 < K; q2++) {
             const int q = q2 - (K - k);
-            if (q >= 0) out_ids[slot * k + q] = q < nn.cnt ? s_slot[nn.ix[q2]] : -1;
+            if (q >= 0) out_ids[slot * k + q] = q < nn.cnt ? (int)(unsigned)nn.key[q2] : -1;
         }
     }
 }

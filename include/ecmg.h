@@ -75,6 +75,7 @@ typedef struct {
     long long proposed;    /* learned mode: LPs that received an active-set proposal */
     long long accepted;    /* learned mode: proposals that passed the exact check     */
     long long gated;       /* learned mode: ticks run without the model (gate closed) */
+    long long replans_host; /* re-plans served by the host planner (the rest were settled on the device) */
 } ecmg_tick_stats;
 
 /* Static obstacles: n_obstacles rings, ring r = xy[2*ring_offsets[r] ..
