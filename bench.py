@@ -272,13 +272,17 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        # K plain ticks, then the learned simulator's K ticks from the same
-        # state (blocks, so that neither sim's timing sees the other's work)
-        for i in range(args.steps):
-            tp.tick()
-        if model is not None:
-            for i in range(args.steps):
-                tl.tick()
+        time.sleep(0.5)  # let the sampler start before the timed ticks
+        # alternating blocks of plain and learned ticks (each simulator ends
+        # K ticks later, in the same state as the other)
+        nblk = 4 if args.steps >= 4 else 1
+        bounds = [args.steps * b // nblk for b in range(nblk + 1)]
+        for b in range(nblk):
+            for i in range(bounds[b], bounds[b + 1]):
+                tp.tick()
+            if model is not None:
+                for i in range(bounds[b], bounds[b + 1]):
+                    tl.tick()
         torch.cuda.synchronize()
     same = bool(np.array_equal(plain.get_position_data(), learned.get_position_data()))
     main_t = tl if model is not None else tp

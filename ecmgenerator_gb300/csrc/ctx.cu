@@ -156,6 +156,15 @@ struct ecmg_ctx {
     /* pinned staging */
     int* h_counters = nullptr; /* [2 * kCounters]: in, out */
     void* hview[4] = {nullptr, nullptr, nullptr, nullptr}; /* ecmg_host_view of the float2 fields */
+    /* the first kListStage entries of the destroyed / re-plan lists, copied
+       back by every tick (no extra copy when a tick's lists fit) */
+    static constexpr int kListStage = 1024;
+    int* h_lists = nullptr; /* destroyed[kListStage], replan[kListStage], replan_pos[2 * kListStage] (float) */
+    /* page-locked staging of the small uploads between two ticks (paths of
+       re-planned agents); the copies are queued on the stream ahead of the
+       next tick */
+    unsigned char* h_up = nullptr;
+    size_t h_up_cap = 0, h_up_used = 0;
     /* graph */
     cudaGraphExec_t graph[2] = {nullptr, nullptr}; /* plain tick, tick with the proposal model */
     bool graph_dirty = true;
@@ -288,6 +297,7 @@ ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max
     CKC(cudaMemset(c->d_active.p, 0, N)); CKC(cudaMemset(c->path_len.p, 0, sizeof(int) * N));
     CKC(cudaMemset(c->path_off.p, 0, sizeof(int) * N));
     CKC(cudaHostAlloc((void**)&c->h_counters, sizeof(int) * 2 * kCounters, cudaHostAllocDefault));
+    CKC(cudaHostAlloc((void**)&c->h_lists, sizeof(int) * 4 * ecmg_ctx::kListStage, cudaHostAllocDefault));
     c->active.assign(N, 0);
     c->clear.assign(N, 0.0f);
     c->speed.assign(N, 0.0f);
@@ -343,6 +353,8 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
     c->d_scenes.free_();
     for (auto& s : c->scenes) s->free_all();
     if (c->h_counters) cudaFreeHost(c->h_counters);
+    if (c->h_lists) cudaFreeHost(c->h_lists);
+    if (c->h_up) cudaFreeHost(c->h_up);
     for (void* h : c->hview)
         if (h) cudaFreeHost(h);
     if (c->ev_t0) cudaEventDestroy(c->ev_t0);
@@ -483,14 +495,37 @@ ecmg_status ecmg_set_planner(ecmg_ctx* c, ecmg_plan_fn fn, void* user)
     return ECMG_OK;
 }
 
+/* queues a copy of host memory to the device on the context's stream,
+   through the page-locked staging area (no wait for the copy) */
+static ecmg_status stage_copy(ecmg_ctx* c, void* dev_dst, const void* src, size_t bytes)
+{
+    if (bytes == 0) return ECMG_OK;
+    if (c->h_up_used + bytes > c->h_up_cap) {
+        CK(cudaStreamSynchronize(c->stream)); /* staged copies done: the area is free */
+        c->h_up_used = 0;
+        if (bytes > c->h_up_cap) {
+            if (c->h_up) cudaFreeHost(c->h_up);
+            c->h_up = nullptr;
+            c->h_up_cap = 0;
+            size_t cap = std::max<size_t>(bytes, 1u << 20);
+            CK(cudaHostAlloc((void**)&c->h_up, cap, cudaHostAllocDefault));
+            c->h_up_cap = cap;
+        }
+    }
+    unsigned char* p = c->h_up + c->h_up_used;
+    std::memcpy(p, src, bytes);
+    c->h_up_used += (bytes + 15) & ~(size_t)15;
+    CK(cudaMemcpyAsync(dev_dst, p, bytes, cudaMemcpyHostToDevice, c->stream));
+    return ECMG_OK;
+}
+
 /* forgets a slot's failed-search edge (its path, goal or clearance changed) */
 static ecmg_status clear_fail_edge(ecmg_ctx* c, int slot)
 {
     if (c->fail_edge[slot] < 0) return ECMG_OK;
     c->fail_edge[slot] = -1;
     const int none = -1;
-    CK(cudaMemcpy(c->d_fail_edge.p + slot, &none, sizeof(int), cudaMemcpyHostToDevice));
-    return ECMG_OK;
+    return stage_copy(c, c->d_fail_edge.p + slot, &none, sizeof(int));
 }
 
 static ecmg_status upload_path(ecmg_ctx* c, int slot)
@@ -502,7 +537,8 @@ static ecmg_status upload_path(ecmg_ctx* c, int slot)
     const std::vector<V2>& p = c->paths[slot];
     size_t n = p.size();
     if (c->path_used + n > c->path_xy.n) {
-        /* grow (x2) and compact: live paths only */
+        /* grow (x2) and compact: live paths only (after the queued uploads) */
+        CK(cudaStreamSynchronize(c->stream));
         size_t live = 0;
         for (int i = 0; i < c->max_agents; i++) live += c->paths[i].size();
         size_t cap = std::max(c->path_xy.n * 2, live * 2 + 1024);
@@ -526,9 +562,10 @@ static ecmg_status upload_path(ecmg_ctx* c, int slot)
         return ECMG_OK;
     }
     int off = (int)c->path_used, len = (int)n;
-    if (n) CK(cudaMemcpy(c->path_xy.p + off, p.data(), sizeof(V2) * n, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(c->path_off.p + slot, &off, sizeof(int), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(c->path_len.p + slot, &len, sizeof(int), cudaMemcpyHostToDevice));
+    ecmg_status s = stage_copy(c, c->path_xy.p + off, p.data(), sizeof(V2) * n);
+    if (s == ECMG_OK) s = stage_copy(c, c->path_off.p + slot, &off, sizeof(int));
+    if (s == ECMG_OK) s = stage_copy(c, c->path_len.p + slot, &len, sizeof(int));
+    if (s != ECMG_OK) return s;
     c->path_used += n;
     return ECMG_OK;
 }
@@ -553,6 +590,7 @@ ecmg_status ecmg_scene_add_agents(ecmg_ctx* c, int scene, int n, const float* po
         return fail(c, ECMG_ERR_INVALID_ARG, "null or negative argument");
     if ((size_t)n > sc->free_stack.size())
         return fail(c, ECMG_ERR_NO_SLOT, "%d agents requested, %zu slots free", n, sc->free_stack.size());
+    CK(cudaStreamSynchronize(c->stream)); /* queued uploads land before the copies below */
     for (int i = 0; i < n; i++) {
         if (!finite2(pos[2 * i], pos[2 * i + 1]) || !std::isfinite(clearance[i]) || !std::isfinite(pref_speed[i]))
             return fail(c, ECMG_ERR_INVALID_ARG, "agent %d: non-finite input", i);
@@ -970,8 +1008,19 @@ static cudaError_t enqueue_tick(ecmg_ctx* c, int launch_slots, bool use_model)
     e = launch_tick(b, t, launch_slots, c->scan_tmp.p, c->block, c->sms, c->stream, c->ev_a0, c->ev_a1,
                     use_model ? propose_cb : nullptr, &pc);
     if (e != cudaSuccess) return e;
-    return cudaMemcpyAsync(c->h_counters + kCounters, c->counters.p, sizeof(int) * kCounters, cudaMemcpyDeviceToHost,
-                           c->stream);
+    e = cudaMemcpyAsync(c->h_counters + kCounters, c->counters.p, sizeof(int) * kCounters, cudaMemcpyDeviceToHost,
+                        c->stream);
+    if (e != cudaSuccess) return e;
+    const size_t ls = (size_t)std::min(ecmg_ctx::kListStage, c->max_agents);
+    int* hl = c->h_lists;
+    e = cudaMemcpyAsync(hl, c->destroyed_list.p, sizeof(int) * ls, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hl + ecmg_ctx::kListStage, c->replan_list.p, sizeof(int) * ls, cudaMemcpyDeviceToHost,
+                            c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hl + 2 * ecmg_ctx::kListStage, c->replan_pos.p, sizeof(V2) * ls, cudaMemcpyDeviceToHost,
+                            c->stream);
+    return e;
 }
 
 void* ecmg_stream(const ecmg_ctx* c) { return c ? (void*)c->stream : nullptr; }
@@ -1038,6 +1087,7 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         }
         CK(cudaEventRecord(c->ev_t1, c->stream));
         CK(cudaStreamSynchronize(c->stream));
+        c->h_up_used = 0; /* every queued upload has been applied */
         auto h0 = std::chrono::steady_clock::now();
         float ms = 0, ams = 0;
         if (cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1) != cudaSuccess) ms = 0;
@@ -1066,7 +1116,8 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         }
         if (nd > 0) {
             std::vector<int> d(std::min(nd, c->max_agents));
-            CK(cudaMemcpy(d.data(), c->destroyed_list.p, sizeof(int) * d.size(), cudaMemcpyDeviceToHost));
+            if ((int)d.size() <= ecmg_ctx::kListStage) std::memcpy(d.data(), c->h_lists, sizeof(int) * d.size());
+            else CK(cudaMemcpy(d.data(), c->destroyed_list.p, sizeof(int) * d.size(), cudaMemcpyDeviceToHost));
             std::sort(d.begin(), d.end()); /* DestroyAgent order: slot order of the loop */
             for (int s : d) {
                 SceneState* sc = c->scenes[c->slot_scene[s]].get();
@@ -1080,8 +1131,13 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             int m = std::min(nr, c->max_agents);
             std::vector<int> r(m);
             std::vector<V2> rp(m);
-            CK(cudaMemcpy(r.data(), c->replan_list.p, sizeof(int) * m, cudaMemcpyDeviceToHost));
-            CK(cudaMemcpy(rp.data(), c->replan_pos.p, sizeof(V2) * m, cudaMemcpyDeviceToHost));
+            if (m <= ecmg_ctx::kListStage) {
+                std::memcpy(r.data(), c->h_lists + ecmg_ctx::kListStage, sizeof(int) * m);
+                std::memcpy(rp.data(), c->h_lists + 2 * ecmg_ctx::kListStage, sizeof(V2) * m);
+            } else {
+                CK(cudaMemcpy(r.data(), c->replan_list.p, sizeof(int) * m, cudaMemcpyDeviceToHost));
+                CK(cudaMemcpy(rp.data(), c->replan_pos.p, sizeof(V2) * m, cudaMemcpyDeviceToHost));
+            }
             std::vector<int> order(m);
             for (int i = 0; i < m; i++) order[i] = i;
             std::sort(order.begin(), order.end(), [&](int a, int b) { return r[a] < r[b]; });
@@ -1122,7 +1178,8 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
                     st.replans_failed++;
                     if (fe[i] >= 0 && c->fail_edge[sl] != fe[i]) {
                         c->fail_edge[sl] = fe[i];
-                        CK(cudaMemcpy(c->d_fail_edge.p + sl, &fe[i], sizeof(int), cudaMemcpyHostToDevice));
+                        ecmg_status fs = stage_copy(c, c->d_fail_edge.p + sl, &fe[i], sizeof(int));
+                        if (fs != ECMG_OK) return fs;
                     }
                 }
             }
@@ -1332,6 +1389,9 @@ ecmg_status ecmg_set_state(ecmg_ctx* c, int field, const void* src)
     case ECMG_FIELD_CLEARANCE:
         std::memcpy(c->clear.data(), src, sizeof(float) * N);
         CK(cudaMemcpy(c->d_clear.p, src, sizeof(float) * N, cudaMemcpyHostToDevice));
+        /* remembered failed searches were for the old clearances */
+        std::fill(c->fail_edge.begin(), c->fail_edge.end(), -1);
+        CK(cudaMemset(c->d_fail_edge.p, 0xff, sizeof(int) * N));
         for (size_t i = 0; i < N; i++)
             if (c->active[i]) note_range(c, c->scenes[c->slot_scene[i]].get(), c->clear[i], c->speed[i]);
         break;

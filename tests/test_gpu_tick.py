@@ -157,3 +157,43 @@ def test_host_view_matches_getters(c1_small, lib):
     with pytest.raises(ValueError):
         v2[0, 0] = 1.0  # read-only
     sim.close()
+
+
+def test_failed_search_is_settled_on_the_device(c1_small, lib, port):
+    """A re-plan whose search failed from an ECM edge fails again from that
+    edge (same goal and clearance): the next failure is settled on the device,
+    with the same outcome (the agent keeps its path)."""
+    from ecmgenerator_gb300.simulator import Planner, Simulator
+
+    scene, st, paths = c1_small
+    pl = Planner(scene)
+    O = port.obstacles(scene)
+    clr = 3.0
+    # an agent too wide for the corridors to its goal, in the open, following
+    # a path that is not near it
+    pick = None
+    for i in range(st.num_agents):
+        p, g = st.pos[i].astype(np.float32), st.goal[i].astype(np.float32)
+        if np.linalg.norm(p - g) < 30.0:
+            continue
+        if pl.find_paths(p[None], g[None], np.array([clr], np.float32))[0] is not None:
+            continue
+        r = 2.0 * 1.3 + clr
+        if len(port.find_obstacles(O, float(p[0]), float(p[1]), r * r)) == 0:
+            pick = (p, g)
+            break
+    assert pick is not None
+    p0, goal = pick
+    far = np.stack([goal + np.float32(0.5), goal]).astype(np.float32)
+    sim = Simulator(scene, 4, 1.0 / 60.0, max_neighbors=10, **ORCA)
+    slot = int(sim.add_agents(p0[None], [clr], [1.3], [far])[0])
+    s1 = sim.update()
+    assert (s1.replans, s1.replans_failed, s1.replans_host) == (1, 1, 1)
+    s2 = sim.update(ticks=5)
+    assert s2.replans == 5 and s2.replans_failed == 5 and s2.replans_host < 5
+    assert np.array_equal(sim.get_path(slot), far)
+    # a caller-supplied planner is always asked
+    sim.set_planner(lambda *a: None)
+    s3 = sim.update(ticks=3)
+    assert s3.replans == 3 and s3.replans_host == 3
+    sim.close()
