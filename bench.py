@@ -346,7 +346,10 @@ def run_ours(args):
                    "seed": args.seed, "mode": "learned proposal" if model is not None else "plain",
                    "launch": launch},
         "plain": {"value": plain_value, "ms_per_step": p_ms_all / args.steps,
-                  "lp3d_per_tick": tp.tot["lp3d"] / args.steps},
+                  "lp3d_per_tick": tp.tot["lp3d"] / args.steps,
+                  "graph_ms_per_tick": tp.tot["device_ms"] / args.steps,
+                  "host_ms_per_tick": tp.tot["host_ms"] / args.steps,
+                  "replans_host_per_tick": tp.tot["replans_host"] / args.steps},
         "learned_vs_plain": value / plain_value if model is not None else None,
         "proposal": None if model is None else {
             **model_info, "proposed_per_tick": T["proposed"] / args.steps,
