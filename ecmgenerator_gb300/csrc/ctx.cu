@@ -97,6 +97,7 @@ struct ecmg_ctx {
     std::string err;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr, ev_a0 = nullptr, ev_a1 = nullptr;
+    cudaEvent_t ev_mid = nullptr; /* after k_attract: destroyed / re-plan lists are final */
     int sms = 1;
     /* launch configuration (autotuned) */
     int block = 128;
@@ -154,7 +155,7 @@ struct ecmg_ctx {
     int trace_rows = 0;
     DBuf<unsigned char> feat, cls, label;
     /* pinned staging */
-    int* h_counters = nullptr; /* [2 * kCounters]: in, out */
+    int* h_counters = nullptr; /* [3 * kCounters]: in, out, after k_attract */
     void* hview[4] = {nullptr, nullptr, nullptr, nullptr}; /* ecmg_host_view of the float2 fields */
     /* the first kListStage entries of the destroyed / re-plan lists, copied
        back by every tick (no extra copy when a tick's lists fit) */
@@ -279,6 +280,7 @@ ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max
     CKC(cudaEventCreate(&c->ev_t1));
     CKC(cudaEventCreate(&c->ev_a0));
     CKC(cudaEventCreate(&c->ev_a1));
+    CKC(cudaEventCreateWithFlags(&c->ev_mid, cudaEventDisableTiming));
     size_t N = (size_t)total;
     CKC(c->pos.alloc(N)); CKC(c->vel.alloc(N)); CKC(c->attr.alloc(N)); CKC(c->pref_vel.alloc(N));
     CKC(c->d_clear.alloc(N)); CKC(c->d_speed.alloc(N)); CKC(c->d_active.alloc(N));
@@ -299,7 +301,7 @@ ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max
     CKC(cudaMemset(c->attr.p, 0, sizeof(V2) * N)); CKC(cudaMemset(c->pref_vel.p, 0, sizeof(V2) * N));
     CKC(cudaMemset(c->d_active.p, 0, N)); CKC(cudaMemset(c->path_len.p, 0, sizeof(int) * N));
     CKC(cudaMemset(c->path_off.p, 0, sizeof(int) * N));
-    CKC(cudaHostAlloc((void**)&c->h_counters, sizeof(int) * 2 * kCounters, cudaHostAllocDefault));
+    CKC(cudaHostAlloc((void**)&c->h_counters, sizeof(int) * 3 * kCounters, cudaHostAllocDefault));
     CKC(cudaHostAlloc((void**)&c->h_lists, sizeof(int) * 4 * ecmg_ctx::kListStage, cudaHostAllocDefault));
     c->active.assign(N, 0);
     c->clear.assign(N, 0.0f);
@@ -364,6 +366,7 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
     if (c->ev_t1) cudaEventDestroy(c->ev_t1);
     if (c->ev_a0) cudaEventDestroy(c->ev_a0);
     if (c->ev_a1) cudaEventDestroy(c->ev_a1);
+    if (c->ev_mid) cudaEventDestroy(c->ev_mid);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return ECMG_OK;
@@ -996,6 +999,26 @@ static cudaError_t propose_cb(void* user, cudaStream_t s)
     return mlp_infer(pc->model, pc->feat, pc->n_dev, pc->n_max, pc->cls, s, pc->sms);
 }
 
+/* after k_attract: the destroyed / re-plan lists are final; copy them and
+   the counters back and mark the point, so that the host can start the
+   re-plans while the neighbour and ORCA kernels run */
+static cudaError_t after_attract_cb(void* user, cudaStream_t s, unsigned evflags)
+{
+    ecmg_ctx* c = (ecmg_ctx*)user;
+    cudaError_t e = cudaMemcpyAsync(c->h_counters + 2 * kCounters, c->counters.p, sizeof(int) * kCounters,
+                                    cudaMemcpyDeviceToHost, s);
+    const size_t ls = (size_t)std::min(ecmg_ctx::kListStage, c->max_agents);
+    int* hl = c->h_lists;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hl, c->destroyed_list.p, sizeof(int) * ls, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hl + ecmg_ctx::kListStage, c->replan_list.p, sizeof(int) * ls, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hl + 2 * ecmg_ctx::kListStage, c->replan_pos.p, sizeof(V2) * ls, cudaMemcpyDeviceToHost,
+                            s);
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(c->ev_mid, s, evflags);
+    return e;
+}
+
 /* the device work of one tick: counters in, kernels, counters out */
 static cudaError_t enqueue_tick(ecmg_ctx* c, int launch_slots, bool use_model)
 {
@@ -1011,21 +1034,10 @@ static cudaError_t enqueue_tick(ecmg_ctx* c, int launch_slots, bool use_model)
     }
     ProposeCall pc{c->model, c->feat.p, c->counters.p + C_NSORTED, launch_slots, c->cls.p, c->sms};
     e = launch_tick(b, t, launch_slots, c->scan_tmp.p, c->block, c->sms, c->stream, c->ev_a0, c->ev_a1,
-                    use_model ? propose_cb : nullptr, &pc);
+                    use_model ? propose_cb : nullptr, &pc, after_attract_cb, c);
     if (e != cudaSuccess) return e;
-    e = cudaMemcpyAsync(c->h_counters + kCounters, c->counters.p, sizeof(int) * kCounters, cudaMemcpyDeviceToHost,
-                        c->stream);
-    if (e != cudaSuccess) return e;
-    const size_t ls = (size_t)std::min(ecmg_ctx::kListStage, c->max_agents);
-    int* hl = c->h_lists;
-    e = cudaMemcpyAsync(hl, c->destroyed_list.p, sizeof(int) * ls, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(hl + ecmg_ctx::kListStage, c->replan_list.p, sizeof(int) * ls, cudaMemcpyDeviceToHost,
-                            c->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(hl + 2 * ecmg_ctx::kListStage, c->replan_pos.p, sizeof(V2) * ls, cudaMemcpyDeviceToHost,
-                            c->stream);
-    return e;
+    return cudaMemcpyAsync(c->h_counters + kCounters, c->counters.p, sizeof(int) * kCounters, cudaMemcpyDeviceToHost,
+                           c->stream);
 }
 
 void* ecmg_stream(const ecmg_ctx* c) { return c ? (void*)c->stream : nullptr; }
@@ -1091,34 +1103,17 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             CK(enqueue_tick(c, last + 1, use_model));
         }
         CK(cudaEventRecord(c->ev_t1, c->stream));
-        CK(cudaStreamSynchronize(c->stream));
-        c->h_up_used = 0; /* every queued upload has been applied */
+        /* the lists are final after k_attract: bookkeeping and re-plans run
+           on the host while the rest of the tick runs on the device; path
+           uploads are queued behind the tick */
+        CK(cudaEventSynchronize(c->ev_mid));
         auto h0 = std::chrono::steady_clock::now();
-        float ms = 0, ams = 0;
-        if (cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1) != cudaSuccess) ms = 0;
-        if (cudaEventElapsedTime(&ams, c->ev_a0, c->ev_a1) != cudaSuccess) ams = 0;
-        cudaGetLastError();
-        st.device_ms += ms;
-        st.agent_kernel_ms += ams;
-        const int* out = c->h_counters + kCounters;
-        int nd = out[C_DESTROYED], nr = out[C_REPLAN];
-        st.replans += out[C_REPLAN_DEV];
-        st.replans_failed += out[C_REPLAN_DEV];
-        st.agent_steps += out[C_NSORTED];
-        st.lp3d += out[C_LP3D];
-        st.proposed += out[C_PROPOSED];
-        st.accepted += out[C_ACCEPTED];
-        if (use_model && c->gate_min > 0.0f && (float)out[C_ACCEPTED] < c->gate_min * (float)out[C_NSORTED])
-            c->gate_left = c->gate_pause;
-        c->trace_rows = out[C_NSORTED];
+        const int* mid = c->h_counters + 2 * kCounters;
+        int nd = mid[C_DESTROYED], nr = mid[C_REPLAN];
         st.destroyed += nd;
-        st.replans += nr;
+        st.replans += nr + mid[C_REPLAN_DEV];
         st.replans_host += nr;
-        if (out[C_ERROR]) {
-            result = fail(c, ECMG_ERR_BOUND, "device bound exceeded (flags 0x%x): %s", out[C_ERROR],
-                          (out[C_ERROR] & ECMG_DEV_ERR_CONSTRAINTS) ? "more than 24 obstacle half-planes for one agent"
-                                                                    : "event list overflow");
-        }
+        st.replans_failed += mid[C_REPLAN_DEV];
         if (nd > 0) {
             std::vector<int> d(std::min(nd, c->max_agents));
             if ((int)d.size() <= ecmg_ctx::kListStage) std::memcpy(d.data(), c->h_lists, sizeof(int) * d.size());
@@ -1149,8 +1144,8 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             /* Simulator::UpdatePath (Simulator.cpp:97-124) from the tick-start
                position, served in slot order.  When no path is found the agent
                keeps its previous path (the reference would keep an empty one and
-               index path.x[-1]).  The built-in planner is re-entrant, so large
-               batches are planned on several host threads. */
+               index path.x[-1]).  The built-in planner is re-entrant, so the
+               searches of a tick run on several host threads. */
             std::vector<std::vector<V2>> res(m);
             std::vector<char> ok(m, 0);
             std::vector<int> fe(m, -1);
@@ -1163,7 +1158,7 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
                     ok[i] = plan(c, sc, rp[q], goal, c->clear[sl], res[i], scr, &fe[i]) == ECMG_OK && !res[i].empty();
                 }
             };
-            int nt = c->plan_fn ? 1 : std::min(16, std::max(1, m / 32));
+            int nt = c->plan_fn ? 1 : std::min(16, m);
             nt = std::min<int>(nt, (int)std::max(1u, std::thread::hardware_concurrency()));
             if (nt > 1) {
                 std::vector<std::thread> th;
@@ -1190,6 +1185,29 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             }
         }
         st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - h0).count();
+        CK(cudaStreamSynchronize(c->stream));
+        c->h_up_used = 0; /* every queued upload has been applied */
+        auto h1 = std::chrono::steady_clock::now();
+        float ms = 0, ams = 0;
+        if (cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1) != cudaSuccess) ms = 0;
+        if (cudaEventElapsedTime(&ams, c->ev_a0, c->ev_a1) != cudaSuccess) ams = 0;
+        cudaGetLastError();
+        st.device_ms += ms;
+        st.agent_kernel_ms += ams;
+        const int* out = c->h_counters + kCounters;
+        st.agent_steps += out[C_NSORTED];
+        st.lp3d += out[C_LP3D];
+        st.proposed += out[C_PROPOSED];
+        st.accepted += out[C_ACCEPTED];
+        if (use_model && c->gate_min > 0.0f && (float)out[C_ACCEPTED] < c->gate_min * (float)out[C_NSORTED])
+            c->gate_left = c->gate_pause;
+        c->trace_rows = out[C_NSORTED];
+        if (out[C_ERROR]) {
+            result = fail(c, ECMG_ERR_BOUND, "device bound exceeded (flags 0x%x): %s", out[C_ERROR],
+                          (out[C_ERROR] & ECMG_DEV_ERR_CONSTRAINTS) ? "more than 24 obstacle half-planes for one agent"
+                                                                    : "event list overflow");
+        }
+        st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - h1).count();
     }
     st.active_agents = c->num_agents;
     st.last_index = c->global_last();

@@ -145,8 +145,13 @@ struct BinArgs {
 /* kernels.cu; propose (may be null) runs between the feature kernel and the
    per-agent kernel and fills TickArgs::cls */
 typedef cudaError_t (*ProposeFn)(void* user, cudaStream_t s);
+/* after_attract (may be null) runs right after the attraction kernel, when
+   the destroyed and re-plan lists are final; evflags are the flags for an
+   event record at that point (external when the stream is being captured) */
+typedef cudaError_t (*HookFn)(void* user, cudaStream_t s, unsigned evflags);
 cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int block, int sms,
-                        cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1, ProposeFn propose, void* propose_user);
+                        cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1, ProposeFn propose, void* propose_user,
+                        HookFn after_attract, void* after_attract_user);
 cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k, float r, AgentGrid g,
                        int* key, int* rank, int* cell_count, int* cell_start, int* s_slot, V2* s_pos,
                        int* scan_tmp, int scan_blocks, int* out_ids, int* out_cnt, cudaStream_t s);

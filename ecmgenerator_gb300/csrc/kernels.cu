@@ -1096,7 +1096,8 @@ static int grid_for(int n, int block, int sms, int per_sm)
 }
 
 cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int block, int sms,
-                        cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1, ProposeFn propose, void* propose_user)
+                        cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1, ProposeFn propose, void* propose_user,
+                        HookFn after_attract, void* after_attract_user)
 {
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(s, &cap);
@@ -1115,6 +1116,10 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
     int gk = grid_for(max_slots, 128, sms, 16);
     int per_sm = 1;
     k_attract<<<gk, 128, 0, s>>>(t);
+    if (after_attract) {
+        e = after_attract(after_attract_user, s, evflags);
+        if (e != cudaSuccess) return e;
+    }
     if (t.k <= 8) k_neighbors<8><<<gk, 128, 0, s>>>(t);
     else if (t.k <= 16) k_neighbors<16><<<gk, 128, 0, s>>>(t);
     else k_neighbors<32><<<gk, 128, 0, s>>>(t);
