@@ -179,7 +179,7 @@ def apply_launch(plain, learned, args):
     from ecmgenerator_gb300.simulator import autotune, set_launch, set_lp_mode
 
     if args.lp_mode == "tune":
-        r = autotune(plain, ticks_per_trial=1)
+        r = autotune(plain, ticks_per_trial=2)
         log(f"[bench] autotune: {r}")
         grab = r["agents_per_warp_grab"]
         for s_ in (plain, learned):
@@ -264,6 +264,8 @@ def run_ours(args):
     model, model_info = load_or_train_model(plain, learned, args) if not args.plain_only else (None, None)
     if model is not None:
         learned.set_proposal(model)
+        if args.no_gate:
+            learned.set_proposal_gate(0.0, 0)
         learned.update()  # capture of the learned graph
         plain.update()
     torch.cuda.synchronize()
@@ -419,6 +421,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="time the plain tick only")
     ap.add_argument("--proposal", default=None, help="proposal weights (.npy)")
+    ap.add_argument("--no-gate", action="store_true", help="keep the proposal model on every tick")
     ap.add_argument("--lp-mode", default="tune", choices=["tune", "thread", "warp"],
                     help="per-agent kernel layout (default: autotuned)")
     args = ap.parse_args()
