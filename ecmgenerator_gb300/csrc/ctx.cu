@@ -118,7 +118,7 @@ struct ecmg_ctx {
     DBuf<V2> pos, vel, attr, pref_vel, replan_pos;
     DBuf<float> d_clear, d_speed;
     DBuf<unsigned char> d_active;
-    DBuf<int> path_off, path_len, key, rank, destroyed_list, replan_list, d_slot_scene, nbr, ncnt, prev_nbr, prev_cnt;
+    DBuf<int> path_off, path_len, key, rank, destroyed_list, replan_list, d_slot_scene, nbr, ncnt;
     DBuf<V2> path_xy;
     size_t path_used = 0;
     /* snapshot */
@@ -290,9 +290,6 @@ ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max
     CKC(c->d_slot_scene.alloc(N));
     CKC(c->nbr.alloc(N * (size_t)prm.max_neighbors));
     CKC(c->ncnt.alloc(N));
-    CKC(c->prev_nbr.alloc(N * (size_t)prm.max_neighbors));
-    CKC(c->prev_cnt.alloc(N));
-    CKC(cudaMemset(c->prev_cnt.p, 0, sizeof(int) * N));
     CKC(c->d_fail_edge.alloc(N));
     CKC(cudaMemset(c->d_fail_edge.p, 0xff, sizeof(int) * N)); /* -1 */
     CKC(c->counters.alloc(kCounters));
@@ -345,7 +342,7 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
                        &c->rec_vorca};
     for (auto* b : v2s) b->free_();
     DBuf<int>* is[] = {&c->path_off, &c->path_len, &c->key, &c->rank, &c->destroyed_list, &c->replan_list,
-                       &c->d_slot_scene, &c->nbr, &c->ncnt, &c->prev_nbr, &c->prev_cnt, &c->d_fail_edge, &c->s_slot, &c->cell_count, &c->cell_start, &c->scan_tmp, &c->counters,
+                       &c->d_slot_scene, &c->nbr, &c->ncnt, &c->d_fail_edge, &c->s_slot, &c->cell_count, &c->cell_start, &c->scan_tmp, &c->counters,
                        &c->rec_nbr, &c->rec_cnt, &c->rec_fail, &c->rec_ncons, &c->rec_nobst};
     for (auto* b : is) b->free_();
     c->d_clear.free_();
@@ -945,8 +942,6 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t, bool use_model)
     t.ncnt = c->ncnt.p;
     t.slot_bucket = c->key.p;
     t.slot_rank = c->rank.p;
-    t.prev_nbr = c->prev_nbr.p;
-    t.prev_cnt = c->prev_cnt.p;
     t.scenes = c->d_scenes.p;
     t.slot_scene = b.slot_scene;
     t.tile = c->lp_mode ? c->wgrab : c->tile;

@@ -91,8 +91,6 @@ struct TickArgs {
     int* ncnt;             /* [n] neighbour count */
     const int* slot_bucket; /* slot -> bucket of this tick's binning */
     const int* slot_rank;   /* slot -> rank inside its bucket */
-    int* prev_nbr;          /* [slots * k] neighbour slots of the last tick (a search bound only) */
-    int* prev_cnt;          /* [slots] their count (0: none) */
     void* feat;            /* [n, kMlpIn] bf16 proposal features (learned mode / tracing) */
     const unsigned char* cls; /* [n] proposed class (null: plain LP) */
     const unsigned char* cls_slot; /* [slots] proposed class by slot (overrides cls) */

@@ -160,7 +160,6 @@ template <int K>
 struct Knn {
     unsigned long long key[K];
     int cnt;
-    unsigned ub; /* bits of an upper bound of the k-th d2 known in advance (+inf: none) */
 };
 
 template <int K>
@@ -172,7 +171,7 @@ __device__ __forceinline__ void knn_consider(Knn<K>& s, int k, int j, V2 p, cons
     float d2 = dx * dx + dy * dy; /* KDTree.cpp:107-108 */
     if (!(d2 > kEps) || !(d2 < r2)) return;
     unsigned hi = __float_as_uint(d2);
-    if (hi > min((unsigned)(s.key[K - 1] >> 32), s.ub)) return;
+    if (hi > (unsigned)(s.key[K - 1] >> 32)) return;
     unsigned long long kk = ((unsigned long long)hi << 32) | (unsigned)s_slot[j];
     if (kk >= s.key[K - 1]) return;
     /* drop key[K-1], shift the larger entries up, place kk */
@@ -187,16 +186,13 @@ __device__ __forceinline__ void knn_consider(Knn<K>& s, int k, int j, V2 p, cons
     if (s.cnt < k) s.cnt++;
 }
 
-/* ub: an upper bound of the k-th smallest d2 known before the search (k
-   distinct candidates within it), or +inf */
 template <int K>
 __device__ void knn_grid(Knn<K>& s, int k, V2 p, float rnb, float r2, const V2* s_pos, const int* s_slot,
-                         const int* cell_start, const AgentGrid& g, float ub = INFINITY)
+                         const int* cell_start, const AgentGrid& g)
 {
 #pragma unroll
     for (int q = 0; q < K; q++) s.key[q] = q < K - k ? 0ull : ~0ull;
     s.cnt = 0;
-    s.ub = __float_as_uint(ub);
     int cx, cy;
     cell_of(g, p, &cx, &cy);
     float x0 = g.x0 + (float)cx * g.cell, y0 = g.y0 + (float)cy * g.cell;
@@ -212,15 +208,14 @@ __device__ void knn_grid(Knn<K>& s, int k, V2 p, float rnb, float r2, const V2* 
                1 cm absorbs the rounding of the bucket assignment */
             float lb = (float)(R - 1) * g.cell + m - 0.01f;
             if (lb >= rnb) break;
-            const float bound = fminf(s.cnt == k ? __uint_as_float((unsigned)(s.key[K - 1] >> 32)) : INFINITY, ub);
-            if (lb > 0.0f && lb * lb > bound) break;
+            if (s.cnt == k && lb > 0.0f && lb * lb > __uint_as_float((unsigned)(s.key[K - 1] >> 32))) break;
         }
         const int ylo = R < 0 ? 0 : cy - R, yhi = R < 0 ? 0 : cy + R;
         for (int y = ylo; y <= yhi; y++) {
             /* cells whose distance from p (less 1 cm for the rounding of the
                bucket assignment) exceeds the current k-th distance, or the
                neighbour distance, cannot hold an accepted candidate */
-            const float kd2 = fminf(s.cnt == k ? __uint_as_float((unsigned)(s.key[K - 1] >> 32)) : r2, ub);
+            const float kd2 = s.cnt == k ? __uint_as_float((unsigned)(s.key[K - 1] >> 32)) : r2;
             float dy = 0.0f;
             if (R >= 0) {
                 const float ry0 = g.y0 + (float)y * g.cell;
@@ -569,28 +564,8 @@ __global__ void __launch_bounds__(128) k_neighbors(TickArgs a)
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int slot = a.s_slot[t];
         const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
-        const V2 p = a.s_pos[t];
-        /* last tick's neighbours, if all k are still in the grid within the
-           neighbour distance, bound this tick's k-th distance from above
-           (pos[] holds the tick-start positions until k_agents) */
-        float ub = INFINITY;
-        int* prev = a.prev_nbr + (size_t)slot * a.k;
-        if (a.prev_cnt[slot] == a.k) {
-            float mx = 0.0f;
-            bool ok = true;
-            for (int q = 0; q < a.k && ok; q++) {
-                const int o = prev[q];
-                if (o == slot || !a.active[o]) { ok = false; break; }
-                const V2 po = a.pos[o];
-                const float dx = po.x - p.x, dy = po.y - p.y;
-                const float d2 = dx * dx + dy * dy;
-                if (!(d2 > kEps) || !(d2 < a.rnb2)) ok = false;
-                mx = fmaxf(mx, d2);
-            }
-            if (ok) ub = mx;
-        }
         Knn<K> nn;
-        knn_grid<K>(nn, a.k, p, a.rnb, a.rnb2, a.s_pos, a.s_slot, a.cell_start + sc.bucket_base, sc.grid, ub);
+        knn_grid<K>(nn, a.k, a.s_pos[t], a.rnb, a.rnb2, a.s_pos, a.s_slot, a.cell_start + sc.bucket_base, sc.grid);
         a.ncnt[t] = nn.cnt;
         int* o = a.nbr + (size_t)t * a.k;
 #pragma unroll
@@ -599,10 +574,8 @@ __global__ void __launch_bounds__(128) k_neighbors(TickArgs a)
             if (q >= 0) {
                 const int sl = (int)(unsigned)nn.key[q2];
                 o[q] = q < nn.cnt ? a.cell_start[a.slot_bucket[sl]] + a.slot_rank[sl] : -1;
-                if (q < nn.cnt) prev[q] = sl;
             }
         }
-        a.prev_cnt[slot] = nn.cnt;
     }
 }
 

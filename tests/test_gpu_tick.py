@@ -197,3 +197,74 @@ def test_failed_search_is_settled_on_the_device(c1_small, lib, port):
     s3 = sim.update(ticks=3)
     assert s3.replans == 3 and s3.replans_host == 3
     sim.close()
+
+
+def test_agents_outside_the_scene_bitexact(port, c1_small):
+    """agents outside the grid rectangle sit in the overflow bucket that every
+    query scans; their IRM fails (no ECM cell), their re-plans fail"""
+    scene, st, paths = c1_small
+    st = st.copy()
+    far = np.array([[-40.0, 10.0], [-40.5, 10.2], [150.0, 150.0], [-39.8, 9.9]], np.float32)
+    st.pos[:4] = far
+    ev = _run(port, scene, st, paths, ticks=6, k=10)
+    assert ev > 0
+
+
+def test_empty_and_single_agent(lib, c1_small):
+    from ecmgenerator_gb300.simulator import Simulator
+
+    scene, st, paths = c1_small
+    sim = Simulator(scene, 8, 1.0 / 60.0, max_neighbors=10, **ORCA)
+    s0 = sim.update(ticks=3)  # nothing to do
+    assert s0.agent_steps == 0 and s0.ticks == 3 and sim.get_num_agents() == 0
+    slot = int(sim.add_agents(st.pos[:1], st.clear[:1], st.pref_speed[:1], paths[:1])[0])
+    s1 = sim.update(ticks=2)
+    assert s1.agent_steps == 2 and sim.get_num_agents() == 1
+    rec_free = sim.get_position_data()[slot]
+    assert np.all(np.isfinite(rec_free))
+    sim.destroy_agent(slot)
+    s2 = sim.update()
+    assert s2.agent_steps == 0 and sim.get_num_agents() == 0
+    sim.close()
+
+
+def test_full_capacity_and_slot_reuse(port, c1_small):
+    """every slot in use; destroyed slots are reused last-in first-out"""
+    from ecmgenerator_gb300.simulator import Simulator
+
+    scene, st, paths = c1_small
+    n = st.num_agents
+    sim = Simulator(scene, n, 1.0 / 60.0, max_neighbors=10, **ORCA)
+    slots = sim.add_agents(st.pos[:n], st.clear[:n], st.pref_speed[:n], paths[:n])
+    assert np.array_equal(slots, np.arange(n))
+    with pytest.raises(Exception):
+        sim.add_agents(st.pos[:1], st.clear[:1], st.pref_speed[:1], paths[:1])
+    sim.destroy_agent(7)
+    sim.destroy_agent(3)
+    again = sim.add_agents(st.pos[:2], st.clear[:2], st.pref_speed[:2], paths[:2])
+    assert list(again) == [3, 7]
+    sim.update(ticks=2)
+    assert sim.get_num_agents() == n
+    sim.close()
+
+
+def test_obstacle_constraint_overflow_is_reported(lib):
+    """more than 24 obstacle half-planes for one agent: the tick returns
+    ECMG_ERR_BOUND (the agent is computed with the first 24)"""
+    from ecmgenerator_gb300 import scene as sc
+    from ecmgenerator_gb300._lib import EcmgError
+    from ecmgenerator_gb300.simulator import Simulator
+
+    # a ring of 40 small boxes around the agent, all within reach
+    ang = np.linspace(0, 2 * np.pi, 40, endpoint=False)
+    cx, cy = 50.0 + 3.0 * np.cos(ang), 50.0 + 3.0 * np.sin(ang)
+    boxes = np.stack([cx, cy, np.full(40, 0.15), np.full(40, 0.15)], 1)  # centre, half extents
+    s = sc.make_scene(100.0, 100.0, boxes)
+    s.ecm = sc.build_ecm(s, h=0.2)
+    sim = Simulator(s, 4, 1.0 / 60.0, max_neighbors=10, **ORCA)
+    sim.add_agents(np.array([[50.0, 50.0]], np.float32), [0.3], [1.4],
+                   [np.array([[50.0, 50.0], [90.0, 90.0]], np.float32)])
+    with pytest.raises(EcmgError) as e:
+        sim.update()
+    assert "24" in str(e.value) or "bound" in str(e.value).lower()
+    sim.close()
