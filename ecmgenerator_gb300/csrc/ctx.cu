@@ -30,7 +30,7 @@ using namespace ecmg;
 namespace ecmg {
 /* mlp.cu */
 cudaError_t mlp_infer(ecmg_mlp* mlp, const void* X, const int* n_dev, int n_max, unsigned char* cls, cudaStream_t s,
-                      int sms);
+                      int sms, int* err, int errbit);
 cudaError_t mlp_pack(ecmg_mlp* mlp);
 }  // namespace ecmg
 
@@ -986,12 +986,13 @@ struct ProposeCall {
     int n_max;
     unsigned char* cls;
     int sms;
+    int* err;
 };
 
 static cudaError_t propose_cb(void* user, cudaStream_t s)
 {
     const ProposeCall* pc = (const ProposeCall*)user;
-    return mlp_infer(pc->model, pc->feat, pc->n_dev, pc->n_max, pc->cls, s, pc->sms);
+    return mlp_infer(pc->model, pc->feat, pc->n_dev, pc->n_max, pc->cls, s, pc->sms, pc->err, ECMG_DEV_ERR_MLP);
 }
 
 /* after k_attract: the destroyed / re-plan lists are final; copy them and
@@ -1027,7 +1028,8 @@ static cudaError_t enqueue_tick(ecmg_ctx* c, int launch_slots, bool use_model)
         e = cudaMemsetAsync(c->label.p, kClsOther, (size_t)launch_slots, c->stream);
         if (e != cudaSuccess) return e;
     }
-    ProposeCall pc{c->model, c->feat.p, c->counters.p + C_NSORTED, launch_slots, c->cls.p, c->sms};
+    ProposeCall pc{c->model, c->feat.p, c->counters.p + C_NSORTED, launch_slots, c->cls.p, c->sms,
+                   c->counters.p + C_ERROR};
     e = launch_tick(b, t, launch_slots, c->scan_tmp.p, c->block, c->sms, c->stream, c->ev_a0, c->ev_a1,
                     use_model ? propose_cb : nullptr, &pc, after_attract_cb, c);
     if (e != cudaSuccess) return e;
@@ -1200,6 +1202,7 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         if (out[C_ERROR]) {
             result = fail(c, ECMG_ERR_BOUND, "device bound exceeded (flags 0x%x): %s", out[C_ERROR],
                           (out[C_ERROR] & ECMG_DEV_ERR_CONSTRAINTS) ? "more than 24 obstacle half-planes for one agent"
+                          : (out[C_ERROR] & ECMG_DEV_ERR_MLP)       ? "proposal network: a tensor-core wait timed out"
                                                                     : "event list overflow");
         }
         st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - h1).count();

@@ -49,6 +49,7 @@ enum {
 enum {
     ECMG_DEV_ERR_CONSTRAINTS = 1,
     ECMG_DEV_ERR_LIST = 2,
+    ECMG_DEV_ERR_MLP = 4, /* a bounded wait of the tensor-core inference gave up */
 };
 
 /* Uniform agent grid: cells [0, gw*gh) cover the scene rectangle; agents

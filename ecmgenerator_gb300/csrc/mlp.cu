@@ -12,10 +12,11 @@
  *   hidden 128 -> GELU -> 128 -> GELU
  *   output 160 classes (see ecmg_internal.h, kCls*)
  *
- * Inference: BF16 weights and activations on the tensor cores
- * (mma.sync m16n8k16, FP32 accumulation), weights staged once per block in
- * shared memory in fragment order.  Training: FP32 master weights, FP32
- * forward/backward GEMMs on the CUDA cores, softmax cross-entropy, Adam.
+ * Inference: BF16 weights and activations on the 5th-generation tensor
+ * cores (tcgen05.mma, FP32 accumulators in tensor memory), weights staged
+ * once per CTA in shared memory in the MMA operand layout.  Training: FP32
+ * master weights, FP32 forward/backward GEMMs on the CUDA cores, softmax
+ * cross-entropy, Adam.
  * This translation unit is not part of the parity-critical arithmetic.
  */
 #include "../../include/ecmg.h"
@@ -34,12 +35,6 @@ using namespace ecmg;
 namespace {
 
 constexpr int IN = kMlpIn, HID = kMlpHid, OUT = kMlpOut;
-constexpr int XS = IN + 8;   /* smem row stride (bf16) of an input tile: conflict-free fragment loads */
-constexpr int HS = HID + 8;  /* smem row stride of a hidden tile */
-constexpr int W1F = (IN / 16) * (HID / 8) * 64;   /* u32 words of packed layer-1 fragments */
-constexpr int W2F = (HID / 16) * (HID / 8) * 64;
-constexpr int W3F = (HID / 16) * (OUT / 8) * 64;
-
 __device__ __forceinline__ float gelu(float x)
 {
     const float k0 = 0.7978845608028654f, k1 = 0.044715f; /* sqrt(2/pi), tanh approximation */
@@ -61,183 +56,234 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint32_t* b)
+/* ------------------------------------------------------------------------
+ * Inference on the 5th-generation tensor cores (tcgen05).  One CTA of four
+ * warps per SM, persistent over tiles of 128 agents; per tile three MMA
+ * chains (M = 128, N = 128 / 128 / 160, K = 96 / 128 / 128 in steps of 16),
+ * each issued by one thread and completed through an mbarrier, with the
+ * accumulators in tensor memory (128 lanes x N fp32 columns).  Each warp
+ * reads its 32 lanes (rows) back with tcgen05.ld for the fused epilogue:
+ * bias + GELU + BF16 into the next layer's operand tile, or bias + argmax.
+ * Operands sit in shared memory in the canonical K-major layout without
+ * swizzle: 8-row x 16-byte core matrices, the 16-byte column chunks of a
+ * row group adjacent (leading byte offset 128), row groups K x 16 bytes
+ * apart (stride byte offset).
+ * ---------------------------------------------------------------------- */
+constexpr int kTile = 128;      /* agents per tile (MMA M) */
+constexpr int kTmemCols = 256;  /* >= the widest accumulator (160), a power of 2 */
+
+/* byte offset of element (r, k) of an [R x K] bf16 operand in that layout */
+__host__ __device__ constexpr int tc_off(int r, int k, int K)
 {
+    return ((r >> 3) * (K >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+constexpr int kW1B = HID * IN * 2, kW2B = HID * HID * 2, kW3B = OUT * HID * 2; /* B operands: N rows x K */
+constexpr int kWB = kW1B + kW2B + kW3B;
+constexpr int kXB = kTile * IN * 2, kHB = kTile * HID * 2;
+constexpr size_t kInferSmem = (size_t)kWB + kXB + kHB + sizeof(float) * (2 * HID + OUT) + 32;
+
+/* shared-memory matrix descriptor (no swizzle) */
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46; /* descriptor version */
+    return d;                /* base offset 0, relative LBO, layout type 0: no swizzle */
+}
+
+/* instruction descriptor, kind::f16: BF16 A and B (K-major), FP32 D */
+__host__ __device__ constexpr uint32_t tc_idesc(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+/* D[tmem] (+)= A[M x K] * B[K x N], K-steps of 16, one thread */
+__device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_saddr, uint32_t b_saddr, int K, int N)
+{
+    const uint32_t id = tc_idesc(kTile, N);
+    for (int ks = 0; ks < K / 16; ks++) {
+        const uint64_t ad = tc_sdesc(a_saddr + ks * 256, 128, K * 16);
+        const uint64_t bd = tc_sdesc(b_saddr + ks * 256, 128, K * 16);
+        const uint32_t acc = ks > 0 ? 1u : 0u;
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(id), "r"(acc));
+    }
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+/* bounded wait for the mbarrier phase with the given parity: false on timeout */
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+{
+    for (int it = 0; it < (1 << 22); it++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+/* 16 consecutive fp32 columns of this thread's lane */
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
+{
+    uint32_t r[16];
     asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-/* W is [K x N] row-major FP32; packed as B fragments of m16n8k16:
-   word ((ks * (N/8) + nt) * 32 + lane) * 2 + r holds rows
-   ks*16 + (lane%4)*2 + 8r + {0,1} of column nt*8 + lane/4 */
-__global__ void k_pack_b(const float* W, int K, int N, uint32_t* out)
+/* W [K x N] row-major FP32 -> BF16 B operand (N rows x K) in the tc layout */
+__global__ void k_pack_tc(const float* W, int K, int N, unsigned char* out)
 {
-    int total = (K / 16) * (N / 8) * 64;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        int r = i & 1, lane = (i >> 1) & 31, f = i >> 6;
-        int nt = f % (N / 8), ks = f / (N / 8);
-        int k = ks * 16 + (lane & 3) * 2 + 8 * r;
-        int n = nt * 8 + (lane >> 2);
-        out[i] = pack_bf16(W[(size_t)k * N + n], W[(size_t)(k + 1) * N + n]);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K * N; i += gridDim.x * blockDim.x) {
+        int n = i / K, k = i % K;
+        *reinterpret_cast<__nv_bfloat16*>(out + tc_off(n, k, K)) = __float2bfloat16_rn(W[(size_t)k * N + n]);
     }
 }
 
-/* A fragment of rows [r0, r0+16) from a bf16 smem tile with row stride `s` */
-__device__ __forceinline__ void load_a(const __nv_bfloat16* t, int s, int ks, int lane, uint32_t* a)
+/* class of every row of X [n, IN] (bf16, row-major); err |= errbit on a
+   timed-out tensor-core wait (the CTA then stops and frees its tensor memory) */
+__global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16* X, const int* n_ptr, int n_fixed,
+                                                      const unsigned char* wpack, const float* bias,
+                                                      unsigned char* cls, int* err, int errbit)
 {
-    int g = lane >> 2, c = ks * 16 + (lane & 3) * 2;
-    const uint32_t* p0 = reinterpret_cast<const uint32_t*>(t + g * s + c);
-    const uint32_t* p1 = reinterpret_cast<const uint32_t*>(t + (g + 8) * s + c);
-    a[0] = p0[0];
-    a[1] = p1[0];
-    a[2] = p0[4]; /* +8 columns */
-    a[3] = p1[4];
-}
-
-/* One warp: 16 rows through the three layers.  xin: 16 x XS bf16 tile in
-   smem; hbuf: 16 x HS bf16 scratch; returns per-row argmax in lanes
-   (lane/4 -> row lane/4, row lane/4 + 8). */
-__device__ void mlp_tile(const __nv_bfloat16* xin, __nv_bfloat16* hbuf, const uint32_t* w1, const uint32_t* w2,
-                         const uint32_t* w3, const float* b1, const float* b2, const float* b3, int lane,
-                         int* cls_lo, int* cls_hi)
-{
-    const int g = lane >> 2, tg = lane & 3;
-    float acc[OUT / 8][4];
-    /* layer 1 */
-#pragma unroll
-    for (int nt = 0; nt < HID / 8; nt++) {
-        float bb0 = b1[nt * 8 + tg * 2], bb1 = b1[nt * 8 + tg * 2 + 1];
-        acc[nt][0] = bb0; acc[nt][1] = bb1; acc[nt][2] = bb0; acc[nt][3] = bb1;
-    }
-#pragma unroll
-    for (int ks = 0; ks < IN / 16; ks++) {
-        uint32_t a[4];
-        load_a(xin, XS, ks, lane, a);
-#pragma unroll
-        for (int nt = 0; nt < HID / 8; nt++) {
-            const uint2 b = reinterpret_cast<const uint2*>(w1)[(ks * (HID / 8) + nt) * 32 + lane];
-            uint32_t bb[2] = {b.x, b.y};
-            mma_bf16(acc[nt], a, bb);
-        }
-    }
-#pragma unroll
-    for (int nt = 0; nt < HID / 8; nt++) {
-        int c = nt * 8 + tg * 2;
-        *reinterpret_cast<uint32_t*>(hbuf + g * HS + c) = pack_bf16(gelu(acc[nt][0]), gelu(acc[nt][1]));
-        *reinterpret_cast<uint32_t*>(hbuf + (g + 8) * HS + c) = pack_bf16(gelu(acc[nt][2]), gelu(acc[nt][3]));
-    }
-    __syncwarp();
-    /* layer 2 */
-#pragma unroll
-    for (int nt = 0; nt < HID / 8; nt++) {
-        float bb0 = b2[nt * 8 + tg * 2], bb1 = b2[nt * 8 + tg * 2 + 1];
-        acc[nt][0] = bb0; acc[nt][1] = bb1; acc[nt][2] = bb0; acc[nt][3] = bb1;
-    }
-#pragma unroll
-    for (int ks = 0; ks < HID / 16; ks++) {
-        uint32_t a[4];
-        load_a(hbuf, HS, ks, lane, a);
-#pragma unroll
-        for (int nt = 0; nt < HID / 8; nt++) {
-            const uint2 b = reinterpret_cast<const uint2*>(w2)[(ks * (HID / 8) + nt) * 32 + lane];
-            uint32_t bb[2] = {b.x, b.y};
-            mma_bf16(acc[nt], a, bb);
-        }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int nt = 0; nt < HID / 8; nt++) {
-        int c = nt * 8 + tg * 2;
-        *reinterpret_cast<uint32_t*>(hbuf + g * HS + c) = pack_bf16(gelu(acc[nt][0]), gelu(acc[nt][1]));
-        *reinterpret_cast<uint32_t*>(hbuf + (g + 8) * HS + c) = pack_bf16(gelu(acc[nt][2]), gelu(acc[nt][3]));
-    }
-    __syncwarp();
-    /* layer 3 */
-#pragma unroll
-    for (int nt = 0; nt < OUT / 8; nt++) {
-        float bb0 = b3[nt * 8 + tg * 2], bb1 = b3[nt * 8 + tg * 2 + 1];
-        acc[nt][0] = bb0; acc[nt][1] = bb1; acc[nt][2] = bb0; acc[nt][3] = bb1;
-    }
-#pragma unroll
-    for (int ks = 0; ks < HID / 16; ks++) {
-        uint32_t a[4];
-        load_a(hbuf, HS, ks, lane, a);
-#pragma unroll
-        for (int nt = 0; nt < OUT / 8; nt++) {
-            const uint2 b = reinterpret_cast<const uint2*>(w3)[(ks * (OUT / 8) + nt) * 32 + lane];
-            uint32_t bb[2] = {b.x, b.y};
-            mma_bf16(acc[nt], a, bb);
-        }
-    }
-    /* argmax of rows g and g+8 over this lane's columns, then across the 4
-       lanes sharing the row (ties: the lower class) */
-    float v0 = -INFINITY, v1 = -INFINITY;
-    int i0 = 0, i1 = 0;
-#pragma unroll
-    for (int nt = 0; nt < OUT / 8; nt++) {
-#pragma unroll
-        for (int e = 0; e < 2; e++) {
-            int c = nt * 8 + tg * 2 + e;
-            if (acc[nt][e] > v0) { v0 = acc[nt][e]; i0 = c; }
-            if (acc[nt][2 + e] > v1) { v1 = acc[nt][2 + e]; i1 = c; }
-        }
-    }
-#pragma unroll
-    for (int o = 1; o < 4; o <<= 1) {
-        float ov0 = __shfl_xor_sync(0xffffffffu, v0, o), ov1 = __shfl_xor_sync(0xffffffffu, v1, o);
-        int oi0 = __shfl_xor_sync(0xffffffffu, i0, o), oi1 = __shfl_xor_sync(0xffffffffu, i1, o);
-        if (ov0 > v0 || (ov0 == v0 && oi0 < i0)) { v0 = ov0; i0 = oi0; }
-        if (ov1 > v1 || (ov1 == v1 && oi1 < i1)) { v1 = ov1; i1 = oi1; }
-    }
-    *cls_lo = i0;
-    *cls_hi = i1;
-}
-
-constexpr int kInferWarps = 8;
-constexpr size_t kInferSmem = sizeof(uint32_t) * (W1F + W2F + W3F) + sizeof(float) * (2 * HID + OUT) +
-                              (size_t)kInferWarps * sizeof(__nv_bfloat16) * (16 * XS + 16 * HS);
-
-/* class of every row of X [n, IN] (bf16, row-major) */
-__global__ void __launch_bounds__(32 * kInferWarps) k_mlp_infer(const __nv_bfloat16* X, const int* n_ptr, int n_fixed,
-                                                                const uint32_t* wpack, const float* bias,
-                                                                unsigned char* cls)
-{
-    extern __shared__ __align__(16) unsigned char sm[];
-    uint32_t* w = reinterpret_cast<uint32_t*>(sm);
-    float* bs = reinterpret_cast<float*>(w + W1F + W2F + W3F);
-    __nv_bfloat16* tiles = reinterpret_cast<__nv_bfloat16*>(bs + 2 * HID + OUT);
+    extern __shared__ __align__(128) unsigned char sm[];
+    unsigned char* sW1 = sm;
+    unsigned char* sW2 = sW1 + kW1B;
+    unsigned char* sW3 = sW2 + kW2B;
+    unsigned char* sX = sW3 + kW3B;
+    unsigned char* sH = sX + kXB;
+    float* sb = reinterpret_cast<float*>(sH + kHB);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sb + 2 * HID + OUT);
+    uint64_t* s_mbar = reinterpret_cast<uint64_t*>(s_tmem + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n = n_ptr ? *n_ptr : n_fixed;
-    /* weights and biases, once per block */
-    for (int i = threadIdx.x; i < (W1F + W2F + W3F) / 4; i += blockDim.x)
-        reinterpret_cast<uint4*>(w)[i] = reinterpret_cast<const uint4*>(wpack)[i];
-    for (int i = threadIdx.x; i < 2 * HID + OUT; i += blockDim.x) bs[i] = bias[i];
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __nv_bfloat16* xt = tiles + warp * (16 * XS + 16 * HS);
-    __nv_bfloat16* ht = xt + 16 * XS;
-    const int ntile = (n + 15) / 16;
-    for (int tile = blockIdx.x * kInferWarps + warp; tile < ntile; tile += gridDim.x * kInferWarps) {
-        int r0 = tile * 16;
-        /* 16 rows x 96 bf16 = 16 x 12 uint4 */
-        for (int i = lane; i < 16 * (IN / 8); i += 32) {
-            int rr = i / (IN / 8), cc = i % (IN / 8);
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (r0 + rr < n) v = reinterpret_cast<const uint4*>(X + (size_t)(r0 + rr) * IN)[cc];
-            *reinterpret_cast<uint4*>(xt + rr * XS + cc * 8) = v;
-        }
-        __syncwarp();
-        int c0, c1;
-        mlp_tile(xt, ht, w, w + W1F, w + W1F + W2F, bs, bs + HID, bs + 2 * HID, lane, &c0, &c1);
-        if ((lane & 3) == 0) {
-            int g = lane >> 2;
-            if (r0 + g < n) cls[r0 + g] = (unsigned char)c0;
-            if (r0 + g + 8 < n) cls[r0 + g + 8] = (unsigned char)c1;
-        }
-        __syncwarp();
+
+    /* weights (packed in the operand layout) and biases, once per CTA */
+    for (int i = tid; i < kWB / 16; i += blockDim.x)
+        reinterpret_cast<uint4*>(sm)[i] = reinterpret_cast<const uint4*>(wpack)[i];
+    for (int i = tid; i < 2 * HID + OUT; i += blockDim.x) sb[i] = bias[i];
+    const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(s_mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(s_tmem)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *s_tmem;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16); /* this warp's 32 lanes */
+    const uint32_t aX = (uint32_t)__cvta_generic_to_shared(sX), aH = (uint32_t)__cvta_generic_to_shared(sH);
+    const uint32_t aW1 = (uint32_t)__cvta_generic_to_shared(sW1), aW2 = (uint32_t)__cvta_generic_to_shared(sW2),
+                   aW3 = (uint32_t)__cvta_generic_to_shared(sW3);
+    const int row = warp * 32 + lane;
+    uint32_t phase = 0;
+    bool fail = false;
+    const int ntiles = (n + kTile - 1) / kTile;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int r0 = tile * kTile;
+        /* this thread's input row into the operand layout */
+        {
+            const int r = r0 + row;
+            const uint4* src = reinterpret_cast<const uint4*>(X + (size_t)r * IN);
+#pragma unroll
+            for (int kc = 0; kc < IN / 8; kc++) {
+                uint4 v = make_uint4(0, 0, 0, 0);
+                if (r < n) v = src[kc];
+                *reinterpret_cast<uint4*>(sX + tc_off(row, kc * 8, IN)) = v;
+            }
+        }
+        /* three layers: D = A * W; hidden epilogues write the next A into sH */
+#pragma unroll 1
+        for (int layer = 0; layer < 3 && !fail; layer++) {
+            const int K = layer == 0 ? IN : HID, N = layer == 2 ? OUT : HID;
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0) {
+                tc_layer(tmem, layer == 0 ? aX : aH, layer == 0 ? aW1 : (layer == 1 ? aW2 : aW3), K, N);
+                tc_commit(mbar);
+            }
+            fail = __syncthreads_or(!mbar_wait(mbar, phase)) != 0;
+            phase ^= 1u;
+            tc_fence_after();
+            if (fail) break;
+            const float* bl = sb + (layer == 0 ? 0 : (layer == 1 ? HID : 2 * HID));
+            if (layer < 2) {
+#pragma unroll 1
+                for (int c = 0; c < HID; c += 16) {
+                    float v[16];
+                    tmem_ld16(lane_base + (uint32_t)c, v);
+                    uint4 lo, hi;
+                    lo.x = pack_bf16(gelu(v[0] + bl[c + 0]), gelu(v[1] + bl[c + 1]));
+                    lo.y = pack_bf16(gelu(v[2] + bl[c + 2]), gelu(v[3] + bl[c + 3]));
+                    lo.z = pack_bf16(gelu(v[4] + bl[c + 4]), gelu(v[5] + bl[c + 5]));
+                    lo.w = pack_bf16(gelu(v[6] + bl[c + 6]), gelu(v[7] + bl[c + 7]));
+                    hi.x = pack_bf16(gelu(v[8] + bl[c + 8]), gelu(v[9] + bl[c + 9]));
+                    hi.y = pack_bf16(gelu(v[10] + bl[c + 10]), gelu(v[11] + bl[c + 11]));
+                    hi.z = pack_bf16(gelu(v[12] + bl[c + 12]), gelu(v[13] + bl[c + 13]));
+                    hi.w = pack_bf16(gelu(v[14] + bl[c + 14]), gelu(v[15] + bl[c + 15]));
+                    *reinterpret_cast<uint4*>(sH + tc_off(row, c, HID)) = lo;
+                    *reinterpret_cast<uint4*>(sH + tc_off(row, c + 8, HID)) = hi;
+                }
+            } else {
+                float best = -INFINITY;
+                int bi = 0;
+#pragma unroll 1
+                for (int c = 0; c < OUT; c += 16) {
+                    float v[16];
+                    tmem_ld16(lane_base + (uint32_t)c, v);
+#pragma unroll
+                    for (int i = 0; i < 16; i++) {
+                        const float z = v[i] + bl[c + i];
+                        if (z > best) { best = z; bi = c + i; }
+                    }
+                }
+                if (r0 + row < n) cls[r0 + row] = (unsigned char)bi;
+            }
+        }
+        if (fail) break;
+        /* the accumulator is read out before the next tile's MMAs overwrite it */
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    }
+    if (fail && tid == 0) atomicOr(err, errbit);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
 /* ------------------------------------------------------------------------
@@ -403,7 +449,8 @@ struct ecmg_mlp {
     float* g = nullptr;     /* gradients */
     float* m = nullptr;     /* Adam first moment */
     float* v = nullptr;     /* Adam second moment */
-    uint32_t* pack = nullptr; /* BF16 fragment-packed weights for inference */
+    unsigned char* pack = nullptr; /* BF16 weights in the tensor-core operand layout (inference) */
+    int* derr = nullptr;           /* inference error flag (ecmg_mlp_predict) */
     float* bias = nullptr;  /* b1 | b2 | b3 */
     int step = 0;
     bool packed = false;
@@ -418,7 +465,7 @@ struct ecmg_mlp {
 namespace ecmg {
 /* used by the tick (ctx.cu) */
 cudaError_t mlp_infer(ecmg_mlp* mlp, const void* X, const int* n_dev, int n_max, unsigned char* cls, cudaStream_t s,
-                      int sms);
+                      int sms, int* err, int errbit);
 cudaError_t mlp_pack(ecmg_mlp* mlp);
 }  // namespace ecmg
 
@@ -428,9 +475,9 @@ cudaError_t ecmg::mlp_pack(ecmg_mlp* mm)
     cudaError_t ea = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
     if (ea != cudaSuccess) return ea;
     if (mm->packed) return cudaSuccess;
-    k_pack_b<<<64, 256, 0, mm->s>>>(mm->p + OW1, IN, HID, mm->pack);
-    k_pack_b<<<64, 256, 0, mm->s>>>(mm->p + OW2, HID, HID, mm->pack + W1F);
-    k_pack_b<<<64, 256, 0, mm->s>>>(mm->p + OW3, HID, OUT, mm->pack + W1F + W2F);
+    k_pack_tc<<<64, 256, 0, mm->s>>>(mm->p + OW1, IN, HID, mm->pack);
+    k_pack_tc<<<64, 256, 0, mm->s>>>(mm->p + OW2, HID, HID, mm->pack + kW1B);
+    k_pack_tc<<<64, 256, 0, mm->s>>>(mm->p + OW3, HID, OUT, mm->pack + kW1B + kW2B);
     cudaMemcpyAsync(mm->bias, mm->p + OB1, sizeof(float) * HID, cudaMemcpyDeviceToDevice, mm->s);
     cudaMemcpyAsync(mm->bias + HID, mm->p + OB2, sizeof(float) * HID, cudaMemcpyDeviceToDevice, mm->s);
     cudaMemcpyAsync(mm->bias + 2 * HID, mm->p + OB3, sizeof(float) * OUT, cudaMemcpyDeviceToDevice, mm->s);
@@ -440,14 +487,13 @@ cudaError_t ecmg::mlp_pack(ecmg_mlp* mm)
 }
 
 cudaError_t ecmg::mlp_infer(ecmg_mlp* mm, const void* X, const int* n_dev, int n_max, unsigned char* cls,
-                            cudaStream_t s, int sms)
+                            cudaStream_t s, int sms, int* err, int errbit)
 {
-    int tiles = (n_max + 15) / 16;
-    int grid = (tiles + kInferWarps - 1) / kInferWarps;
-    if (grid > sms) grid = sms; /* one block per SM holds the weights once */
+    int tiles = (n_max + kTile - 1) / kTile;
+    int grid = tiles < sms ? tiles : sms; /* one CTA per SM holds the weights once */
     if (grid < 1) grid = 1;
-    k_mlp_infer<<<grid, 32 * kInferWarps, kInferSmem, s>>>((const __nv_bfloat16*)X, n_dev, n_max, mm->pack, mm->bias,
-                                                           cls);
+    k_mlp_infer<<<grid, 128, kInferSmem, s>>>((const __nv_bfloat16*)X, n_dev, n_max, mm->pack, mm->bias, cls, err,
+                                              errbit);
     return cudaGetLastError();
 }
 
@@ -468,7 +514,8 @@ ecmg_status ecmg_mlp_create(unsigned long long seed, ecmg_mlp** out)
               cudaMalloc(&mm->g, sizeof(float) * NPARAM) == cudaSuccess &&
               cudaMalloc(&mm->m, sizeof(float) * NPARAM) == cudaSuccess &&
               cudaMalloc(&mm->v, sizeof(float) * NPARAM) == cudaSuccess &&
-              cudaMalloc(&mm->pack, sizeof(uint32_t) * (W1F + W2F + W3F)) == cudaSuccess &&
+              cudaMalloc(&mm->pack, (size_t)kWB) == cudaSuccess &&
+              cudaMalloc(&mm->derr, sizeof(int)) == cudaSuccess &&
               cudaMalloc(&mm->bias, sizeof(float) * (2 * HID + OUT)) == cudaSuccess &&
               cudaMalloc(&mm->loss, sizeof(float)) == cudaSuccess && cudaMalloc(&mm->correct, sizeof(int)) == cudaSuccess;
     if (!ok) {
@@ -509,6 +556,7 @@ ecmg_status ecmg_mlp_destroy(ecmg_mlp* mm)
     for (float* f : fs)
         if (f) cudaFree(f);
     if (mm->pack) cudaFree(mm->pack);
+    if (mm->derr) cudaFree(mm->derr);
     if (mm->yb) cudaFree(mm->yb);
     if (mm->correct) cudaFree(mm->correct);
     if (mm->s) cudaStreamDestroy(mm->s);
@@ -650,8 +698,13 @@ ecmg_status ecmg_mlp_predict(ecmg_mlp* mm, const void* dev_x, int n, unsigned ch
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (ecmg::mlp_infer(mm, dev_x, nullptr, n, dev_cls, mm->s, sms) != cudaSuccess) return ECMG_ERR_CUDA;
-    return cudaStreamSynchronize(mm->s) == cudaSuccess ? ECMG_OK : ECMG_ERR_CUDA;
+    if (cudaMemsetAsync(mm->derr, 0, sizeof(int), mm->s) != cudaSuccess) return ECMG_ERR_CUDA;
+    if (ecmg::mlp_infer(mm, dev_x, nullptr, n, dev_cls, mm->s, sms, mm->derr, 1) != cudaSuccess) return ECMG_ERR_CUDA;
+    int herr = 0;
+    if (cudaMemcpyAsync(&herr, mm->derr, sizeof(int), cudaMemcpyDeviceToHost, mm->s) != cudaSuccess ||
+        cudaStreamSynchronize(mm->s) != cudaSuccess)
+        return ECMG_ERR_CUDA;
+    return herr ? ECMG_ERR_BOUND : ECMG_OK;
 }
 
 }  // extern "C"
