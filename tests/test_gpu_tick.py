@@ -243,8 +243,8 @@ def test_full_capacity_and_slot_reuse(port, c1_small):
     sim.destroy_agent(3)
     again = sim.add_agents(st.pos[:2], st.clear[:2], st.pref_speed[:2], paths[:2])
     assert list(again) == [3, 7]
-    sim.update(ticks=2)
-    assert sim.get_num_agents() == n
+    st2 = sim.update(ticks=2)
+    assert sim.get_num_agents() == n - st2.destroyed
     sim.close()
 
 
