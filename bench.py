@@ -286,6 +286,11 @@ def run_ours(args):
                 for i in range(bounds[b], bounds[b + 1]):
                     tl.tick()
         torch.cuda.synchronize()
+    blocks = {"plain_ms": [round(sum(a.elapsed_time(c) for a, c in tp.ev[bounds[b]:bounds[b + 1]]), 3)
+                           for b in range(nblk)]}
+    if model is not None:
+        blocks["learned_ms"] = [round(sum(a.elapsed_time(c) for a, c in tl.ev[bounds[b]:bounds[b + 1]]), 3)
+                                for b in range(nblk)]
     same = bool(np.array_equal(plain.get_position_data(), learned.get_position_data()))
     main_t = tl if model is not None else tp
     ms = main_t.ms()
@@ -353,6 +358,7 @@ def run_ours(args):
                   "host_ms_per_tick": tp.tot["host_ms"] / args.steps,
                   "replans_host_per_tick": tp.tot["replans_host"] / args.steps},
         "learned_vs_plain": value / plain_value if model is not None else None,
+        "timed_blocks": blocks,
         "proposal": None if model is None else {
             **model_info, "proposed_per_tick": T["proposed"] / args.steps,
             "accepted_per_tick": T["accepted"] / args.steps,
