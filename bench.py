@@ -74,6 +74,12 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the first query of a fresh nvidia-smi holds the driver for ~10 ms:
+            # let it happen before the timed region starts
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0:
+                time.sleep(0.02)
+            time.sleep(0.3)
         except OSError:
             self.proc = None
         return self
@@ -89,6 +95,7 @@ class ClockSampler:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+            time.sleep(0.3)  # the sampler's exit, like its start, briefly holds the driver
 
     def summary(self):
         sm, mx, reasons = [], None, set()
@@ -274,7 +281,6 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        time.sleep(0.5)  # let the sampler start before the timed ticks
         # alternating blocks of plain and learned ticks (each simulator ends
         # K ticks later, in the same state as the other)
         nblk = 4 if args.steps >= 4 else 1

@@ -22,12 +22,14 @@
 #include "../../include/ecmg.h"
 #include "ecmg_internal.h"
 
+#include <cuda.h> /* CUtensorMap (the encoder is reached through the runtime) */
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdint.h>
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 using namespace ecmg;
@@ -65,17 +67,20 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
  * reads its 32 lanes (rows) back with tcgen05.ld for the fused epilogue:
  * bias + GELU + BF16 into the next layer's operand tile, or bias + argmax.
  * Operands sit in shared memory in the canonical K-major layout without
- * swizzle: 8-row x 16-byte core matrices, the 16-byte column chunks of a
- * row group adjacent (leading byte offset 128), row groups K x 16 bytes
- * apart (stride byte offset).
+ * swizzle: 8-row x 16-byte core matrices; the row groups of one 8-column
+ * chunk are adjacent (stride byte offset 128), chunks R x 16 bytes apart
+ * (leading byte offset) for an operand of R rows.  One chunk of a 128-row
+ * feature tile is then one 2 KB TMA box (8 columns x 128 rows), so the
+ * tile arrives by 12 cp.async.bulk.tensor copies, prefetched for the next
+ * tile while the hidden layers of this one run.
  * ---------------------------------------------------------------------- */
 constexpr int kTile = 128;      /* agents per tile (MMA M) */
 constexpr int kTmemCols = 256;  /* >= the widest accumulator (160), a power of 2 */
 
 /* byte offset of element (r, k) of an [R x K] bf16 operand in that layout */
-__host__ __device__ constexpr int tc_off(int r, int k, int K)
+__host__ __device__ constexpr int tc_off(int r, int k, int R)
 {
-    return ((r >> 3) * (K >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+    return ((k >> 3) * (R >> 3) + (r >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
 }
 
 constexpr int kW1B = HID * IN * 2, kW2B = HID * HID * 2, kW3B = OUT * HID * 2; /* B operands: N rows x K */
@@ -103,13 +108,13 @@ __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence:
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-/* D[tmem] (+)= A[M x K] * B[K x N], K-steps of 16, one thread */
+/* D[tmem] (+)= A[M x K] * B[K x N], K-steps of 16 (two chunks), one thread */
 __device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_saddr, uint32_t b_saddr, int K, int N)
 {
     const uint32_t id = tc_idesc(kTile, N);
     for (int ks = 0; ks < K / 16; ks++) {
-        const uint64_t ad = tc_sdesc(a_saddr + ks * 256, 128, K * 16);
-        const uint64_t bd = tc_sdesc(b_saddr + ks * 256, 128, K * 16);
+        const uint64_t ad = tc_sdesc(a_saddr + ks * 2 * (kTile * 16), kTile * 16, 128);
+        const uint64_t bd = tc_sdesc(b_saddr + ks * 2 * (N * 16), N * 16, 128);
         const uint32_t acc = ks > 0 ? 1u : 0u;
         asm volatile(
             "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
@@ -158,14 +163,28 @@ __global__ void k_pack_tc(const float* W, int K, int N, unsigned char* out)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K * N; i += gridDim.x * blockDim.x) {
         int n = i / K, k = i % K;
-        *reinterpret_cast<__nv_bfloat16*>(out + tc_off(n, k, K)) = __float2bfloat16_rn(W[(size_t)k * N + n]);
+        *reinterpret_cast<__nv_bfloat16*>(out + tc_off(n, k, N)) = __float2bfloat16_rn(W[(size_t)k * N + n]);
     }
+}
+
+/* the 12 TMA boxes (8 columns x 128 rows) of the feature tile at row r0 */
+__device__ __forceinline__ void tma_tile(const CUtensorMap* tm, uint32_t sdst, int r0, uint32_t mbar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"((uint32_t)kXB)
+                 : "memory");
+#pragma unroll 1
+    for (int kc = 0; kc < IN / 8; kc++)
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+                "r"(sdst + (uint32_t)(kc * kTile * 16)),
+            "l"(tm), "r"(kc * 8), "r"(r0), "r"(mbar)
+            : "memory");
 }
 
 /* class of every row of X [n, IN] (bf16, row-major); err |= errbit on a
    timed-out tensor-core wait (the CTA then stops and frees its tensor memory) */
-__global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16* X, const int* n_ptr, int n_fixed,
-                                                      const unsigned char* wpack, const float* bias,
+__global__ void __launch_bounds__(128, 1) k_mlp_infer(const __grid_constant__ CUtensorMap tmX, const int* n_ptr,
+                                                      int n_fixed, const unsigned char* wpack, const float* bias,
                                                       unsigned char* cls, int* err, int errbit)
 {
     extern __shared__ __align__(128) unsigned char sm[];
@@ -176,7 +195,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16* X, co
     unsigned char* sH = sX + kXB;
     float* sb = reinterpret_cast<float*>(sH + kHB);
     uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sb + 2 * HID + OUT);
-    uint64_t* s_mbar = reinterpret_cast<uint64_t*>(s_tmem + 2);
+    uint64_t* s_mbar = reinterpret_cast<uint64_t*>(s_tmem + 2); /* [0] MMA done, [1] feature tile landed */
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n = n_ptr ? *n_ptr : n_fixed;
 
@@ -185,8 +204,10 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16* X, co
         reinterpret_cast<uint4*>(sm)[i] = reinterpret_cast<const uint4*>(wpack)[i];
     for (int i = tid; i < 2 * HID + OUT; i += blockDim.x) sb[i] = bias[i];
     const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(s_mbar);
+    const uint32_t mbar_x = mbar + 8;
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_x) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -206,22 +227,20 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16* X, co
     const uint32_t aW1 = (uint32_t)__cvta_generic_to_shared(sW1), aW2 = (uint32_t)__cvta_generic_to_shared(sW2),
                    aW3 = (uint32_t)__cvta_generic_to_shared(sW3);
     const int row = warp * 32 + lane;
-    uint32_t phase = 0;
-    bool fail = false;
+    uint32_t phase = 0, phase_x = 0;
+    bool fail = false, x_pending = false;
     const int ntiles = (n + kTile - 1) / kTile;
+    if ((int)blockIdx.x < ntiles) {
+        if (tid == 0) tma_tile(&tmX, aX, blockIdx.x * kTile, mbar_x);
+        x_pending = true;
+    }
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int r0 = tile * kTile;
-        /* this thread's input row into the operand layout */
-        {
-            const int r = r0 + row;
-            const uint4* src = reinterpret_cast<const uint4*>(X + (size_t)r * IN);
-#pragma unroll
-            for (int kc = 0; kc < IN / 8; kc++) {
-                uint4 v = make_uint4(0, 0, 0, 0);
-                if (r < n) v = src[kc];
-                *reinterpret_cast<uint4*>(sX + tc_off(row, kc * 8, IN)) = v;
-            }
-        }
+        /* this tile's features (rows beyond the tensor read as zeros) */
+        fail = __syncthreads_or(!mbar_wait(mbar_x, phase_x)) != 0;
+        phase_x ^= 1u;
+        x_pending = false;
+        if (fail) break;
         /* three layers: D = A * W; hidden epilogues write the next A into sH */
 #pragma unroll 1
         for (int layer = 0; layer < 3 && !fail; layer++) {
@@ -238,6 +257,11 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16* X, co
             phase ^= 1u;
             tc_fence_after();
             if (fail) break;
+            if (layer == 0 && tile + (int)gridDim.x < ntiles) {
+                /* sX has been read: bring in the next tile meanwhile */
+                if (tid == 0) tma_tile(&tmX, aX, (tile + (int)gridDim.x) * kTile, mbar_x);
+                x_pending = true;
+            }
             const float* bl = sb + (layer == 0 ? 0 : (layer == 1 ? HID : 2 * HID));
             if (layer < 2) {
 #pragma unroll 1
@@ -253,8 +277,8 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16* X, co
                     hi.y = pack_bf16(gelu(v[10] + bl[c + 10]), gelu(v[11] + bl[c + 11]));
                     hi.z = pack_bf16(gelu(v[12] + bl[c + 12]), gelu(v[13] + bl[c + 13]));
                     hi.w = pack_bf16(gelu(v[14] + bl[c + 14]), gelu(v[15] + bl[c + 15]));
-                    *reinterpret_cast<uint4*>(sH + tc_off(row, c, HID)) = lo;
-                    *reinterpret_cast<uint4*>(sH + tc_off(row, c + 8, HID)) = hi;
+                    *reinterpret_cast<uint4*>(sH + tc_off(row, c, kTile)) = lo;
+                    *reinterpret_cast<uint4*>(sH + tc_off(row, c + 8, kTile)) = hi;
                 }
             } else {
                 float best = -INFINITY;
@@ -279,6 +303,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16* X, co
         tc_fence_after();
     }
     if (fail && tid == 0) atomicOr(err, errbit);
+    if (x_pending) (void)mbar_wait(mbar_x, phase_x); /* no copy may land after the CTA ends */
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -486,14 +511,54 @@ cudaError_t ecmg::mlp_pack(ecmg_mlp* mm)
     return e;
 }
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+/* the driver's tensor-map encoder, reached through the runtime (no link
+   against the driver library) */
+static EncodeTiledFn tensor_map_encoder()
+{
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+/* X [rows, IN] bf16 row-major as a 2D tensor; boxes of 8 columns x 128 rows,
+   rows beyond `rows` read as zeros */
+static cudaError_t feature_map(CUtensorMap* tm, const void* X, int rows)
+{
+    EncodeTiledFn enc = tensor_map_encoder();
+    if (!enc) return cudaErrorNotSupported;
+    const cuuint64_t dims[2] = {(cuuint64_t)IN, (cuuint64_t)(rows > 0 ? rows : 1)};
+    const cuuint64_t strides[1] = {(cuuint64_t)IN * 2};
+    const cuuint32_t box[2] = {8, (cuuint32_t)kTile};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(X), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 cudaError_t ecmg::mlp_infer(ecmg_mlp* mm, const void* X, const int* n_dev, int n_max, unsigned char* cls,
                             cudaStream_t s, int sms, int* err, int errbit)
 {
+    CUtensorMap tm;
+    cudaError_t e = feature_map(&tm, X, n_max);
+    if (e != cudaSuccess) return e;
     int tiles = (n_max + kTile - 1) / kTile;
     int grid = tiles < sms ? tiles : sms; /* one CTA per SM holds the weights once */
     if (grid < 1) grid = 1;
-    k_mlp_infer<<<grid, 128, kInferSmem, s>>>((const __nv_bfloat16*)X, n_dev, n_max, mm->pack, mm->bias, cls, err,
-                                              errbit);
+    k_mlp_infer<<<grid, 128, kInferSmem, s>>>(tm, n_dev, n_max, mm->pack, mm->bias, cls, err, errbit);
     return cudaGetLastError();
 }
 
