@@ -214,6 +214,7 @@ class TickTimer:
         self.stream = torch.cuda.ExternalStream(sim.L.ecmg_stream(sim.h))
         self.flush = flush
         self.ev = []
+        self.per_tick = []  # (graph ms, host ms) of each timed tick
         self.steps = 0
         self.agent_ms = 0.0
         self.tot = dict(lp3d=0, replans=0, replans_failed=0, replans_host=0, destroyed=0, device_ms=0.0, host_ms=0.0,
@@ -230,6 +231,7 @@ class TickTimer:
         with torch.cuda.stream(self.stream):
             e1.record(self.stream)
         self.ev.append((e0, e1))
+        self.per_tick.append((round(s.device_ms, 3), round(s.host_ms, 3)))
         self.steps += s.agent_steps
         self.agent_ms += s.agent_kernel_ms
         for k in self.tot:
@@ -293,7 +295,9 @@ def run_ours(args):
                     tl.tick()
         torch.cuda.synchronize()
     blocks = {"plain_ms": [round(sum(a.elapsed_time(c) for a, c in tp.ev[bounds[b]:bounds[b + 1]]), 3)
-                           for b in range(nblk)]}
+                           for b in range(nblk)],
+              "plain_tick_ms": [round(a.elapsed_time(c), 3) for a, c in tp.ev],
+              "plain_graph_host_ms": tp.per_tick}
     if model is not None:
         blocks["learned_ms"] = [round(sum(a.elapsed_time(c) for a, c in tl.ev[bounds[b]:bounds[b + 1]]), 3)
                                 for b in range(nblk)]
