@@ -19,6 +19,7 @@ Under torchrun (N > 1) every rank runs an independent replica on its GPU
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import subprocess
@@ -278,6 +279,12 @@ def run_ours(args):
         learned.update()  # capture of the learned graph
         plain.update()
     torch.cuda.synchronize()
+    # the workload holds ~1M small path arrays: a cyclic-GC pass over them
+    # stalls the host for ~10 ms, so collect now and keep the collector off
+    # while timing
+    gc.collect()
+    gc.freeze()
+    gc.disable()
     tp, tl = TickTimer(plain, flush), TickTimer(learned, flush)
     if world > 1:
         dist.barrier()
@@ -323,6 +330,7 @@ def run_ours(args):
             e2e_steps += s.agent_steps
         t1 = time.perf_counter()
         e2e[name] = e2e_steps * max(world, 1) / (t1 - t0)
+    gc.enable()
     e2e_main = {"value": e2e["learned" if model is not None else "plain"], "unit": "agent-steps/s",
                 "h2d_bytes_per_step": 64, "d2h_bytes_per_step": 16 * n + 64,
                 "plain": e2e["plain"], "note": "wall clock of Simulator.update() + the position and velocity getters "
