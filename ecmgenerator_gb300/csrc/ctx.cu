@@ -949,6 +949,12 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t, bool use_model)
     const ecmg_params& p = c->prm;
     t.dt = p.dt;
     t.tau_a = p.tau_agent;
+    {
+        /* a power of two (normal, so that 1/tau is exact too) */
+        int ex = 0;
+        const float fr = std::frexp(p.tau_agent, &ex);
+        t.inv_tau_a = (fr == 0.5f && ex > -125 && ex < 126) ? 1.0f / p.tau_agent : 0.0f;
+    }
     t.tau_o = p.tau_obst;
     t.rnb = p.neighbor_dist;
     t.rnb2 = p.neighbor_dist * p.neighbor_dist;

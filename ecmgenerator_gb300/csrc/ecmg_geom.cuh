@@ -458,14 +458,19 @@ EG_NI bool obstacle_constraint(const ObstView& o, int L, V2 position, V2 velocit
     }
 }
 
-/* agent part of ORCA::GenerateConstraints (ORCA.cpp:339-423) for one neighbour */
-EG_HD Con agent_constraint(V2 position, V2 velocity, float clr, V2 np, V2 nv, float nclr, float tau, float dt)
+/* agent part of ORCA::GenerateConstraints (ORCA.cpp:339-423) for one
+   neighbour.  inv_tau != 0 must be 1/tau for a power-of-two tau: x / tau and
+   x * (1/tau) are then the same correctly rounded value (the quotient is an
+   exact scaling), and the multiplication is cheaper. */
+EG_HD Con agent_constraint(V2 position, V2 velocity, float clr, V2 np, V2 nv, float nclr, float tau, float dt,
+                           float inv_tau = 0.0f)
 {
     Con c;
-    V2 VOPos = mk((np.x - position.x) / tau, (np.y - position.y) / tau);
+    const float rx = np.x - position.x, ry = np.y - position.y;
+    V2 VOPos = inv_tau != 0.0f ? mk(rx * inv_tau, ry * inv_tau) : mk(rx / tau, ry / tau);
     float VOPosLength = len(VOPos);
     float combinedRadius = nclr + clr;
-    float VORadius = combinedRadius / tau;
+    float VORadius = inv_tau != 0.0f ? combinedRadius * inv_tau : combinedRadius / tau;
     V2 relVel = mk(velocity.x - nv.x, velocity.y - nv.y);
     V2 relPos = mk(np.x - position.x, np.y - position.y);
     float relPosLength = len(relPos);

@@ -102,6 +102,7 @@ struct TickArgs {
     int lp_mode;           /* 0: one thread per agent, 1: one warp per agent */
     /* parameters */
     float dt, tau_a, tau_o, rnb, rnb2, max_speed, mass_recip, arr_sq, del_sq;
+    float inv_tau_a;       /* 1 / tau_a when tau_a is a power of two (exact), else 0 */
     int k;
     int lp3d_fp64;
     int replan_dev_fail;   /* built-in planner: settle known-failing re-plans on the device */

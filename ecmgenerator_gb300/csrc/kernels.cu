@@ -387,9 +387,9 @@ __device__ __noinline__ bool verify_proposal(const Get& get, int m, int nObst, i
 /* out-of-line copies keep the per-agent kernel small enough for the
    instruction cache: each is called from a loop or a rare branch */
 __device__ __noinline__ Con agent_constraint_ni(V2 position, V2 velocity, float clr, V2 np, V2 nv, float nclr,
-                                                float tau, float dt)
+                                                float tau, float dt, float inv_tau)
 {
-    return agent_constraint(position, velocity, clr, np, nv, nclr, tau, dt);
+    return agent_constraint(position, velocity, clr, np, nv, nclr, tau, dt, inv_tau);
 }
 
 template <int MC>
@@ -507,7 +507,8 @@ __device__ void orca_tick(const TickArgs& a, int t)
     const int nObst = m;
     for (int q = 0; q < ncnt; q++) {
         int j = nbr[q];
-        cons[m++] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt);
+        cons[m++] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
+                                        a.inv_tau_a);
     }
     if (overflow) atomicOr(&a.counters[C_ERROR], ECMG_DEV_ERR_CONSTRAINTS);
 
@@ -962,7 +963,8 @@ __device__ void orca_warp(const TickArgs& a, int t, int lane, Con* cons, Con* bi
     const int nObst = m;
     if (lane < ncnt) {
         const int j = nbr[lane];
-        cons[m + lane] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt);
+        cons[m + lane] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
+                                             a.inv_tau_a);
     }
     m += ncnt;
     __syncwarp();

@@ -9,11 +9,11 @@ pytestmark = pytest.mark.gpu
 ORCA = dict(tau_agent=2.0, tau_obst=2.0, neighbor_dist=5.0)
 
 
-def _pair(scene, st, paths, k, n_slots=None, lp_mode=None, grab=4, **kw):
+def _pair(scene, st, paths, k, n_slots=None, lp_mode=None, grab=4, orca=None, **kw):
     from ecmgenerator_gb300.simulator import Simulator, set_lp_mode
 
     n = st.num_agents
-    sim = Simulator(scene, n_slots or st.n_slots, 1.0 / 60.0, max_neighbors=k, **ORCA, **kw)
+    sim = Simulator(scene, n_slots or st.n_slots, 1.0 / 60.0, max_neighbors=k, **(orca or ORCA), **kw)
     if lp_mode:
         set_lp_mode(sim, lp_mode, grab)
     sim.set_record(True)
@@ -36,11 +36,11 @@ def _compare(sim, st, res, k):
     assert np.array_equal(sim.get_preferred_velocity_data()[live], st.pref_vel[live])
 
 
-def _run(port, scene, st, paths, ticks, k, **kw):
+def _run(port, scene, st, paths, ticks, k, orca=None, **kw):
     st = st.copy()
-    sim = _pair(scene, st, paths, k, **kw)
+    sim = _pair(scene, st, paths, k, orca=orca, **kw)
     O, E = port.obstacles(scene), port.ecm(scene.ecm)
-    P = port.params(k=k, libm=0, **ORCA)
+    P = port.params(k=k, libm=0, **(orca or ORCA))
     events = 0
     for t in range(ticks):
         stats = sim.update()
@@ -99,6 +99,14 @@ def test_tick_bitexact_warp_dense(port):
     for mode in ("thread", "warp"):
         ev = _run(port, scene, st, paths, ticks=6, k=16, lp_mode=mode)
         assert ev > 1000
+
+
+@pytest.mark.parametrize("tau", [1.5, 4.0])
+def test_tick_bitexact_time_horizon(port, c1_small, tau):
+    """agent time horizons off and on a power of two (the latter divides by
+    multiplying with the exact reciprocal)"""
+    scene, st, paths = c1_small
+    _run(port, scene, st, paths, ticks=6, k=10, orca=dict(tau_agent=tau, tau_obst=2.0, neighbor_dist=5.0))
 
 
 def test_knn_standalone(lib, c1_small):
