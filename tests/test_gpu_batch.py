@@ -91,3 +91,34 @@ def test_autotune_restores_state(port):
     assert np.array_equal(sim.get_record()["nbr_ids"][live], res["nbr_ids"][live])
     assert np.array_equal(sim.get_position_data(), st2.pos)
     sim.close()
+
+
+def test_batch_with_learned_proposal_matches_plain(lib):
+    """the learned mode over a batch of scenes leaves every scene's
+    trajectories as the plain tick's"""
+    import os
+
+    from ecmgenerator_gb300 import proposal as P
+    from ecmgenerator_gb300.simulator import BatchSimulator
+
+    specs = [(31, 200, 40.0), (32, 350, 60.0)]
+    data = [_scene(*sp) for sp in specs]
+    caps = [d[1].n_slots for d in data]
+    sims = [BatchSimulator([d[0] for d in data], caps, 1.0 / 60.0, max_neighbors=10, **ORCA) for _ in range(2)]
+    for sim in sims:
+        for i, (s, st, paths) in enumerate(data):
+            sim.add_agents(st.pos, st.clear, st.pref_speed, paths, scene=i)
+    model = P.ProposalModel(seed=0)
+    model.load(os.path.join(os.path.dirname(P.__file__), "data", "proposal.npy"))
+    sims[1].set_proposal(model)
+    sims[1].set_proposal_gate(0.0, 0)
+    acc = 0
+    for t in range(20):
+        sims[0].update()
+        acc += sims[1].update().accepted
+        assert np.array_equal(sims[0].get_position_data(), sims[1].get_position_data()), t
+        assert np.array_equal(sims[0].get_velocity_data(), sims[1].get_velocity_data()), t
+    assert acc > 0
+    for sim in sims:
+        sim.close()
+    model.close()
