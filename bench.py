@@ -34,9 +34,6 @@ sys.path.insert(0, HERE)
 
 from ecmgenerator_gb300.workloads import DT, ORCA, WORKLOADS  # noqa: E402
 
-# algorithmic state bytes per agent and tick: read pos 8, vel 8, radius 4, speed 4,
-# path cursor 4, attraction 8; write pos 8, vel 8, attraction 8, cursor 4
-ALG_BYTES_PER_AGENT = 64
 
 
 def log(*a):
@@ -219,7 +216,8 @@ class TickTimer:
         self.steps = 0
         self.agent_ms = 0.0
         self.tot = dict(lp3d=0, replans=0, replans_failed=0, replans_host=0, destroyed=0, device_ms=0.0, host_ms=0.0,
-                        proposed=0, accepted=0, gated=0)
+                        proposed=0, accepted=0, gated=0, attract_ms=0.0, neighbors_ms=0.0, proposal_ms=0.0,
+                        orca_ms=0.0)
 
     def tick(self):
         import torch
@@ -336,7 +334,6 @@ def run_ours(args):
                 "plain": e2e["plain"], "note": "wall clock of Simulator.update() + the position and velocity getters "
                 "(ecmg_host_view: device -> page-locked host copy) per tick; h2d = counters, d2h = positions and "
                 "velocities + counters"}
-    kern_ms = main_t.agent_ms / max(args.steps, 1)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
@@ -344,15 +341,25 @@ def run_ours(args):
         pass
     hbm = peaks.get("hbm_gbs") or 6800.0
     per_tick = main_t.steps / max(args.steps, 1)
-    achieved = ALG_BYTES_PER_AGENT * per_tick / (kern_ms / 1e3) / 1e9 if kern_ms > 0 else 0.0
+    # the dominant kernel of the tick by measured device time, with its
+    # algorithmic bytes per agent: k_neighbors reads its snapshot position and
+    # writes k neighbour indices (candidate positions are cache reuse);
+    # k_agents reads the snapshot (pos, vel, radius), speed, preferred
+    # velocity, active flag, slot, neighbour count and k indices, and writes
+    # pos and vel
+    kern = {"k_neighbors": (main_t.tot["neighbors_ms"], 8 + 4 * k), "k_agents": (main_t.tot["orca_ms"], 57 + 4 * k)}
+    kname = max(kern, key=lambda q: kern[q][0])
+    kern_ms = kern[kname][0] / max(args.steps, 1)
+    alg_bytes = kern[kname][1]
+    achieved = alg_bytes * per_tick / (kern_ms / 1e3) / 1e9 if kern_ms > 0 else 0.0
     traffic = None
-    tf = os.path.join(HERE, "profiles", "k_agents_traffic.json")
+    tf = os.path.join(HERE, "profiles", "kernel_traffic.json")
     if os.path.exists(tf):
         try:
-            t = json.load(open(tf)).get(args.workload)
+            t = json.load(open(tf)).get(kname, {}).get(args.workload)
             if t:
-                traffic = t["dram_bytes_per_agent"] * per_tick
-        except (OSError, ValueError, KeyError):
+                traffic = t * per_tick
+        except (OSError, ValueError, AttributeError):
             traffic = None
     T = main_t.tot
     launches = plain.L.ecmg_kernels_per_tick(plain.h) * args.steps
@@ -384,8 +391,12 @@ def run_ours(args):
             "trajectories_identical": same},
         "e2e": e2e_main,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "kernel": "k_agents", "kernel_ms": kern_ms,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"},
+                     "traffic": traffic, "kernel": kname, "kernel_ms": kern_ms, "alg_bytes_per_agent": alg_bytes,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
+                     "kernel_ms_per_tick": {"k_attract": main_t.tot["attract_ms"] / args.steps,
+                                            "k_neighbors": main_t.tot["neighbors_ms"] / args.steps,
+                                            "features+k_mlp_infer": main_t.tot["proposal_ms"] / args.steps,
+                                            "k_agents": main_t.tot["orca_ms"] / args.steps}},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "tick_stats": {"lp3d_per_tick": T["lp3d"] / args.steps, "replans_per_tick": T["replans"] / args.steps,

@@ -38,7 +38,9 @@ class TickStats(C.Structure):
                 ("agent_steps", C.c_longlong), ("destroyed", C.c_longlong), ("replans", C.c_longlong),
                 ("replans_failed", C.c_longlong), ("lp3d", C.c_longlong), ("device_ms", C.c_float),
                 ("agent_kernel_ms", C.c_float), ("host_ms", C.c_float), ("proposed", C.c_longlong),
-                ("accepted", C.c_longlong), ("gated", C.c_longlong), ("replans_host", C.c_longlong)]
+                ("accepted", C.c_longlong), ("gated", C.c_longlong), ("replans_host", C.c_longlong),
+                ("attract_ms", C.c_float), ("neighbors_ms", C.c_float), ("proposal_ms", C.c_float),
+                ("orca_ms", C.c_float)]
 
 
 class TuneResult(C.Structure):

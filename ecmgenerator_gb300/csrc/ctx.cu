@@ -96,7 +96,8 @@ struct ecmg_ctx {
     int max_agents = 0;
     std::string err;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr, ev_a0 = nullptr, ev_a1 = nullptr;
+    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
+    cudaEvent_t ev_k[5] = {}; /* around the attraction, neighbour, proposal and per-agent kernels */
     cudaEvent_t ev_mid = nullptr; /* after k_attract: destroyed / re-plan lists are final */
     int sms = 1;
     /* launch configuration (autotuned) */
@@ -278,8 +279,7 @@ ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max
     CKC(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CKC(cudaEventCreate(&c->ev_t0));
     CKC(cudaEventCreate(&c->ev_t1));
-    CKC(cudaEventCreate(&c->ev_a0));
-    CKC(cudaEventCreate(&c->ev_a1));
+    for (auto& e : c->ev_k) CKC(cudaEventCreate(&e));
     CKC(cudaEventCreateWithFlags(&c->ev_mid, cudaEventDisableTiming));
     size_t N = (size_t)total;
     CKC(c->pos.alloc(N)); CKC(c->vel.alloc(N)); CKC(c->attr.alloc(N)); CKC(c->pref_vel.alloc(N));
@@ -361,8 +361,8 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
         if (h) cudaFreeHost(h);
     if (c->ev_t0) cudaEventDestroy(c->ev_t0);
     if (c->ev_t1) cudaEventDestroy(c->ev_t1);
-    if (c->ev_a0) cudaEventDestroy(c->ev_a0);
-    if (c->ev_a1) cudaEventDestroy(c->ev_a1);
+    for (auto& e : c->ev_k)
+        if (e) cudaEventDestroy(e);
     if (c->ev_mid) cudaEventDestroy(c->ev_mid);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1036,7 +1036,7 @@ static cudaError_t enqueue_tick(ecmg_ctx* c, int launch_slots, bool use_model)
     }
     ProposeCall pc{c->model, c->feat.p, c->counters.p + C_NSORTED, launch_slots, c->cls.p, c->sms,
                    c->counters.p + C_ERROR};
-    e = launch_tick(b, t, launch_slots, c->scan_tmp.p, c->block, c->sms, c->stream, c->ev_a0, c->ev_a1,
+    e = launch_tick(b, t, launch_slots, c->scan_tmp.p, c->block, c->sms, c->stream, c->ev_k,
                     use_model ? propose_cb : nullptr, &pc, after_attract_cb, c);
     if (e != cudaSuccess) return e;
     return cudaMemcpyAsync(c->h_counters + kCounters, c->counters.p, sizeof(int) * kCounters, cudaMemcpyDeviceToHost,
@@ -1191,12 +1191,17 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         CK(cudaStreamSynchronize(c->stream));
         c->h_up_used = 0; /* every queued upload has been applied */
         auto h1 = std::chrono::steady_clock::now();
-        float ms = 0, ams = 0;
+        float ms = 0, kms[4] = {0, 0, 0, 0};
         if (cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1) != cudaSuccess) ms = 0;
-        if (cudaEventElapsedTime(&ams, c->ev_a0, c->ev_a1) != cudaSuccess) ams = 0;
+        for (int q = 0; q < 4; q++)
+            if (cudaEventElapsedTime(&kms[q], c->ev_k[q], c->ev_k[q + 1]) != cudaSuccess) kms[q] = 0;
         cudaGetLastError();
         st.device_ms += ms;
-        st.agent_kernel_ms += ams;
+        st.agent_kernel_ms += kms[0] + kms[1] + kms[2] + kms[3];
+        st.attract_ms += kms[0];
+        st.neighbors_ms += kms[1];
+        st.proposal_ms += kms[2];
+        st.orca_ms += kms[3];
         const int* out = c->h_counters + kCounters;
         st.agent_steps += out[C_NSORTED];
         st.lp3d += out[C_LP3D];

@@ -1071,7 +1071,7 @@ static int grid_for(int n, int block, int sms, int per_sm)
 }
 
 cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int block, int sms,
-                        cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1, ProposeFn propose, void* propose_user,
+                        cudaStream_t s, const cudaEvent_t* ev, ProposeFn propose, void* propose_user,
                         HookFn after_attract, void* after_attract_user)
 {
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -1086,7 +1086,7 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
     if (e != cudaSuccess) return e;
     k_scatter<<<gb, 256, 0, s>>>(b);
     /* external event nodes when captured, so that the kernel can be timed */
-    if (ev0) cudaEventRecordWithFlags(ev0, s, evflags);
+    if (ev) cudaEventRecordWithFlags(ev[0], s, evflags);
     if (block != 64 && block != 128 && block != 256) block = 128;
     int gk = grid_for(max_slots, 128, sms, 16);
     int per_sm = 1;
@@ -1095,9 +1095,11 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
         e = after_attract(after_attract_user, s, evflags);
         if (e != cudaSuccess) return e;
     }
+    if (ev) cudaEventRecordWithFlags(ev[1], s, evflags);
     if (t.k <= 8) k_neighbors<8><<<gk, 128, 0, s>>>(t);
     else if (t.k <= 16) k_neighbors<16><<<gk, 128, 0, s>>>(t);
     else k_neighbors<32><<<gk, 128, 0, s>>>(t);
+    if (ev) cudaEventRecordWithFlags(ev[2], s, evflags);
     if (t.feat) {
         k_features<<<gk, 128, 0, s>>>(t);
         if (propose) {
@@ -1105,6 +1107,7 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
             if (e2 != cudaSuccess) return e2;
         }
     }
+    if (ev) cudaEventRecordWithFlags(ev[3], s, evflags);
     if (t.lp_mode == 1) {
         if (t.k <= 8) {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_warp<8>, 256, 0);
@@ -1126,7 +1129,7 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<32>, block, 0);
         k_agents<32><<<sms * (per_sm > 0 ? per_sm : 1), block, 0, s>>>(t);
     }
-    if (ev1) cudaEventRecordWithFlags(ev1, s, evflags);
+    if (ev) cudaEventRecordWithFlags(ev[4], s, evflags);
     return cudaGetLastError();
 }
 

@@ -70,12 +70,16 @@ typedef struct {
     long long replans_failed;
     long long lp3d;        /* agents whose 2D LP was infeasible                   */
     float device_ms;       /* device time of the ticks (CUDA events)              */
-    float agent_kernel_ms; /* device time of the neighbour + per-agent kernels    */
+    float agent_kernel_ms; /* device time of the attraction, neighbour, proposal and per-agent kernels */
     float host_ms;         /* host time between ticks (bookkeeping, re-planning)  */
     long long proposed;    /* learned mode: LPs that received an active-set proposal */
     long long accepted;    /* learned mode: proposals that passed the exact check     */
     long long gated;       /* learned mode: ticks run without the model (gate closed) */
     long long replans_host; /* re-plans served by the host planner (the rest were settled on the device) */
+    float attract_ms;      /* device time of the attraction / steering kernel      */
+    float neighbors_ms;    /* device time of the neighbour (kNN) kernel            */
+    float proposal_ms;     /* learned mode: feature and inference kernels          */
+    float orca_ms;         /* device time of the per-agent ORCA kernel             */
 } ecmg_tick_stats;
 
 /* Static obstacles: n_obstacles rings, ring r = xy[2*ring_offsets[r] ..
