@@ -192,7 +192,7 @@ def apply_launch(plain, learned, args):
                 set_launch(s_, 128, 32, r["grid_cell_scale"])
                 set_lp_mode(s_, "warp", grab)
             else:
-                set_launch(s_, r["block_size"], grab, r["grid_cell_scale"])
+                set_launch(s_, r["block_size"], grab, r["grid_cell_scale"], r["occupancy_divisor"])
                 set_lp_mode(s_, "thread", 1)
         return r
     grab = 4 if args.lp_mode == "warp" else 32

@@ -45,7 +45,8 @@ class TickStats(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("block_size", C.c_int), ("agents_per_warp_grab", C.c_int), ("grid_cell_scale", C.c_float),
-                ("best_tick_ms", C.c_float), ("trials", C.c_int), ("lp_mode", C.c_int)]
+                ("best_tick_ms", C.c_float), ("trials", C.c_int), ("lp_mode", C.c_int),
+                ("occupancy_divisor", C.c_int)]
 
 
 class Obstacles(C.Structure):
@@ -127,6 +128,7 @@ def load(build_if_missing: bool = False):
         "ecmg_scene_counts": (C.c_int, [vp, C.c_int, ip, ip, ip, ip]),
         "ecmg_set_launch": (C.c_int, [vp, C.c_int, C.c_int, C.c_float]),
         "ecmg_set_lp_mode": (C.c_int, [vp, C.c_int, C.c_int]),
+        "ecmg_set_occupancy": (C.c_int, [vp, C.c_int]),
         "ecmg_autotune": (C.c_int, [vp, C.c_int, C.POINTER(TuneResult)]),
         "ecmg_knn_noalloc": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
                                        C.c_float, C.c_float, vp, vp, vp]),

@@ -75,6 +75,7 @@ struct SceneState {
     DBuf<unsigned char> d_ob_convex;
     DBuf<float> d_special_y;
     DBuf<int> d_sp_start, d_sp_items;
+    DBuf<unsigned> d_sp_bloom;
     int slot_base = 0, slot_cap = 0;
     std::vector<int> free_stack; /* back() = top */
     int num_agents = 0;
@@ -85,7 +86,7 @@ struct SceneState {
         d_ob_p.free_(); d_v_pos.free_(); d_he_left.free_(); d_he_right.free_();
         d_ob_next.free_(); d_ob_prev.free_(); d_v_idx.free_(); d_he_target.free_();
         d_ob_gstart.free_(); d_ob_gitems.free_(); d_ecm_gstart.free_(); d_ecm_gitems.free_();
-        d_ob_convex.free_(); d_special_y.free_(); d_sp_start.free_(); d_sp_items.free_();
+        d_ob_convex.free_(); d_special_y.free_(); d_sp_start.free_(); d_sp_items.free_(); d_sp_bloom.free_();
     }
 };
 
@@ -105,6 +106,7 @@ struct ecmg_ctx {
     int tile = 32;
     float cell_scale = 0.4f;
     int lp_mode = 0; /* 0: one thread per agent, 1: one warp per agent */
+    int occ_div = 1; /* per-thread layout: resident blocks per SM divided by this */
     int wgrab = 4;   /* agents per work grab in warp mode */
 
     /* host mirrors (Simulator bookkeeping, Simulator.h:164-171) */
@@ -466,6 +468,9 @@ ecmg_status ecmg_scene_set_ecm(ecmg_ctx* c, int scene, const ecmg_ecm* e)
         CK(cudaMemcpy(sc->d_sp_start.p, s.sp_start.data(), sizeof(int) * s.sp_start.size(), cudaMemcpyHostToDevice));
     if (!s.sp_items.empty())
         CK(cudaMemcpy(sc->d_sp_items.p, s.sp_items.data(), sizeof(int) * s.sp_items.size(), cudaMemcpyHostToDevice));
+    CK(sc->d_sp_bloom.alloc(std::max<size_t>(1, s.sp_bloom.size())));
+    if (!s.sp_bloom.empty())
+        CK(cudaMemcpy(sc->d_sp_bloom.p, s.sp_bloom.data(), sizeof(unsigned) * s.sp_bloom.size(), cudaMemcpyHostToDevice));
     if (V) {
         CK(cudaMemcpy(sc->d_v_pos.p, s.v_pos.data(), sizeof(V2) * V, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(sc->d_v_idx.p, s.v_idx.data(), sizeof(int) * V, cudaMemcpyHostToDevice));
@@ -877,6 +882,7 @@ static ecmg_status ensure_grids(ecmg_ctx* c)
             e.n_special = (int)s.special_y.size();
             e.sp_start = sc->d_sp_start.p;
             e.sp_items = sc->d_sp_items.p;
+            e.sp_bloom = s.sp_bloom.empty() ? nullptr : sc->d_sp_bloom.p;
         }
         c->total_buckets = base;
         CK(c->d_scenes.alloc(tab.size()));
@@ -946,6 +952,7 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t, bool use_model)
     t.slot_scene = b.slot_scene;
     t.tile = c->lp_mode ? c->wgrab : c->tile;
     t.lp_mode = c->lp_mode;
+    t.occ_div = c->occ_div;
     const ecmg_params& p = c->prm;
     t.dt = p.dt;
     t.tau_a = p.tau_agent;
@@ -1268,55 +1275,77 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
         c->num_agents = num;
         return ECMG_OK;
     };
+    struct Launch {
+        float scale;
+        int mode, block, tile, occ_div, wgrab;
+    };
+    Launch bestL{c->cell_scale, c->lp_mode, c->block, c->tile, c->occ_div, c->wgrab};
+    float best = 1e30f;
+    int trials = 0;
+    c->replan_enabled = false;
+    auto trial = [&](const Launch& L, bool* better) -> ecmg_status {
+        if (L.scale != c->cell_scale) {
+            c->cell_scale = L.scale;
+            for (auto& s : c->scenes) s->grid_ready = false;
+        }
+        c->lp_mode = L.mode;
+        c->block = L.block;
+        c->tile = L.tile;
+        c->occ_div = L.occ_div;
+        c->wgrab = L.wgrab;
+        c->graph_dirty = true;
+        ecmg_tick_stats ts{};
+        ecmg_status st = run_ticks(c, 1, &ts); /* warm-up and graph capture */
+        if (st == ECMG_OK) st = run_ticks(c, ticks_per_trial, &ts);
+        ecmg_status rs = restore();
+        if (st != ECMG_OK) return st;
+        if (rs != ECMG_OK) return rs;
+        trials++;
+        const float ms = ts.device_ms / (float)ticks_per_trial;
+        *better = ms < best;
+        if (*better) {
+            best = ms;
+            bestL = L;
+        }
+        return ECMG_OK;
+    };
+    /* stage 1: the agent-grid cell (mostly the neighbour search), default
+       launch; stage 2: the per-agent kernel's launch at the best cell */
+    const float scales[] = {0.3f, 0.4f, 0.5f, 0.6f, 0.8f};
     const int blocks[] = {64, 128, 256};
     const int tiles[] = {32, 64, 128};
+    const int divs[] = {1, 2, 3};
     const int wgrabs[] = {1, 2, 4, 8};
-    const float scales[] = {0.3f, 0.4f, 0.5f, 0.6f, 0.8f};
-    int bb = c->block, bt = c->tile, bmode = c->lp_mode, bw = c->wgrab;
-    float bs = c->cell_scale, best = 1e30f;
     const bool fixed_cell = c->prm.grid_cell > 0.0f;
-    c->replan_enabled = false;
-    int trials = 0;
+    const int def_block = c->prm.block_size ? c->prm.block_size : 128;
+    bool better = false;
+    ecmg_status st = ECMG_OK;
     for (float sc : scales) {
         if (fixed_cell && sc != scales[0]) break;
-        c->cell_scale = sc;
-        for (auto& s : c->scenes) s->grid_ready = false;
-        /* per-thread mode: block x work grab; warp mode: work grab */
-        for (int mode = 0; mode < 2; mode++) {
-            const int nb = mode ? 1 : 3, nt = 4;
-            for (int bi = 0; bi < nb; bi++) {
-                const int b = mode ? 256 : blocks[bi];
-                if (!mode && c->prm.block_size && b != c->prm.block_size) continue;
-                for (int ti = 0; ti < nt; ti++) {
-                    if (!mode && ti == 3) break;
-                    c->lp_mode = mode;
-                    if (mode) c->wgrab = wgrabs[ti];
-                    else {
-                        c->block = b;
-                        c->tile = tiles[ti];
-                    }
-                    c->graph_dirty = true;
-                    ecmg_tick_stats ts{};
-                    ecmg_status st = run_ticks(c, 1, &ts); /* warm-up and graph capture */
-                    if (st == ECMG_OK) st = run_ticks(c, ticks_per_trial, &ts);
-                    ecmg_status rs = restore();
-                    if (st != ECMG_OK || rs != ECMG_OK) {
-                        c->replan_enabled = true;
-                        return st != ECMG_OK ? st : rs;
-                    }
-                    trials++;
-                    float ms = ts.device_ms / (float)ticks_per_trial;
-                    if (ms < best) {
-                        best = ms;
-                        bmode = mode;
-                        bs = sc;
-                        if (mode) bw = c->wgrab;
-                        else { bb = c->block; bt = c->tile; }
-                    }
-                }
-            }
-        }
+        st = trial(Launch{sc, 0, def_block, 32, 1, c->wgrab}, &better);
+        if (st != ECMG_OK) break;
     }
+    const float cell = bestL.scale;
+    for (int b : blocks) {
+        if (st != ECMG_OK) break;
+        if (c->prm.block_size && b != c->prm.block_size) continue;
+        for (int tl : tiles)
+            for (int dv : divs) {
+                if (st != ECMG_OK) break;
+                st = trial(Launch{cell, 0, b, tl, dv, c->wgrab}, &better);
+            }
+    }
+    for (int w : wgrabs) {
+        if (st != ECMG_OK) break;
+        st = trial(Launch{cell, 1, bestL.block, bestL.tile, 1, w}, &better);
+    }
+    if (st != ECMG_OK) {
+        c->replan_enabled = true;
+        return st;
+    }
+    int bb = bestL.block, bt = bestL.tile, bmode = bestL.mode, bw = bestL.wgrab;
+    float bs = bestL.scale;
+    c->occ_div = bestL.occ_div;
     c->replan_enabled = true;
     c->block = bb;
     c->tile = bt;
@@ -1333,6 +1362,7 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
         out->grid_cell_scale = bs;
         out->best_tick_ms = best;
         out->trials = trials;
+        out->occupancy_divisor = bestL.occ_div;
     }
     return ECMG_OK;
 }
@@ -1343,6 +1373,14 @@ ecmg_status ecmg_set_lp_mode(ecmg_ctx* c, int mode, int agents_per_warp_grab)
     if (mode == ECMG_LP_WARP && (agents_per_warp_grab < 1 || agents_per_warp_grab > 64)) return ECMG_ERR_INVALID_ARG;
     c->lp_mode = mode;
     if (mode == ECMG_LP_WARP) c->wgrab = agents_per_warp_grab;
+    c->graph_dirty = true;
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_set_occupancy(ecmg_ctx* c, int divisor)
+{
+    if (!c || divisor < 1 || divisor > 8) return ECMG_ERR_INVALID_ARG;
+    c->occ_div = divisor;
     c->graph_dirty = true;
     return ECMG_OK;
 }

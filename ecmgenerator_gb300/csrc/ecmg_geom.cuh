@@ -121,7 +121,21 @@ struct EcmView {
     int n_special;
     const int* sp_start;
     const int* sp_items;
+    /* 65536-bit filter of the special heights (bit sp_hash(y) set for each):
+       a clear bit proves that y is not special (null: no filter) */
+    const unsigned* sp_bloom;
 };
+
+/* bit index of a height in the filter; -0 and +0 hash alike (they compare equal) */
+EG_HD unsigned sp_hash(float y)
+{
+    union {
+        float f;
+        unsigned u;
+    } b;
+    b.f = (y == 0.0f) ? 0.0f : y;
+    return (b.u * 2654435769u) >> 16;
+}
 
 /* quad of PointLocationQueryLinear (ECMCellCollection.cpp:67-80):
    [v(he1.target), boundary.p0, boundary.p1, v(he0.target)] */
@@ -162,6 +176,10 @@ EG_HD bool contains_quad(V2 p, const V2* q)
 /* index s with special_y[s] == y, or -1 */
 EG_HD int special_index(const EcmView& e, float y)
 {
+    if (e.sp_bloom) {
+        const unsigned h = sp_hash(y);
+        if (!((e.sp_bloom[h >> 5] >> (h & 31u)) & 1u)) return -1;
+    }
     int lo = 0, hi = e.n_special;
     while (lo < hi) {
         int mid = (lo + hi) >> 1;

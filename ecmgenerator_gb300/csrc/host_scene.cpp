@@ -33,6 +33,7 @@ EcmView HostScene::ecm_view() const
     e.n_special = (int)special_y.size();
     e.sp_start = sp_start.data();
     e.sp_items = sp_items.data();
+    e.sp_bloom = sp_bloom.empty() ? nullptr : sp_bloom.data();
     return e;
 }
 
@@ -110,6 +111,11 @@ void build_ecm_grid(HostScene& s)
     std::sort(ys.begin(), ys.end());
     ys.erase(std::unique(ys.begin(), ys.end()), ys.end());
     s.special_y = ys;
+    s.sp_bloom.assign(2048, 0u);
+    for (float y : ys) {
+        unsigned h = sp_hash(y);
+        s.sp_bloom[h >> 5] |= 1u << (h & 31u);
+    }
     /* per special height, the quads with a corner there (ascending) */
     {
         std::vector<int> cnt(ys.size() + 1, 0);

@@ -32,6 +32,7 @@ struct HostScene {
     GridCSR ecm_grid;
     std::vector<float> special_y;
     std::vector<int> sp_start, sp_items; /* quads with a corner at special_y[s] */
+    std::vector<unsigned> sp_bloom;      /* 2048 words: filter of the special heights */
     /* scene rectangle (ECM and obstacle bounding box) */
     float bx0 = 0, by0 = 0, bx1 = 0, by1 = 0;
     bool has_ecm = false;

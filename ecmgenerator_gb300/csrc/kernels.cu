@@ -1119,15 +1119,20 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_warp<32>, 256, 0);
             k_agents_warp<32><<<sms * (per_sm > 0 ? per_sm : 1), 256, 0, s>>>(t);
         }
-    } else if (t.k <= 8) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<8>, block, 0);
-        k_agents<8><<<sms * (per_sm > 0 ? per_sm : 1), block, 0, s>>>(t);
-    } else if (t.k <= 16) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<16>, block, 0);
-        k_agents<16><<<sms * (per_sm > 0 ? per_sm : 1), block, 0, s>>>(t);
     } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<32>, block, 0);
-        k_agents<32><<<sms * (per_sm > 0 ? per_sm : 1), block, 0, s>>>(t);
+        /* persistent grid: the resident blocks per SM, divided by occ_div
+           (fewer resident warps leave each more L1 for its local arrays) */
+        const int div = t.occ_div > 1 ? t.occ_div : 1;
+        if (t.k <= 8) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<8>, block, 0);
+            k_agents<8><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
+        } else if (t.k <= 16) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<16>, block, 0);
+            k_agents<16><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
+        } else {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<32>, block, 0);
+            k_agents<32><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
+        }
     }
     if (ev) cudaEventRecordWithFlags(ev[4], s, evflags);
     return cudaGetLastError();

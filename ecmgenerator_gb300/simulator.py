@@ -380,11 +380,14 @@ def autotune(sim: Simulator, ticks_per_trial: int = 2) -> dict:
     sim._ck(sim.L.ecmg_autotune(sim.h, int(ticks_per_trial), C.byref(r)))
     return dict(block_size=r.block_size, agents_per_warp_grab=r.agents_per_warp_grab,
                 grid_cell_scale=r.grid_cell_scale, best_tick_ms=r.best_tick_ms, trials=r.trials,
-                lp_mode=("warp" if r.lp_mode == 1 else "thread"))
+                lp_mode=("warp" if r.lp_mode == 1 else "thread"), occupancy_divisor=r.occupancy_divisor)
 
 
-def set_launch(sim: Simulator, block_size: int, agents_per_warp_grab: int, grid_cell_scale: float):
+def set_launch(sim: Simulator, block_size: int, agents_per_warp_grab: int, grid_cell_scale: float,
+               occupancy_divisor: int = 1):
     sim._ck(sim.L.ecmg_set_launch(sim.h, int(block_size), int(agents_per_warp_grab), float(grid_cell_scale)))
+    if occupancy_divisor != 1:
+        sim._ck(sim.L.ecmg_set_occupancy(sim.h, int(occupancy_divisor)))
 
 
 def set_lp_mode(sim: Simulator, mode: str = "warp", agents_per_warp_grab: int = 4):

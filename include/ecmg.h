@@ -226,6 +226,7 @@ typedef struct {
     float best_tick_ms;
     int trials;
     int lp_mode;             /* ECMG_LP_THREAD or ECMG_LP_WARP */
+    int occupancy_divisor;   /* per-thread layout: resident blocks per SM divided by this */
 } ecmg_tune_result;
 ecmg_status ecmg_set_launch(ecmg_ctx* ctx, int block_size, int agents_per_warp_grab, float grid_cell_scale);
 /* Per-agent kernel layout.  ECMG_LP_THREAD: one thread per agent (work
@@ -233,11 +234,16 @@ ecmg_status ecmg_set_launch(ecmg_ctx* ctx, int block_size, int agents_per_warp_g
    warp per agent -- the lanes build the constraints in parallel and share
    the inner loops of the LPs -- taking agents_per_warp_grab agents per work
    grab (1..64).  Both give identical results. */
+/* per-thread layout: run the persistent per-agent kernel with the resident
+   blocks per SM divided by `divisor` (1..8; fewer resident warps leave more
+   L1 to each thread's local constraint arrays) */
+ecmg_status ecmg_set_occupancy(ecmg_ctx* ctx, int divisor);
 #define ECMG_LP_THREAD 0
 #define ECMG_LP_WARP 1
 ecmg_status ecmg_set_lp_mode(ecmg_ctx* ctx, int mode, int agents_per_warp_grab);
-/* times ticks_per_trial ticks per configuration (per-agent kernel layout x
-   block size x work grab x grid cell) on a copy of the current state, restores the state after each
+/* times ticks_per_trial ticks per configuration -- first the grid cell with
+   the default launch, then, at the best cell, the per-agent kernel's layout,
+   block size, work grab and occupancy -- on a copy of the current state, restores the state after each
    trial (no re-plans are served during trials) and keeps the fastest */
 ecmg_status ecmg_autotune(ecmg_ctx* ctx, int ticks_per_trial, ecmg_tune_result* out);
 

@@ -64,7 +64,7 @@ def test_autotune_restores_state(port):
     sim.update(ticks=3)
     before = (sim.get_position_data(), sim.get_velocity_data(), sim.get_attraction_point_data(), sim.get_num_agents())
     r = autotune(sim, ticks_per_trial=1)
-    assert r["trials"] >= 13 and r["lp_mode"] in ("thread", "warp")
+    assert r["trials"] >= 13 and r["lp_mode"] in ("thread", "warp") and r["occupancy_divisor"] in (1, 2, 3)
     if r["lp_mode"] == "thread":
         assert r["block_size"] in (64, 128, 256) and r["agents_per_warp_grab"] in (32, 64, 128)
     else:
