@@ -100,6 +100,8 @@ struct ecmg_ctx {
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
     cudaEvent_t ev_k[5] = {}; /* around the attraction, neighbour, proposal and per-agent kernels */
     cudaEvent_t ev_mid = nullptr; /* after k_attract: destroyed / re-plan lists are final */
+    cudaStream_t stream2 = nullptr; /* the attraction kernel, beside the neighbour search */
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int sms = 1;
     /* launch configuration (autotuned) */
     int block = 128;
@@ -283,6 +285,9 @@ ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max
     CKC(cudaEventCreate(&c->ev_t1));
     for (auto& e : c->ev_k) CKC(cudaEventCreate(&e));
     CKC(cudaEventCreateWithFlags(&c->ev_mid, cudaEventDisableTiming));
+    CKC(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    CKC(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    CKC(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
     size_t N = (size_t)total;
     CKC(c->pos.alloc(N)); CKC(c->vel.alloc(N)); CKC(c->attr.alloc(N)); CKC(c->pref_vel.alloc(N));
     CKC(c->d_clear.alloc(N)); CKC(c->d_speed.alloc(N)); CKC(c->d_active.alloc(N));
@@ -366,6 +371,9 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
     for (auto& e : c->ev_k)
         if (e) cudaEventDestroy(e);
     if (c->ev_mid) cudaEventDestroy(c->ev_mid);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return ECMG_OK;
@@ -1043,7 +1051,8 @@ static cudaError_t enqueue_tick(ecmg_ctx* c, int launch_slots, bool use_model)
     }
     ProposeCall pc{c->model, c->feat.p, c->counters.p + C_NSORTED, launch_slots, c->cls.p, c->sms,
                    c->counters.p + C_ERROR};
-    e = launch_tick(b, t, launch_slots, c->scan_tmp.p, c->block, c->sms, c->stream, c->ev_k,
+    e = launch_tick(b, t, launch_slots, c->scan_tmp.p, c->block, c->sms, c->stream, c->stream2, c->ev_fork,
+                    c->ev_join, c->ev_k,
                     use_model ? propose_cb : nullptr, &pc, after_attract_cb, c);
     if (e != cudaSuccess) return e;
     return cudaMemcpyAsync(c->h_counters + kCounters, c->counters.p, sizeof(int) * kCounters, cudaMemcpyDeviceToHost,
@@ -1198,17 +1207,22 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         CK(cudaStreamSynchronize(c->stream));
         c->h_up_used = 0; /* every queued upload has been applied */
         auto h1 = std::chrono::steady_clock::now();
-        float ms = 0, kms[4] = {0, 0, 0, 0};
+        /* attraction and neighbour kernels run side by side: both are timed
+           from their common start */
+        float ms = 0, tot = 0, att = 0, nbr = 0, prop = 0, orca = 0;
         if (cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1) != cudaSuccess) ms = 0;
-        for (int q = 0; q < 4; q++)
-            if (cudaEventElapsedTime(&kms[q], c->ev_k[q], c->ev_k[q + 1]) != cudaSuccess) kms[q] = 0;
+        if (cudaEventElapsedTime(&tot, c->ev_k[0], c->ev_k[4]) != cudaSuccess) tot = 0;
+        if (cudaEventElapsedTime(&att, c->ev_k[0], c->ev_k[1]) != cudaSuccess) att = 0;
+        if (cudaEventElapsedTime(&nbr, c->ev_k[0], c->ev_k[2]) != cudaSuccess) nbr = 0;
+        if (cudaEventElapsedTime(&prop, c->ev_k[2], c->ev_k[3]) != cudaSuccess) prop = 0;
+        if (cudaEventElapsedTime(&orca, c->ev_k[3], c->ev_k[4]) != cudaSuccess) orca = 0;
         cudaGetLastError();
         st.device_ms += ms;
-        st.agent_kernel_ms += kms[0] + kms[1] + kms[2] + kms[3];
-        st.attract_ms += kms[0];
-        st.neighbors_ms += kms[1];
-        st.proposal_ms += kms[2];
-        st.orca_ms += kms[3];
+        st.agent_kernel_ms += tot;
+        st.attract_ms += att;
+        st.neighbors_ms += nbr;
+        st.proposal_ms += prop;
+        st.orca_ms += orca;
         const int* out = c->h_counters + kCounters;
         st.agent_steps += out[C_NSORTED];
         st.lp3d += out[C_LP3D];

@@ -150,10 +150,13 @@ typedef cudaError_t (*ProposeFn)(void* user, cudaStream_t s);
    the destroyed and re-plan lists are final; evflags are the flags for an
    event record at that point (external when the stream is being captured) */
 typedef cudaError_t (*HookFn)(void* user, cudaStream_t s, unsigned evflags);
-/* ev (may be null): five events recorded before the attraction, neighbour,
-   proposal (features + inference) and per-agent kernels and after the last */
+/* The attraction kernel runs on s2 beside the neighbour kernel on s (fork and
+   join through ev_fork / ev_join).  ev (may be null): five events -- before
+   both, after the attraction kernel (on s2), after the neighbour kernel, after
+   the proposal (features + inference) and after the per-agent kernel. */
 cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int block, int sms,
-                        cudaStream_t s, const cudaEvent_t* ev, ProposeFn propose, void* propose_user,
+                        cudaStream_t s, cudaStream_t s2, cudaEvent_t ev_fork, cudaEvent_t ev_join,
+                        const cudaEvent_t* ev, ProposeFn propose, void* propose_user,
                         HookFn after_attract, void* after_attract_user);
 cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k, float r, AgentGrid g,
                        int* key, int* rank, int* cell_count, int* cell_start, int* s_slot, V2* s_pos,

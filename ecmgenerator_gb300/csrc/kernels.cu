@@ -1071,7 +1071,8 @@ static int grid_for(int n, int block, int sms, int per_sm)
 }
 
 cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int block, int sms,
-                        cudaStream_t s, const cudaEvent_t* ev, ProposeFn propose, void* propose_user,
+                        cudaStream_t s, cudaStream_t s2, cudaEvent_t ev_fork, cudaEvent_t ev_join,
+                        const cudaEvent_t* ev, ProposeFn propose, void* propose_user,
                         HookFn after_attract, void* after_attract_user)
 {
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -1090,16 +1091,25 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
     if (block != 64 && block != 128 && block != 256) block = 128;
     int gk = grid_for(max_slots, 128, sms, 16);
     int per_sm = 1;
-    k_attract<<<gk, 128, 0, s>>>(t);
+    /* the attraction kernel (second stream) and the neighbour search are
+       independent: they run side by side and join before the features /
+       per-agent kernels */
+    e = cudaEventRecord(ev_fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, ev_fork, 0);
+    if (e != cudaSuccess) return e;
+    k_attract<<<gk, 128, 0, s2>>>(t);
     if (after_attract) {
-        e = after_attract(after_attract_user, s, evflags);
+        e = after_attract(after_attract_user, s2, evflags);
         if (e != cudaSuccess) return e;
     }
-    if (ev) cudaEventRecordWithFlags(ev[1], s, evflags);
+    if (ev) cudaEventRecordWithFlags(ev[1], s2, evflags);
     if (t.k <= 8) k_neighbors<8><<<gk, 128, 0, s>>>(t);
     else if (t.k <= 16) k_neighbors<16><<<gk, 128, 0, s>>>(t);
     else k_neighbors<32><<<gk, 128, 0, s>>>(t);
     if (ev) cudaEventRecordWithFlags(ev[2], s, evflags);
+    e = cudaEventRecord(ev_join, s2);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_join, 0);
+    if (e != cudaSuccess) return e;
     if (t.feat) {
         k_features<<<gk, 128, 0, s>>>(t);
         if (propose) {

@@ -76,8 +76,8 @@ typedef struct {
     long long accepted;    /* learned mode: proposals that passed the exact check     */
     long long gated;       /* learned mode: ticks run without the model (gate closed) */
     long long replans_host; /* re-plans served by the host planner (the rest were settled on the device) */
-    float attract_ms;      /* device time of the attraction / steering kernel      */
-    float neighbors_ms;    /* device time of the neighbour (kNN) kernel            */
+    float attract_ms;      /* attraction / steering kernel (from the common start)  */
+    float neighbors_ms;    /* neighbour (kNN) kernel, which runs beside it          */
     float proposal_ms;     /* learned mode: feature and inference kernels          */
     float orca_ms;         /* device time of the per-agent ORCA kernel             */
 } ecmg_tick_stats;
