@@ -217,7 +217,8 @@ class TickTimer:
         self.agent_ms = 0.0
         self.tot = dict(lp3d=0, replans=0, replans_failed=0, replans_host=0, destroyed=0, device_ms=0.0, host_ms=0.0,
                         proposed=0, accepted=0, gated=0, attract_ms=0.0, neighbors_ms=0.0, proposal_ms=0.0,
-                        orca_ms=0.0)
+                        orca_ms=0.0, spawned=0, spawn_failed=0, spawn_refused=0, spawn_ms=0.0, spawn_check_ms=0.0,
+                        spawn_candidates=0)
 
     def tick(self):
         import torch
@@ -251,15 +252,26 @@ def run_ours(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     from ecmgenerator_gb300.simulator import Simulator
+    from ecmgenerator_gb300.workloads import add_spawn_areas
 
     cfg, scene, st, paths, k = make_workload(args.workload, args.seed)
     n = st.num_agents
     # two simulators in the same state: the plain tick and the tick with the
     # learned proposal (their trajectories are identical)
     sims = []
+    spawn_slots = 0
+    if args.spawn_rate > 0:
+        # room for the spawned agents; every simulator draws the same
+        # recorded random stream (the C library's rand() is shared)
+        spawn_slots = min(200_000, int(args.spawn_rate * DT * 4 * 2000) + 1024)
+        stream = np.random.default_rng(args.seed + 99).integers(
+            0, 2147483647, 33 * (int(args.spawn_rate * DT) + 1) * 4 * 4000, dtype=np.int32)
     for _ in range(2):
-        s_ = Simulator(scene, n, DT, max_neighbors=k, **ORCA)
+        s_ = Simulator(scene, n + spawn_slots, DT, max_neighbors=k, **ORCA)
         s_.add_agents(st.pos[:n], st.clear[:n], st.pref_speed[:n], paths)
+        if args.spawn_rate > 0:
+            add_spawn_areas(s_, scene, args.spawn_rate)
+            s_.push_spawn_random(stream)
         sims.append(s_)
     plain, learned = sims
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
@@ -406,6 +418,17 @@ def run_ours(args):
                        "graph_ms_per_tick": T["device_ms"] / args.steps,
                        "host_ms_per_tick": T["host_ms"] / args.steps},
     }
+    if args.spawn_rate > 0:
+        K = max(args.steps, 1)
+        out["spawn"] = {"areas": 4, "rate_per_area": args.spawn_rate, "spawned_per_tick": T["spawned"] / K,
+                        "no_location_per_tick": T["spawn_failed"] / K, "refused_per_tick": T["spawn_refused"] / K,
+                        "candidates_per_tick": T["spawn_candidates"] / K, "stage_ms_per_tick": T["spawn_ms"] / K,
+                        "check_ms_per_tick": T["spawn_check_ms"] / K,
+                        "note": "UpdateSpawnAreas at the start of every timed tick (inside the timed region): "
+                                "candidate locations tested on the device against all agents, spawned agents "
+                                "planned on the host; stage_ms includes the planning, check_ms the device test "
+                                "with its copies and wait"}
+        out["config"]["spawn_rate_per_area"] = args.spawn_rate
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(scene, st, k, threads=1, budget_s=args.cpu_budget)
     for s_ in sims:
@@ -455,6 +478,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="time the plain tick only")
+    ap.add_argument("--spawn-rate", type=float, default=0.0,
+                    help="agents/s per spawn area, 4 spawn areas (UpdateSpawnAreas every tick); 0: none")
     ap.add_argument("--proposal", default=None, help="proposal weights (.npy)")
     ap.add_argument("--no-gate", action="store_true", help="keep the proposal model on every tick")
     ap.add_argument("--lp-mode", default="tune", choices=["tune", "thread", "warp"],

@@ -40,7 +40,19 @@ class TickStats(C.Structure):
                 ("agent_kernel_ms", C.c_float), ("host_ms", C.c_float), ("proposed", C.c_longlong),
                 ("accepted", C.c_longlong), ("gated", C.c_longlong), ("replans_host", C.c_longlong),
                 ("attract_ms", C.c_float), ("neighbors_ms", C.c_float), ("proposal_ms", C.c_float),
-                ("orca_ms", C.c_float)]
+                ("orca_ms", C.c_float), ("spawned", C.c_longlong), ("spawn_failed", C.c_longlong),
+                ("spawn_refused", C.c_longlong), ("spawn_ms", C.c_float), ("spawn_check_ms", C.c_float),
+                ("spawn_candidates", C.c_longlong)]
+
+
+class SpawnConfig(C.Structure):
+    _fields_ = [("preferred_speed_min", C.c_float), ("preferred_speed_max", C.c_float),
+                ("clearance_min", C.c_float), ("clearance_max", C.c_float)]
+
+
+class AreaInfo(C.Structure):
+    _fields_ = [("id", C.c_int), ("x", C.c_float), ("y", C.c_float), ("half_w", C.c_float), ("half_h", C.c_float),
+                ("config", SpawnConfig), ("n_connected", C.c_int), ("n_timers", C.c_int)]
 
 
 class TuneResult(C.Structure):
@@ -58,6 +70,9 @@ class Ecm(C.Structure):
                 ("v_halfedge", C.c_void_p), ("n_edges", C.c_int), ("he_target", C.c_void_p),
                 ("he_next", C.c_void_p), ("he_left", C.c_void_p), ("he_right", C.c_void_p)]
 
+
+RAND_FN = C.CFUNCTYPE(C.c_int, C.c_void_p)
+AREA_SPAWN, AREA_GOAL = 2, 3
 
 PLAN_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                       C.POINTER(C.c_float), C.c_int)
@@ -148,6 +163,20 @@ def load(build_if_missing: bool = False):
         "ecmg_set_proposal_gate": (C.c_int, [vp, C.c_float, C.c_int]),
         "ecmg_get_trace": (C.c_int, [vp, vp, vp, vp, C.c_int, ip]),
         "ecmg_set_proposal_classes": (C.c_int, [vp, vp]),
+        "ecmg_add_spawn_area": (C.c_int, [vp, C.c_float, C.c_float, C.c_float, C.c_float, C.POINTER(SpawnConfig),
+                                          C.c_int, ip]),
+        "ecmg_add_goal_area": (C.c_int, [vp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, ip]),
+        "ecmg_remove_area": (C.c_int, [vp, C.c_int, C.c_int]),
+        "ecmg_connect_areas": (C.c_int, [vp, C.c_int, C.c_int, C.c_float]),
+        "ecmg_disconnect_areas": (C.c_int, [vp, C.c_int, C.c_int]),
+        "ecmg_set_area": (C.c_int, [vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float]),
+        "ecmg_get_area": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(AreaInfo), vp, vp, vp, C.c_int]),
+        "ecmg_area_ids": (C.c_int, [vp, C.c_int, vp, C.c_int, ip]),
+        "ecmg_set_spawn_rng": (C.c_int, [vp, RAND_FN, vp, C.c_int]),
+        "ecmg_push_spawn_random": (C.c_int, [vp, vp, C.c_int]),
+        "ecmg_spawn_random_pending": (C.c_int, [vp, C.POINTER(C.c_longlong)]),
+        "ecmg_update_spawn_areas": (C.c_int, [vp, C.POINTER(TickStats)]),
+        "ecmg_get_spawned": (C.c_int, [vp, vp, vp, vp, C.c_int, ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -15,9 +15,17 @@
 #include "host_scene.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
+#include <map>
+#include <tuple>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -59,8 +67,100 @@ struct DBuf {
     }
 };
 
+/* SpawnArea / GoalArea (Area.h:30-101) */
+struct SpawnAreaH {
+    int id = 0;
+    float x = 0, y = 0, hw = 0, hh = 0;
+    ecmg_spawn_config cfg{5.0f, 10.0f, 5.0f, 10.0f};
+    std::vector<int> goals;   /* connectedGoalAreas */
+    std::vector<float> rate;  /* spawnRate */
+    std::vector<float> since; /* timeSinceLastSpawn */
+};
+struct GoalAreaH {
+    int id = 0;
+    float x = 0, y = 0, hw = 0, hh = 0;
+};
+
+/* Host threads for the planner calls of a tick (re-plans, spawned agents):
+   started once, idle on a condition variable between ticks.  run(m, fn)
+   calls fn(i, w) for i in [0, m) on the calling thread (w = 0) and the
+   workers (w = 1..size()), each with its own planner scratch. */
+class HostPool {
+public:
+    ~HostPool()
+    {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : th_) t.join();
+    }
+    int size() const { return (int)th_.size(); }
+    std::vector<PlanScratch> scratch; /* [size() + 1] */
+    void start(int n)
+    {
+        if (!th_.empty() || n < 1) return;
+        scratch.resize((size_t)n + 1);
+        for (int w = 1; w <= n; w++) th_.emplace_back([this, w] { loop(w); });
+    }
+    void run(int m, const std::function<void(int, int)>& fn)
+    {
+        if (th_.empty() || m < 2) {
+            for (int i = 0; i < m; i++) fn(i, 0);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            job_ = &fn;
+            m_ = m;
+            next_ = 0;
+            busy_ = (int)th_.size();
+            gen_++;
+        }
+        cv_.notify_all();
+        for (int i; (i = next_.fetch_add(1)) < m;) fn(i, 0);
+        std::unique_lock<std::mutex> l(mu_);
+        done_.wait(l, [this] { return busy_ == 0; });
+        job_ = nullptr;
+    }
+
+private:
+    void loop(int w)
+    {
+        unsigned seen = 0;
+        for (;;) {
+            const std::function<void(int, int)>* job;
+            int m;
+            {
+                std::unique_lock<std::mutex> l(mu_);
+                cv_.wait(l, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+                job = job_;
+                m = m_;
+            }
+            for (int i; (i = next_.fetch_add(1)) < m;) (*job)(i, w);
+            std::lock_guard<std::mutex> l(mu_);
+            if (--busy_ == 0) done_.notify_one();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int, int)>* job_ = nullptr;
+    int m_ = 0, busy_ = 0;
+    unsigned gen_ = 0;
+    std::atomic<int> next_{0};
+    bool stop_ = false;
+};
+
 struct SceneState {
     HostScene hs;
+    /* spawn and goal areas in ID order (std::map, as Simulator.h:173-174) */
+    std::map<int, SpawnAreaH> spawn_areas;
+    std::map<int, GoalAreaH> goal_areas;
+    int next_spawn_id = 0, next_goal_id = 0;
     bool has_obst = false;
     GridCSR ob_grid;  /* device candidate grid */
     GridCSR vis_grid; /* planner visibility grid */
@@ -139,7 +239,9 @@ struct ecmg_ctx {
     ecmg_plan_fn plan_fn = nullptr;
     void* plan_user = nullptr;
     PlanScratch scratch;
+    HostPool pool; /* planner threads (built-in planner only: it is re-entrant) */
     bool replan_enabled = true;
+    bool spawn_enabled = true; /* off while the autotuner runs its trial ticks */
     /* per slot: the start edge from which the built-in planner's search
        failed for the slot's current goal and clearance (-1: none) */
     std::vector<int> fail_edge;
@@ -171,6 +273,23 @@ struct ecmg_ctx {
        next tick */
     unsigned char* h_up = nullptr;
     size_t h_up_cap = 0, h_up_used = 0;
+    /* spawn stage: queued random values (rq[rq_head..] not yet consumed),
+       their source, page-locked candidate / area / hit tables and the
+       agents the last stage placed */
+    ecmg_rand_fn rng_fn = nullptr;
+    void* rng_user = nullptr;
+    int rand_max = RAND_MAX;
+    std::vector<int> rq;
+    size_t rq_head = 0;
+    V2* h_cand = nullptr;
+    SpawnAreaDev* h_sarea = nullptr;
+    int* h_hit = nullptr;
+    DBuf<V2> d_cand;
+    DBuf<SpawnAreaDev> d_sarea;
+    DBuf<int> d_hit;
+    DBuf<SpawnRec> d_spawn_rec;
+    std::vector<int> spawned_slot;
+    std::vector<V2> spawned_start, spawned_goal;
     /* graph */
     cudaGraphExec_t graph[2] = {nullptr, nullptr}; /* plain tick, tick with the proposal model */
     bool graph_dirty = true;
@@ -364,6 +483,13 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
     if (c->h_counters) cudaFreeHost(c->h_counters);
     if (c->h_lists) cudaFreeHost(c->h_lists);
     if (c->h_up) cudaFreeHost(c->h_up);
+    if (c->h_cand) cudaFreeHost(c->h_cand);
+    if (c->h_sarea) cudaFreeHost(c->h_sarea);
+    if (c->h_hit) cudaFreeHost(c->h_hit);
+    c->d_cand.free_();
+    c->d_sarea.free_();
+    c->d_hit.free_();
+    c->d_spawn_rec.free_();
     for (void* h : c->hview)
         if (h) cudaFreeHost(h);
     if (c->ev_t0) cudaEventDestroy(c->ev_t0);
@@ -544,20 +670,15 @@ static ecmg_status clear_fail_edge(ecmg_ctx* c, int slot)
     return stage_copy(c, c->d_fail_edge.p + slot, &none, sizeof(int));
 }
 
-static ecmg_status upload_path(ecmg_ctx* c, int slot)
+/* makes room for `need` more path points at path_used: grows (x2) and
+   compacts the path store (after the queued uploads) when it is full */
+static ecmg_status ensure_path_room(ecmg_ctx* c, size_t need)
 {
-    {
-        ecmg_status fs = clear_fail_edge(c, slot);
-        if (fs != ECMG_OK) return fs;
-    }
-    const std::vector<V2>& p = c->paths[slot];
-    size_t n = p.size();
-    if (c->path_used + n > c->path_xy.n) {
-        /* grow (x2) and compact: live paths only (after the queued uploads) */
+    if (c->path_used + need > c->path_xy.n) {
         CK(cudaStreamSynchronize(c->stream));
         size_t live = 0;
         for (int i = 0; i < c->max_agents; i++) live += c->paths[i].size();
-        size_t cap = std::max(c->path_xy.n * 2, live * 2 + 1024);
+        size_t cap = std::max(c->path_xy.n * 2, (live + need) * 2 + 1024);
         DBuf<V2> nb;
         CK(nb.alloc(cap));
         std::vector<V2> host;
@@ -575,7 +696,21 @@ static ecmg_status upload_path(ecmg_ctx* c, int slot)
         c->path_xy = nb;
         c->path_used = host.size();
         c->graph_dirty = true;
-        return ECMG_OK;
+    }
+    return ECMG_OK;
+}
+
+static ecmg_status upload_path(ecmg_ctx* c, int slot)
+{
+    {
+        ecmg_status fs = clear_fail_edge(c, slot);
+        if (fs != ECMG_OK) return fs;
+    }
+    const std::vector<V2>& p = c->paths[slot];
+    size_t n = p.size();
+    if (c->path_used + n > c->path_xy.n) {
+        /* the compaction uploads every slot's path, this one included */
+        return ensure_path_room(c, n);
     }
     int off = (int)c->path_used, len = (int)n;
     ecmg_status s = stage_copy(c, c->path_xy.p + off, p.data(), sizeof(V2) * n);
@@ -690,6 +825,22 @@ ecmg_status ecmg_add_agents(ecmg_ctx* c, int n, const float* pos, const float* c
     return ecmg_scene_add_agents(c, 0, n, pos, clearance, pref_speed, path_off, path_len, path_xy, out_slots);
 }
 
+/* fn(i, scratch) for i in [0, m): on the pool's threads with the built-in
+   planner, on the calling thread with a caller-supplied one */
+static void plan_jobs(ecmg_ctx* c, int m, const std::function<void(int, PlanScratch&)>& fn)
+{
+    if (c->plan_fn || m < 2) {
+        for (int i = 0; i < m; i++) fn(i, c->scratch);
+        return;
+    }
+    c->pool.start(std::min(15, (int)std::max(1u, std::thread::hardware_concurrency()) - 1));
+    if (c->pool.size() == 0) {
+        for (int i = 0; i < m; i++) fn(i, c->scratch);
+        return;
+    }
+    c->pool.run(m, [&](int i, int w) { fn(i, c->pool.scratch[w]); });
+}
+
 static ecmg_status plan(ecmg_ctx* c, SceneState* sc, V2 s, V2 g, float clr, std::vector<V2>& out, PlanScratch& scr,
                         int* astar_fail_edge = nullptr)
 {
@@ -757,6 +908,528 @@ ecmg_status ecmg_spawn_agent(ecmg_ctx* c, float sx, float sy, float gx, float gy
     int off = 0, len = (int)p.size();
     float pos[2] = {sx, sy};
     return ecmg_scene_add_agents(c, 0, 1, pos, &clearance, &pref_speed, &off, &len, xy.data(), out_slot);
+}
+
+/* ---------------------------------------------------------------------- */
+/* Spawn stage: Simulator::UpdateSpawnAreas (Simulator.cpp:494-536).
+
+   The reference walks spawn areas in ID order and, per connected goal area,
+   spawns n = (int)(timeSinceLastSpawn * rate) agents, each with up to 10
+   random locations (3 random values per location, Area.h:39-53) tested by
+   the O(N) ValidSpawnLocation; a valid location is followed by the goal's 3
+   values.  Which values a location uses depends on how many earlier
+   locations were rejected, but every location uses a whole triple of the
+   stream, and a triple is either a candidate location in one of the stage's
+   spawn areas or a goal.  So the stage tests triples t0..t0+w-1 as
+   locations in each spawn area still due (w = 11 x the agents left, at most
+   kSpawnMaxCand candidates) against the device-resident agents in one
+   launch, then replays the reference's loop on the host, where the agents
+   placed earlier in the same stage are checked directly.  A window that
+   runs out is followed by another one (another launch). */
+
+static int rq_at(ecmg_ctx* c, size_t i)
+{
+    while (c->rq.size() - c->rq_head <= i) c->rq.push_back(c->rng_fn ? c->rng_fn(c->rng_user) : std::rand());
+    return c->rq[c->rq_head + i];
+}
+
+static void rq_consume(ecmg_ctx* c, size_t n)
+{
+    c->rq_head += n;
+    if (c->rq_head > 4096 && 2 * c->rq_head > c->rq.size()) {
+        c->rq.erase(c->rq.begin(), c->rq.begin() + (std::ptrdiff_t)c->rq_head);
+        c->rq_head = 0;
+    }
+}
+
+/* Area::GetRandomPositionInArea (Area.h:39-53) from the second and third
+   value of a triple (the first feeds an unused variable), in the reference's
+   float operations: x = xMin + v1 / ((float)RAND_MAX / (xMax - xMin)) */
+static V2 area_point(float px, float py, float hw, float hh, int v1, int v2, int rand_max)
+{
+    const float xMin = px - hw, xMax = px + hw, yMin = py - hh, yMax = py + hh;
+    const float rm = (float)rand_max;
+    return mk(xMin + (float)v1 / (rm / (xMax - xMin)), yMin + (float)v2 / (rm / (yMax - yMin)));
+}
+
+/* int agentsToSpawn = time * rate (Simulator.cpp:505) as x86-64 converts:
+   truncation toward zero, INT_MIN for NaN and out-of-range values */
+static int spawn_count(float x)
+{
+    if (!(x > -2147483904.0f && x < 2147483648.0f)) return INT_MIN;
+    return (int)x;
+}
+
+struct SpawnWindow {
+    size_t t0 = 0, w = 0;                 /* triples [t0, t0 + w) */
+    std::vector<const SpawnAreaH*> areas; /* candidate block a: locations in areas[a] */
+    int find(const SpawnAreaH* a, size_t t) const
+    {
+        if (t < t0 || t >= t0 + w) return -1;
+        for (size_t i = 0; i < areas.size(); i++)
+            if (areas[i] == a) return (int)i;
+        return -1;
+    }
+};
+
+/* the window's candidates against the active agents of the scene's slots
+   (one launch, one copy back) */
+static ecmg_status spawn_check(ecmg_ctx* c, SceneState* sc, const SpawnWindow& win, ecmg_tick_stats& st)
+{
+    const auto h0 = std::chrono::steady_clock::now();
+    if (!c->h_cand) {
+        CK(cudaHostAlloc((void**)&c->h_cand, sizeof(V2) * kSpawnMaxCand, cudaHostAllocDefault));
+        CK(cudaHostAlloc((void**)&c->h_sarea, sizeof(SpawnAreaDev) * kSpawnMaxAreas, cudaHostAllocDefault));
+        CK(cudaHostAlloc((void**)&c->h_hit, sizeof(int) * kSpawnMaxCand, cudaHostAllocDefault));
+        CK(c->d_cand.alloc(kSpawnMaxCand));
+        CK(c->d_sarea.alloc(kSpawnMaxAreas));
+        CK(c->d_hit.alloc(kSpawnMaxCand));
+    }
+    const int na = (int)win.areas.size(), w = (int)win.w;
+    for (int a = 0; a < na; a++) {
+        const SpawnAreaH& A = *win.areas[a];
+        float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+        for (int q = 0; q < w; q++) {
+            const size_t t = win.t0 + (size_t)q;
+            const V2 p = area_point(A.x, A.y, A.hw, A.hh, rq_at(c, 3 * t + 1), rq_at(c, 3 * t + 2), c->rand_max);
+            c->h_cand[a * w + q] = p;
+            x0 = std::fmin(x0, p.x); y0 = std::fmin(y0, p.y);
+            x1 = std::fmax(x1, p.x); y1 = std::fmax(y1, p.y);
+        }
+        /* an agent the exact test finds is within clearance * (1 + 2^-21) of
+           a candidate on each axis; the margin covers that and the rounding
+           of the box bounds */
+        const float cl = A.cfg.clearance_min;
+        const float big = std::fmax(std::fmax(std::fabs(x0), std::fabs(x1)), std::fmax(std::fabs(y0), std::fabs(y1)));
+        const float m = std::fabs(cl) * 1.001f + 1e-3f + 1e-6f * (std::isfinite(big) ? big : 0.0f);
+        SpawnAreaDev& D = c->h_sarea[a];
+        D.x0 = x0 - m; D.y0 = y0 - m; D.x1 = x1 + m; D.y1 = y1 + m;
+        D.c2 = cl * cl;
+        D.first = a * w;
+        D.count = w;
+        D.pad = 0;
+    }
+    const size_t nc = (size_t)na * (size_t)w;
+    CK(cudaMemcpyAsync(c->d_cand.p, c->h_cand, sizeof(V2) * nc, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_sarea.p, c->h_sarea, sizeof(SpawnAreaDev) * na, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->d_hit.p, 0, sizeof(int) * nc, c->stream));
+    CK(launch_spawn_check(c->pos.p, c->d_active.p, sc->slot_base, sc->last_idx + 1, c->d_cand.p, c->d_sarea.p, na,
+                          c->d_hit.p, c->sms, c->stream));
+    CK(cudaMemcpyAsync(c->h_hit, c->d_hit.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    st.spawn_candidates += (long long)nc;
+    st.spawn_check_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - h0).count();
+    return ECMG_OK;
+}
+
+struct SpawnPair {
+    SpawnAreaH* a;
+    int ga, n;
+};
+struct SpawnPick {
+    V2 start, goal;
+    float clr, speed;
+};
+
+/* SpawnAgent (Simulator.cpp:168-200) for the agents a stage placed, in
+   order: LIFO slots, components, zero velocities and the planned paths.  The
+   device side is one copy of the new path points, one copy of per-agent
+   records and one scatter kernel, queued ahead of the tick. */
+static ecmg_status place_agents(ecmg_ctx* c, SceneState* sc, const std::vector<SpawnPick>& picks,
+                                std::vector<std::vector<V2>>& paths)
+{
+    const int n = (int)picks.size();
+    if (n == 0) return ECMG_OK;
+    size_t total = 0;
+    for (auto& p : paths) total += p.size();
+    {
+        ecmg_status rs = ensure_path_room(c, total);
+        if (rs != ECMG_OK) return rs;
+    }
+    std::vector<SpawnRec> rec((size_t)n);
+    std::vector<V2> pts;
+    pts.reserve(total);
+    for (int i = 0; i < n; i++) {
+        const SpawnPick& p = picks[i];
+        const int idx = sc->free_stack.back();
+        sc->free_stack.pop_back();
+        sc->num_agents++;
+        c->num_agents++;
+        sc->last_idx = std::max(sc->last_idx, idx);
+        c->active[idx] = 1;
+        c->clear[idx] = p.clr;
+        c->speed[idx] = p.speed;
+        c->fail_edge[idx] = -1;
+        note_range(c, sc, p.clr, p.speed);
+        rec[i] = SpawnRec{idx, p.start.x, p.start.y, p.clr, p.speed, (int)(c->path_used + pts.size()),
+                          (int)paths[i].size(), 0};
+        pts.insert(pts.end(), paths[i].begin(), paths[i].end());
+        c->paths[idx].swap(paths[i]);
+        c->spawned_slot.push_back(idx);
+        c->spawned_start.push_back(p.start);
+        c->spawned_goal.push_back(p.goal);
+    }
+    ecmg_status s = stage_copy(c, c->path_xy.p + c->path_used, pts.data(), sizeof(V2) * pts.size());
+    if (s != ECMG_OK) return s;
+    c->path_used += pts.size();
+    CK(c->d_spawn_rec.alloc((size_t)n));
+    s = stage_copy(c, c->d_spawn_rec.p, rec.data(), sizeof(SpawnRec) * rec.size());
+    if (s != ECMG_OK) return s;
+    SpawnTargets tg{c->pos.p, c->vel.p, c->pref_vel.p, c->d_clear.p, c->d_speed.p, c->d_active.p,
+                    c->path_off.p, c->path_len.p, c->d_fail_edge.p};
+    CK(launch_spawn_place(c->d_spawn_rec.p, n, tg, c->stream));
+    if (sc->grid_agents == 0 || sc->num_agents > 2 * sc->grid_agents) {
+        sc->grid_ready = false;
+        c->table_dirty = true;
+    }
+    return ECMG_OK;
+}
+
+/* One replay of the reference's loop over the stage's agents.  Agents with a
+   valid location and a free slot are placed unless the planner is known to
+   fail for their (start, goal, clearance); their paths are planned after the
+   walk (on several host threads), and a walk in which an unplanned agent then
+   turns out to have no path is replayed with that knowledge -- an agent that
+   is not placed frees its location for the ones after it. */
+struct PlanKey {
+    float sx, sy, gx, gy, c;
+    bool operator<(const PlanKey& o) const
+    {
+        return std::tie(sx, sy, gx, gy, c) < std::tie(o.sx, o.sy, o.gx, o.gy, o.c);
+    }
+};
+
+static ecmg_status spawn_walk(ecmg_ctx* c, SceneState* sc, const std::vector<SpawnPair>& pairs, long long total,
+                              const std::map<PlanKey, std::vector<V2>>& planned, std::vector<SpawnPick>& picks,
+                              size_t* triples, long long* failed, long long* refused, ecmg_tick_stats& st)
+{
+    picks.clear();
+    *failed = *refused = 0;
+    SpawnWindow win;
+    std::vector<V2> placed; /* this stage's agents: tested on the host */
+    long long left = total;
+    size_t free_left = sc->free_stack.size();
+    size_t t = 0; /* triples used so far */
+    for (size_t pi = 0; pi < pairs.size(); pi++) {
+        const SpawnPair& P = pairs[pi];
+        const SpawnAreaH& A = *P.a;
+        const float clr = A.cfg.clearance_min, speed = A.cfg.preferred_speed_min;
+        const float c2 = clr * clr;
+        for (int i = 0; i < P.n; i++, left--) {
+            bool found = false;
+            V2 start = mk(0.0f, 0.0f);
+            for (int att = 0; att < 10 && !found; att++, t++) {
+                int ai = win.find(&A, t);
+                if (ai < 0) {
+                    win.t0 = t;
+                    win.areas.assign(1, &A);
+                    for (size_t q = pi + 1; q < pairs.size() && (int)win.areas.size() < kSpawnMaxAreas; q++)
+                        if (pairs[q].n > 0 &&
+                            std::find(win.areas.begin(), win.areas.end(), pairs[q].a) == win.areas.end())
+                            win.areas.push_back(pairs[q].a);
+                    const long long cap = kSpawnMaxCand / (long long)win.areas.size();
+                    win.w = (size_t)std::max(1LL, std::min(11 * left, cap));
+                    ecmg_status cs = spawn_check(c, sc, win, st);
+                    if (cs != ECMG_OK) return cs;
+                    ai = 0;
+                }
+                const size_t j = (size_t)ai * win.w + (t - win.t0);
+                start = c->h_cand[j];
+                bool occupied = c->h_hit[j] != 0;
+                for (size_t q = 0; q < placed.size() && !occupied; q++) {
+                    const float dx = start.x - placed[q].x, dy = start.y - placed[q].y;
+                    occupied = dx * dx + dy * dy < c2;
+                }
+                found = !occupied;
+            }
+            if (!found) { /* "Could not find a valid spawn position" */
+                (*failed)++;
+                continue;
+            }
+            /* the goal's triple; a goal area that no longer exists gives (0, 0)
+               (the reference would default-construct one) */
+            const int v1 = rq_at(c, 3 * t + 1), v2 = rq_at(c, 3 * t + 2);
+            t++;
+            auto git = sc->goal_areas.find(A.goals[P.ga]);
+            const V2 goal = git != sc->goal_areas.end()
+                                ? area_point(git->second.x, git->second.y, git->second.hw, git->second.hh, v1, v2,
+                                             c->rand_max)
+                                : mk(0.0f, 0.0f);
+            if (free_left == 0) { /* SpawnAgent returns -1 (Simulator.cpp:170) */
+                (*refused)++;
+                continue;
+            }
+            auto it = planned.find(PlanKey{start.x, start.y, goal.x, goal.y, clr});
+            if (it != planned.end() && it->second.empty()) { /* no path */
+                (*refused)++;
+                continue;
+            }
+            free_left--;
+            placed.push_back(start);
+            picks.push_back({start, goal, clr, speed});
+        }
+    }
+    *triples = t;
+    return ECMG_OK;
+}
+
+static ecmg_status spawn_stage(ecmg_ctx* c, ecmg_tick_stats& st)
+{
+    c->spawned_slot.clear();
+    c->spawned_start.clear();
+    c->spawned_goal.clear();
+    for (auto& scp : c->scenes) {
+        SceneState* sc = scp.get();
+        if (sc->spawn_areas.empty()) continue;
+        std::vector<SpawnPair> pairs;
+        long long total = 0;
+        for (auto& kv : sc->spawn_areas) {
+            SpawnAreaH& A = kv.second;
+            for (int ga = 0; ga < (int)A.goals.size(); ga++) {
+                A.since[ga] += c->prm.dt;
+                const int n = spawn_count(A.since[ga] * A.rate[ga]);
+                pairs.push_back({&A, ga, n});
+                if (n > 0) total += n;
+            }
+        }
+        std::map<PlanKey, std::vector<V2>> planned; /* empty path: the planner failed */
+        std::vector<SpawnPick> picks;
+        size_t triples = 0;
+        long long failed = 0, refused = 0;
+        for (;;) {
+            ecmg_status ws = spawn_walk(c, sc, pairs, total, planned, picks, &triples, &failed, &refused, st);
+            if (ws != ECMG_OK) return ws;
+            std::vector<int> todo;
+            for (int i = 0; i < (int)picks.size(); i++)
+                if (!planned.count(PlanKey{picks[i].start.x, picks[i].start.y, picks[i].goal.x, picks[i].goal.y,
+                                           picks[i].clr}))
+                    todo.push_back(i);
+            if (todo.empty()) break;
+            /* SpawnAgent's UpdatePath (Simulator.cpp:190); the built-in planner
+               is re-entrant, a caller-supplied one runs on this thread */
+            const int m = (int)todo.size();
+            std::vector<std::vector<V2>> res(m);
+            plan_jobs(c, m, [&](int q, PlanScratch& scr) {
+                const SpawnPick& p = picks[todo[q]];
+                if (plan(c, sc, p.start, p.goal, p.clr, res[q], scr) != ECMG_OK) res[q].clear();
+            });
+            bool replay = false;
+            for (int q = 0; q < m; q++) {
+                const SpawnPick& p = picks[todo[q]];
+                if (res[q].empty()) replay = true;
+                planned[PlanKey{p.start.x, p.start.y, p.goal.x, p.goal.y, p.clr}] = std::move(res[q]);
+            }
+            if (!replay) break;
+        }
+        std::vector<std::vector<V2>> paths(picks.size());
+        for (size_t i = 0; i < picks.size(); i++) {
+            const SpawnPick& p = picks[i];
+            paths[i] = planned[PlanKey{p.start.x, p.start.y, p.goal.x, p.goal.y, p.clr}];
+        }
+        ecmg_status ps = place_agents(c, sc, picks, paths);
+        if (ps != ECMG_OK) return ps;
+        st.spawned += (long long)picks.size();
+        st.spawn_failed += failed;
+        st.spawn_refused += refused;
+        for (const SpawnPair& P : pairs) P.a->since[P.ga] -= (float)P.n / P.a->rate[P.ga];
+        rq_consume(c, 3 * triples);
+    }
+    return ECMG_OK;
+}
+
+/* an area whose corners and extent are finite floats (its random locations
+   are then finite too) */
+static bool area_ok(float x, float y, float hw, float hh)
+{
+    const float x0 = x - hw, x1 = x + hw, y0 = y - hh, y1 = y + hh;
+    return finite2(x, y) && finite2(hw, hh) && finite2(x0, x1) && finite2(y0, y1) && std::isfinite(x1 - x0) &&
+           std::isfinite(y1 - y0);
+}
+
+ecmg_status ecmg_add_spawn_area(ecmg_ctx* c, float x, float y, float half_w, float half_h,
+                                const ecmg_spawn_config* config, int id, int* out_id)
+{
+    if (!c || !out_id) return ECMG_ERR_INVALID_ARG;
+    if (!area_ok(x, y, half_w, half_h)) return fail(c, ECMG_ERR_INVALID_ARG, "non-finite area");
+    if (config && !(finite2(config->preferred_speed_min, config->preferred_speed_max) &&
+                    finite2(config->clearance_min, config->clearance_max)))
+        return fail(c, ECMG_ERR_INVALID_ARG, "non-finite spawn configuration");
+    SceneState* sc = c->scenes[0].get();
+    SpawnAreaH a;
+    a.id = id == -1 ? sc->next_spawn_id++ : id;
+    a.x = x; a.y = y; a.hw = half_w; a.hh = half_h;
+    if (config) a.cfg = *config;
+    sc->spawn_areas.emplace(a.id, a);
+    *out_id = a.id;
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_add_goal_area(ecmg_ctx* c, float x, float y, float half_w, float half_h, int id, int* out_id)
+{
+    if (!c || !out_id) return ECMG_ERR_INVALID_ARG;
+    if (!area_ok(x, y, half_w, half_h)) return fail(c, ECMG_ERR_INVALID_ARG, "non-finite area");
+    SceneState* sc = c->scenes[0].get();
+    GoalAreaH g;
+    g.id = id == -1 ? sc->next_goal_id++ : id;
+    g.x = x; g.y = y; g.hw = half_w; g.hh = half_h;
+    sc->goal_areas.emplace(g.id, g);
+    *out_id = g.id;
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_remove_area(ecmg_ctx* c, int type, int id)
+{
+    if (!c) return ECMG_ERR_INVALID_ARG;
+    SceneState* sc = c->scenes[0].get();
+    if (type == ECMG_AREA_SPAWN) sc->spawn_areas.erase(id);
+    if (type == ECMG_AREA_GOAL) sc->goal_areas.erase(id);
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_connect_areas(ecmg_ctx* c, int spawn_id, int goal_id, float spawn_rate)
+{
+    if (!c) return ECMG_ERR_INVALID_ARG;
+    if (!std::isfinite(spawn_rate)) return fail(c, ECMG_ERR_INVALID_ARG, "non-finite spawn rate");
+    SceneState* sc = c->scenes[0].get();
+    auto it = sc->spawn_areas.find(spawn_id);
+    if (it == sc->spawn_areas.end()) return fail(c, ECMG_ERR_INVALID_ARG, "no spawn area %d", spawn_id);
+    SpawnAreaH& a = it->second;
+    for (int g : a.goals)
+        if (g == goal_id) return ECMG_OK;
+    a.goals.push_back(goal_id);
+    a.since.push_back(0.0f);
+    a.rate.push_back(spawn_rate);
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_disconnect_areas(ecmg_ctx* c, int spawn_id, int goal_id)
+{
+    if (!c) return ECMG_ERR_INVALID_ARG;
+    SceneState* sc = c->scenes[0].get();
+    if (spawn_id < 0 || spawn_id >= (int)sc->spawn_areas.size()) return ECMG_OK;
+    auto it = sc->spawn_areas.find(spawn_id);
+    if (it == sc->spawn_areas.end()) return ECMG_OK;
+    std::vector<int>& g = it->second.goals;
+    auto q = std::find(g.begin(), g.end(), goal_id);
+    if (q != g.end()) g.erase(q); /* rates and timers keep their entries */
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_set_area(ecmg_ctx* c, int type, int id, float x, float y, float half_w, float half_h)
+{
+    if (!c) return ECMG_ERR_INVALID_ARG;
+    if (!area_ok(x, y, half_w, half_h)) return fail(c, ECMG_ERR_INVALID_ARG, "non-finite area");
+    SceneState* sc = c->scenes[0].get();
+    if (type == ECMG_AREA_SPAWN) {
+        auto it = sc->spawn_areas.find(id);
+        if (it == sc->spawn_areas.end()) return fail(c, ECMG_ERR_INVALID_ARG, "no spawn area %d", id);
+        it->second.x = x; it->second.y = y; it->second.hw = half_w; it->second.hh = half_h;
+        return ECMG_OK;
+    }
+    if (type == ECMG_AREA_GOAL) {
+        auto it = sc->goal_areas.find(id);
+        if (it == sc->goal_areas.end()) return fail(c, ECMG_ERR_INVALID_ARG, "no goal area %d", id);
+        it->second.x = x; it->second.y = y; it->second.hw = half_w; it->second.hh = half_h;
+        return ECMG_OK;
+    }
+    return fail(c, ECMG_ERR_INVALID_ARG, "area type %d", type);
+}
+
+ecmg_status ecmg_get_area(ecmg_ctx* c, int type, int id, ecmg_area_info* out, int* goal_ids, float* rates,
+                          float* since_last_spawn, int cap)
+{
+    if (!c || !out) return ECMG_ERR_INVALID_ARG;
+    SceneState* sc = c->scenes[0].get();
+    std::memset(out, 0, sizeof(*out));
+    if (type == ECMG_AREA_SPAWN) {
+        auto it = sc->spawn_areas.find(id);
+        if (it == sc->spawn_areas.end()) return fail(c, ECMG_ERR_INVALID_ARG, "no spawn area %d", id);
+        const SpawnAreaH& a = it->second;
+        out->id = a.id; out->x = a.x; out->y = a.y; out->half_w = a.hw; out->half_h = a.hh;
+        out->config = a.cfg;
+        out->n_connected = (int)a.goals.size();
+        out->n_timers = (int)a.rate.size();
+        for (int i = 0; i < cap && i < (int)a.goals.size(); i++)
+            if (goal_ids) goal_ids[i] = a.goals[i];
+        for (int i = 0; i < cap && i < (int)a.rate.size(); i++) {
+            if (rates) rates[i] = a.rate[i];
+            if (since_last_spawn) since_last_spawn[i] = a.since[i];
+        }
+        return ECMG_OK;
+    }
+    if (type == ECMG_AREA_GOAL) {
+        auto it = sc->goal_areas.find(id);
+        if (it == sc->goal_areas.end()) return fail(c, ECMG_ERR_INVALID_ARG, "no goal area %d", id);
+        const GoalAreaH& g = it->second;
+        out->id = g.id; out->x = g.x; out->y = g.y; out->half_w = g.hw; out->half_h = g.hh;
+        return ECMG_OK;
+    }
+    return fail(c, ECMG_ERR_INVALID_ARG, "area type %d", type);
+}
+
+ecmg_status ecmg_area_ids(ecmg_ctx* c, int type, int* ids, int cap, int* n)
+{
+    if (!c || !n || (cap > 0 && !ids)) return ECMG_ERR_INVALID_ARG;
+    SceneState* sc = c->scenes[0].get();
+    int k = 0;
+    if (type == ECMG_AREA_SPAWN)
+        for (auto& kv : sc->spawn_areas) { if (k < cap) ids[k] = kv.first; k++; }
+    else if (type == ECMG_AREA_GOAL)
+        for (auto& kv : sc->goal_areas) { if (k < cap) ids[k] = kv.first; k++; }
+    else
+        return fail(c, ECMG_ERR_INVALID_ARG, "area type %d", type);
+    *n = k;
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_set_spawn_rng(ecmg_ctx* c, ecmg_rand_fn fn, void* user, int rand_max)
+{
+    if (!c || (fn && rand_max < 1)) return ECMG_ERR_INVALID_ARG;
+    c->rng_fn = fn;
+    c->rng_user = user;
+    c->rand_max = fn ? rand_max : RAND_MAX;
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_push_spawn_random(ecmg_ctx* c, const int* values, int n)
+{
+    if (!c || n < 0 || (n > 0 && !values)) return ECMG_ERR_INVALID_ARG;
+    c->rq.insert(c->rq.end(), values, values + n);
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_spawn_random_pending(const ecmg_ctx* c, long long* n)
+{
+    if (!c || !n) return ECMG_ERR_INVALID_ARG;
+    *n = (long long)(c->rq.size() - c->rq_head);
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_update_spawn_areas(ecmg_ctx* c, ecmg_tick_stats* stats)
+{
+    if (!c) return ECMG_ERR_INVALID_ARG;
+    ecmg_tick_stats st{};
+    auto h0 = std::chrono::steady_clock::now();
+    CK(cudaStreamSynchronize(c->stream));
+    ecmg_status s = spawn_stage(c, st);
+    st.spawn_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - h0).count();
+    st.active_agents = c->num_agents;
+    st.last_index = c->global_last();
+    if (stats) *stats = st;
+    return s;
+}
+
+ecmg_status ecmg_get_spawned(const ecmg_ctx* c, int* slots, float* start_xy, float* goal_xy, int cap, int* n)
+{
+    if (!c || !n || cap < 0) return ECMG_ERR_INVALID_ARG;
+    const int m = (int)c->spawned_slot.size();
+    for (int i = 0; i < m && i < cap; i++) {
+        if (slots) slots[i] = c->spawned_slot[i];
+        if (start_xy) { start_xy[2 * i] = c->spawned_start[i].x; start_xy[2 * i + 1] = c->spawned_start[i].y; }
+        if (goal_xy) { goal_xy[2 * i] = c->spawned_goal[i].x; goal_xy[2 * i + 1] = c->spawned_goal[i].y; }
+    }
+    *n = m;
+    return ECMG_OK;
 }
 
 ecmg_status ecmg_destroy_agent(ecmg_ctx* c, int slot)
@@ -1085,6 +1758,12 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             while (sc->last_idx >= sc->slot_base && !c->active[sc->last_idx]) sc->last_idx--;
         }
         st.ticks++;
+        if (c->spawn_enabled) { /* UpdateSpawnAreas (Simulator.cpp:317) */
+            auto s0 = std::chrono::steady_clock::now();
+            ecmg_status ss = spawn_stage(c, st);
+            if (ss != ECMG_OK) return ss;
+            st.spawn_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - s0).count();
+        }
         int last = c->global_last();
         if (last < 0) continue;
         ecmg_status gs = ensure_grids(c);
@@ -1168,25 +1847,12 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             std::vector<std::vector<V2>> res(m);
             std::vector<char> ok(m, 0);
             std::vector<int> fe(m, -1);
-            auto serve = [&](int t, int nt) {
-                PlanScratch scr;
-                for (int i = t; i < m; i += nt) {
-                    int q = order[i], sl = r[q];
-                    SceneState* sc = c->scenes[c->slot_scene[sl]].get();
-                    V2 goal = c->paths[sl].back();
-                    ok[i] = plan(c, sc, rp[q], goal, c->clear[sl], res[i], scr, &fe[i]) == ECMG_OK && !res[i].empty();
-                }
-            };
-            int nt = c->plan_fn ? 1 : std::min(16, m);
-            nt = std::min<int>(nt, (int)std::max(1u, std::thread::hardware_concurrency()));
-            if (nt > 1) {
-                std::vector<std::thread> th;
-                for (int t = 1; t < nt; t++) th.emplace_back(serve, t, nt);
-                serve(0, nt);
-                for (auto& x : th) x.join();
-            } else {
-                serve(0, 1);
-            }
+            plan_jobs(c, m, [&](int i, PlanScratch& scr) {
+                int q = order[i], sl = r[q];
+                SceneState* sc = c->scenes[c->slot_scene[sl]].get();
+                V2 goal = c->paths[sl].back();
+                ok[i] = plan(c, sc, rp[q], goal, c->clear[sl], res[i], scr, &fe[i]) == ECMG_OK && !res[i].empty();
+            });
             for (int i = 0; i < m; i++) {
                 int sl = r[order[i]];
                 if (ok[i]) {
@@ -1297,6 +1963,7 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
     float best = 1e30f;
     int trials = 0;
     c->replan_enabled = false;
+    c->spawn_enabled = false;
     auto trial = [&](const Launch& L, bool* better) -> ecmg_status {
         if (L.scale != c->cell_scale) {
             c->cell_scale = L.scale;
@@ -1355,12 +2022,14 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
     }
     if (st != ECMG_OK) {
         c->replan_enabled = true;
+        c->spawn_enabled = true;
         return st;
     }
     int bb = bestL.block, bt = bestL.tile, bmode = bestL.mode, bw = bestL.wgrab;
     float bs = bestL.scale;
     c->occ_div = bestL.occ_div;
     c->replan_enabled = true;
+    c->spawn_enabled = true;
     c->block = bb;
     c->tile = bt;
     c->lp_mode = bmode;

@@ -163,5 +163,37 @@ cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k,
                        int* scan_tmp, int scan_blocks, int* out_ids, int* out_cnt, cudaStream_t s);
 int scan_tmp_ints(int n);
 
+/* spawn.cu: Simulator::ValidSpawnLocation (Simulator.cpp:295-311) for a batch
+   of candidate locations.  Candidates of one spawn area share a clearance;
+   an agent is tested against an area's candidates only when it lies in the
+   area's box (the candidates' bounding box grown by more than the
+   clearance, so no agent the exact test would find is skipped). */
+constexpr int kSpawnMaxAreas = 64;
+constexpr int kSpawnMaxCand = 4096;
+struct SpawnAreaDev {
+    float x0, y0, x1, y1; /* box of the candidates, grown */
+    float c2;             /* clearance * clearance */
+    int first, count, pad;
+};
+/* hit[j] = 1 when an active agent in slots [b, e) is closer than the area's
+   clearance to candidate j (hit must be zeroed by the caller) */
+cudaError_t launch_spawn_check(const V2* pos, const unsigned char* active, int b, int e, const V2* cand,
+                               const SpawnAreaDev* areas, int n_areas, int* hit, int sms, cudaStream_t s);
+/* one spawned agent: its slot, start, clearance, preferred speed and path */
+struct SpawnRec {
+    int slot;
+    float x, y, clr, speed;
+    int path_off, path_len, pad;
+};
+struct SpawnTargets {
+    V2 *pos, *vel, *pref_vel;
+    float *clear, *speed;
+    unsigned char* active;
+    int *path_off, *path_len, *fail_edge;
+};
+/* writes the records into the agent arrays (velocities zeroed, active set,
+   failed-search edge cleared) */
+cudaError_t launch_spawn_place(const SpawnRec* rec, int n, const SpawnTargets& t, cudaStream_t s);
+
 }  // namespace ecmg
 #endif

@@ -181,6 +181,92 @@ class Simulator:
     def destroy_agent(self, idx: int):
         self._ck(self.L.ecmg_destroy_agent(self.h, int(idx)))
 
+    # ---- spawn and goal areas (Simulator.h:92-104) ----------------------
+    def add_spawn_area(self, position, half_size, config: dict | None = None, ID: int = -1) -> int:
+        """Simulator::AddSpawnArea (Simulator.cpp:336-360); config keys as
+        SpawnConfiguration (Area.h:82-88), reference defaults 5 / 10 / 5 / 10."""
+        cfg = _lib.SpawnConfig(5.0, 10.0, 5.0, 10.0)
+        for k, v in (config or {}).items():
+            setattr(cfg, k, float(v))
+        out = C.c_int()
+        self._ck(self.L.ecmg_add_spawn_area(self.h, float(position[0]), float(position[1]), float(half_size[0]),
+                                            float(half_size[1]), C.byref(cfg), int(ID), C.byref(out)))
+        return out.value
+
+    def add_goal_area(self, position, half_size, ID: int = -1) -> int:
+        """Simulator::AddGoalArea (Simulator.cpp:362-381)"""
+        out = C.c_int()
+        self._ck(self.L.ecmg_add_goal_area(self.h, float(position[0]), float(position[1]), float(half_size[0]),
+                                           float(half_size[1]), int(ID), C.byref(out)))
+        return out.value
+
+    def remove_area(self, area_type: int, ID: int):
+        """Simulator::RemoveArea; area_type 2 = SPAWN, 3 = GOAL (Area.h:11-18)"""
+        self._ck(self.L.ecmg_remove_area(self.h, int(area_type), int(ID)))
+
+    def connect_spawn_goal_areas(self, spawn_id: int, goal_id: int, spawn_rate: float = 0.0):
+        self._ck(self.L.ecmg_connect_areas(self.h, int(spawn_id), int(goal_id), float(spawn_rate)))
+
+    def deconnect_spawn_goal_areas(self, spawn_id: int, goal_id: int):
+        self._ck(self.L.ecmg_disconnect_areas(self.h, int(spawn_id), int(goal_id)))
+
+    def set_area(self, area_type: int, ID: int, position, half_size):
+        self._ck(self.L.ecmg_set_area(self.h, int(area_type), int(ID), float(position[0]), float(position[1]),
+                                      float(half_size[0]), float(half_size[1])))
+
+    def get_area(self, area_type: int, ID: int) -> dict:
+        info = _lib.AreaInfo()
+        cap = 256
+        g, r, t = np.zeros(cap, I32), np.zeros(cap, F32), np.zeros(cap, F32)
+        self._ck(self.L.ecmg_get_area(self.h, int(area_type), int(ID), C.byref(info), _ptr(g), _ptr(r), _ptr(t), cap))
+        c = info.config
+        return dict(id=info.id, position=(info.x, info.y), half_size=(info.half_w, info.half_h),
+                    config=dict(preferred_speed_min=c.preferred_speed_min, preferred_speed_max=c.preferred_speed_max,
+                                clearance_min=c.clearance_min, clearance_max=c.clearance_max),
+                    connected=g[:min(cap, info.n_connected)].tolist(), spawn_rate=r[:min(cap, info.n_timers)].tolist(),
+                    time_since_last_spawn=t[:min(cap, info.n_timers)].tolist())
+
+    def area_ids(self, area_type: int) -> list:
+        n = C.c_int()
+        self._ck(self.L.ecmg_area_ids(self.h, int(area_type), None, 0, C.byref(n)))
+        ids = np.zeros(max(1, n.value), I32)
+        self._ck(self.L.ecmg_area_ids(self.h, int(area_type), _ptr(ids), n.value, C.byref(n)))
+        return ids[:n.value].tolist()
+
+    def set_spawn_rng(self, fn=None, rand_max: int = 2147483647):
+        """fn() -> int in [0, rand_max] replaces the C library's rand();
+        None restores it"""
+        if fn is None:
+            self._rand_cb = None
+            self._ck(self.L.ecmg_set_spawn_rng(self.h, _lib.RAND_FN(), None, 0))
+            return
+        self._rand_cb = _lib.RAND_FN(lambda user: int(fn()))
+        self._ck(self.L.ecmg_set_spawn_rng(self.h, self._rand_cb, None, int(rand_max)))
+
+    def push_spawn_random(self, values):
+        v = _a(values, I32)
+        self._ck(self.L.ecmg_push_spawn_random(self.h, _ptr(v), int(v.size)))
+
+    def spawn_random_pending(self) -> int:
+        n = C.c_longlong()
+        self._ck(self.L.ecmg_spawn_random_pending(self.h, C.byref(n)))
+        return n.value
+
+    def update_spawn_areas(self) -> _lib.TickStats:
+        """Simulator::UpdateSpawnAreas alone (Simulator.cpp:494-536)"""
+        st = _lib.TickStats()
+        self._ck(self.L.ecmg_update_spawn_areas(self.h, C.byref(st)))
+        return st
+
+    def get_spawned(self):
+        """(slots, start [n,2], goal [n,2]) of the last spawn stage"""
+        n = C.c_int()
+        self._ck(self.L.ecmg_get_spawned(self.h, None, None, None, 0, C.byref(n)))
+        m = n.value
+        sl, a, b = np.zeros(max(1, m), I32), np.zeros((max(1, m), 2), F32), np.zeros((max(1, m), 2), F32)
+        self._ck(self.L.ecmg_get_spawned(self.h, _ptr(sl), _ptr(a), _ptr(b), m, C.byref(n)))
+        return sl[:m], a[:m], b[:m]
+
     def update(self, dt: float | None = None, ticks: int = 1) -> _lib.TickStats:
         """Simulator::Update; like the reference, dt is ignored and the step
         time given at construction is used (Simulator.cpp:313-323)."""

@@ -66,3 +66,39 @@ def make_simulator(name, seed, **kw):
     sim = Simulator(scene, n, DT, max_neighbors=k, **ORCA, **kw)
     sim.add_agents(st.pos[:n], st.clear[:n], st.pref_speed[:n], paths)
     return sim, (cfg, scene, st, paths, k)
+
+
+def add_spawn_areas(sim, scene, rate, n_areas=4, half=2.5, clearance=0.3, speed=1.3, seed=0):
+    """Spawn areas for a workload (Simulator::AddSpawnArea / AddGoalArea /
+    ConnectSpawnGoalAreas): n_areas squares of half size `half` at
+    obstacle-free spots of the scene's middle half, each feeding, at `rate`
+    agents per second, a goal area at the free spot nearest to its mirror
+    image through the scene centre.  Returns the spawn area IDs."""
+    rng = np.random.default_rng(seed)
+    b = np.asarray(scene.boxes, np.float64).reshape(-1, 4)
+    W, H = scene.width, scene.height
+
+    def free(x, y):
+        m = half + 1.0
+        return not (b.size and np.any((np.abs(b[:, 0] - x) < b[:, 2] + m) & (np.abs(b[:, 1] - y) < b[:, 3] + m)))
+
+    def spot_near(x, y):
+        for r in np.linspace(0.0, min(W, H) / 4, 200):
+            for _ in range(8):
+                a = rng.uniform(0, 2 * np.pi)
+                px, py = x + r * np.cos(a), y + r * np.sin(a)
+                if half < px < W - half and half < py < H - half and free(px, py):
+                    return float(px), float(py)
+        raise RuntimeError("no obstacle-free spot for a spawn area")
+
+    ids = []
+    cfg = dict(clearance_min=clearance, preferred_speed_min=speed, clearance_max=clearance, preferred_speed_max=speed)
+    for i in range(n_areas):
+        a = 2 * np.pi * (i + 0.5) / n_areas
+        sx, sy = spot_near(W / 2 + W / 4 * np.cos(a), H / 2 + H / 4 * np.sin(a))
+        gx, gy = spot_near(W - sx, H - sy)
+        s = sim.add_spawn_area((sx, sy), (half, half), cfg)
+        g = sim.add_goal_area((gx, gy), (half, half))
+        sim.connect_spawn_goal_areas(s, g, float(rate))
+        ids.append(s)
+    return ids

@@ -80,6 +80,12 @@ typedef struct {
     float neighbors_ms;    /* neighbour (kNN) kernel, which runs beside it          */
     float proposal_ms;     /* learned mode: feature and inference kernels          */
     float orca_ms;         /* device time of the per-agent ORCA kernel             */
+    long long spawned;       /* agents placed by the spawn areas                   */
+    long long spawn_failed;  /* no valid location in 10 attempts (Simulator.cpp:526-530) */
+    long long spawn_refused; /* valid location, but no free slot or no path        */
+    float spawn_ms;          /* host time of the spawn stage, device check included */
+    float spawn_check_ms;    /* of which the location tests on the device (copies and wait included) */
+    long long spawn_candidates; /* candidate locations tested on the device      */
 } ecmg_tick_stats;
 
 /* Static obstacles: n_obstacles rings, ring r = xy[2*ring_offsets[r] ..
@@ -173,6 +179,77 @@ ecmg_status ecmg_planner_find_paths(ecmg_planner* p, int n, const float* starts,
                                     float* out_xy, int* out_n);
 /* ECMGraph::FindCell for n points: cell index (2*edge + side) or -1 */
 ecmg_status ecmg_planner_locate(ecmg_planner* p, int n, const float* xy, int* out_cell);
+
+/* ---- spawn and goal areas (Simulator.h:92-104, Area.h) ---------------------
+   Every tick starts with the reference's UpdateSpawnAreas
+   (Simulator.cpp:494-536): per spawn area in ID order and per connected goal
+   area, timeSinceLastSpawn += dt, n = (int)(time * rate) agents are spawned
+   with up to 10 random locations each, then time -= n / rate.  A location is
+   valid when no active agent is closer than the area's clearanceMin
+   (ValidSpawnLocation, Simulator.cpp:295-311); the library tests the
+   candidate locations of a tick against the device-resident agents in one
+   batched kernel and the agents placed earlier in the same stage on the
+   host.  Spawned agents get clearanceMin / preferredSpeedMin as in the
+   reference and a path from the context's planner; a spawn with no free slot
+   or no path is refused (the reference would keep an agent with an empty
+   path) -- its random numbers are consumed all the same.
+   Random numbers: Area::GetRandomPositionInArea (Area.h:39-53) draws three
+   values per location, x = xMin + v1 / ((float)RAND_MAX / (xMax - xMin)),
+   likewise y with v2 (v0 is unused).  Values come first from the queue
+   filled by ecmg_push_spawn_random, then from the source set by
+   ecmg_set_spawn_rng (default: the C library's rand() with RAND_MAX).  The
+   library draws up to 33 values per agent due in a tick ahead of use; values
+   a tick does not use stay queued for the next one, so the values consumed
+   are those the reference's sequence of rand() calls would see. */
+#define ECMG_AREA_SPAWN 2 /* SimAreaType::SPAWN (Area.h:11-18) */
+#define ECMG_AREA_GOAL 3  /* SimAreaType::GOAL                 */
+/* SpawnConfiguration (Area.h:82-88); the reference's defaults are 5/10/5/10 */
+typedef struct {
+    float preferred_speed_min, preferred_speed_max;
+    float clearance_min, clearance_max;
+} ecmg_spawn_config;
+typedef struct {
+    int id;
+    float x, y;              /* Area::Position                              */
+    float half_w, half_h;    /* Area::HalfWidth, Area::HalfHeight           */
+    ecmg_spawn_config config; /* spawn areas                                */
+    int n_connected;         /* spawn areas: connectedGoalAreas.size()      */
+    int n_timers;            /* spawn areas: spawnRate.size() (see disconnect) */
+} ecmg_area_info;
+typedef int (*ecmg_rand_fn)(void* user);
+/* AddSpawnArea / AddGoalArea (Simulator.cpp:336-381): id -1 takes the
+   counter's next value; *out_id = the area's ID.  An ID already present
+   keeps its area (std::map::emplace does not replace). */
+ecmg_status ecmg_add_spawn_area(ecmg_ctx* ctx, float x, float y, float half_w, float half_h,
+                                const ecmg_spawn_config* config, int id, int* out_id);
+ecmg_status ecmg_add_goal_area(ecmg_ctx* ctx, float x, float y, float half_w, float half_h, int id, int* out_id);
+/* RemoveArea (Simulator.cpp:414-424); connections to a removed goal area stay */
+ecmg_status ecmg_remove_area(ecmg_ctx* ctx, int type, int id);
+/* ConnectSpawnGoalAreas (Simulator.cpp:426-438): no-op if already connected */
+ecmg_status ecmg_connect_areas(ecmg_ctx* ctx, int spawn_id, int goal_id, float spawn_rate);
+/* DeconnectSpawnGoalAreas (Simulator.cpp:440-457), as the reference: the goal
+   leaves connectedGoalAreas while spawnRate / timeSinceLastSpawn keep their
+   entries, so later goals are paired with the rates of earlier positions;
+   ignored when spawn_id is not below the number of spawn areas */
+ecmg_status ecmg_disconnect_areas(ecmg_ctx* ctx, int spawn_id, int goal_id);
+/* Area::Translate / Area::Scale as absolute values */
+ecmg_status ecmg_set_area(ecmg_ctx* ctx, int type, int id, float x, float y, float half_w, float half_h);
+/* GetSpawnArea / GetGoalArea (Simulator.cpp:459-479); for spawn areas the
+   connected goal IDs, rates and timers (up to cap entries each, any NULL) */
+ecmg_status ecmg_get_area(ecmg_ctx* ctx, int type, int id, ecmg_area_info* out, int* goal_ids, float* rates,
+                          float* since_last_spawn, int cap);
+/* IDs of the spawn or goal areas in ascending order (GetSpawnAreas / GetGoalAreas) */
+ecmg_status ecmg_area_ids(ecmg_ctx* ctx, int type, int* ids, int cap, int* n);
+/* source of random values in [0, rand_max]; fn NULL: rand() / RAND_MAX */
+ecmg_status ecmg_set_spawn_rng(ecmg_ctx* ctx, ecmg_rand_fn fn, void* user, int rand_max);
+/* appends recorded values to the queue consumed before the source */
+ecmg_status ecmg_push_spawn_random(ecmg_ctx* ctx, const int* values, int n);
+/* values queued and not yet consumed */
+ecmg_status ecmg_spawn_random_pending(const ecmg_ctx* ctx, long long* n);
+/* UpdateSpawnAreas alone (the stage every ecmg_tick starts with) */
+ecmg_status ecmg_update_spawn_areas(ecmg_ctx* ctx, ecmg_tick_stats* stats);
+/* agents placed by the last spawn stage: slot, start and goal (float[2] each) */
+ecmg_status ecmg_get_spawned(const ecmg_ctx* ctx, int* slots, float* start_xy, float* goal_xy, int cap, int* n);
 
 /* n_ticks x Simulator::Update (Simulator.cpp:314-323).  Re-planning requests
    raised by a tick are served on the host before the next tick starts. */

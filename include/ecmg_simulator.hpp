@@ -27,6 +27,17 @@ namespace ecmg {
 struct Point {
     float x = 0, y = 0;
 };
+struct Vec2 {
+    float x = 0, y = 0;
+};
+/* Area.h:11-18, 82-88 */
+enum SimAreaType { NONE, WALKABLE, SPAWN, GOAL, OBSTACLE };
+struct SpawnConfiguration {
+    float preferredSpeedMin = 5.0f;
+    float preferredSpeedMax = 10.0f;
+    float clearanceMin = 5.0f;
+    float clearanceMax = 10.0f;
+};
 /* component layouts of Simulator.h:29-49 */
 struct PositionComponent {
     float x, y;
@@ -92,6 +103,62 @@ public:
         m_Dirty = 0x7fu;
     }
     void SetPlanner(ecmg_plan_fn fn, void* user) { check(ecmg_set_planner(m_Ctx, fn, user), "ecmg_set_planner"); }
+
+    /* spawn / goal areas (Simulator.h:92-104); Update() runs their spawn stage */
+    int AddSpawnArea(const Point& position, const Vec2& halfSize, const SpawnConfiguration& config, int ID = -1)
+    {
+        ecmg_spawn_config c{config.preferredSpeedMin, config.preferredSpeedMax, config.clearanceMin,
+                            config.clearanceMax};
+        int id = -1;
+        check(ecmg_add_spawn_area(m_Ctx, position.x, position.y, halfSize.x, halfSize.y, &c, ID, &id),
+              "ecmg_add_spawn_area");
+        return id;
+    }
+    int AddGoalArea(const Point& position, const Vec2& halfSize, int ID = -1)
+    {
+        int id = -1;
+        check(ecmg_add_goal_area(m_Ctx, position.x, position.y, halfSize.x, halfSize.y, ID, &id), "ecmg_add_goal_area");
+        return id;
+    }
+    void RemoveArea(SimAreaType areaType, int ID) { check(ecmg_remove_area(m_Ctx, (int)areaType, ID), "ecmg_remove_area"); }
+    void ConnectSpawnGoalAreas(int spawnID, int goalID, float spawnRate = 0.0f)
+    {
+        check(ecmg_connect_areas(m_Ctx, spawnID, goalID, spawnRate), "ecmg_connect_areas");
+    }
+    void DeconnectSpawnGoalAreas(int spawnID, int goalID)
+    {
+        check(ecmg_disconnect_areas(m_Ctx, spawnID, goalID), "ecmg_disconnect_areas");
+    }
+    /* SPAWN: the goal areas a spawn area feeds; GOAL: the spawn areas that
+       feed a goal area (Simulator.cpp:126-166 intends this; its GOAL branch
+       compares goal IDs by list position) */
+    std::vector<int> GetConnectedAreas(int sourceID, SimAreaType type) const
+    {
+        std::vector<int> out;
+        ecmg_area_info info;
+        if (type == SPAWN) {
+            if (ecmg_get_area(m_Ctx, ECMG_AREA_SPAWN, sourceID, &info, nullptr, nullptr, nullptr, 0) != ECMG_OK)
+                return out;
+            out.resize(info.n_connected);
+            ecmg_get_area(m_Ctx, ECMG_AREA_SPAWN, sourceID, &info, out.data(), nullptr, nullptr, info.n_connected);
+            return out;
+        }
+        if (type == GOAL) {
+            if (ecmg_get_area(m_Ctx, ECMG_AREA_GOAL, sourceID, &info, nullptr, nullptr, nullptr, 0) != ECMG_OK)
+                return out;
+            int n = 0;
+            ecmg_area_ids(m_Ctx, ECMG_AREA_SPAWN, nullptr, 0, &n);
+            std::vector<int> ids(n);
+            ecmg_area_ids(m_Ctx, ECMG_AREA_SPAWN, ids.data(), n, &n);
+            for (int id : ids)
+                for (int g : GetConnectedAreas(id, SPAWN))
+                    if (g == sourceID) {
+                        out.push_back(id);
+                        break;
+                    }
+        }
+        return out;
+    }
 
     int GetNumAgents() const
     {

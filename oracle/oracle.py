@@ -368,3 +368,69 @@ class Ref:
         out = np.zeros(nv, U8)
         self.lib.ref_obstacle_convexity(self.h, _addr(out))
         return out
+
+    # ---- spawn and goal areas --------------------------------------------
+    def _spawn_sigs(self):
+        L, vp = self.lib, C.c_void_p
+        if getattr(self, "_spawn_ready", False):
+            return L
+        L.ref_add_spawn_area.argtypes = [vp] + [C.c_float] * 8 + [C.c_int]
+        L.ref_add_goal_area.argtypes = [vp] + [C.c_float] * 4 + [C.c_int]
+        L.ref_remove_area.argtypes = [vp, C.c_int, C.c_int]
+        L.ref_connect_areas.argtypes = [vp, C.c_int, C.c_int, C.c_float]
+        L.ref_disconnect_areas.argtypes = [vp, C.c_int, C.c_int]
+        L.ref_update_spawn_areas.argtypes = [vp]
+        L.ref_srand.argtypes = [C.c_uint]
+        L.ref_spawn_area_state.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
+        L.ref_free_top.argtypes = [vp, vp]
+        self._spawn_ready = True
+        return L
+
+    def add_spawn_area(self, x, y, hw, hh, cfg=None, ID=-1):
+        c = dict(preferred_speed_min=5.0, preferred_speed_max=10.0, clearance_min=5.0, clearance_max=10.0)
+        c.update(cfg or {})
+        return self._spawn_sigs().ref_add_spawn_area(self.h, x, y, hw, hh, c["preferred_speed_min"],
+                                                     c["preferred_speed_max"], c["clearance_min"],
+                                                     c["clearance_max"], ID)
+
+    def add_goal_area(self, x, y, hw, hh, ID=-1):
+        return self._spawn_sigs().ref_add_goal_area(self.h, x, y, hw, hh, ID)
+
+    def remove_area(self, area_type, ID):
+        self._spawn_sigs().ref_remove_area(self.h, area_type, ID)
+
+    def connect(self, spawn_id, goal_id, rate=0.0):
+        self._spawn_sigs().ref_connect_areas(self.h, spawn_id, goal_id, rate)
+
+    def disconnect(self, spawn_id, goal_id):
+        self._spawn_sigs().ref_disconnect_areas(self.h, spawn_id, goal_id)
+
+    def update_spawn_areas(self):
+        self._spawn_sigs().ref_update_spawn_areas(self.h)
+
+    def srand(self, seed):
+        self._spawn_sigs().ref_srand(seed)
+
+    def rand(self):
+        return self._spawn_sigs().ref_rand()
+
+    def rand_max(self):
+        return self._spawn_sigs().ref_rand_max()
+
+    def spawn_area_state(self, ID, cap=64):
+        g, r, t = np.zeros(cap, I32), np.zeros(cap, F32), np.zeros(cap, F32)
+        ng = C.c_int()
+        n = self._spawn_sigs().ref_spawn_area_state(self.h, ID, _addr(g), C.byref(ng), _addr(r), _addr(t), cap)
+        if n < 0:
+            return None
+        return dict(goals=g[:ng.value].tolist(), rate=r[:n].copy(), since=t[:n].copy())
+
+    def free_top(self):
+        size = C.c_int()
+        top = self._spawn_sigs().ref_free_top(self.h, C.byref(size))
+        return top, size.value
+
+    def get_path(self, idx, cap=4096):
+        out = np.zeros((cap, 2), F32)
+        n = self.lib.ref_get_path(self.h, idx, _addr(out), cap)
+        return out[:min(n, cap)].copy()

@@ -416,4 +416,54 @@ void ref_obstacle_convexity(void* h, unsigned char* out)
         for (size_t i = 0; i < o.verts.size(); i++) out[g++] = o.verts[i]->isConvex ? 1 : 0;
 }
 
+/* ---- spawn and goal areas (Simulator.cpp:336-457, 494-536) ------------ */
+int ref_add_spawn_area(void* h, float x, float y, float hw, float hh, float speed_min, float speed_max,
+                       float clear_min, float clear_max, int id)
+{
+    SpawnConfiguration cfg;
+    cfg.preferredSpeedMin = speed_min;
+    cfg.preferredSpeedMax = speed_max;
+    cfg.clearanceMin = clear_min;
+    cfg.clearanceMax = clear_max;
+    return ((RefSim*)h)->sim->AddSpawnArea(Point(x, y), Vec2(hw, hh), cfg, id);
+}
+
+int ref_add_goal_area(void* h, float x, float y, float hw, float hh, int id)
+{
+    return ((RefSim*)h)->sim->AddGoalArea(Point(x, y), Vec2(hw, hh), id);
+}
+
+void ref_remove_area(void* h, int type, int id) { ((RefSim*)h)->sim->RemoveArea((SimAreaType)type, id); }
+void ref_connect_areas(void* h, int s, int g, float rate) { ((RefSim*)h)->sim->ConnectSpawnGoalAreas(s, g, rate); }
+void ref_disconnect_areas(void* h, int s, int g) { ((RefSim*)h)->sim->DeconnectSpawnGoalAreas(s, g); }
+/* the reference's UpdateSpawnAreas alone (private, opened by pre.h) */
+void ref_update_spawn_areas(void* h) { ((RefSim*)h)->sim->UpdateSpawnAreas(); }
+/* the C library's generator the reference draws from */
+void ref_srand(unsigned seed) { srand(seed); }
+int ref_rand(void) { return rand(); }
+int ref_rand_max(void) { return RAND_MAX; }
+
+/* connected goals, rates and timers of a spawn area; returns the size of
+   the rate vector, or -1 when the area does not exist */
+int ref_spawn_area_state(void* h, int id, int* goals, int* n_goals, float* rates, float* since, int cap)
+{
+    SpawnArea* a = ((RefSim*)h)->sim->GetSpawnArea(id);
+    if (!a) return -1;
+    *n_goals = (int)a->connectedGoalAreas.size();
+    for (int i = 0; i < *n_goals && i < cap; i++) goals[i] = a->connectedGoalAreas[i];
+    for (int i = 0; i < (int)a->spawnRate.size() && i < cap; i++) {
+        rates[i] = a->spawnRate[i];
+        since[i] = a->timeSinceLastSpawn[i];
+    }
+    return (int)a->spawnRate.size();
+}
+
+/* the top of the free-slot stack (-1 when empty) and its size */
+int ref_free_top(void* h, int* size)
+{
+    Simulator* s = ((RefSim*)h)->sim;
+    *size = (int)s->m_freeEntitySpaces.size();
+    return s->m_freeEntitySpaces.empty() ? -1 : s->m_freeEntitySpaces.top();
+}
+
 } /* extern "C" */

@@ -49,6 +49,26 @@ int main(int argc, char** argv)
         if (sim.GetNumAgents() != 1) return 1;
         sim.Reset();
         if (sim.GetNumAgents() != 0) return 1;
+        /* spawn areas, as the editor's commands set them up (Command.cpp:31-160) */
+        ecmg::SpawnConfiguration cfg;
+        cfg.clearanceMin = 0.3f;
+        cfg.preferredSpeedMin = 1.2f;
+        int sa = sim.AddSpawnArea({12, 4}, {2, 1}, cfg);
+        int ga = sim.AddGoalArea({35, 28}, {1, 1});
+        sim.ConnectSpawnGoalAreas(sa, ga, 30.0f);
+        if (sim.GetConnectedAreas(sa, ecmg::SPAWN).size() != 1 || sim.GetConnectedAreas(ga, ecmg::GOAL).size() != 1)
+            return 1;
+        long long refused = 0, failed = 0;
+        for (int t = 0; t < 60; t++) {
+            sim.Update(1.0f / 60.0f);
+            refused += sim.LastTickStats().spawn_refused;
+            failed += sim.LastTickStats().spawn_failed;
+        }
+        std::printf("spawned agents %d (no location %lld, refused %lld)\n", sim.GetNumAgents(), failed, refused);
+        if (sim.GetNumAgents() < 10) return 1;
+        sim.DeconnectSpawnGoalAreas(sa, ga);
+        if (!sim.GetConnectedAreas(sa, ecmg::SPAWN).empty()) return 1;
+        sim.RemoveArea(ecmg::SPAWN, sa);
     } catch (const std::runtime_error& e) {
         std::string m = e.what();
         std::printf("%s\n", m.c_str());
