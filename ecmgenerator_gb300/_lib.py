@@ -144,6 +144,7 @@ def load(build_if_missing: bool = False):
         "ecmg_set_launch": (C.c_int, [vp, C.c_int, C.c_int, C.c_float]),
         "ecmg_set_lp_mode": (C.c_int, [vp, C.c_int, C.c_int]),
         "ecmg_set_occupancy": (C.c_int, [vp, C.c_int]),
+        "ecmg_set_neighbor_mode": (C.c_int, [vp, C.c_int]),
         "ecmg_autotune": (C.c_int, [vp, C.c_int, C.POINTER(TuneResult)]),
         "ecmg_knn_noalloc": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
                                        C.c_float, C.c_float, vp, vp, vp]),

@@ -18,7 +18,7 @@ OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libecmg.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["kernels.cu", "ctx.cu", "api_host.cu", "knn_static.cu", "mlp.cu", "spawn.cu"]
+CU_SOURCES = ["kernels.cu", "ctx.cu", "api_host.cu", "knn_static.cu", "mlp.cu", "spawn.cu", "kdtree.cu"]
 CXX_SOURCES = ["host_scene.cpp"]
 
 

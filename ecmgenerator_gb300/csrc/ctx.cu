@@ -290,6 +290,24 @@ struct ecmg_ctx {
     DBuf<SpawnRec> d_spawn_rec;
     std::vector<int> spawned_slot;
     std::vector<V2> spawned_start, spawned_goal;
+    /* neighbour mode: 0 exact kNN, 1 the reference's kd-tree (kdtree.cu) */
+    int nbr_mode = 0;
+    struct KdBufs {
+        DBuf<unsigned char> mark, side;
+        DBuf<int> n_dev, iscan, ids0, vtmp, X0, X[2], Y[2], seg_lo, seg_hi, seg_node, scan_tmp32, hist, tree, map,
+            kfound, agg, prev_in, cache;
+        DBuf<unsigned> keys, ktmp;
+        DBuf<unsigned long long> flags, scan_tmp64;
+        int levels = 0, tree_cap = 0;
+        void free_all()
+        {
+            mark.free_(); side.free_();
+            DBuf<int>* is[] = {&n_dev, &iscan, &ids0, &vtmp, &X0, &X[0], &X[1], &Y[0], &Y[1], &seg_lo, &seg_hi,
+                               &seg_node, &scan_tmp32, &hist, &tree, &map, &kfound, &agg, &prev_in, &cache};
+            for (auto* b : is) b->free_();
+            keys.free_(); ktmp.free_(); flags.free_(); scan_tmp64.free_();
+        }
+    } kd;
     /* graph */
     cudaGraphExec_t graph[2] = {nullptr, nullptr}; /* plain tick, tick with the proposal model */
     bool graph_dirty = true;
@@ -424,6 +442,7 @@ ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max
     CKC(cudaMemset(c->attr.p, 0, sizeof(V2) * N)); CKC(cudaMemset(c->pref_vel.p, 0, sizeof(V2) * N));
     CKC(cudaMemset(c->d_active.p, 0, N)); CKC(cudaMemset(c->path_len.p, 0, sizeof(int) * N));
     CKC(cudaMemset(c->path_off.p, 0, sizeof(int) * N));
+    CKC(cudaMemset(c->d_clear.p, 0, sizeof(float) * N)); CKC(cudaMemset(c->d_speed.p, 0, sizeof(float) * N));
     CKC(cudaHostAlloc((void**)&c->h_counters, sizeof(int) * 3 * kCounters, cudaHostAllocDefault));
     CKC(cudaHostAlloc((void**)&c->h_lists, sizeof(int) * 4 * ecmg_ctx::kListStage, cudaHostAllocDefault));
     c->active.assign(N, 0);
@@ -490,6 +509,7 @@ ecmg_status ecmg_destroy(ecmg_ctx* c)
     c->d_sarea.free_();
     c->d_hit.free_();
     c->d_spawn_rec.free_();
+    c->kd.free_all();
     for (void* h : c->hview)
         if (h) cudaFreeHost(h);
     if (c->ev_t0) cudaEventDestroy(c->ev_t0);
@@ -1724,9 +1744,49 @@ static cudaError_t enqueue_tick(ecmg_ctx* c, int launch_slots, bool use_model)
     }
     ProposeCall pc{c->model, c->feat.p, c->counters.p + C_NSORTED, launch_slots, c->cls.p, c->sms,
                    c->counters.p + C_ERROR};
+    KdArgs kd{};
+    if (c->nbr_mode == 1) {
+        auto& K = c->kd;
+        kd.max_slots = c->max_agents;
+        kd.cap = c->max_agents;
+        kd.k = c->prm.max_neighbors;
+        kd.levels = K.levels;
+        kd.tree_cap = K.tree_cap;
+        kd.pos = c->pos.p;
+        kd.s_slot = c->s_slot.p;
+        kd.counters = c->counters.p;
+        kd.active = c->d_active.p;
+        kd.cell_start = c->cell_start.p;
+        kd.slot_bucket = c->key.p;
+        kd.slot_rank = c->rank.p;
+        kd.mark = K.mark.p;
+        kd.n_dev = K.n_dev.p;
+        kd.iscan = K.iscan.p;
+        kd.ids0 = K.ids0.p;
+        kd.keys = K.keys.p;
+        kd.ktmp = K.ktmp.p;
+        kd.vtmp = K.vtmp.p;
+        kd.X0 = K.X0.p;
+        kd.X[0] = K.X[0].p; kd.X[1] = K.X[1].p;
+        kd.Y[0] = K.Y[0].p; kd.Y[1] = K.Y[1].p;
+        kd.seg_lo = K.seg_lo.p; kd.seg_hi = K.seg_hi.p; kd.seg_node = K.seg_node.p;
+        kd.side = K.side.p;
+        kd.flags = K.flags.p;
+        kd.scan_tmp32 = K.scan_tmp32.p;
+        kd.scan_tmp64 = K.scan_tmp64.p;
+        kd.hist = K.hist.p;
+        kd.tree = K.tree.p;
+        kd.map = K.map.p;
+        kd.kfound = K.kfound.p;
+        kd.agg = K.agg.p;
+        kd.prev_in = K.prev_in.p;
+        kd.cache = K.cache.p;
+        kd.nbr = c->nbr.p;
+        kd.ncnt = c->ncnt.p;
+    }
     e = launch_tick(b, t, launch_slots, c->scan_tmp.p, c->block, c->sms, c->stream, c->stream2, c->ev_fork,
                     c->ev_join, c->ev_k,
-                    use_model ? propose_cb : nullptr, &pc, after_attract_cb, c);
+                    use_model ? propose_cb : nullptr, &pc, after_attract_cb, c, c->nbr_mode == 1 ? &kd : nullptr);
     if (e != cudaSuccess) return e;
     return cudaMemcpyAsync(c->h_counters + kCounters, c->counters.p, sizeof(int) * kCounters, cudaMemcpyDeviceToHost,
                            c->stream);
@@ -1740,7 +1800,15 @@ int ecmg_kernels_per_tick(const ecmg_ctx* c)
        k_neighbors, k_agents; k_features with a proposal model or a trace;
        k_mlp_infer with a proposal model */
     if (!c) return 8;
-    return 8 + ((c->model || c->trace) ? 1 : 0) + (c->model ? 1 : 0);
+    int n = 8 + ((c->model || c->trace) ? 1 : 0) + (c->model ? 1 : 0);
+    /* kd-tree mode, instead of k_neighbors: members and slot-order list (6),
+       four radix sorts of four passes (84), segment init (1), level 0 (11),
+       levels 1.. (side + partition), the query (1) and the composition (3) */
+    if (c->nbr_mode == ECMG_NEIGHBORS_KDTREE) {
+        const int L = c->kd.levels;
+        n += -1 + 6 + 84 + 1 + 11 + (L - 1) + 5 * std::max(0, L - 2) + 1 + 3;
+    }
+    return n;
 }
 
 static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
@@ -1935,6 +2003,12 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
     CK(cudaMemcpy(sa.p, c->attr.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
     CK(cudaMemcpy(spv.p, c->pref_vel.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
     CK(cudaMemcpy(sact.p, c->d_active.p, N, cudaMemcpyDeviceToDevice));
+    /* kd-tree mode: the neighbour cache the next tick starts from */
+    std::vector<int> kd_cache;
+    if (c->nbr_mode == ECMG_NEIGHBORS_KDTREE) {
+        kd_cache.resize((size_t)c->prm.max_neighbors);
+        CK(cudaMemcpy(kd_cache.data(), c->kd.cache.p, sizeof(int) * kd_cache.size(), cudaMemcpyDeviceToHost));
+    }
     std::vector<unsigned char> act = c->active;
     std::vector<std::vector<int>> stacks;
     std::vector<int> nums, lasts;
@@ -1946,6 +2020,8 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
         CK(cudaMemcpy(c->attr.p, sa.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
         CK(cudaMemcpy(c->pref_vel.p, spv.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
         CK(cudaMemcpy(c->d_active.p, sact.p, N, cudaMemcpyDeviceToDevice));
+        if (!kd_cache.empty())
+            CK(cudaMemcpy(c->kd.cache.p, kd_cache.data(), sizeof(int) * kd_cache.size(), cudaMemcpyHostToDevice));
         c->active = act;
         for (size_t i = 0; i < c->scenes.size(); i++) {
             c->scenes[i]->free_stack = stacks[i];
@@ -2017,7 +2093,7 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
             }
     }
     for (int w : wgrabs) {
-        if (st != ECMG_OK) break;
+        if (st != ECMG_OK || c->nbr_mode == ECMG_NEIGHBORS_KDTREE) break; /* one thread per agent there */
         st = trial(Launch{cell, 1, bestL.block, bestL.tile, 1, w}, &better);
     }
     if (st != ECMG_OK) {
@@ -2050,9 +2126,48 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
     return ECMG_OK;
 }
 
+ecmg_status ecmg_set_neighbor_mode(ecmg_ctx* c, int mode)
+{
+    if (!c || (mode != ECMG_NEIGHBORS_EXACT && mode != ECMG_NEIGHBORS_KDTREE)) return ECMG_ERR_INVALID_ARG;
+    if (mode == c->nbr_mode) return ECMG_OK;
+    if (mode == ECMG_NEIGHBORS_KDTREE) {
+        if (c->model || c->trace || c->cls_override)
+            return fail(c, ECMG_ERR_STATE, "the kd-tree neighbour mode runs without the learned proposal and trace");
+        if (c->max_agents > (1 << 24)) return fail(c, ECMG_ERR_BOUND, "the kd-tree neighbour mode supports 2^24 slots");
+        const size_t N = (size_t)c->max_agents;
+        const int k = c->prm.max_neighbors;
+        auto& K = c->kd;
+        K.levels = 32 - __builtin_clz((unsigned)c->max_agents); /* depth 0 .. bit length - 1 */
+        K.tree_cap = (int)((1u << K.levels) - 1u);
+        const int hist = kd_hist_ints(c->max_agents);
+        CK(K.mark.alloc(N)); CK(K.side.alloc(N));
+        CK(K.n_dev.alloc(2)); CK(K.iscan.alloc(N)); CK(K.ids0.alloc(N)); CK(K.vtmp.alloc(N)); CK(K.X0.alloc(N));
+        CK(K.X[0].alloc(N)); CK(K.X[1].alloc(N)); CK(K.Y[0].alloc(N)); CK(K.Y[1].alloc(N));
+        CK(K.seg_lo.alloc(N)); CK(K.seg_hi.alloc(N)); CK(K.seg_node.alloc(N));
+        CK(K.scan_tmp32.alloc((size_t)kd_scan_tmp(std::max<int>(c->max_agents, hist))));
+        CK(K.scan_tmp64.alloc((size_t)kd_scan_tmp(c->max_agents)));
+        CK(K.hist.alloc((size_t)hist)); CK(K.tree.alloc((size_t)K.tree_cap));
+        CK(K.map.alloc(N * (size_t)k)); CK(K.kfound.alloc(N));
+        CK(K.agg.alloc((size_t)kd_compose_blocks(c->max_agents) * k));
+        CK(K.prev_in.alloc((size_t)kd_compose_blocks(c->max_agents) * k));
+        CK(K.cache.alloc((size_t)k));
+        CK(K.keys.alloc(N)); CK(K.ktmp.alloc(N)); CK(K.flags.alloc(N));
+        /* ORCA::m_NeighborCache starts as std::vector<Entity>(k): zeros */
+        CK(cudaMemset(K.cache.p, 0, sizeof(int) * (size_t)k));
+        c->lp_mode = ECMG_LP_THREAD;
+    } else {
+        c->kd.free_all();
+    }
+    c->nbr_mode = mode;
+    c->graph_dirty = true;
+    return ECMG_OK;
+}
+
 ecmg_status ecmg_set_lp_mode(ecmg_ctx* c, int mode, int agents_per_warp_grab)
 {
     if (!c || (mode != ECMG_LP_THREAD && mode != ECMG_LP_WARP)) return ECMG_ERR_INVALID_ARG;
+    if (mode == ECMG_LP_WARP && c->nbr_mode == ECMG_NEIGHBORS_KDTREE)
+        return fail(c, ECMG_ERR_STATE, "the kd-tree neighbour mode runs one thread per agent");
     if (mode == ECMG_LP_WARP && (agents_per_warp_grab < 1 || agents_per_warp_grab > 64)) return ECMG_ERR_INVALID_ARG;
     c->lp_mode = mode;
     if (mode == ECMG_LP_WARP) c->wgrab = agents_per_warp_grab;
@@ -2193,6 +2308,8 @@ ecmg_status ecmg_set_record(ecmg_ctx* c, int on)
 ecmg_status ecmg_set_proposal(ecmg_ctx* c, ecmg_mlp* model)
 {
     if (!c) return ECMG_ERR_INVALID_ARG;
+    if (model && c->nbr_mode == ECMG_NEIGHBORS_KDTREE)
+        return fail(c, ECMG_ERR_STATE, "the learned proposal and the trace need the exact neighbour mode");
     if (model != c->model) {
         c->model = model;
         c->gate_left = 0;
@@ -2213,6 +2330,8 @@ ecmg_status ecmg_set_proposal_gate(ecmg_ctx* c, float min_accept_rate, int pause
 ecmg_status ecmg_set_trace(ecmg_ctx* c, int on)
 {
     if (!c) return ECMG_ERR_INVALID_ARG;
+    if (on && c->nbr_mode == ECMG_NEIGHBORS_KDTREE)
+        return fail(c, ECMG_ERR_STATE, "the learned proposal and the trace need the exact neighbour mode");
     if ((on != 0) != c->trace) {
         c->trace = on != 0;
         c->trace_rows = 0;
@@ -2224,6 +2343,8 @@ ecmg_status ecmg_set_trace(ecmg_ctx* c, int on)
 ecmg_status ecmg_set_proposal_classes(ecmg_ctx* c, const unsigned char* dev_cls_by_slot)
 {
     if (!c) return ECMG_ERR_INVALID_ARG;
+    if (dev_cls_by_slot && c->nbr_mode == ECMG_NEIGHBORS_KDTREE)
+        return fail(c, ECMG_ERR_STATE, "the learned proposal and the trace need the exact neighbour mode");
     if (dev_cls_by_slot != c->cls_override) {
         c->cls_override = dev_cls_by_slot;
         c->graph_dirty = true;

@@ -154,10 +154,12 @@ typedef cudaError_t (*HookFn)(void* user, cudaStream_t s, unsigned evflags);
    join through ev_fork / ev_join).  ev (may be null): five events -- before
    both, after the attraction kernel (on s2), after the neighbour kernel, after
    the proposal (features + inference) and after the per-agent kernel. */
+struct KdArgs;
+/* kd (may be null): the kd-tree neighbour mode replaces the neighbour kernel */
 cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int block, int sms,
                         cudaStream_t s, cudaStream_t s2, cudaEvent_t ev_fork, cudaEvent_t ev_join,
                         const cudaEvent_t* ev, ProposeFn propose, void* propose_user,
-                        HookFn after_attract, void* after_attract_user);
+                        HookFn after_attract, void* after_attract_user, const KdArgs* kd);
 cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k, float r, AgentGrid g,
                        int* key, int* rank, int* cell_count, int* cell_start, int* s_slot, V2* s_pos,
                        int* scan_tmp, int scan_blocks, int* out_ids, int* out_cnt, cudaStream_t s);
@@ -194,6 +196,52 @@ struct SpawnTargets {
 /* writes the records into the agent arrays (velocities zeroed, active set,
    failed-search edge cleared) */
 cudaError_t launch_spawn_place(const SpawnRec* rec, int n, const SpawnTargets& t, cudaStream_t s);
+
+/* kdtree.cu: the reference's kd-tree neighbour query (neighbour mode
+   ECMG_NEIGHBORS_KDTREE).  Members = agents in this tick's grid (active at
+   the start of the tick); lists hold slots. */
+constexpr int kKdMaxDepth = 30;
+struct KdArgs {
+    int max_slots, cap, k, levels, tree_cap;
+    const V2* pos;              /* slot-indexed positions at the start of the tick */
+    const int* s_slot;          /* grid order -> slot */
+    const int* counters;        /* C_NSORTED (members), C_LAST */
+    const unsigned char* active; /* after the attraction kernel (kd_finish) */
+    const int* cell_start;
+    const int* slot_bucket;
+    const int* slot_rank;
+    unsigned char* mark;        /* [max_slots] member flags */
+    int* n_dev;                 /* [2] members, max depth */
+    int* iscan;                 /* [max_slots] */
+    int* ids0;                  /* [cap] members in slot order */
+    unsigned* keys;
+    unsigned* ktmp;
+    int* vtmp;                  /* [cap] radix buffers */
+    int* X0;                    /* [cap] (x, index) */
+    int* X[2];                  /* [cap] (x, y, index), partitioned per level */
+    int* Y[2];                  /* [cap] (y, x, index), partitioned per level */
+    int* seg_lo;
+    int* seg_hi;
+    int* seg_node;              /* [cap] segment of each position */
+    unsigned char* side;        /* [max_slots] 0 left, 1 node, 2 right */
+    unsigned long long* flags;  /* [cap] left | right << 32 */
+    int* scan_tmp32;
+    unsigned long long* scan_tmp64;
+    int* hist;                  /* [kd_hist_ints(cap)] */
+    int* tree;                  /* [tree_cap] KDTree::m_Tree */
+    int* map;                   /* [max_slots * k] per-member cache maps, then local prefixes */
+    int* kfound;                /* [max_slots] */
+    int* agg;
+    int* prev_in;               /* [kd_compose_blocks * k] */
+    int* cache;                 /* [k] ORCA::m_NeighborCache, kept across ticks */
+    int* nbr;                   /* [cap * k] per-agent kernel input, grid order */
+    int* ncnt;                  /* [cap] */
+};
+int kd_compose_blocks(int max_slots);
+int kd_hist_ints(int cap);
+int kd_scan_tmp(int n);
+cudaError_t kd_build_and_query(const KdArgs& a, cudaStream_t s, int sms);
+cudaError_t kd_finish(const KdArgs& a, cudaStream_t s, int sms);
 
 }  // namespace ecmg
 #endif

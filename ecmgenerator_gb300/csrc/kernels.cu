@@ -506,9 +506,17 @@ __device__ void orca_tick(const TickArgs& a, int t)
     }
     const int nObst = m;
     for (int q = 0; q < ncnt; q++) {
-        int j = nbr[q];
-        cons[m++] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
-                                        a.inv_tau_a);
+        const int j = nbr[q];
+        if (j >= 0) {
+            cons[m++] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
+                                            a.inv_tau_a);
+        } else {
+            /* kd-tree mode: a cache entry left by an earlier agent that is
+               not in this tick's grid; its slot is not written this tick */
+            const int sl = -j - 1;
+            cons[m++] = agent_constraint_ni(pos, vel, clr, a.pos[sl], a.vel[sl], a.clear[sl], a.tau_a, a.dt,
+                                            a.inv_tau_a);
+        }
     }
     if (overflow) atomicOr(&a.counters[C_ERROR], ECMG_DEV_ERR_CONSTRAINTS);
 
@@ -548,7 +556,8 @@ __device__ void orca_tick(const TickArgs& a, int t)
 
     if (a.rec_cnt) {
         a.rec_cnt[slot] = ncnt;
-        for (int q = 0; q < a.k; q++) a.rec_nbr[slot * a.k + q] = q < ncnt ? a.s_slot[nbr[q]] : -1;
+        for (int q = 0; q < a.k; q++)
+            a.rec_nbr[slot * a.k + q] = q < ncnt ? (nbr[q] >= 0 ? a.s_slot[nbr[q]] : -nbr[q] - 1) : -1;
         a.rec_vorca[slot] = v;
         a.rec_fail[slot] = failed;
         a.rec_ncons[slot] = m;
@@ -1073,7 +1082,7 @@ static int grid_for(int n, int block, int sms, int per_sm)
 cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int* scan_tmp, int block, int sms,
                         cudaStream_t s, cudaStream_t s2, cudaEvent_t ev_fork, cudaEvent_t ev_join,
                         const cudaEvent_t* ev, ProposeFn propose, void* propose_user,
-                        HookFn after_attract, void* after_attract_user)
+                        HookFn after_attract, void* after_attract_user, const KdArgs* kd)
 {
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(s, &cap);
@@ -1103,13 +1112,27 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
         if (e != cudaSuccess) return e;
     }
     if (ev) cudaEventRecordWithFlags(ev[1], s2, evflags);
-    if (t.k <= 8) k_neighbors<8><<<gk, 128, 0, s>>>(t);
-    else if (t.k <= 16) k_neighbors<16><<<gk, 128, 0, s>>>(t);
-    else k_neighbors<32><<<gk, 128, 0, s>>>(t);
-    if (ev) cudaEventRecordWithFlags(ev[2], s, evflags);
+    if (kd) {
+        /* the reference's kd-tree: build and per-member query beside the
+           attraction kernel, the cache composition after it */
+        e = kd_build_and_query(*kd, s, sms);
+        if (e != cudaSuccess) return e;
+    } else if (t.k <= 8) {
+        k_neighbors<8><<<gk, 128, 0, s>>>(t);
+    } else if (t.k <= 16) {
+        k_neighbors<16><<<gk, 128, 0, s>>>(t);
+    } else {
+        k_neighbors<32><<<gk, 128, 0, s>>>(t);
+    }
+    if (ev && !kd) cudaEventRecordWithFlags(ev[2], s, evflags);
     e = cudaEventRecord(ev_join, s2);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_join, 0);
     if (e != cudaSuccess) return e;
+    if (kd) {
+        e = kd_finish(*kd, s, sms);
+        if (e != cudaSuccess) return e;
+        if (ev) cudaEventRecordWithFlags(ev[2], s, evflags);
+    }
     if (t.feat) {
         k_features<<<gk, 128, 0, s>>>(t);
         if (propose) {

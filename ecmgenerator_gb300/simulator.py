@@ -481,3 +481,11 @@ def set_lp_mode(sim: Simulator, mode: str = "warp", agents_per_warp_grab: int = 
     (one warp per agent); results are identical"""
     m = {"thread": 0, "warp": 1}[mode]
     sim._ck(sim.L.ecmg_set_lp_mode(sim.h, m, int(agents_per_warp_grab)))
+
+
+def set_neighbor_mode(sim: Simulator, mode: str = "kdtree"):
+    """'exact' (default): the exact k nearest within neighbor_dist;
+    'kdtree': the reference's kd-tree query with its neighbour cache, the
+    lists of the unmodified Simulator::Update (ecmg_set_neighbor_mode)"""
+    m = {"exact": 0, "kdtree": 1}[mode]
+    sim._ck(sim.L.ecmg_set_neighbor_mode(sim.h, m))

@@ -318,6 +318,19 @@ ecmg_status ecmg_set_occupancy(ecmg_ctx* ctx, int divisor);
 #define ECMG_LP_THREAD 0
 #define ECMG_LP_WARP 1
 ecmg_status ecmg_set_lp_mode(ecmg_ctx* ctx, int mode, int agents_per_warp_grab);
+/* Neighbour query of the tick.  ECMG_NEIGHBORS_EXACT (default): the exact k
+   nearest within neighbor_dist, ordered by (d^2, index).
+   ECMG_NEIGHBORS_KDTREE: the reference's own query -- KDTree::Construct and
+   KNearestAgents_R (KDTree.cpp:22-202), quirks included, with ORCA's
+   neighbour cache carried from agent to agent and from tick to tick
+   (ORCA.h:87,100) -- i.e. the neighbour lists of the unmodified
+   Simulator::Update; agents whose x (or y) coordinates are equal keep the
+   order of the level above (std::sort agrees on subtrees of up to 16 agents).
+   neighbor_dist is not used.  Runs the per-agent kernel one thread per agent,
+   without the learned proposal or the trace; up to 2^24 slots. */
+#define ECMG_NEIGHBORS_EXACT 0
+#define ECMG_NEIGHBORS_KDTREE 1
+ecmg_status ecmg_set_neighbor_mode(ecmg_ctx* ctx, int mode);
 /* times ticks_per_trial ticks per configuration -- first the grid cell with
    the default launch, then, at the best cell, the per-agent kernel's layout,
    block size, work grab and occupancy -- on a copy of the current state, restores the state after each

@@ -99,3 +99,51 @@ def test_custom_transcendentals_divergence(port, c1_ref):
     assert np.array_equal(ra["nbr_ids"][live], rb["nbr_ids"][live])
     rel = np.abs(ra["v_orca"][live] - rb["v_orca"][live]).max(1) / np.maximum(np.abs(ra["v_orca"][live]).max(1), 1e-3)
     assert rel.max() <= 1e-5
+
+
+@pytest.mark.ref
+def test_mode_a_ticks_bitexact_vs_unmodified_update(port):
+    """The oracle's kd-tree mode (knn_mode 1: KDTree::Construct and
+    KNearestAgents_R with the neighbour cache carried across agents and ticks)
+    against the unmodified Simulator::Update, tick by tick.  Re-plans happen
+    inside the reference's Update with its own planner; the oracle takes the
+    same paths afterwards (a failed re-plan keeps the old path on both
+    sides, where the reference would read path.x[-1])."""
+    cfg = ag.scaled("c1")
+    s = ag.build_scene(cfg, seed=2)
+    st = ag.spawn_agents(cfg, s, seed=2)
+    ref = orc.Ref(s, st.n_slots, 1.0 / 60.0, cfg["k"], 2.0, 2.0)
+    paths = []
+    for i in range(st.num_agents):
+        p = ref.find_path(st.pos[i], st.goal[i], float(st.clear[i]))
+        paths.append(p if p is not None else np.stack([st.pos[i], st.goal[i]]).astype(np.float32))
+    st.set_paths(paths)
+    for i in range(st.num_agents):
+        assert ref.spawn_direct(float(st.pos[i, 0]), float(st.pos[i, 1]), float(st.clear[i]),
+                                float(st.pref_speed[i]), paths[i]) == i
+    O, E = port.obstacles(s), port.ecm(s.ecm)
+    P = port.params(k=cfg["k"], libm=1, knn_mode=1, **ORCA)
+    kd = port.kdtree(cfg["k"])
+    replans = lp3d = 0
+    for t in range(400):
+        old = {}
+        res = port.tick(O, E, st, P, kd=kd, record=False)
+        ref.update()
+        lp3d += res["n_lp3d"]
+        for slot in res["replan"]:
+            slot = int(slot)
+            p = ref.get_path(slot)
+            if len(p) == 0:
+                ref.set_path(slot, st.path(slot))
+            else:
+                st.replace_path(slot, p)
+            replans += 1
+        r = ref.get_state()
+        live = r["active"].astype(bool)
+        live[r["last_idx"] + 1:] = False
+        assert np.array_equal(live, st.active.astype(bool)), t
+        assert np.array_equal(r["pos"][live], st.pos[live]), t
+        assert np.array_equal(r["vel"][live], st.vel[live]), t
+    port.lib.og_kdtree_destroy(kd)
+    ref.close()
+    assert replans > 0 and lp3d > 0
