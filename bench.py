@@ -30,6 +30,15 @@ import time
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def KD_BYTES_PER_AGENT(k, levels=20):
+    """algorithmic bytes per agent of the kd-tree neighbour pipeline: member
+    list and slot-order compaction 31, four key gathers 80, four 4-pass radix
+    sorts of (key, value) 320, segment init 12, per level side / flags /
+    scan / partition 95 (level 0 partitions two lists, +61), query 12 + 4k,
+    composition 2 + 8k, emission 14 + 17k"""
+    return 532 + 95 * levels + 29 * k
 sys.path.insert(0, HERE)
 
 from ecmgenerator_gb300.workloads import DT, ORCA, WORKLOADS  # noqa: E402
@@ -218,7 +227,7 @@ class TickTimer:
         self.tot = dict(lp3d=0, replans=0, replans_failed=0, replans_host=0, destroyed=0, device_ms=0.0, host_ms=0.0,
                         proposed=0, accepted=0, gated=0, attract_ms=0.0, neighbors_ms=0.0, proposal_ms=0.0,
                         orca_ms=0.0, spawned=0, spawn_failed=0, spawn_refused=0, spawn_ms=0.0, spawn_check_ms=0.0,
-                        spawn_candidates=0)
+                        spawn_candidates=0, graph_builds=0)
 
     def tick(self):
         import torch
@@ -274,6 +283,15 @@ def run_ours(args):
             s_.push_spawn_random(stream)
         sims.append(s_)
     plain, learned = sims
+    if args.neighbors == "kdtree":
+        # the reference's kd-tree query (no learned proposal in this mode)
+        from ecmgenerator_gb300.simulator import set_neighbor_mode
+
+        for s_ in sims:
+            set_neighbor_mode(s_, "kdtree")
+        args.plain_only = True
+        if args.lp_mode == "warp":
+            args.lp_mode = "thread"
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     plain.update()
     learned.update()
@@ -360,6 +378,11 @@ def run_ours(args):
     # velocity, active flag, slot, neighbour count and k indices, and writes
     # pos and vel
     kern = {"k_neighbors": (main_t.tot["neighbors_ms"], 8 + 4 * k), "k_agents": (main_t.tot["orca_ms"], 57 + 4 * k)}
+    if args.neighbors == "kdtree":
+        # the kd-tree pipeline (build, query, cache composition) in place of
+        # k_neighbors; its algorithmic bytes per agent are derived in DESIGN
+        kern = {"kd-tree pipeline": (main_t.tot["neighbors_ms"], KD_BYTES_PER_AGENT(k, (n + spawn_slots).bit_length())),
+                "k_agents": (main_t.tot["orca_ms"], 57 + 4 * k)}
     kname = max(kern, key=lambda q: kern[q][0])
     kern_ms = kern[kname][0] / max(args.steps, 1)
     alg_bytes = kern[kname][1]
@@ -388,6 +411,7 @@ def run_ours(args):
                    "time_horizon_s": 2.0, "dt_s": DT, "scene": f'{cfg["w"]:.0f}x{cfg["h"]:.0f} m, {cfg["boxes"]} boxes',
                    "l2": "flushed before every timed tick (512 MB write)", "parallelism": f"replicas x{world}",
                    "seed": args.seed, "mode": "learned proposal" if model is not None else "plain",
+                   "neighbors": args.neighbors,
                    "launch": launch},
         "plain": {"value": plain_value, "ms_per_step": p_ms_all / args.steps,
                   "lp3d_per_tick": tp.tot["lp3d"] / args.steps,
@@ -416,7 +440,8 @@ def run_ours(args):
                        "replans_host_per_tick": T["replans_host"] / args.steps,
                        "destroyed_per_tick": T["destroyed"] / args.steps,
                        "graph_ms_per_tick": T["device_ms"] / args.steps,
-                       "host_ms_per_tick": T["host_ms"] / args.steps},
+                       "host_ms_per_tick": T["host_ms"] / args.steps,
+                       "graph_builds": T["graph_builds"]},
     }
     if args.spawn_rate > 0:
         K = max(args.steps, 1)
@@ -478,6 +503,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="time the plain tick only")
+    ap.add_argument("--neighbors", default="exact", choices=["exact", "kdtree"],
+                    help="exact kNN (default) or the reference's kd-tree query with its neighbour cache")
     ap.add_argument("--spawn-rate", type=float, default=0.0,
                     help="agents/s per spawn area, 4 spawn areas (UpdateSpawnAreas every tick); 0: none")
     ap.add_argument("--proposal", default=None, help="proposal weights (.npy)")

@@ -1803,10 +1803,10 @@ int ecmg_kernels_per_tick(const ecmg_ctx* c)
     int n = 8 + ((c->model || c->trace) ? 1 : 0) + (c->model ? 1 : 0);
     /* kd-tree mode, instead of k_neighbors: members and slot-order list (6),
        four radix sorts of four passes (84), segment init (1), level 0 (11),
-       levels 1.. (side + partition), the query (1) and the composition (3) */
+       levels 1.. (side + partition), the query (1) and the composition (4) */
     if (c->nbr_mode == ECMG_NEIGHBORS_KDTREE) {
         const int L = c->kd.levels;
-        n += -1 + 6 + 84 + 1 + 11 + (L - 1) + 5 * std::max(0, L - 2) + 1 + 3;
+        n += -1 + 6 + 84 + 1 + 11 + (L - 1) + 5 * std::max(0, L - 2) + 1 + 4;
     }
     return n;
 }
@@ -1844,7 +1844,6 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             c->gate_left--;
             st.gated++;
         }
-        CK(cudaEventRecord(c->ev_t0, c->stream));
         if (c->prm.use_graph) {
             /* a graph bakes in launch sizes covering slots [0, max_agents) */
             if (c->graph_dirty) {
@@ -1863,9 +1862,13 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
                 if (e2 != cudaSuccess) return fail(c, ECMG_ERR_CUDA, "end capture: %s", cudaGetErrorString(e2));
                 CK(cudaGraphInstantiate(&ge, g, 0));
                 cudaGraphDestroy(g);
+                st.graph_builds++;
             }
+            /* device time from here: a (re)capture is host time */
+            CK(cudaEventRecord(c->ev_t0, c->stream));
             CK(cudaGraphLaunch(ge, c->stream));
         } else {
+            CK(cudaEventRecord(c->ev_t0, c->stream));
             CK(enqueue_tick(c, last + 1, use_model));
         }
         CK(cudaEventRecord(c->ev_t1, c->stream));

@@ -372,12 +372,17 @@ __global__ void __launch_bounds__(128) k_kd_query(KdArgs a, const int* members)
             nd[q] = FLT_MAX;  /* Utility::MAX_FLOAT */
         }
         int kfound = 0;
-        /* frames: node, depth and stage (0 visit, 1 first child done, 2 both) */
+        /* frames: node, depth and stage (0 visit, 1 first child done, 2
+           both), and the least |x - target.x|, |y - target.y| of the
+           subtree's region known from the split planes above it */
         int st_node[kKdMaxDepth + 2];
         int st_ds[kKdMaxDepth + 2];
+        float st_bx[kKdMaxDepth + 2], st_by[kKdMaxDepth + 2];
         int sp = 0;
         st_node[0] = 0;
         st_ds[0] = 0;
+        st_bx[0] = 0.0f;
+        st_by[0] = 0.0f;
         sp = 1;
         while (sp > 0) {
             const int node = st_node[sp - 1];
@@ -387,6 +392,18 @@ __global__ void __launch_bounds__(128) k_kd_query(KdArgs a, const int* members)
                 if (depth > max_depth || a.tree[node] == -1) {
                     sp--;
                     continue;
+                }
+                /* Once k are found, visiting a node changes nothing unless
+                   d < nd[0]; every node of this subtree has
+                   d >= bx^2 + by^2 (rounding is monotonic), so when that
+                   bound reaches nd[0] the whole subtree is visited by the
+                   reference without effect and is skipped here. */
+                if (kfound == k) {
+                    const float bx = st_bx[sp - 1], by = st_by[sp - 1];
+                    if (bx * bx + by * by >= nd[0]) {
+                        sp--;
+                        continue;
+                    }
                 }
                 const int cur = a.tree[node];
                 const V2 cp = a.pos[cur];
@@ -432,6 +449,8 @@ __global__ void __launch_bounds__(128) k_kd_query(KdArgs a, const int* members)
                 st_ds[sp - 1] = depth | (1 << 8);
                 st_node[sp] = tv < cv ? 2 * node + 1 : 2 * node + 2;
                 st_ds[sp] = depth + 1;
+                st_bx[sp] = st_bx[sp - 1]; /* the near side: no new bound */
+                st_by[sp] = st_by[sp - 1];
                 sp++;
             } else if (stage == 1) {
                 const V2 cp = a.pos[a.tree[node]];
@@ -442,6 +461,9 @@ __global__ void __launch_bounds__(128) k_kd_query(KdArgs a, const int* members)
                     st_ds[sp - 1] = depth | (2 << 8);
                     st_node[sp] = tv < cv ? 2 * node + 2 : 2 * node + 1;
                     st_ds[sp] = depth + 1;
+                    /* the far side: at least |db| away along this axis */
+                    st_bx[sp] = (depth & 1) == 0 ? fmaxf(st_bx[sp - 1], fabsf(db)) : st_bx[sp - 1];
+                    st_by[sp] = (depth & 1) == 0 ? st_by[sp - 1] : fmaxf(st_by[sp - 1], fabsf(db));
                     sp++;
                 } else {
                     sp--;
@@ -480,6 +502,7 @@ __global__ void __launch_bounds__(32) k_kd_compose_local(KdArgs a)
         const int cn = min(32, s1 - c0);
         use[q] = q < cn && querying(a, c0 + q);
         __syncwarp();
+#pragma unroll 8
         for (int j = 0; j < cn; j++)
             if (use[j] && q < k) rows[j][q] = a.map[(size_t)(c0 + j) * k + q];
         __syncwarp();
@@ -493,6 +516,7 @@ __global__ void __launch_bounds__(32) k_kd_compose_local(KdArgs a)
             if (q < k) rows[j][q] = v;
         }
         __syncwarp();
+#pragma unroll 8
         for (int j = 0; j < cn; j++)
             if (use[j] && q < k) a.map[(size_t)(c0 + j) * k + q] = rows[j][q];
         __syncwarp();
@@ -527,22 +551,30 @@ __global__ void __launch_bounds__(32) k_kd_compose_top(KdArgs a, int nblk)
     if (q < k) a.cache[q] = prev;
 }
 
+/* grid index of every slot (members), -(slot + 1) for the others */
+__global__ void k_kd_gidx(KdArgs a)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < a.max_slots; s += gridDim.x * blockDim.x)
+        a.iscan[s] = a.mark[s] ? a.cell_start[a.slot_bucket[s]] + a.slot_rank[s] : -(s + 1);
+}
+
 /* final lists -> the per-agent kernel's inputs (grid order): a neighbour in
    this tick's grid by its grid index, any other slot as -(slot + 1) */
 __global__ void k_kd_emit(KdArgs a)
 {
     const int k = a.k;
     const int last = a.counters[C_LAST];
+    const int* gidx = a.iscan;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s <= last; s += gridDim.x * blockDim.x) {
         if (!querying(a, s)) continue;
-        const int t = a.cell_start[a.slot_bucket[s]] + a.slot_rank[s];
+        const int t = gidx[s];
         const int b = s / kComposeSlots;
         const int cnt = a.kfound[s];
         int* out = a.nbr + (size_t)t * k;
-        for (int q = 0; q < k; q++) {
+        for (int q = 0; q < cnt; q++) {
             int v = a.map[(size_t)s * k + q];
             if (v < 0) v = a.prev_in[(size_t)b * k + (-v - 1)];
-            if (q < cnt) out[q] = a.mark[v] ? a.cell_start[a.slot_bucket[v]] + a.slot_rank[v] : -(v + 1);
+            out[q] = gidx[v];
         }
         a.ncnt[t] = cnt;
     }
@@ -620,7 +652,9 @@ cudaError_t kd_build_and_query(const KdArgs& a, cudaStream_t s, int sms)
             }
         }
     }
-    k_kd_query<<<grid_n(a.cap, 128, sms), 128, 0, s>>>(a, a.X0);
+    /* queries in grid order: the agents of a warp are neighbours, so their
+       traversals share nodes in cache */
+    k_kd_query<<<grid_n(a.cap, 128, sms), 128, 0, s>>>(a, a.s_slot);
     return cudaGetLastError();
 }
 
@@ -631,6 +665,7 @@ cudaError_t kd_finish(const KdArgs& a, cudaStream_t s, int sms)
     const int nblk = kd_compose_blocks(a.max_slots);
     k_kd_compose_local<<<nblk, 32, 0, s>>>(a);
     k_kd_compose_top<<<1, 32, 0, s>>>(a, nblk);
+    k_kd_gidx<<<grid_n(a.max_slots, 256, sms), 256, 0, s>>>(a);
     k_kd_emit<<<grid_n(a.max_slots, 256, sms), 256, 0, s>>>(a);
     return cudaGetLastError();
 }

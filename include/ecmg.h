@@ -86,6 +86,7 @@ typedef struct {
     float spawn_ms;          /* host time of the spawn stage, device check included */
     float spawn_check_ms;    /* of which the location tests on the device (copies and wait included) */
     long long spawn_candidates; /* candidate locations tested on the device      */
+    int graph_builds;        /* tick graphs captured and instantiated (host time; after launch-configuration, mode or path-store changes) */
 } ecmg_tick_stats;
 
 /* Static obstacles: n_obstacles rings, ring r = xy[2*ring_offsets[r] ..
