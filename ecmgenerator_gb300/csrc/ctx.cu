@@ -298,6 +298,7 @@ struct ecmg_ctx {
             kfound, agg, prev_in, cache;
         DBuf<unsigned> keys, ktmp;
         DBuf<unsigned long long> flags, scan_tmp64;
+        DBuf<V2> tree_pos;
         int levels = 0, tree_cap = 0;
         void free_all()
         {
@@ -305,7 +306,7 @@ struct ecmg_ctx {
             DBuf<int>* is[] = {&n_dev, &iscan, &ids0, &vtmp, &X0, &X[0], &X[1], &Y[0], &Y[1], &seg_lo, &seg_hi,
                                &seg_node, &scan_tmp32, &hist, &tree, &map, &kfound, &agg, &prev_in, &cache};
             for (auto* b : is) b->free_();
-            keys.free_(); ktmp.free_(); flags.free_(); scan_tmp64.free_();
+            keys.free_(); ktmp.free_(); flags.free_(); scan_tmp64.free_(); tree_pos.free_();
         }
     } kd;
     /* graph */
@@ -1776,6 +1777,7 @@ static cudaError_t enqueue_tick(ecmg_ctx* c, int launch_slots, bool use_model)
         kd.scan_tmp64 = K.scan_tmp64.p;
         kd.hist = K.hist.p;
         kd.tree = K.tree.p;
+        kd.tree_pos = K.tree_pos.p;
         kd.map = K.map.p;
         kd.kfound = K.kfound.p;
         kd.agg = K.agg.p;
@@ -1803,10 +1805,10 @@ int ecmg_kernels_per_tick(const ecmg_ctx* c)
     int n = 8 + ((c->model || c->trace) ? 1 : 0) + (c->model ? 1 : 0);
     /* kd-tree mode, instead of k_neighbors: members and slot-order list (6),
        four radix sorts of four passes (84), segment init (1), level 0 (11),
-       levels 1.. (side + partition), the query (1) and the composition (4) */
+       levels 1.. (side + partition), the query (2) and the composition (4) */
     if (c->nbr_mode == ECMG_NEIGHBORS_KDTREE) {
         const int L = c->kd.levels;
-        n += -1 + 6 + 84 + 1 + 11 + (L - 1) + 5 * std::max(0, L - 2) + 1 + 4;
+        n += -1 + 6 + 84 + 1 + 11 + (L - 1) + 5 * std::max(0, L - 2) + 2 + 4;
     }
     return n;
 }
@@ -2150,6 +2152,7 @@ ecmg_status ecmg_set_neighbor_mode(ecmg_ctx* c, int mode)
         CK(K.scan_tmp32.alloc((size_t)kd_scan_tmp(std::max<int>(c->max_agents, hist))));
         CK(K.scan_tmp64.alloc((size_t)kd_scan_tmp(c->max_agents)));
         CK(K.hist.alloc((size_t)hist)); CK(K.tree.alloc((size_t)K.tree_cap));
+        CK(K.tree_pos.alloc((size_t)K.tree_cap));
         CK(K.map.alloc(N * (size_t)k)); CK(K.kfound.alloc(N));
         CK(K.agg.alloc((size_t)kd_compose_blocks(c->max_agents) * k));
         CK(K.prev_in.alloc((size_t)kd_compose_blocks(c->max_agents) * k));

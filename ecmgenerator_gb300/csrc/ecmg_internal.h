@@ -229,6 +229,7 @@ struct KdArgs {
     unsigned long long* scan_tmp64;
     int* hist;                  /* [kd_hist_ints(cap)] */
     int* tree;                  /* [tree_cap] KDTree::m_Tree */
+    V2* tree_pos;               /* [tree_cap] position of each node's agent */
     int* map;                   /* [max_slots * k] per-member cache maps, then local prefixes */
     int* kfound;                /* [max_slots] */
     int* agg;

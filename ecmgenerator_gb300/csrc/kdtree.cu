@@ -356,6 +356,15 @@ __global__ void k_kd_partition(KdArgs a, const int* B, int* Bout, int update_seg
     }
 }
 
+/* positions in tree order (one dependent load per visit in the query) */
+__global__ void k_kd_tree_pos(KdArgs a)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.tree_cap; i += gridDim.x * blockDim.x) {
+        const int id = a.tree[i];
+        a.tree_pos[i] = id >= 0 ? a.pos[id] : mk(0.0f, 0.0f);
+    }
+}
+
 /* ---- KNearestAgents_R (KDTree.cpp:98-202) with a symbolic cache ---------- */
 __global__ void __launch_bounds__(128) k_kd_query(KdArgs a, const int* members)
 {
@@ -372,24 +381,29 @@ __global__ void __launch_bounds__(128) k_kd_query(KdArgs a, const int* members)
             nd[q] = FLT_MAX;  /* Utility::MAX_FLOAT */
         }
         int kfound = 0;
-        /* frames: node, depth and stage (0 visit, 1 first child done, 2
-           both), and the least |x - target.x|, |y - target.y| of the
-           subtree's region known from the split planes above it */
-        int st_node[kKdMaxDepth + 2];
-        int st_ds[kKdMaxDepth + 2];
-        float st_bx[kKdMaxDepth + 2], st_by[kKdMaxDepth + 2];
-        int sp = 0;
-        st_node[0] = 0;
-        st_ds[0] = 0;
-        st_bx[0] = 0.0f;
-        st_by[0] = 0.0f;
-        sp = 1;
+        /* frames: node and stage (0 visit, 1 first child done, 2 both),
+           and the least |x - target.x|, |y - target.y| of the subtree's
+           region known from the split planes above it */
+        /* frame j holds a node of depth j: node | stage << 28 */
+        int st[kKdMaxDepth + 2];
+        float2 stb[kKdMaxDepth + 2];
+        st[0] = 0;
+        stb[0] = make_float2(0.0f, 0.0f);
+        int sp = 1;
         while (sp > 0) {
-            const int node = st_node[sp - 1];
-            const int depth = st_ds[sp - 1] & 0xff;
-            const int stage = st_ds[sp - 1] >> 8;
+            const int node = st[sp - 1] & 0x0fffffff;
+            const int depth = sp - 1;
+            const int stage = st[sp - 1] >> 28;
             if (stage == 0) {
-                if (depth > max_depth || a.tree[node] == -1) {
+                if (depth > max_depth) {
+                    sp--;
+                    continue;
+                }
+                /* the node's slot and its position (tree order, loaded
+                   side by side) */
+                const int cur = a.tree[node];
+                const V2 cp = a.tree_pos[node];
+                if (cur == -1) {
                     sp--;
                     continue;
                 }
@@ -399,14 +413,12 @@ __global__ void __launch_bounds__(128) k_kd_query(KdArgs a, const int* members)
                    bound reaches nd[0] the whole subtree is visited by the
                    reference without effect and is skipped here. */
                 if (kfound == k) {
-                    const float bx = st_bx[sp - 1], by = st_by[sp - 1];
+                    const float bx = stb[sp - 1].x, by = stb[sp - 1].y;
                     if (bx * bx + by * by >= nd[0]) {
                         sp--;
                         continue;
                     }
                 }
-                const int cur = a.tree[node];
-                const V2 cp = a.pos[cur];
                 const float dx = cp.x - target.x, dy = cp.y - target.y;
                 const float d = dx * dx + dy * dy;
                 if (kfound < k && d > 1e-4f) {
@@ -446,24 +458,23 @@ __global__ void __launch_bounds__(128) k_kd_query(KdArgs a, const int* members)
                 }
                 const float cv = (depth & 1) == 0 ? cp.x : cp.y;
                 const float tv = (depth & 1) == 0 ? target.x : target.y;
-                st_ds[sp - 1] = depth | (1 << 8);
-                st_node[sp] = tv < cv ? 2 * node + 1 : 2 * node + 2;
-                st_ds[sp] = depth + 1;
-                st_bx[sp] = st_bx[sp - 1]; /* the near side: no new bound */
-                st_by[sp] = st_by[sp - 1];
+                st[sp - 1] = node | (1 << 28);
+                st[sp] = tv < cv ? 2 * node + 1 : 2 * node + 2;
+                stb[sp] = stb[sp - 1]; /* the near side: no new bound */
                 sp++;
             } else if (stage == 1) {
-                const V2 cp = a.pos[a.tree[node]];
+                const V2 cp = a.tree_pos[node];
                 const float cv = (depth & 1) == 0 ? cp.x : cp.y;
                 const float tv = (depth & 1) == 0 ? target.x : target.y;
                 const float db = tv - cv;
                 if (db * db < nd[k - 1]) {
-                    st_ds[sp - 1] = depth | (2 << 8);
-                    st_node[sp] = tv < cv ? 2 * node + 2 : 2 * node + 1;
-                    st_ds[sp] = depth + 1;
+                    st[sp - 1] = node | (2 << 28);
+                    st[sp] = tv < cv ? 2 * node + 2 : 2 * node + 1;
                     /* the far side: at least |db| away along this axis */
-                    st_bx[sp] = (depth & 1) == 0 ? fmaxf(st_bx[sp - 1], fabsf(db)) : st_bx[sp - 1];
-                    st_by[sp] = (depth & 1) == 0 ? st_by[sp - 1] : fmaxf(st_by[sp - 1], fabsf(db));
+                    float2 b = stb[sp - 1];
+                    if ((depth & 1) == 0) b.x = fmaxf(b.x, fabsf(db));
+                    else b.y = fmaxf(b.y, fabsf(db));
+                    stb[sp] = b;
                     sp++;
                 } else {
                     sp--;
@@ -654,6 +665,7 @@ cudaError_t kd_build_and_query(const KdArgs& a, cudaStream_t s, int sms)
     }
     /* queries in grid order: the agents of a warp are neighbours, so their
        traversals share nodes in cache */
+    k_kd_tree_pos<<<grid_n(a.tree_cap, 256, sms), 256, 0, s>>>(a);
     k_kd_query<<<grid_n(a.cap, 128, sms), 128, 0, s>>>(a, a.s_slot);
     return cudaGetLastError();
 }
