@@ -282,27 +282,65 @@ static bool segs_cross(V2 a, V2 b, V2 c, V2 d)
     return ((o1 > 0) != (o2 > 0)) && ((o3 > 0) != (o4 > 0));
 }
 
-/* straight piece a->b keeps `clr` from every obstacle edge near it */
-static bool clear_line(const HostScene& s, const GridCSR& g, V2 a, V2 b, double clr)
+/* straight piece a->b keeps `clr` from every obstacle edge near it; each
+   edge is tested once per call (it may be listed in several cells) */
+static bool clear_line(const HostScene& s, const GridCSR& g, V2 a, V2 b, double clr, PlanScratch& scr)
 {
     if (g.gw == 0) return true;
+    if (scr.ob_stamp.size() != s.ob_p.size()) {
+        scr.ob_stamp.assign(s.ob_p.size(), 0);
+        scr.ob_gen = 0;
+    }
+    const unsigned gen = ++scr.ob_gen;
+    if (gen == 0) std::fill(scr.ob_stamp.begin(), scr.ob_stamp.end(), 0u);
+    /* an edge whose bounding box is farther than clr (plus a rounding
+       margin) from the segment's on either axis neither crosses it nor comes
+       closer than clr: skipping it leaves the result unchanged */
+    const double sx0 = std::min(a.x, b.x), sx1 = std::max(a.x, b.x);
+    const double sy0 = std::min(a.y, b.y), sy1 = std::max(a.y, b.y);
+    const double far = clr + 1e-6 + 1e-9 * std::max(std::max(std::fabs(sx0), std::fabs(sx1)),
+                                                     std::max(std::fabs(sy0), std::fabs(sy1)));
     double pad = clr + 0.01;
-    int ix0 = std::max(0, (int)std::floor((std::min(a.x, b.x) - pad - g.x0) * g.inv));
     int iy0 = std::max(0, (int)std::floor((std::min(a.y, b.y) - pad - g.y0) * g.inv));
-    int ix1 = std::min(g.gw - 1, (int)std::floor((std::max(a.x, b.x) + pad - g.x0) * g.inv));
     int iy1 = std::min(g.gh - 1, (int)std::floor((std::max(a.y, b.y) + pad - g.y0) * g.inv));
-    for (int y = iy0; y <= iy1; y++)
+    const double ax = a.x, ay = a.y, bx = b.x, by = b.y;
+    const double cell = 1.0 / g.inv;
+    /* only the cells within pad of the segment: per grid row, the x-range of
+       the part of the segment whose y lies within pad of the row (a superset
+       of the cells closer than pad, so every obstacle edge closer than clr is
+       tested; the bounding box of a long diagonal would hold far more) */
+    for (int y = iy0; y <= iy1; y++) {
+        const double ylo = g.y0 + y * cell - pad, yhi = g.y0 + (y + 1) * cell + pad;
+        double t0 = 0.0, t1 = 1.0;
+        if (by != ay) {
+            double ta = (ylo - ay) / (by - ay), tb = (yhi - ay) / (by - ay);
+            if (ta > tb) std::swap(ta, tb);
+            t0 = std::max(t0, ta);
+            t1 = std::min(t1, tb);
+            if (t0 > t1) continue;
+        } else if (ay < ylo || ay > yhi) {
+            continue;
+        }
+        const double xa = ax + (bx - ax) * t0, xb = ax + (bx - ax) * t1;
+        int ix0 = std::max(0, (int)std::floor((std::min(xa, xb) - pad - g.x0) * g.inv) - 1);
+        int ix1 = std::min(g.gw - 1, (int)std::floor((std::max(xa, xb) + pad - g.x0) * g.inv) + 1);
         for (int x = ix0; x <= ix1; x++) {
             size_t c = (size_t)y * g.gw + x;
             for (int q = g.start[c]; q < g.start[c + 1]; q++) {
                 int i = g.items[(size_t)q];
+                if (scr.ob_stamp[i] == gen) continue;
+                scr.ob_stamp[i] = gen;
                 V2 c0 = s.ob_p[i], c1 = s.ob_p[s.ob_next[i]];
+                const double cx0 = std::min(c0.x, c1.x), cx1 = std::max(c0.x, c1.x);
+                const double cy0 = std::min(c0.y, c1.y), cy1 = std::max(c0.y, c1.y);
+                if (cx0 - sx1 >= far || sx0 - cx1 >= far || cy0 - sy1 >= far || sy0 - cy1 >= far) continue;
                 if (segs_cross(a, b, c0, c1)) return false;
                 double d = std::min(std::min(pt_seg_d(a, c0, c1), pt_seg_d(b, c0, c1)),
                                     std::min(pt_seg_d(c0, a, b), pt_seg_d(c1, a, b)));
                 if (d < clr) return false;
             }
         }
+    }
     /* the walkable rectangle's border */
     double lo = std::min(std::min(a.x - s.bx0, b.x - s.bx0), std::min(a.y - s.by0, b.y - s.by0));
     double hi = std::min(std::min(s.bx1 - a.x, s.bx1 - b.x), std::min(s.by1 - a.y, s.by1 - b.y));
@@ -344,7 +382,15 @@ bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float 
     };
     auto dist = [](V2 a, V2 b) { return std::sqrt((a.x - b.x) * (a.x - b.x) + (a.y - b.y) * (a.y - b.y)); };
     typedef std::pair<float, int> QE;
-    std::priority_queue<QE, std::vector<QE>, std::greater<QE>> open;
+    /* min-heap on (f, vertex): a total order, so the pops are those of any
+       other min-heap; the storage is reused from search to search */
+    std::vector<QE>& open = scr.open;
+    open.clear();
+    const std::greater<QE> later;
+    auto push = [&](QE e) {
+        open.push_back(e);
+        std::push_heap(open.begin(), open.end(), later);
+    };
     int sa = s.he_target[2 * es], sb = s.he_target[2 * es + 1];
     int ga = s.he_target[2 * eg], gb = s.he_target[2 * eg + 1];
     for (int v : {sa, sb}) {
@@ -352,13 +398,14 @@ bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float 
         float g0 = dist(start, s.v_pos[v]);
         if (g0 < scr.g[v]) {
             scr.g[v] = g0;
-            open.push(QE(g0 + dist(s.v_pos[v], goal), v));
+            push(QE(g0 + dist(s.v_pos[v], goal), v));
         }
     }
     int found = -1;
     while (!open.empty()) {
-        QE top = open.top();
-        open.pop();
+        std::pop_heap(open.begin(), open.end(), later);
+        QE top = open.back();
+        open.pop_back();
         int v = top.second;
         if (scr.closed[v]) continue;
         scr.closed[v] = 1;
@@ -375,7 +422,7 @@ bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float 
                 if (ng < scr.g[w]) {
                     scr.g[w] = ng;
                     scr.parent[w] = v;
-                    open.push(QE(ng + dist(s.v_pos[w], goal), w));
+                    push(QE(ng + dist(s.v_pos[w], goal), w));
                 }
             }
             h = s.he_next[h];
@@ -396,7 +443,7 @@ bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float 
     size_t i = 0;
     while (i + 1 < pts.size()) {
         size_t j = i + 1;
-        while (j + 1 < pts.size() && clear_line(s, vis, pts[i], pts[j + 1], clr)) j++;
+        while (j + 1 < pts.size() && clear_line(s, vis, pts[i], pts[j + 1], clr, scr)) j++;
         out.push_back(pts[j]);
         i = j;
     }

@@ -53,7 +53,10 @@ struct PlanScratch {
     std::vector<int> parent;
     std::vector<int> stamp;
     std::vector<unsigned char> closed;
+    std::vector<std::pair<float, int>> open; /* binary min-heap, kept between searches */
     int gen = 0;
+    std::vector<unsigned> ob_stamp; /* obstacle edges tested by the current straight-piece check */
+    unsigned ob_gen = 0;
 };
 
 /* ECMPathPlanner::FindPath (ECMGenerator/ECMPathPlanner.cpp:22-136) as an
