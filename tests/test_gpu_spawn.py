@@ -242,3 +242,75 @@ def test_spawn_refused_without_path_frees_its_location(lib):
         p.tick(t)
     assert p.totals["refused"] > 10 and p.totals["spawned"] > 10, p.totals
     p.close()
+
+
+@pytest.mark.parametrize("mode", ["exact", "kdtree"])
+def test_spawn_areas_inside_full_ticks_match_oracle(port, lib, mode):
+    """The whole Simulator::Update with spawn areas: the restatement's spawn
+    stage feeds the C oracle's tick (exact kNN or the reference's kd-tree with
+    its carried cache), the library runs ecmg_tick; positions, velocities and
+    neighbour lists stay identical while agents keep appearing."""
+    from ecmgenerator_gb300.simulator import Simulator, set_neighbor_mode
+
+    scene, (pos, clr, spd, paths) = _c1(300)
+    n = pos.shape[0]
+    slots = 700
+    sim = Simulator(scene, slots, DT, max_neighbors=10, **ORCA)
+    if mode == "kdtree":
+        set_neighbor_mode(sim, "kdtree")
+    sim.set_record(True)
+    sim.add_agents(pos, clr, spd, paths)
+    areas = so.Areas()
+    cases.standard_areas(scene, cases.Ops(sim, "lib"))
+    cases.standard_areas(scene, cases.Ops(areas, "oracle"))
+    stream = np.random.default_rng(17).integers(0, 2147483648, 200000, dtype=np.int64)
+    sim.push_spawn_random(stream.astype(np.int32))
+    # the oracle's state
+    from ecmgenerator_gb300 import agents as ag
+
+    st = ag.AgentState.empty(slots)
+    st.pos[:n], st.clear[:n], st.pref_speed[:n], st.active[:n] = pos, clr, spd, 1
+    st.num_agents, st.last_idx = n, n - 1
+    st.set_paths(list(paths) + [None] * (slots - n))
+    free = list(range(slots - 1, n - 1, -1))
+    O, E = port.obstacles(scene), port.ecm(scene.ecm)
+    P = port.params(k=10, libm=0, knn_mode=1 if mode == "kdtree" else 0, **ORCA)
+    kd = port.kdtree(10) if mode == "kdtree" else None
+    head, spawned = 0, 0
+    same = lambda a, b: np.array_equal(a, b, equal_nan=True)  # noqa: E731
+    for t in range(90):
+        # UpdateMaxAgentIndex, then UpdateSpawnAreas on the oracle's state
+        while st.last_idx >= 0 and not st.active[st.last_idx]:
+            st.last_idx -= 1
+        spawns, head, _ = so.spawn_stage(areas, st.pos, st.active.astype(bool), free, stream, head, DT, 2147483647,
+                                         plan_ok=lambda a, b, c: sim.find_path(
+                                             (float(a[0]), float(a[1])), (float(b[0]), float(b[1])), float(c)) is not None)
+        sim.update()
+        lib_slots, _, _ = sim.get_spawned()
+        assert lib_slots.tolist() == [sp[0] for sp in spawns], t
+        for slot, start, goal, c, v in spawns:
+            st.pos[slot] = start
+            st.vel[slot] = 0.0
+            st.pref_vel[slot] = 0.0
+            st.clear[slot], st.pref_speed[slot], st.active[slot] = c, v, 1
+            st.num_agents += 1
+            st.last_idx = max(st.last_idx, slot)
+            st.replace_path(slot, sim.get_path(slot))
+        spawned += len(spawns)
+        before = st.active.copy()
+        res = port.tick(O, E, st, P, kd=kd)
+        live = st.active == 1
+        rec = sim.get_record()
+        assert np.array_equal(rec["nbr_ids"][live], res["nbr_ids"][live]), t
+        assert np.array_equal(sim.get_active_flags(), st.active), t
+        assert same(sim.get_position_data(), st.pos), t
+        assert same(sim.get_velocity_data(), st.vel), t
+        free.extend(np.nonzero((before == 1) & (st.active == 0))[0].tolist())
+        for s_ in res["replan"]:
+            st.replace_path(int(s_), sim.get_path(int(s_)))
+        if np.isnan(st.pos[st.active == 1]).any():
+            break
+    if kd is not None:
+        port.lib.og_kdtree_destroy(kd)
+    sim.close()
+    assert spawned > 50, spawned
