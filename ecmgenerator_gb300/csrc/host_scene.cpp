@@ -92,8 +92,76 @@ static void bbox_grow(float& x0, float& y0, float& x1, float& y1, V2 p)
     y1 = std::max(y1, p.y);
 }
 
+/* Landmarks for the planner's A* (the ALT bound): graph distances from a
+   few vertices spread over the ECM (each the vertex farthest, by graph
+   distance, from those chosen before).  For every vertex pair,
+   |d(L, v) - d(L, t)| <= d(v, t), a lower bound of the remaining route that
+   is much closer to it than the straight line when obstacles force
+   detours.  Edge lengths are the search's own. */
+static void build_landmarks(HostScene& s)
+{
+    const int V = (int)s.v_pos.size();
+    s.n_land = 0;
+    s.land_d.clear();
+    if (V == 0) return;
+    const int L = std::min(8, V);
+    const float INF = std::numeric_limits<float>::infinity();
+    std::vector<float> best(V, INF); /* distance to the nearest chosen landmark */
+    std::vector<double> d(V);
+    s.land_d.assign((size_t)V * L, INF);
+    auto elen = [&](int v, int w) {
+        V2 a = s.v_pos[v], b = s.v_pos[w];
+        return std::sqrt((a.x - b.x) * (a.x - b.x) + (a.y - b.y) * (a.y - b.y));
+    };
+    /* the first landmark: the vertex farthest from the ECM's centroid */
+    double cx = 0, cy = 0;
+    for (auto& p : s.v_pos) { cx += p.x; cy += p.y; }
+    cx /= V; cy /= V;
+    int next = 0;
+    double far = -1;
+    for (int v = 0; v < V; v++) {
+        double dd = (s.v_pos[v].x - cx) * (s.v_pos[v].x - cx) + (s.v_pos[v].y - cy) * (s.v_pos[v].y - cy);
+        if (dd > far) { far = dd; next = v; }
+    }
+    typedef std::pair<double, int> QE;
+    for (int l = 0; l < L; l++) {
+        std::fill(d.begin(), d.end(), std::numeric_limits<double>::infinity());
+        std::priority_queue<QE, std::vector<QE>, std::greater<QE>> q;
+        d[next] = 0;
+        q.push(QE(0.0, next));
+        while (!q.empty()) {
+            QE e = q.top();
+            q.pop();
+            int v = e.second;
+            if (e.first > d[v]) continue;
+            int h0 = s.v_halfedge[v];
+            if (h0 < 0) continue;
+            int h = h0, guard = 0;
+            do {
+                int w = s.he_target[h];
+                double nd = d[v] + elen(v, w);
+                if (nd < d[w]) {
+                    d[w] = nd;
+                    q.push(QE(nd, w));
+                }
+                h = s.he_next[h];
+            } while (h != h0 && ++guard < 1024);
+        }
+        for (int v = 0; v < V; v++) {
+            s.land_d[(size_t)v * L + l] = std::isfinite(d[v]) ? (float)d[v] : INF;
+            if (std::isfinite(d[v])) best[v] = std::min(best[v], (float)d[v]);
+        }
+        /* the next one: the connected vertex farthest from all chosen */
+        float bf = -1;
+        for (int v = 0; v < V; v++)
+            if (std::isfinite(best[v]) && best[v] > bf) { bf = best[v]; next = v; }
+    }
+    s.n_land = L;
+}
+
 void build_ecm_grid(HostScene& s)
 {
+    build_landmarks(s);
     int E = (int)(s.he_target.size() / 2);
     int C = 2 * E;
     EcmView ev = s.ecm_view();
@@ -381,6 +449,31 @@ bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float 
         }
     };
     auto dist = [](V2 a, V2 b) { return std::sqrt((a.x - b.x) * (a.x - b.x) + (a.y - b.y) * (a.y - b.y)); };
+    /* Heuristic: the search ends at a vertex t of the goal's edge, with
+       f = g(t) + |t - goal|, so the remaining cost from v is at least
+       min over t of (d(v, t) + |t - goal|) >= |v - goal|.  d(v, t) is bounded
+       below by |v - t| and by the landmark bound (scaled down by 1e-5 for
+       float rounding); both bounds are consistent, so A* stays optimal. */
+    const int nl = s.n_land;
+    float tl[2][8];
+    V2 tp[2];
+    float tg[2];
+    int tv[2];
+    auto h_of = [&](int v) -> float {
+        float h = dist(s.v_pos[v], goal);
+        if (nl == 0) return h;
+        const float* dv = s.land_d.data() + (size_t)v * nl;
+        float hm = std::numeric_limits<float>::infinity();
+        for (int t = 0; t < 2; t++) {
+            float lb = dist(s.v_pos[v], tp[t]);
+            for (int l = 0; l < nl; l++) {
+                const float a = dv[l], b = tl[t][l];
+                if (std::isfinite(a) && std::isfinite(b)) lb = std::max(lb, std::fabs(a - b) * 0.99999f);
+            }
+            hm = std::min(hm, lb + tg[t]);
+        }
+        return std::max(h, hm);
+    };
     typedef std::pair<float, int> QE;
     /* min-heap on (f, vertex): a total order, so the pops are those of any
        other min-heap; the storage is reused from search to search */
@@ -393,12 +486,19 @@ bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float 
     };
     int sa = s.he_target[2 * es], sb = s.he_target[2 * es + 1];
     int ga = s.he_target[2 * eg], gb = s.he_target[2 * eg + 1];
+    tv[0] = ga;
+    tv[1] = gb;
+    for (int t = 0; t < 2; t++) {
+        tp[t] = s.v_pos[tv[t]];
+        tg[t] = dist(tp[t], goal);
+        for (int l = 0; l < nl; l++) tl[t][l] = s.land_d[(size_t)tv[t] * nl + l];
+    }
     for (int v : {sa, sb}) {
         touch(v);
         float g0 = dist(start, s.v_pos[v]);
         if (g0 < scr.g[v]) {
             scr.g[v] = g0;
-            push(QE(g0 + dist(s.v_pos[v], goal), v));
+            push(QE(g0 + h_of(v), v));
         }
     }
     int found = -1;
@@ -422,7 +522,7 @@ bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float 
                 if (ng < scr.g[w]) {
                     scr.g[w] = ng;
                     scr.parent[w] = v;
-                    push(QE(ng + dist(s.v_pos[w], goal), w));
+                    push(QE(ng + h_of(w), w));
                 }
             }
             h = s.he_next[h];

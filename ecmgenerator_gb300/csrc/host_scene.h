@@ -36,6 +36,10 @@ struct HostScene {
     /* scene rectangle (ECM and obstacle bounding box) */
     float bx0 = 0, by0 = 0, bx1 = 0, by1 = 0;
     bool has_ecm = false;
+    /* planner landmarks: graph distance from each of n_land vertices to
+       every vertex, vertex-major [V * n_land] (infinity: not connected) */
+    int n_land = 0;
+    std::vector<float> land_d;
 
     EcmView ecm_view() const;
     ObstView obst_view(const GridCSR* g) const;
@@ -43,7 +47,8 @@ struct HostScene {
 
 /* Obstacle::Initialize (ECMDataTypes.cpp:23-61): links and convexity */
 void set_obstacles(HostScene& s, int n_obst, const int* off, const float* xy);
-/* point-location grid + special y list over the ECM cell quads */
+/* point-location grid + special y list over the ECM cell quads, and the
+   planner's landmark distances */
 void build_ecm_grid(HostScene& s);
 /* candidate lists: every obstacle edge within `reach` of each cell */
 void build_obst_grid(const HostScene& s, float reach, float cell, GridCSR& g);
