@@ -252,11 +252,17 @@ struct ecmg_ctx {
     DBuf<V2> rec_vorca;
     /* learned proposal / trace */
     ecmg_mlp* model = nullptr;
-    /* gating: a tick whose acceptance rate is below gate_min pauses the
-       model for gate_pause ticks (plain ticks), then it is tried again */
+    /* gating: a tick whose acceptance rate is below gate_min, or whose
+       device time per agent exceeds that of the plain tick by 2 %, pauses
+       the model for gate_pause ticks (plain ticks), then it is tried again.
+       The per-agent times are running averages of the ticks with and
+       without the model; without a plain time yet, 8 model ticks are
+       followed by 8 plain ones to measure it. */
     float gate_min = 0.1f;
     int gate_pause = 64;
     int gate_left = 0;
+    float gate_t_model = -1.0f, gate_t_plain = -1.0f; /* ms per agent, running averages */
+    int gate_model_ticks = 0;
     const unsigned char* cls_override = nullptr;
     bool trace = false;
     int trace_rows = 0;
@@ -1967,8 +1973,21 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         st.lp3d += out[C_LP3D];
         st.proposed += out[C_PROPOSED];
         st.accepted += out[C_ACCEPTED];
-        if (use_model && c->gate_min > 0.0f && (float)out[C_ACCEPTED] < c->gate_min * (float)out[C_NSORTED])
-            c->gate_left = c->gate_pause;
+        if (c->model && c->gate_min > 0.0f && out[C_NSORTED] > 0 && tot > 0.0f) {
+            const float per = tot / (float)out[C_NSORTED];
+            float& avg = use_model ? c->gate_t_model : c->gate_t_plain;
+            avg = avg < 0.0f ? per : 0.75f * avg + 0.25f * per;
+        }
+        if (use_model && c->gate_min > 0.0f) {
+            c->gate_model_ticks++;
+            if ((float)out[C_ACCEPTED] < c->gate_min * (float)out[C_NSORTED])
+                c->gate_left = c->gate_pause;
+            else if (c->gate_t_plain < 0.0f && c->gate_model_ticks >= 8)
+                c->gate_left = 8; /* measure the plain tick */
+            else if (c->gate_t_plain > 0.0f && c->gate_model_ticks >= 4 && c->gate_t_model > 1.02f * c->gate_t_plain)
+                c->gate_left = c->gate_pause;
+            if (c->gate_left > 0) c->gate_model_ticks = 0;
+        }
         c->trace_rows = out[C_NSORTED];
         if (out[C_ERROR]) {
             result = fail(c, ECMG_ERR_BOUND, "device bound exceeded (flags 0x%x): %s", out[C_ERROR],
@@ -2319,6 +2338,8 @@ ecmg_status ecmg_set_proposal(ecmg_ctx* c, ecmg_mlp* model)
     if (model != c->model) {
         c->model = model;
         c->gate_left = 0;
+        c->gate_t_model = c->gate_t_plain = -1.0f;
+        c->gate_model_ticks = 0;
         c->graph_dirty = true;
     }
     return ECMG_OK;
@@ -2330,6 +2351,8 @@ ecmg_status ecmg_set_proposal_gate(ecmg_ctx* c, float min_accept_rate, int pause
     c->gate_min = min_accept_rate;
     c->gate_pause = pause_ticks;
     c->gate_left = 0;
+    c->gate_t_model = c->gate_t_plain = -1.0f;
+    c->gate_model_ticks = 0;
     return ECMG_OK;
 }
 
