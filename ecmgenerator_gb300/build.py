@@ -19,7 +19,7 @@ LIB = os.path.join(OUT, "libecmg.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["kernels.cu", "ctx.cu", "api_host.cu", "knn_static.cu", "mlp.cu", "spawn.cu", "kdtree.cu"]
-CXX_SOURCES = ["host_scene.cpp"]
+CXX_SOURCES = ["host_scene.cpp", "ref_planner.cpp"]
 
 
 def nvcc() -> str:

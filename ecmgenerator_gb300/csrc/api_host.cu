@@ -19,6 +19,7 @@ extern "C" {
 struct ecmg_planner {
     HostScene scene;
     GridCSR vis;
+    int mode = ECMG_PLANNER_FAST;
 };
 
 ecmg_status ecmg_planner_create(const ecmg_obstacles* o, const ecmg_ecm* e, ecmg_planner** out)
@@ -81,8 +82,9 @@ ecmg_status ecmg_planner_find_paths(ecmg_planner* pl, int n, const float* starts
         PlanScratch scr;
         std::vector<V2> p;
         for (int i = t; i < n; i += threads) {
-            bool ok = plan_path(pl->scene, pl->vis, mk(starts[2 * i], starts[2 * i + 1]),
-                                mk(goals[2 * i], goals[2 * i + 1]), clearances[i], p, scr);
+            const V2 a = mk(starts[2 * i], starts[2 * i + 1]), b = mk(goals[2 * i], goals[2 * i + 1]);
+            bool ok = pl->mode == ECMG_PLANNER_REFERENCE ? plan_path_reference(pl->scene, a, b, clearances[i], p, scr.ref)
+                                                         : plan_path(pl->scene, pl->vis, a, b, clearances[i], p, scr);
             if (!ok) { out_n[i] = -1; continue; }
             if ((int)p.size() > cap) { out_n[i] = -2; continue; }
             out_n[i] = (int)p.size();
@@ -96,6 +98,13 @@ ecmg_status ecmg_planner_find_paths(ecmg_planner* pl, int n, const float* starts
     for (int t = 1; t < threads; t++) th.emplace_back(work, t);
     work(0);
     for (auto& x : th) x.join();
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_planner_set_mode(ecmg_planner* pl, int mode)
+{
+    if (!pl || (mode != ECMG_PLANNER_FAST && mode != ECMG_PLANNER_REFERENCE)) return ECMG_ERR_INVALID_ARG;
+    pl->mode = mode;
     return ECMG_OK;
 }
 

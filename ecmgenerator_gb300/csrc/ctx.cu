@@ -240,6 +240,7 @@ struct ecmg_ctx {
     void* plan_user = nullptr;
     PlanScratch scratch;
     HostPool pool; /* planner threads (built-in planner only: it is re-entrant) */
+    int planner_mode = ECMG_PLANNER_FAST;
     bool replan_enabled = true;
     bool spawn_enabled = true; /* off while the autotuner runs its trial ticks */
     /* per slot: the start edge from which the built-in planner's search
@@ -655,6 +656,18 @@ ecmg_status ecmg_scene_set_ecm(ecmg_ctx* c, int scene, const ecmg_ecm* e)
 ecmg_status ecmg_set_obstacles(ecmg_ctx* c, const ecmg_obstacles* o) { return ecmg_scene_set_obstacles(c, 0, o); }
 ecmg_status ecmg_set_ecm(ecmg_ctx* c, const ecmg_ecm* e) { return ecmg_scene_set_ecm(c, 0, e); }
 
+ecmg_status ecmg_set_planner_mode(ecmg_ctx* c, int mode)
+{
+    if (!c || (mode != ECMG_PLANNER_FAST && mode != ECMG_PLANNER_REFERENCE)) return ECMG_ERR_INVALID_ARG;
+    if (mode != c->planner_mode) {
+        c->planner_mode = mode;
+        /* the failed-search memo belongs to the planner that made it */
+        std::fill(c->fail_edge.begin(), c->fail_edge.end(), -1);
+        CK(cudaMemset(c->d_fail_edge.p, 0xff, sizeof(int) * (size_t)c->max_agents));
+    }
+    return ECMG_OK;
+}
+
 ecmg_status ecmg_set_planner(ecmg_ctx* c, ecmg_plan_fn fn, void* user)
 {
     if (!c) return ECMG_ERR_INVALID_ARG;
@@ -882,7 +895,10 @@ static ecmg_status plan(ecmg_ctx* c, SceneState* sc, V2 s, V2 g, float clr, std:
         return n > 0 ? ECMG_OK : ECMG_ERR_NO_PATH;
     }
     if (!sc->hs.has_ecm) return ECMG_ERR_STATE;
-    return plan_path(sc->hs, sc->vis_grid, s, g, clr, out, scr, astar_fail_edge) ? ECMG_OK : ECMG_ERR_NO_PATH;
+    const bool ok = c->planner_mode == ECMG_PLANNER_REFERENCE
+                        ? plan_path_reference(sc->hs, s, g, clr, out, scr.ref, astar_fail_edge)
+                        : plan_path(sc->hs, sc->vis_grid, s, g, clr, out, scr, astar_fail_edge);
+    return ok ? ECMG_OK : ECMG_ERR_NO_PATH;
 }
 
 ecmg_status ecmg_find_path(ecmg_ctx* c, float sx, float sy, float gx, float gy, float clearance, float* out_xy,

@@ -53,6 +53,14 @@ void build_ecm_grid(HostScene& s);
 /* candidate lists: every obstacle edge within `reach` of each cell */
 void build_obst_grid(const HostScene& s, float reach, float cell, GridCSR& g);
 
+/* working arrays of the reference planner's A* (ref_planner.cpp) */
+struct RefPlanScratch {
+    std::vector<float> g, f;
+    std::vector<int> parent;
+    std::vector<unsigned char> visited;
+    std::vector<int> heap;
+};
+
 struct PlanScratch {
     std::vector<float> g;
     std::vector<int> parent;
@@ -62,6 +70,7 @@ struct PlanScratch {
     int gen = 0;
     std::vector<unsigned> ob_stamp; /* obstacle edges tested by the current straight-piece check */
     unsigned ob_gen = 0;
+    RefPlanScratch ref;
 };
 
 /* ECMPathPlanner::FindPath (ECMGenerator/ECMPathPlanner.cpp:22-136) as an
@@ -75,6 +84,12 @@ struct PlanScratch {
    else to -1 */
 bool plan_path(const HostScene& s, const GridCSR& vis, V2 start, V2 goal, float clearance,
                std::vector<V2>& out, PlanScratch& scr, int* astar_fail_edge = nullptr);
+
+/* ECMPathPlanner::FindPath (ECMPathPlanner.cpp:22-136) restated: the
+   reference's A*, corridor, portals and funnel (ref_planner.cpp); the same
+   paths as the reference planner */
+bool plan_path_reference(const HostScene& s, V2 start, V2 goal, float clearance, std::vector<V2>& out,
+                         RefPlanScratch& r, int* astar_fail_edge = nullptr);
 
 }  // namespace ecmg
 #endif

@@ -27,7 +27,9 @@ def _ptr(x):
 class Planner:
     """Host-only ECM planner (ecmg_planner_*); needs no GPU."""
 
-    def __init__(self, scene):
+    def __init__(self, scene, mode: str = "fast"):
+        """mode 'fast' (A* with landmark bounds, greedy shortening) or
+        'reference' (ECMPathPlanner::FindPath restated: the reference's paths)"""
         L = self.L = _lib.load()
         self._keep, o, e = _scene_structs(scene)
         h = C.c_void_p()
@@ -35,6 +37,10 @@ class Planner:
         if rc:
             raise EcmgError(rc, "ecmg_planner_create failed")
         self.h = h
+        if mode != "fast":
+            rc = L.ecmg_planner_set_mode(self.h, {"fast": 0, "reference": 1}[mode])
+            if rc:
+                raise EcmgError(rc, "ecmg_planner_set_mode failed")
 
     def find_paths(self, starts, goals, clearances, threads=0, cap=1024):
         starts, goals, clr = _a(starts, F32).reshape(-1, 2), _a(goals, F32).reshape(-1, 2), _a(clearances, F32)
@@ -489,3 +495,9 @@ def set_neighbor_mode(sim: Simulator, mode: str = "kdtree"):
     lists of the unmodified Simulator::Update (ecmg_set_neighbor_mode)"""
     m = {"exact": 0, "kdtree": 1}[mode]
     sim._ck(sim.L.ecmg_set_neighbor_mode(sim.h, m))
+
+
+def set_planner_mode(sim: Simulator, mode: str = "reference"):
+    """built-in planner of re-plans and spawns: 'fast' (default) or
+    'reference' (the reference planner's paths), ecmg_set_planner_mode"""
+    sim._ck(sim.L.ecmg_set_planner_mode(sim.h, {"fast": 0, "reference": 1}[mode]))

@@ -147,6 +147,16 @@ ecmg_status ecmg_set_obstacles(ecmg_ctx* ctx, const ecmg_obstacles* o);
 ecmg_status ecmg_set_ecm(ecmg_ctx* ctx, const ecmg_ecm* e);
 /* replaces the built-in A* planner (NULL restores it) */
 ecmg_status ecmg_set_planner(ecmg_ctx* ctx, ecmg_plan_fn fn, void* user);
+/* Built-in planner.  ECMG_PLANNER_FAST (default): A* over the ECM vertices
+   with the clearance filter (landmark lower bounds), then the polyline is
+   shortened greedily where a straight piece keeps the clearance.
+   ECMG_PLANNER_REFERENCE: ECMPathPlanner::FindPath restated
+   (ECMPathPlanner.cpp:22-411, AStar.cpp:44-210): the reference's A* --
+   its open list included --, corridor, portals and funnel, giving the
+   reference planner's paths. */
+#define ECMG_PLANNER_FAST 0
+#define ECMG_PLANNER_REFERENCE 1
+ecmg_status ecmg_set_planner_mode(ecmg_ctx* ctx, int mode);
 
 /* Simulator::SpawnAgent (Simulator.cpp:168-200): ValidSpawnLocation, then a
    planned path.  *out_slot = slot, or -1 with ECMG_ERR_NO_SLOT /
@@ -178,6 +188,8 @@ ecmg_status ecmg_planner_destroy(ecmg_planner* p);
 ecmg_status ecmg_planner_find_paths(ecmg_planner* p, int n, const float* starts, const float* goals,
                                     const float* clearances, int threads, int cap_per_path,
                                     float* out_xy, int* out_n);
+/* ECMG_PLANNER_FAST (default) or ECMG_PLANNER_REFERENCE, as ecmg_set_planner_mode */
+ecmg_status ecmg_planner_set_mode(ecmg_planner* p, int mode);
 /* ECMGraph::FindCell for n points: cell index (2*edge + side) or -1 */
 ecmg_status ecmg_planner_locate(ecmg_planner* p, int n, const float* xy, int* out_cell);
 

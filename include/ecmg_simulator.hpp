@@ -9,8 +9,8 @@
  * Scene input: the reference hands the Simulator an ECM, a planner and an
  * Environment (Simulator.h:63).  Here the constructor takes the flattened
  * obstacle rings and ECM graph (ecmg_obstacles / ecmg_ecm); path planning uses
- * the library's host planner unless SetPlanner() installs another one (e.g. a
- * wrapper around the reference's ECMPathPlanner::FindPath).
+ * the library's restatement of the reference planner (ECMG_PLANNER_REFERENCE,
+ * the reference's paths) unless SetPlanner() installs another one.
  */
 #ifndef ECMG_SIMULATOR_HPP
 #define ECMG_SIMULATOR_HPP
@@ -66,6 +66,8 @@ public:
         check(ecmg_create(&p, maxAgents, &m_Ctx), "ecmg_create");
         check(ecmg_set_obstacles(m_Ctx, &obstacles), "ecmg_set_obstacles");
         check(ecmg_set_ecm(m_Ctx, &ecm), "ecmg_set_ecm");
+        /* spawns and re-plans get the reference planner's paths */
+        check(ecmg_set_planner_mode(m_Ctx, ECMG_PLANNER_REFERENCE), "ecmg_set_planner_mode");
     }
     ~Simulator()
     {

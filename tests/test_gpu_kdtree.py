@@ -17,13 +17,15 @@ pytestmark = pytest.mark.gpu
 ORCA = dict(tau_agent=2.0, tau_obst=2.0, neighbor_dist=5.0)
 
 
-def _run(port, scene, st, paths, ticks, k, n_slots=None, autotune_at=None, **kw):
-    from ecmgenerator_gb300.simulator import Simulator, autotune, set_neighbor_mode
+def _run(port, scene, st, paths, ticks, k, n_slots=None, autotune_at=None, planner=None, **kw):
+    from ecmgenerator_gb300.simulator import Simulator, autotune, set_neighbor_mode, set_planner_mode
 
     st = st.copy()
     n = st.num_agents
     sim = Simulator(scene, n_slots or st.n_slots, 1.0 / 60.0, max_neighbors=k, **ORCA, **kw)
     set_neighbor_mode(sim, "kdtree")
+    if planner:
+        set_planner_mode(sim, planner)
     sim.set_record(True)
     sim.add_agents(st.pos[:n], st.clear[:n], st.pref_speed[:n], paths[:n])
     O, E = port.obstacles(scene), port.ecm(scene.ecm)
@@ -92,6 +94,14 @@ def test_kdtree_mode_small_population_keeps_stale_entries(port):
     done, events, stale = _run(port, scene, st, paths, 150, 4, n_slots=16)
     print("ticks compared", done, "stale entries", stale)
     assert done >= 1 and stale > 0
+
+
+def test_kdtree_mode_with_the_reference_planner(port, c1_small):
+    """re-plans served by the restated reference planner (the reference's
+    own paths): with the kd-tree mode, the tick of the unmodified reference"""
+    scene, st, paths = c1_small
+    done, events, _ = _run(port, scene, st, paths, 120, 10, planner="reference")
+    assert done >= 100 and events > 0
 
 
 def test_kdtree_mode_autotune_keeps_the_cache(port, c1_small):
