@@ -912,21 +912,47 @@ ecmg_status ecmg_find_path(ecmg_ctx* c, float sx, float sy, float gx, float gy, 
     return st;
 }
 
-/* Simulator::ValidSpawnLocation (Simulator.cpp:295-311) on the device state */
+/* page-locked and device tables of the location checks (spawn.cu) */
+static cudaError_t ensure_check_buffers(ecmg_ctx* c)
+{
+    if (c->h_cand) return cudaSuccess;
+    cudaError_t e = cudaHostAlloc((void**)&c->h_cand, sizeof(V2) * kSpawnMaxCand, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&c->h_sarea, sizeof(SpawnAreaDev) * kSpawnMaxAreas, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&c->h_hit, sizeof(int) * kSpawnMaxCand, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = c->d_cand.alloc(kSpawnMaxCand);
+    if (e == cudaSuccess) e = c->d_sarea.alloc(kSpawnMaxAreas);
+    if (e == cudaSuccess) e = c->d_hit.alloc(kSpawnMaxCand);
+    return e;
+}
+
+/* the candidate table in h_cand / h_sarea (na areas, nc candidates) against
+   the active agents of the scene's slots: one launch, hits back in h_hit */
+static ecmg_status check_candidates(ecmg_ctx* c, SceneState* sc, int na, size_t nc)
+{
+    CK(cudaMemcpyAsync(c->d_cand.p, c->h_cand, sizeof(V2) * nc, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_sarea.p, c->h_sarea, sizeof(SpawnAreaDev) * na, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->d_hit.p, 0, sizeof(int) * nc, c->stream));
+    CK(launch_spawn_check(c->pos.p, c->d_active.p, sc->slot_base, sc->last_idx + 1, c->d_cand.p, c->d_sarea.p, na,
+                          c->d_hit.p, c->sms, c->stream));
+    CK(cudaMemcpyAsync(c->h_hit, c->d_hit.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return ECMG_OK;
+}
+
+static void candidate_box(SpawnAreaDev& D, float x0, float y0, float x1, float y1, float cl, int first, int count);
+
+/* Simulator::ValidSpawnLocation (Simulator.cpp:295-311): one candidate
+   tested on the device (no copy of the agent state) */
 static ecmg_status valid_spawn(ecmg_ctx* c, SceneState* sc, V2 loc, float clearance, bool* ok)
 {
     *ok = true;
     if (sc->last_idx < sc->slot_base) return ECMG_OK;
-    int b = sc->slot_base, n = sc->last_idx - b + 1;
-    std::vector<V2> p((size_t)n);
-    CK(cudaStreamSynchronize(c->stream));
-    CK(cudaMemcpy(p.data(), c->pos.p + b, sizeof(V2) * p.size(), cudaMemcpyDeviceToHost));
-    float cs = clearance * clearance;
-    for (int i = 0; i < n; i++) {
-        if (!c->active[b + i]) continue;
-        float dx = loc.x - p[i].x, dy = loc.y - p[i].y;
-        if (dx * dx + dy * dy < cs) { *ok = false; return ECMG_OK; }
-    }
+    CK(ensure_check_buffers(c));
+    c->h_cand[0] = loc;
+    candidate_box(c->h_sarea[0], loc.x, loc.y, loc.x, loc.y, clearance, 0, 1);
+    ecmg_status cs = check_candidates(c, sc, 1, 1);
+    if (cs != ECMG_OK) return cs;
+    *ok = c->h_hit[0] == 0;
     return ECMG_OK;
 }
 
@@ -1017,17 +1043,25 @@ struct SpawnWindow {
 
 /* the window's candidates against the active agents of the scene's slots
    (one launch, one copy back) */
+/* the box of an area's candidates, grown so that no agent the exact test
+   would find lies outside: such an agent is within clearance * (1 + 2^-21)
+   of a candidate on each axis; the margin covers that and the rounding of
+   the box bounds */
+static void candidate_box(SpawnAreaDev& D, float x0, float y0, float x1, float y1, float cl, int first, int count)
+{
+    const float big = std::fmax(std::fmax(std::fabs(x0), std::fabs(x1)), std::fmax(std::fabs(y0), std::fabs(y1)));
+    const float m = std::fabs(cl) * 1.001f + 1e-3f + 1e-6f * (std::isfinite(big) ? big : 0.0f);
+    D.x0 = x0 - m; D.y0 = y0 - m; D.x1 = x1 + m; D.y1 = y1 + m;
+    D.c2 = cl * cl;
+    D.first = first;
+    D.count = count;
+    D.pad = 0;
+}
+
 static ecmg_status spawn_check(ecmg_ctx* c, SceneState* sc, const SpawnWindow& win, ecmg_tick_stats& st)
 {
     const auto h0 = std::chrono::steady_clock::now();
-    if (!c->h_cand) {
-        CK(cudaHostAlloc((void**)&c->h_cand, sizeof(V2) * kSpawnMaxCand, cudaHostAllocDefault));
-        CK(cudaHostAlloc((void**)&c->h_sarea, sizeof(SpawnAreaDev) * kSpawnMaxAreas, cudaHostAllocDefault));
-        CK(cudaHostAlloc((void**)&c->h_hit, sizeof(int) * kSpawnMaxCand, cudaHostAllocDefault));
-        CK(c->d_cand.alloc(kSpawnMaxCand));
-        CK(c->d_sarea.alloc(kSpawnMaxAreas));
-        CK(c->d_hit.alloc(kSpawnMaxCand));
-    }
+    CK(ensure_check_buffers(c));
     const int na = (int)win.areas.size(), w = (int)win.w;
     for (int a = 0; a < na; a++) {
         const SpawnAreaH& A = *win.areas[a];
@@ -1039,27 +1073,13 @@ static ecmg_status spawn_check(ecmg_ctx* c, SceneState* sc, const SpawnWindow& w
             x0 = std::fmin(x0, p.x); y0 = std::fmin(y0, p.y);
             x1 = std::fmax(x1, p.x); y1 = std::fmax(y1, p.y);
         }
-        /* an agent the exact test finds is within clearance * (1 + 2^-21) of
-           a candidate on each axis; the margin covers that and the rounding
-           of the box bounds */
-        const float cl = A.cfg.clearance_min;
-        const float big = std::fmax(std::fmax(std::fabs(x0), std::fabs(x1)), std::fmax(std::fabs(y0), std::fabs(y1)));
-        const float m = std::fabs(cl) * 1.001f + 1e-3f + 1e-6f * (std::isfinite(big) ? big : 0.0f);
-        SpawnAreaDev& D = c->h_sarea[a];
-        D.x0 = x0 - m; D.y0 = y0 - m; D.x1 = x1 + m; D.y1 = y1 + m;
-        D.c2 = cl * cl;
-        D.first = a * w;
-        D.count = w;
-        D.pad = 0;
+        candidate_box(c->h_sarea[a], x0, y0, x1, y1, A.cfg.clearance_min, a * w, w);
     }
     const size_t nc = (size_t)na * (size_t)w;
-    CK(cudaMemcpyAsync(c->d_cand.p, c->h_cand, sizeof(V2) * nc, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->d_sarea.p, c->h_sarea, sizeof(SpawnAreaDev) * na, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemsetAsync(c->d_hit.p, 0, sizeof(int) * nc, c->stream));
-    CK(launch_spawn_check(c->pos.p, c->d_active.p, sc->slot_base, sc->last_idx + 1, c->d_cand.p, c->d_sarea.p, na,
-                          c->d_hit.p, c->sms, c->stream));
-    CK(cudaMemcpyAsync(c->h_hit, c->d_hit.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
+    {
+        ecmg_status cs = check_candidates(c, sc, na, nc);
+        if (cs != ECMG_OK) return cs;
+    }
     st.spawn_candidates += (long long)nc;
     st.spawn_check_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - h0).count();
     return ECMG_OK;
