@@ -2193,6 +2193,8 @@ ecmg_status ecmg_set_neighbor_mode(ecmg_ctx* c, int mode)
     if (mode == ECMG_NEIGHBORS_KDTREE) {
         if (c->model || c->trace || c->cls_override)
             return fail(c, ECMG_ERR_STATE, "the kd-tree neighbour mode runs without the learned proposal and trace");
+        if (c->scenes.size() != 1)
+            return fail(c, ECMG_ERR_STATE, "the kd-tree neighbour mode needs a single-scene context (one tree, one cache)");
         if (c->max_agents > (1 << 24)) return fail(c, ECMG_ERR_BOUND, "the kd-tree neighbour mode supports 2^24 slots");
         const size_t N = (size_t)c->max_agents;
         const int k = c->prm.max_neighbors;

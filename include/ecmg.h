@@ -340,7 +340,8 @@ ecmg_status ecmg_set_lp_mode(ecmg_ctx* ctx, int mode, int agents_per_warp_grab);
    Simulator::Update; agents whose x (or y) coordinates are equal keep the
    order of the level above (std::sort agrees on subtrees of up to 16 agents).
    neighbor_dist is not used.  Runs the per-agent kernel one thread per agent,
-   without the learned proposal or the trace; up to 2^24 slots. */
+   without the learned proposal or the trace; single-scene contexts, up to
+   2^24 slots. */
 #define ECMG_NEIGHBORS_EXACT 0
 #define ECMG_NEIGHBORS_KDTREE 1
 ecmg_status ecmg_set_neighbor_mode(ecmg_ctx* ctx, int mode);
