@@ -2337,6 +2337,235 @@ ecmg_status ecmg_set_state(ecmg_ctx* c, int field, const void* src)
     return ECMG_OK;
 }
 
+/* ---------------------------------------------------------------------- */
+/* Checkpoint / resume: a binary snapshot of everything a tick depends on.
+   Layout: "ECMGSNAP", version, sizes, then the sections in a fixed order
+   (device state as slot arrays, host mirrors, paths, per-scene bookkeeping
+   and areas, queued random values, neighbour cache, failed-search memo). */
+}  /* extern "C" */
+namespace {
+struct SnapWriter {
+    FILE* f;
+    bool ok = true;
+    template <class T>
+    void put(const T& v) { ok = ok && fwrite(&v, sizeof(T), 1, f) == 1; }
+    template <class T>
+    void arr(const T* p, size_t n)
+    {
+        put<unsigned long long>(n);
+        if (n) ok = ok && fwrite(p, sizeof(T), n, f) == n;
+    }
+};
+struct SnapReader {
+    FILE* f;
+    bool ok = true;
+    template <class T>
+    void get(T& v) { ok = ok && fread(&v, sizeof(T), 1, f) == 1; }
+    template <class T>
+    void arr(std::vector<T>& v, size_t expect = (size_t)-1)
+    {
+        unsigned long long n = 0;
+        get(n);
+        if (!ok || (expect != (size_t)-1 && n != expect) || n > (1ull << 34)) { ok = false; return; }
+        v.resize((size_t)n);
+        if (n) ok = ok && fread(v.data(), sizeof(T), (size_t)n, f) == n;
+    }
+};
+constexpr unsigned kSnapVersion = 1;
+}  // namespace
+extern "C" {
+
+ecmg_status ecmg_save_state(ecmg_ctx* c, const char* path)
+{
+    if (!c || !path) return ECMG_ERR_INVALID_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    const size_t N = (size_t)c->max_agents;
+    std::vector<V2> pos(N), vel(N), attr(N), pv(N);
+    CK(cudaMemcpy(pos.data(), c->pos.p, sizeof(V2) * N, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(vel.data(), c->vel.p, sizeof(V2) * N, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(attr.data(), c->attr.p, sizeof(V2) * N, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(pv.data(), c->pref_vel.p, sizeof(V2) * N, cudaMemcpyDeviceToHost));
+    std::vector<int> kd_cache;
+    if (c->nbr_mode == ECMG_NEIGHBORS_KDTREE) {
+        kd_cache.resize((size_t)c->prm.max_neighbors);
+        CK(cudaMemcpy(kd_cache.data(), c->kd.cache.p, sizeof(int) * kd_cache.size(), cudaMemcpyDeviceToHost));
+    }
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(c, ECMG_ERR_INVALID_ARG, "cannot write %s", path);
+    SnapWriter w{f};
+    fwrite("ECMGSNAP", 1, 8, f);
+    w.put(kSnapVersion);
+    w.put(c->max_agents);
+    w.put((int)c->scenes.size());
+    w.put(c->prm.max_neighbors);
+    w.put(c->nbr_mode);
+    w.put(c->num_agents);
+    w.arr(pos.data(), N);
+    w.arr(vel.data(), N);
+    w.arr(attr.data(), N);
+    w.arr(pv.data(), N);
+    w.arr(c->clear.data(), N);
+    w.arr(c->speed.data(), N);
+    w.arr(c->active.data(), N);
+    w.arr(c->fail_edge.data(), N);
+    std::vector<int> plen(N);
+    size_t total = 0;
+    for (size_t i = 0; i < N; i++) {
+        plen[i] = (int)c->paths[i].size();
+        total += c->paths[i].size();
+    }
+    std::vector<V2> pts;
+    pts.reserve(total);
+    for (size_t i = 0; i < N; i++) pts.insert(pts.end(), c->paths[i].begin(), c->paths[i].end());
+    w.arr(plen.data(), N);
+    w.arr(pts.data(), pts.size());
+    for (auto& scp : c->scenes) {
+        const SceneState* sc = scp.get();
+        w.put(sc->num_agents);
+        w.put(sc->last_idx);
+        w.arr(sc->free_stack.data(), sc->free_stack.size());
+        w.put(sc->next_spawn_id);
+        w.put(sc->next_goal_id);
+        w.put((int)sc->spawn_areas.size());
+        for (auto& kv : sc->spawn_areas) {
+            const SpawnAreaH& a = kv.second;
+            w.put(a.id); w.put(a.x); w.put(a.y); w.put(a.hw); w.put(a.hh); w.put(a.cfg);
+            w.arr(a.goals.data(), a.goals.size());
+            w.arr(a.rate.data(), a.rate.size());
+            w.arr(a.since.data(), a.since.size());
+        }
+        w.put((int)sc->goal_areas.size());
+        for (auto& kv : sc->goal_areas) {
+            const GoalAreaH& g = kv.second;
+            w.put(g.id); w.put(g.x); w.put(g.y); w.put(g.hw); w.put(g.hh);
+        }
+    }
+    w.arr(c->rq.data() + c->rq_head, c->rq.size() - c->rq_head);
+    w.put(c->rand_max);
+    w.arr(kd_cache.data(), kd_cache.size());
+    const bool ok = w.ok && fclose(f) == 0;
+    if (!ok) return fail(c, ECMG_ERR_INVALID_ARG, "writing %s failed", path);
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_load_state(ecmg_ctx* c, const char* path)
+{
+    if (!c || !path) return ECMG_ERR_INVALID_ARG;
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(c, ECMG_ERR_INVALID_ARG, "cannot read %s", path);
+    SnapReader r{f};
+    char magic[8] = {};
+    r.ok = fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "ECMGSNAP", 8) == 0;
+    unsigned ver = 0;
+    int n_slots = 0, n_scenes = 0, k = 0, mode = 0, num = 0;
+    r.get(ver); r.get(n_slots); r.get(n_scenes); r.get(k); r.get(mode); r.get(num);
+    if (!r.ok || ver != kSnapVersion || n_slots != c->max_agents || n_scenes != (int)c->scenes.size() ||
+        k != c->prm.max_neighbors) {
+        fclose(f);
+        return fail(c, ECMG_ERR_INVALID_ARG, "%s is not a snapshot of a context like this one", path);
+    }
+    const size_t N = (size_t)c->max_agents;
+    std::vector<V2> pos, vel, attr, pv, pts;
+    std::vector<float> clear, speed;
+    std::vector<unsigned char> active;
+    std::vector<int> fe, plen;
+    r.arr(pos, N); r.arr(vel, N); r.arr(attr, N); r.arr(pv, N);
+    r.arr(clear, N); r.arr(speed, N); r.arr(active, N); r.arr(fe, N);
+    r.arr(plen, N); r.arr(pts);
+    struct SceneSnap {
+        int num, last, next_spawn, next_goal;
+        std::vector<int> free_stack;
+        std::map<int, SpawnAreaH> spawn;
+        std::map<int, GoalAreaH> goal;
+    };
+    std::vector<SceneSnap> ss((size_t)n_scenes);
+    for (auto& q : ss) {
+        r.get(q.num); r.get(q.last);
+        r.arr(q.free_stack);
+        r.get(q.next_spawn); r.get(q.next_goal);
+        int ns = 0;
+        r.get(ns);
+        for (int i = 0; r.ok && i < ns; i++) {
+            SpawnAreaH a;
+            r.get(a.id); r.get(a.x); r.get(a.y); r.get(a.hw); r.get(a.hh); r.get(a.cfg);
+            r.arr(a.goals); r.arr(a.rate); r.arr(a.since);
+            if (a.rate.size() != a.since.size() || a.goals.size() > a.rate.size()) r.ok = false;
+            q.spawn.emplace(a.id, a);
+        }
+        int ng = 0;
+        r.get(ng);
+        for (int i = 0; r.ok && i < ng; i++) {
+            GoalAreaH g;
+            r.get(g.id); r.get(g.x); r.get(g.y); r.get(g.hw); r.get(g.hh);
+            q.goal.emplace(g.id, g);
+        }
+    }
+    std::vector<int> rq, kd_cache;
+    int rand_max = RAND_MAX;
+    r.arr(rq);
+    r.get(rand_max);
+    r.arr(kd_cache);
+    fclose(f);
+    size_t total = 0;
+    for (size_t i = 0; r.ok && i < N; i++) {
+        if (plen[i] < 0) r.ok = false;
+        total += (size_t)std::max(0, plen[i]);
+    }
+    if (!r.ok || total != pts.size() || (mode == ECMG_NEIGHBORS_KDTREE && (int)kd_cache.size() != k))
+        return fail(c, ECMG_ERR_INVALID_ARG, "%s is damaged", path);
+    /* the neighbour mode of the snapshot */
+    {
+        ecmg_status ms = ecmg_set_neighbor_mode(c, mode);
+        if (ms != ECMG_OK) return ms;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(c->pos.p, pos.data(), sizeof(V2) * N, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->vel.p, vel.data(), sizeof(V2) * N, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->attr.p, attr.data(), sizeof(V2) * N, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->pref_vel.p, pv.data(), sizeof(V2) * N, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->d_clear.p, clear.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->d_speed.p, speed.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->d_active.p, active.data(), N, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->d_fail_edge.p, fe.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    c->clear = clear;
+    c->speed = speed;
+    c->active = active;
+    c->fail_edge = fe;
+    c->num_agents = num;
+    size_t o = 0;
+    for (size_t i = 0; i < N; i++) {
+        c->paths[i].assign(pts.begin() + (std::ptrdiff_t)o, pts.begin() + (std::ptrdiff_t)(o + (size_t)plen[i]));
+        o += (size_t)plen[i];
+    }
+    /* every path again, packed (the compaction path of the path store) */
+    c->path_used = c->path_xy.n; /* forces the repack */
+    {
+        ecmg_status ps = ensure_path_room(c, 1);
+        if (ps != ECMG_OK) return ps;
+    }
+    for (size_t s = 0; s < ss.size(); s++) {
+        SceneState* sc = c->scenes[s].get();
+        sc->num_agents = ss[s].num;
+        sc->last_idx = ss[s].last;
+        sc->free_stack = ss[s].free_stack;
+        sc->next_spawn_id = ss[s].next_spawn;
+        sc->next_goal_id = ss[s].next_goal;
+        sc->spawn_areas = ss[s].spawn;
+        sc->goal_areas = ss[s].goal;
+        sc->grid_ready = false;
+        for (int i = sc->slot_base; i <= sc->last_idx; i++)
+            if (c->active[i]) note_range(c, sc, c->clear[i], c->speed[i]);
+    }
+    c->rq = rq;
+    c->rq_head = 0;
+    c->rand_max = rand_max;
+    if (mode == ECMG_NEIGHBORS_KDTREE)
+        CK(cudaMemcpy(c->kd.cache.p, kd_cache.data(), sizeof(int) * kd_cache.size(), cudaMemcpyHostToDevice));
+    c->table_dirty = true;
+    c->graph_dirty = true;
+    return ECMG_OK;
+}
+
 ecmg_status ecmg_get_counts(const ecmg_ctx* c, int* num_agents, int* last_index, int* max_agents)
 {
     if (!c) return ECMG_ERR_INVALID_ARG;

@@ -187,6 +187,14 @@ class Simulator:
     def destroy_agent(self, idx: int):
         self._ck(self.L.ecmg_destroy_agent(self.h, int(idx)))
 
+    def save_state(self, path: str):
+        """checkpoint (ecmg_save_state)"""
+        self._ck(self.L.ecmg_save_state(self.h, str(path).encode()))
+
+    def load_state(self, path: str):
+        """resume from a checkpoint of a context like this one (ecmg_load_state)"""
+        self._ck(self.L.ecmg_load_state(self.h, str(path).encode()))
+
     # ---- spawn and goal areas (Simulator.h:92-104) ----------------------
     def add_spawn_area(self, position, half_size, config: dict | None = None, ID: int = -1) -> int:
         """Simulator::AddSpawnArea (Simulator.cpp:336-360); config keys as

@@ -279,6 +279,16 @@ ecmg_status ecmg_host_view(ecmg_ctx* ctx, int field, const void** out);
    used to start a tick from a given state. */
 ecmg_status ecmg_set_state(ecmg_ctx* ctx, int field, const void* host_src);
 ecmg_status ecmg_get_counts(const ecmg_ctx* ctx, int* num_agents, int* last_index, int* max_agents);
+/* Checkpoint / resume (no reference counterpart): everything the following
+   ticks depend on -- agent state, paths, free-slot stacks, spawn and goal
+   areas with their timers, queued random values, the kd-tree mode's
+   neighbour cache, the failed-search memo -- to a binary file, and back
+   into a context created with the same slot capacity, scene count,
+   max_neighbors and scene.  Ticks after a load reproduce the ticks after the
+   save bit for bit.  The random source set by ecmg_set_spawn_rng, the
+   planner and the launch configuration are not part of a snapshot. */
+ecmg_status ecmg_save_state(ecmg_ctx* ctx, const char* path);
+ecmg_status ecmg_load_state(ecmg_ctx* ctx, const char* path);
 ecmg_status ecmg_get_path(ecmg_ctx* ctx, int slot, float* out_xy, int cap, int* out_n);
 
 /* Record per-agent results of the following ticks for inspection:
