@@ -227,7 +227,7 @@ class TickTimer:
         self.tot = dict(lp3d=0, replans=0, replans_failed=0, replans_host=0, destroyed=0, device_ms=0.0, host_ms=0.0,
                         proposed=0, accepted=0, gated=0, attract_ms=0.0, neighbors_ms=0.0, proposal_ms=0.0,
                         orca_ms=0.0, spawned=0, spawn_failed=0, spawn_refused=0, spawn_ms=0.0, spawn_check_ms=0.0,
-                        spawn_candidates=0, graph_builds=0)
+                        spawn_candidates=0, graph_builds=0, spawn_kernels=0)
 
     def tick(self):
         import torch
@@ -397,10 +397,10 @@ def run_ours(args):
         except (OSError, ValueError, AttributeError):
             traffic = None
     T = main_t.tot
-    launches = plain.L.ecmg_kernels_per_tick(plain.h) * args.steps
+    launches = plain.L.ecmg_kernels_per_tick(plain.h) * args.steps + tp.tot["spawn_kernels"]
     if model is not None:
         launches += learned.L.ecmg_kernels_per_tick(learned.h) * (args.steps - T["gated"]) + \
-            plain.L.ecmg_kernels_per_tick(plain.h) * T["gated"]
+            plain.L.ecmg_kernels_per_tick(plain.h) * T["gated"] + tl.tot["spawn_kernels"]
     out = {
         "metric": "agent-steps/s at 1M agents: learned-proposal vs plain GPU ORCA; ms/tick",
         "value": value, "unit": "agent-steps/s",

@@ -42,7 +42,7 @@ class TickStats(C.Structure):
                 ("attract_ms", C.c_float), ("neighbors_ms", C.c_float), ("proposal_ms", C.c_float),
                 ("orca_ms", C.c_float), ("spawned", C.c_longlong), ("spawn_failed", C.c_longlong),
                 ("spawn_refused", C.c_longlong), ("spawn_ms", C.c_float), ("spawn_check_ms", C.c_float),
-                ("spawn_candidates", C.c_longlong), ("graph_builds", C.c_int)]
+                ("spawn_candidates", C.c_longlong), ("graph_builds", C.c_int), ("spawn_kernels", C.c_int)]
 
 
 class SpawnConfig(C.Structure):

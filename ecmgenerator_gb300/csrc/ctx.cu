@@ -1081,6 +1081,7 @@ static ecmg_status spawn_check(ecmg_ctx* c, SceneState* sc, const SpawnWindow& w
         if (cs != ECMG_OK) return cs;
     }
     st.spawn_candidates += (long long)nc;
+    st.spawn_kernels++;
     st.spawn_check_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - h0).count();
     return ECMG_OK;
 }
@@ -1291,6 +1292,7 @@ static ecmg_status spawn_stage(ecmg_ctx* c, ecmg_tick_stats& st)
         }
         ecmg_status ps = place_agents(c, sc, picks, paths);
         if (ps != ECMG_OK) return ps;
+        if (!picks.empty()) st.spawn_kernels++;
         st.spawned += (long long)picks.size();
         st.spawn_failed += failed;
         st.spawn_refused += refused;

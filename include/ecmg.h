@@ -87,6 +87,7 @@ typedef struct {
     float spawn_check_ms;    /* of which the location tests on the device (copies and wait included) */
     long long spawn_candidates; /* candidate locations tested on the device      */
     int graph_builds;        /* tick graphs captured and instantiated (host time; after launch-configuration, mode or path-store changes) */
+    int spawn_kernels;       /* kernel launches of the spawn stage (location checks, placement) */
 } ecmg_tick_stats;
 
 /* Static obstacles: n_obstacles rings, ring r = xy[2*ring_offsets[r] ..
