@@ -30,6 +30,9 @@ import time
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+from ecmgenerator_gb300.workloads import DT, ORCA, WORKLOADS  # noqa: E402
 
 
 def KD_BYTES_PER_AGENT(k, levels=20):
@@ -39,10 +42,6 @@ def KD_BYTES_PER_AGENT(k, levels=20):
     scan / partition 95 (level 0 partitions two lists, +61), query 12 + 4k,
     composition 2 + 8k, emission 14 + 17k"""
     return 532 + 95 * levels + 29 * k
-sys.path.insert(0, HERE)
-
-from ecmgenerator_gb300.workloads import DT, ORCA, WORKLOADS  # noqa: E402
-
 
 
 def log(*a):
@@ -263,19 +262,43 @@ def run_ours(args):
     from ecmgenerator_gb300.simulator import Simulator
     from ecmgenerator_gb300.workloads import add_spawn_areas
 
-    cfg, scene, st, paths, k = make_workload(args.workload, args.seed)
-    n = st.num_agents
+    batch = WORKLOADS[args.workload].get("batch")
+    if batch:
+        if args.spawn_rate > 0 or args.neighbors != "exact":
+            raise SystemExit("batch workloads run the exact neighbour mode without spawn areas")
+        from ecmgenerator_gb300.simulator import BatchSimulator
+        from ecmgenerator_gb300.workloads import make_batch_workload
+
+        cfgs, scenes, states, pathss, k = make_batch_workload(args.workload, args.seed)
+        n = sum(x.num_agents for x in states)
+        big = int(np.argmax([x.num_agents for x in states]))
+        # the CPU baseline samples the largest scene
+        cfg, scene, st, paths = cfgs[big], scenes[big], states[big], pathss[big]
+        scene_desc = (f"{len(scenes)} independent scenes, side U[50,500] m, side/5 boxes of side U[2,8] m, "
+                      f"{min(x.num_agents for x in states)}-{max(x.num_agents for x in states)} agents per scene")
+        sims = []
+        for _ in range(2):
+            s_ = BatchSimulator(scenes, [x.num_agents for x in states], DT, max_neighbors=k, **ORCA)
+            for i, x in enumerate(states):
+                m = x.num_agents
+                s_.add_agents(x.pos[:m], x.clear[:m], x.pref_speed[:m], pathss[i], scene=i)
+            sims.append(s_)
+        spawn_slots = 0
+    else:
+        cfg, scene, st, paths, k = make_workload(args.workload, args.seed)
+        n = st.num_agents
+        scene_desc = f'{cfg["w"]:.0f}x{cfg["h"]:.0f} m, {cfg["boxes"]} boxes'
+        sims = []
+        spawn_slots = 0
     # two simulators in the same state: the plain tick and the tick with the
     # learned proposal (their trajectories are identical)
-    sims = []
-    spawn_slots = 0
     if args.spawn_rate > 0:
         # room for the spawned agents; every simulator draws the same
         # recorded random stream (the C library's rand() is shared)
         spawn_slots = min(200_000, int(args.spawn_rate * DT * 4 * 2000) + 1024)
         stream = np.random.default_rng(args.seed + 99).integers(
             0, 2147483647, 33 * (int(args.spawn_rate * DT) + 1) * 4 * 4000, dtype=np.int32)
-    for _ in range(2):
+    for _ in range(0 if batch else 2):
         s_ = Simulator(scene, n + spawn_slots, DT, max_neighbors=k, **ORCA)
         s_.add_agents(st.pos[:n], st.clear[:n], st.pref_speed[:n], paths)
         if args.spawn_rate > 0:
@@ -408,7 +431,7 @@ def run_ours(args):
         "ms_per_step": ms_all / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded scene, agents and paths)",
         "config": {"workload": args.workload, "agents": n, "max_neighbors": k, "neighbor_dist_m": 5.0,
-                   "time_horizon_s": 2.0, "dt_s": DT, "scene": f'{cfg["w"]:.0f}x{cfg["h"]:.0f} m, {cfg["boxes"]} boxes',
+                   "time_horizon_s": 2.0, "dt_s": DT, "scene": scene_desc,
                    "l2": "flushed before every timed tick (512 MB write)", "parallelism": f"replicas x{world}",
                    "seed": args.seed, "mode": "learned proposal" if model is not None else "plain",
                    "neighbors": args.neighbors,

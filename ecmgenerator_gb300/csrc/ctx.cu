@@ -257,8 +257,8 @@ struct ecmg_ctx {
        device time per agent exceeds that of the plain tick by 2 %, pauses
        the model for gate_pause ticks (plain ticks), then it is tried again.
        The per-agent times are running averages of the ticks with and
-       without the model; without a plain time yet, 8 model ticks are
-       followed by 8 plain ones to measure it. */
+       without the model; without a plain time yet, 3 model ticks are
+       followed by 3 plain ones to measure it. */
     float gate_min = 0.1f;
     int gate_pause = 64;
     int gate_left = 0;
@@ -2014,15 +2014,15 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         if (c->model && c->gate_min > 0.0f && out[C_NSORTED] > 0 && tot > 0.0f) {
             const float per = tot / (float)out[C_NSORTED];
             float& avg = use_model ? c->gate_t_model : c->gate_t_plain;
-            avg = avg < 0.0f ? per : 0.75f * avg + 0.25f * per;
+            avg = avg < 0.0f ? per : 0.5f * avg + 0.5f * per;
         }
         if (use_model && c->gate_min > 0.0f) {
             c->gate_model_ticks++;
             if ((float)out[C_ACCEPTED] < c->gate_min * (float)out[C_NSORTED])
                 c->gate_left = c->gate_pause;
-            else if (c->gate_t_plain < 0.0f && c->gate_model_ticks >= 8)
-                c->gate_left = 8; /* measure the plain tick */
-            else if (c->gate_t_plain > 0.0f && c->gate_model_ticks >= 4 && c->gate_t_model > 1.02f * c->gate_t_plain)
+            else if (c->gate_t_plain < 0.0f && c->gate_model_ticks >= 3)
+                c->gate_left = 3; /* measure the plain tick */
+            else if (c->gate_t_plain > 0.0f && c->gate_model_ticks >= 2 && c->gate_t_model > 1.02f * c->gate_t_plain)
                 c->gate_left = c->gate_pause;
             if (c->gate_left > 0) c->gate_model_ticks = 0;
         }

@@ -7,6 +7,10 @@
     boxes_100k     1000x1000 m, 4,000 boxes of side U[2,8] m, 100,000 agents
                    spawned without overlap, goals uniform in free space, k = 10
     boxes_1k       100x100 m, 40 boxes, 1,000 agents, k = 10
+    batch_256      256 independent scenes in one context: side U[50,500] m,
+                   side/5 boxes of side U[2,8] m, agents per scene log-uniform
+                   in [200, 20,000] scaled to 1.3M in total (overlap allowed
+                   where a scene is dense), goals uniform in free space, k = 10
 
 Radius U[0.2,0.35] m, preferred speed U[1.2,1.5] m/s, ORCA time horizons
 2 s, neighbour distance 5 m, dt = 1/60 s.
@@ -23,6 +27,7 @@ WORKLOADS = {
     "crossing_100k": dict(cfg="c3", agents=100_000, k=16),
     "boxes_100k": dict(cfg="c2", agents=100_000, k=10),
     "boxes_1k": dict(cfg="c1", agents=1_000, k=10),
+    "batch_256": dict(batch=256, agents=1_300_000, k=10),
 }
 ORCA = dict(tau_agent=2.0, tau_obst=2.0, neighbor_dist=5.0)
 DT = 1.0 / 60.0
@@ -102,3 +107,48 @@ def add_spawn_areas(sim, scene, rate, n_areas=4, half=2.5, clearance=0.3, speed=
         sim.connect_spawn_goal_areas(s, g, float(rate))
         ids.append(s)
     return ids
+
+
+def _batch_scene(job):
+    """one scene of a batch workload (runs in a worker process)"""
+    from . import agents as ag
+    from .simulator import Planner
+
+    side, n, seed = job
+    dense = n * np.pi * 0.275 ** 2 > 0.3 * side * side
+    cfg = dict(w=side, h=side, boxes=int(side // 5), side=(2.0, 8.0), agents=n, k=10, overlap=bool(dense),
+               h_ecm=0.25)
+    scene = ag.build_scene(cfg, seed)
+    st = ag.spawn_agents(cfg, scene, seed)
+    pl = Planner(scene)
+    got = pl.find_paths(st.pos[:n], st.goal[:n], st.clear[:n], threads=1, cap=64)
+    pl.close()
+    paths = [np.asarray(p if p is not None else np.stack([st.pos[i], st.goal[i]]), np.float32)
+             for i, p in enumerate(got)]
+    st.set_paths(paths)
+    return cfg, scene, st, paths
+
+
+def make_batch_workload(name, seed, procs=None, verbose=True):
+    """(cfgs, scenes, agent states, paths per scene, k) of a batch workload;
+    the scenes are built on worker processes (spawned: safe before and after
+    CUDA initialisation)"""
+    import multiprocessing as mp
+    import os
+
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(seed)
+    n_sc = w["batch"]
+    sides = rng.uniform(50.0, 500.0, n_sc)
+    counts = np.exp(rng.uniform(np.log(200.0), np.log(20000.0), n_sc))
+    counts = np.maximum(200, np.round(counts * w["agents"] / counts.sum())).astype(int)
+    jobs = [(float(sides[i]), int(counts[i]), int(seed * 100003 + i)) for i in range(n_sc)]
+    t0 = time.time()
+    procs = procs or max(1, min(32, os.cpu_count() or 1))
+    with mp.get_context("spawn").Pool(procs) as pool:
+        res = pool.map(_batch_scene, jobs, chunksize=1)
+    if verbose:
+        print(f"[workload] {name}: {n_sc} scenes, {int(counts.sum())} agents, setup {time.time() - t0:.1f}s "
+              f"on {procs} processes", file=sys.stderr, flush=True)
+    cfgs, scenes, states, paths = zip(*res)
+    return list(cfgs), list(scenes), list(states), list(paths), w["k"]

@@ -436,7 +436,7 @@ ecmg_status ecmg_set_proposal(ecmg_ctx* ctx, ecmg_mlp* model);
 /* Gate of the learned mode: a tick whose accepted proposals are fewer than
    min_accept_rate x its agents, or whose device time per agent exceeds the
    plain tick's by more than 2 % (running averages of both kinds of tick; the
-   plain time is measured by 8 plain ticks after the first 8 model ticks),
+   plain time is measured by 3 plain ticks after the first 3 model ticks),
    runs the next pause_ticks ticks without the model (no features, no
    inference), then tries it again.  Default 0.1 / 64; min_accept_rate 0
    keeps the model on every tick. */
