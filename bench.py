@@ -411,12 +411,17 @@ def run_ours(args):
     alg_bytes = kern[kname][1]
     achieved = alg_bytes * per_tick / (kern_ms / 1e3) / 1e9 if kern_ms > 0 else 0.0
     traffic = None
+    limiter = None
     tf = os.path.join(HERE, "profiles", "kernel_traffic.json")
     if os.path.exists(tf):
         try:
-            t = json.load(open(tf)).get(kname, {}).get(args.workload)
+            rec = json.load(open(tf)).get(kname, {})
+            t = rec.get(args.workload)
             if t:
                 traffic = t * per_tick
+            # the pipe that bounds the kernel in its ncu capture (neither kernel
+            # streams memory, so the HBM fraction alone does not name the bound)
+            limiter = rec.get("limiter")
         except (OSError, ValueError, AttributeError):
             traffic = None
     T = main_t.tot
@@ -451,6 +456,7 @@ def run_ours(args):
         "e2e": e2e_main,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": kname, "kernel_ms": kern_ms, "alg_bytes_per_agent": alg_bytes,
+                     "limiter": limiter,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
                      "kernel_ms_per_tick": {"k_attract": main_t.tot["attract_ms"] / args.steps,
                                             "k_neighbors": main_t.tot["neighbors_ms"] / args.steps,
