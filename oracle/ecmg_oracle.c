@@ -817,6 +817,31 @@ static void* orca_thread(void* arg)
     return NULL;
 }
 
+/* one agent of UpdateAttractionPointSystem (Simulator.cpp:538-590): writes
+   the attraction point to *attr (left as it is when the IRM query fails);
+   returns 0, 1 when the agent is to be destroyed, 2 when it needs a replan */
+static int attract_one(const og_ecm* e, const og_state* s, const og_params* p, int i, og_v2* attr)
+{
+    const float delSq = p->delete_radius * p->delete_radius;
+    const float arrSq = p->arrival_radius * p->arrival_radius;
+    const og_v2* path = s->path_xy + s->path_off[i];
+    int np = s->path_len[i];
+    og_v2 pos = s->pos[i];
+    og_v2 g = path[np - 1];
+    float dx = pos.x - g.x, dy = pos.y - g.y; /* SquareDistance(x0,y0,x1,y1) */
+    float dist = dx * dx + dy * dy;
+    if (dist < arrSq) {
+        *attr = g;
+        return dist < delSq ? 1 : 0;
+    }
+    og_v2 ap = v2(0.0f, 0.0f); /* Point attractionPoint; */
+    if (og_irm(e, pos, path, np, &ap)) {
+        *attr = ap;
+        return 0;
+    }
+    return 2;
+}
+
 int og_tick(const og_obstacles* o, const og_ecm* e, og_state* s, const og_params* p,
             og_kdtree* kd, og_tick_out* out)
 {
@@ -841,35 +866,20 @@ int og_tick(const og_obstacles* o, const og_ecm* e, og_state* s, const og_params
     if (out) { out->n_destroyed = 0; out->n_replan = 0; out->n_lp3d = 0; }
 
     /* UpdateAttractionPointSystem (Simulator.cpp:538-590) */
-    const float delSq = p->delete_radius * p->delete_radius;
-    const float arrSq = p->arrival_radius * p->arrival_radius;
     for (int i = 0; i <= last; i++) {
         if (!s->active[i]) continue;
-        const og_v2* path = s->path_xy + s->path_off[i];
-        int np = s->path_len[i];
-        og_v2 pos = s->pos[i];
-        og_v2 g = path[np - 1];
-        float dx = pos.x - g.x, dy = pos.y - g.y; /* SquareDistance(x0,y0,x1,y1) */
-        float dist = dx * dx + dy * dy;
-        if (dist < arrSq) {
-            s->attr[i] = g;
-            if (dist < delSq) { /* DestroyAgent (Simulator.cpp:202-208) */
-                s->num_agents--;
-                s->active[i] = 0;
-                if (out) {
-                    if (out->destroyed) out->destroyed[out->n_destroyed] = i;
-                    out->n_destroyed++;
-                }
+        int r = attract_one(e, s, p, i, &s->attr[i]);
+        if (r == 1) { /* DestroyAgent (Simulator.cpp:202-208) */
+            s->num_agents--;
+            s->active[i] = 0;
+            if (out) {
+                if (out->destroyed) out->destroyed[out->n_destroyed] = i;
+                out->n_destroyed++;
             }
-        } else {
-            og_v2 ap = v2(0.0f, 0.0f); /* Point attractionPoint; */
-            if (og_irm(e, pos, path, np, &ap)) {
-                s->attr[i] = ap;
-            } else if (out) {
-                if (out->replan) out->replan[out->n_replan] = i;
-                if (out->replan_pos) out->replan_pos[out->n_replan] = pos;
-                out->n_replan++;
-            }
+        } else if (r == 2 && out) {
+            if (out->replan) out->replan[out->n_replan] = i;
+            if (out->replan_pos) out->replan_pos[out->n_replan] = s->pos[i];
+            out->n_replan++;
         }
     }
 
@@ -1046,3 +1056,90 @@ int og_time_sample(const og_obstacles* o, const og_ecm* e, const og_state* s, co
 /* the shared transcendentals, exported for their accuracy tests */
 float og_test_atanf(float x) { return ecmg_atanf(x); }
 void og_test_sincosf(float a, float* s, float* c) { ecmg_sincosf(a, s, c); }
+
+/* ---------------------------------------------------------------------------
+ * One tick for a sample of agents (see ecmg_oracle.h)
+ * ------------------------------------------------------------------------- */
+typedef struct {
+    const og_obstacles* o;
+    const og_ecm* e;
+    const og_state* s;
+    const og_params* p;
+    const int* sample;
+    og_sample_out* out;
+    int lo, hi;
+} og_tjob;
+
+static void* tick_sample_thread(void* arg)
+{
+    og_tjob* j = (og_tjob*)arg;
+    const og_state* s = j->s;
+    const og_params* p = j->p;
+    og_sample_out* out = j->out;
+    int k = p->k;
+    int* ids = (int*)malloc(sizeof(int) * (size_t)(k > 0 ? k : 1));
+    float* d2 = (float*)malloc(sizeof(float) * (size_t)(k > 0 ? k : 1));
+    const float r2 = p->neighbor_dist * p->neighbor_dist;
+    const float massRecip = 1.0f / p->mass;
+    for (int q = j->lo; q < j->hi; q++) {
+        int i = j->sample[q];
+        for (int c = 0; c < k; c++) out->nbr_ids[(size_t)q * k + c] = -1;
+        out->nbr_count[q] = 0;
+        if (i < 0 || i > s->last_idx || !s->active[i]) {
+            out->status[q] = 3;
+            continue;
+        }
+        og_v2 attr = s->attr[i];
+        int r = attract_one(j->e, s, p, i, &attr);
+        out->attr[q] = attr;
+        out->status[q] = (unsigned char)r;
+        if (r == 1) continue;
+        /* ApplySteeringForce (Simulator.cpp:638-657) */
+        og_v2 pv = vmul(vnormalize(vsub(attr, s->pos[i])), s->pref_speed[i]);
+        /* ApplyObstacleAvoidanceForce: neighbours among the agents active at
+           the start of the tick */
+        int nn = og_knn_exact(s, i, k, r2, ids, d2);
+        og_v2 v;
+        int nob = 0, fail = 0;
+        og_orca_velocity(j->o, s, p, i, ids, nn, pv, &v, &nob, &fail);
+        for (int c = 0; c < nn; c++) out->nbr_ids[(size_t)q * k + c] = ids[c];
+        out->nbr_count[q] = nn;
+        out->v_orca[q] = v;
+        /* UpdateVelocitySystem, UpdatePositionSystem */
+        og_v2 vel = s->vel[i];
+        float fx = v.x - vel.x;
+        float fy = v.y - vel.y;
+        vel.x += fx * massRecip * p->dt;
+        vel.y += fy * massRecip * p->dt;
+        og_v2 pos = s->pos[i];
+        pos.x += (vel.x * p->dt);
+        pos.y += (vel.y * p->dt);
+        out->vel[q] = vel;
+        out->pos[q] = pos;
+    }
+    free(ids);
+    free(d2);
+    return NULL;
+}
+
+int og_tick_sample(const og_obstacles* o, const og_ecm* e, const og_state* s, const og_params* p,
+                   const int* sample, int n_sample, int threads, og_sample_out* out)
+{
+    int th = threads > 1 ? threads : 1;
+    og_tjob* jobs = (og_tjob*)calloc((size_t)th, sizeof(og_tjob));
+    pthread_t* tid = (pthread_t*)calloc((size_t)th, sizeof(pthread_t));
+    int span = (n_sample + th - 1) / th;
+    for (int t = 0; t < th; t++) {
+        jobs[t].o = o; jobs[t].e = e; jobs[t].s = s; jobs[t].p = p;
+        jobs[t].sample = sample;
+        jobs[t].out = out;
+        jobs[t].lo = t * span < n_sample ? t * span : n_sample;
+        jobs[t].hi = (t + 1) * span < n_sample ? (t + 1) * span : n_sample;
+    }
+    for (int t = 1; t < th; t++) pthread_create(&tid[t], NULL, tick_sample_thread, &jobs[t]);
+    tick_sample_thread(&jobs[0]);
+    for (int t = 1; t < th; t++) pthread_join(tid[t], NULL);
+    free(jobs);
+    free(tid);
+    return 0;
+}

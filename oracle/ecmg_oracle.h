@@ -143,6 +143,28 @@ int og_tick(const og_obstacles* o, const og_ecm* e, og_state* s, const og_params
 int og_time_sample(const og_obstacles* o, const og_ecm* e, const og_state* s, const og_params* p,
                    const int* sample, int n_sample, int threads, double* t_build, double* t_agents);
 
+/* One Simulator::Update (exact-kNN mode) for the n_sample listed agents only,
+   from the state at the start of the tick, on `threads` host threads; the
+   state is not modified.  For sample q: status[q] = 0 (updated), 1 (destroyed
+   by the attraction stage), 2 (updated, re-plan flagged) or 3 (not active);
+   attr[q] the attraction point after the attraction stage; nbr_ids[q * k ..]
+   (-1 padded) and nbr_count[q] its neighbours among the agents active at the
+   start of the tick; v_orca[q], vel[q], pos[q] the LP result and the new
+   velocity and position.  For parity checks at sizes where a whole-tick
+   oracle run would take minutes. */
+typedef struct {
+    unsigned char* status;
+    og_v2* attr;
+    int* nbr_ids;
+    int* nbr_count;
+    og_v2* v_orca;
+    og_v2* vel;
+    og_v2* pos;
+} og_sample_out;
+
+int og_tick_sample(const og_obstacles* o, const og_ecm* e, const og_state* s, const og_params* p,
+                   const int* sample, int n_sample, int threads, og_sample_out* out);
+
 #ifdef __cplusplus
 }
 #endif

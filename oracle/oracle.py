@@ -76,6 +76,11 @@ class TickOut(C.Structure):
                 ("n_obst_constraints", C.c_void_p), ("lp_fail", C.c_void_p), ("n_lp3d", C.c_int)]
 
 
+class SampleOut(C.Structure):
+    _fields_ = [("status", C.c_void_p), ("attr", C.c_void_p), ("nbr_ids", C.c_void_p), ("nbr_count", C.c_void_p),
+                ("v_orca", C.c_void_p), ("vel", C.c_void_p), ("pos", C.c_void_p)]
+
+
 def _addr(a):
     return a.ctypes.data if a is not None else None
 
@@ -199,6 +204,23 @@ class Port:
 
     def kdtree(self, k):
         return self.lib.og_kdtree_create(k)
+
+    def tick_sample(self, obst_s, ecm_s, st, params, sample, threads=1):
+        """One exact-kNN tick for the listed slots only, from ``st`` (not
+        modified); see og_tick_sample.  Returns a dict of per-sample arrays."""
+        L = self.lib
+        L.og_tick_sample.argtypes = [C.POINTER(Obst), C.POINTER(EcmS), C.POINTER(State), C.POINTER(Params),
+                                     C.c_void_p, C.c_int, C.c_int, C.POINTER(SampleOut)]
+        sample = np.ascontiguousarray(sample, I32)
+        m, k = int(sample.shape[0]), max(int(params.k), 1)
+        res = dict(status=np.zeros(m, U8), attr=np.zeros((m, 2), F32), nbr_ids=np.full((m, k), -1, I32),
+                   nbr_count=np.zeros(m, I32), v_orca=np.zeros((m, 2), F32), vel=np.zeros((m, 2), F32),
+                   pos=np.zeros((m, 2), F32))
+        out = SampleOut(*[_addr(res[f]) for f in ("status", "attr", "nbr_ids", "nbr_count", "v_orca", "vel", "pos")])
+        s = self.state(st)
+        L.og_tick_sample(C.byref(obst_s), C.byref(ecm_s), C.byref(s), C.byref(params), _addr(sample), m,
+                         int(threads), C.byref(out))
+        return res
 
     def time_sample(self, obst_s, ecm_s, st, params, sample, threads=1):
         """Seconds spent building the kd-tree and running the per-agent tick
