@@ -1,6 +1,8 @@
 """Parity at the workloads' full sizes: the 1M-agent crossing (four flows of
-250k, k = 16) and the 100k-agent 1000 m box scene (k = 10).  A whole-tick
-oracle run takes tens of seconds there, so every tick is checked two ways:
+250k, k = 16) and the 100k-agent 1000 m box scene (k = 10), 600 ticks each.
+A whole-tick oracle run takes tens of seconds there, so the GPU runs the 600
+ticks and six of them (the first three, ticks 100, 300 and 599) are checked
+two ways:
 
 * 2,000 random agents against the oracle's sampled tick (og_tick_sample),
   started from the GPU's own tick-start state and paths: attraction point,
@@ -76,10 +78,15 @@ def test_full_size_ticks_match_the_oracle(port, name):
     r2 = np.float32(ORCA["neighbor_dist"]) * np.float32(ORCA["neighbor_dist"])
     rng = np.random.default_rng(11)
     checked = entries = 0
-    for t in range(3):
+    check = {0, 1, 2, 100, 300, 599}
+    for t in range(600):
+        if t not in check:
+            sim.update()
+            continue
         act0 = sim.get_active_flags().astype(bool)
         pos0 = sim.get_position_data().copy()
-        sample = np.sort(rng.choice(np.nonzero(act0)[0], 2000, replace=False)).astype(np.int32)
+        alive = np.nonzero(act0)[0]
+        sample = np.sort(rng.choice(alive, min(2000, len(alive)), replace=False)).astype(np.int32)
         cur = _oracle_view(st, sim, sample)
         want = port.tick_sample(O, E, cur, P, sample, threads=16)
         sim.update()
@@ -100,4 +107,93 @@ def test_full_size_ticks_match_the_oracle(port, name):
         entries += _list_properties(rec["nbr_ids"], rec["nbr_count"], pos0, act0, live, r2)
         checked += len(keep)
     sim.close()
-    assert checked > 5000 and entries > 0
+    assert checked > 10000 and entries > 0
+
+
+def test_full_size_batch_matches_the_oracle(port):
+    """the 256-scene batch (1.3M agents, one context, one graph per tick):
+    sampled agents of 16 scenes (the largest and the smallest among them)
+    against the oracle's sampled tick of their own scene; every agent's
+    neighbours from its own scene"""
+    from ecmgenerator_gb300.simulator import BatchSimulator
+    from ecmgenerator_gb300.workloads import DT, ORCA, make_batch_workload
+
+    cfgs, scenes, states, pathss, k = make_batch_workload("batch_256", 1, verbose=False)
+    caps = [st.num_agents for st in states]
+    sim = BatchSimulator(scenes, caps, DT, max_neighbors=k, **ORCA)
+    sim.set_record(True)
+    bases = []
+    for i, st in enumerate(states):
+        m = st.num_agents
+        sim.add_agents(st.pos[:m], st.clear[:m], st.pref_speed[:m], pathss[i], scene=i)
+        bases.append(sim.scene_counts(i)["slot_base"])
+    bases = np.array(bases)
+    assert np.array_equal(bases, np.concatenate([[0], np.cumsum(caps)[:-1]]))
+    scene_of = np.repeat(np.arange(len(caps)), caps)
+    P = port.params(k=k, libm=0, **ORCA)
+    r2 = np.float32(ORCA["neighbor_dist"]) * np.float32(ORCA["neighbor_dist"])
+    rng = np.random.default_rng(5)
+    order = np.argsort(caps)
+    picks = np.unique(np.concatenate([order[:2], order[-2:], rng.choice(len(caps), 12, replace=False)]))
+    OE = {int(i): (port.obstacles(scenes[i]), port.ecm(scenes[i].ecm)) for i in picks}
+    checked = 0
+    check = {0, 1, 2, 100, 300, 599}
+
+    class View:  # one scene's slice of the batch, with scene-local slots
+        def __init__(self, b, n):
+            self.b, self.n = b, n
+
+        def get_position_data(self):
+            return sim.get_position_data()[self.b:self.b + self.n]
+
+        def get_velocity_data(self):
+            return sim.get_velocity_data()[self.b:self.b + self.n]
+
+        def get_attraction_point_data(self):
+            return sim.get_attraction_point_data()[self.b:self.b + self.n]
+
+        def get_active_flags(self):
+            return sim.get_active_flags()[self.b:self.b + self.n]
+
+        def get_path(self, s):
+            return sim.get_path(self.b + s)
+
+    for t in range(600):
+        if t not in check:
+            sim.update()
+            continue
+        act0 = sim.get_active_flags().astype(bool)
+        pos0 = sim.get_position_data().copy()
+        want = {}
+        for i in picks.tolist():
+            b, n = int(bases[i]), caps[i]
+            alive = np.nonzero(act0[b:b + n])[0]
+            sample = np.sort(rng.choice(alive, min(200, len(alive)), replace=False)).astype(np.int32)
+            cur = _oracle_view(states[i], View(b, n), sample)
+            want[i] = (sample, port.tick_sample(*OE[i], cur, P, sample, threads=16))
+        sim.update()
+        rec = sim.get_record()
+        act1 = sim.get_active_flags()
+        pos1, vel1 = sim.get_position_data(), sim.get_velocity_data()
+        for i, (sample, w) in want.items():
+            b = int(bases[i])
+            gone = w["status"] == 1
+            g = b + sample
+            assert (act1[g[gone]] == 0).all() and (act1[g[~gone]] == 1).all(), (t, i)
+            keep = g[~gone]
+            nb = rec["nbr_ids"][keep].copy()
+            nb[nb >= 0] -= b  # global -> scene-local slots
+            assert np.array_equal(rec["nbr_count"][keep], w["nbr_count"][~gone]), (t, i)
+            assert np.array_equal(nb, w["nbr_ids"][~gone]), (t, i)
+            assert np.array_equal(rec["v_orca"][keep], w["v_orca"][~gone]), (t, i)
+            assert np.array_equal(vel1[keep], w["vel"][~gone]), (t, i)
+            assert np.array_equal(pos1[keep], w["pos"][~gone]), (t, i)
+            checked += len(keep)
+        live = (act0 == 1) & (act1 == 1)
+        _list_properties(rec["nbr_ids"], rec["nbr_count"], pos0, act0, live, r2)
+        ids, cnt = rec["nbr_ids"][live], rec["nbr_count"][live]
+        own = scene_of[np.nonzero(live)[0]]
+        filled = np.arange(k)[None, :] < cnt[:, None]
+        assert (scene_of[np.where(filled, ids, 0)] == own[:, None])[filled].all(), "neighbour from another scene"
+    sim.close()
+    assert checked > 5000
