@@ -2,8 +2,8 @@
  * ecmg_oracle.c -- CPU oracle (test infrastructure, see ecmg_oracle.h).
  *
  * Each function restates one reference function; the comment above it gives
- * the file:line it follows.  Operand order of every float expression is the
- * reference's; build with -ffp-contract=off.
+ * the file:line it follows.  Operand order of every arithmetic expression is
+ * the reference's; build with -ffp-contract=off.
  */
 #define _POSIX_C_SOURCE 200809L
 #include "ecmg_oracle.h"
@@ -15,27 +15,49 @@
 #include <stdlib.h>
 #include <string.h>
 
+#ifdef OG_REAL_DOUBLE
+#define og_sqrt sqrt
+#define og_fabs fabs
+#define og_fmax fmax
+#define og_fmin fmin
+#define og_atan atan
+#define og_sin sin
+#define og_cos cos
+#define og_pow pow
+#define OG_REAL_MAX DBL_MAX
+#else
+#define og_sqrt sqrtf
+#define og_fabs fabsf
+#define og_fmax fmaxf
+#define og_fmin fminf
+#define og_atan atanf
+#define og_sin sinf
+#define og_cos cosf
+#define og_pow powf
+#define OG_REAL_MAX FLT_MAX
+#endif
+
 #define OG_EPS 0.0001f /* Utility::EPSILON, ECMGenerator/Configuration.h:14 */
 
 /* ---------------------------------------------------------------------------
  * Vec2 / Point algebra, ECMGenerator/ECMDataTypes.h:13-104 and
  * MathUtility, ECMGenerator/UtilityFunctions.cpp:15-349
  * ------------------------------------------------------------------------- */
-static inline og_v2 v2(float x, float y) { og_v2 r; r.x = x; r.y = y; return r; }
+static inline og_v2 v2(og_real x, og_real y) { og_v2 r; r.x = x; r.y = y; return r; }
 static inline og_v2 vadd(og_v2 a, og_v2 b) { return v2(a.x + b.x, a.y + b.y); }
 static inline og_v2 vsub(og_v2 a, og_v2 b) { return v2(a.x - b.x, a.y - b.y); }
-static inline og_v2 vmul(og_v2 a, float s) { return v2(a.x * s, a.y * s); }
-static inline og_v2 vdiv(og_v2 a, float s) { return v2(a.x / s, a.y / s); }
-static inline float vlen(og_v2 a) { return sqrtf(a.x * a.x + a.y * a.y); }
-static inline float vlen2(og_v2 a) { return a.x * a.x + a.y * a.y; }
-static inline float vdot(og_v2 a, og_v2 b) { return a.x * b.x + a.y * b.y; }
-static inline float vdet(og_v2 a, og_v2 b) { return a.x * b.y - a.y * b.x; }
+static inline og_v2 vmul(og_v2 a, og_real s) { return v2(a.x * s, a.y * s); }
+static inline og_v2 vdiv(og_v2 a, og_real s) { return v2(a.x / s, a.y / s); }
+static inline og_real vlen(og_v2 a) { return og_sqrt(a.x * a.x + a.y * a.y); }
+static inline og_real vlen2(og_v2 a) { return a.x * a.x + a.y * a.y; }
+static inline og_real vdot(og_v2 a, og_v2 b) { return a.x * b.x + a.y * b.y; }
+static inline og_real vdet(og_v2 a, og_v2 b) { return a.x * b.y - a.y * b.x; }
 static inline og_v2 vright(og_v2 a) { return v2(a.y, -a.x); }
 static inline og_v2 vleft(og_v2 a) { return v2(-a.y, a.x); }
 /* Vec2::Normalize (ECMDataTypes.h:45-52) */
 static inline og_v2 vnormalize(og_v2 a)
 {
-    float l = vlen(a);
+    og_real l = vlen(a);
     if (l == 0.0f) return a;
     a.x /= l;
     a.y /= l;
@@ -45,7 +67,7 @@ static inline og_v2 vnormalize(og_v2 a)
    uninitialised Vec2 for a zero vector, this returns (0,0). */
 static inline og_v2 vnormalized(og_v2 a)
 {
-    float l = vlen(a);
+    og_real l = vlen(a);
     if (l == 0.0f) return v2(0.0f, 0.0f);
     return v2(a.x / l, a.y / l);
 }
@@ -55,9 +77,9 @@ static inline int vapprox(og_v2 p, og_v2 a)
     return p.x < (a.x + OG_EPS) && p.x > (a.x - OG_EPS) && p.y < (a.y + OG_EPS) && p.y > (a.y - OG_EPS);
 }
 /* MathUtility::SquareDistance(Point,Point) (UtilityFunctions.cpp:32-39): p2 - p1 */
-static inline float vsqdist(og_v2 p1, og_v2 p2)
+static inline og_real vsqdist(og_v2 p1, og_v2 p2)
 {
-    float dx = p2.x - p1.x, dy = p2.y - p1.y;
+    og_real dx = p2.x - p1.x, dy = p2.y - p1.y;
     return dx * dx + dy * dy;
 }
 /* MathUtility::GetClosestPointOnSegment (UtilityFunctions.cpp:287-306) */
@@ -66,24 +88,27 @@ static og_v2 closest_on_segment(og_v2 point, og_v2 s1, og_v2 s2)
     if (vapprox(s1, s2)) return s1;
     og_v2 seg = vsub(s2, s1);
     og_v2 pts = vsub(point, s1);
-    float tsq = vsqdist(s1, s2);
-    float d = (pts.x * seg.x + pts.y * seg.y) / tsq;
+    og_real tsq = vsqdist(s1, s2);
+    og_real d = (pts.x * seg.x + pts.y * seg.y) / tsq;
     if (d > 1.0f) d = 1.0f;
     if (d < 0.0f) d = 0.0f;
     return v2(s1.x + d * seg.x, s1.y + d * seg.y);
 }
 /* MathUtility::RotateVector (UtilityFunctions.cpp:233-242) */
-static og_v2 rotate(og_v2 v, float rad, int libm)
+static og_v2 rotate(og_v2 v, og_real rad, int libm)
 {
-    float cs, sn;
+    og_real cs, sn;
     if (libm) {
-        cs = cosf(rad);
-        sn = sinf(rad);
+        cs = og_cos(rad);
+        sn = og_sin(rad);
     } else {
-        ecmg_sincosf(rad, &sn, &cs);
+        float s32, c32;
+        ecmg_sincosf((float)rad, &s32, &c32);
+        sn = s32;
+        cs = c32;
     }
-    float px = v.x * cs - v.y * sn;
-    float py = v.x * sn + v.y * cs;
+    og_real px = v.x * cs - v.y * sn;
+    og_real py = v.x * sn + v.y * cs;
     return v2(px, py);
 }
 
@@ -96,15 +121,15 @@ static og_v2 rotate(og_v2 v, float rad, int libm)
    kd-tree (below) is a different, approximate query.  d2 is computed exactly
    as KDTree.cpp:107-108 computes it, self and coincident agents are excluded
    by the same d2 > EPSILON test (KDTree.cpp:112). */
-int og_knn_exact(const og_state* s, int agent, int k, float r2, int* out_ids, float* out_d2)
+int og_knn_exact(const og_state* s, int agent, int k, og_real r2, int* out_ids, og_real* out_d2)
 {
     og_v2 t = s->pos[agent];
     int n = 0;
     for (int j = 0; j <= s->last_idx; j++) {
         if (!s->active[j]) continue;
-        float dx = s->pos[j].x - t.x;
-        float dy = s->pos[j].y - t.y;
-        float d2 = dx * dx + dy * dy;
+        og_real dx = s->pos[j].x - t.x;
+        og_real dy = s->pos[j].y - t.y;
+        og_real d2 = dx * dx + dy * dy;
         if (!(d2 > OG_EPS) || !(d2 < r2)) continue;
         /* insertion into the sorted top-k list */
         if (n == k && !(d2 < out_d2[k - 1])) continue; /* ties: ids arrive ascending */
@@ -128,7 +153,7 @@ struct og_kdtree {
     int tree_size;
     int max_depth;
     int* cache;   /* ORCA::m_NeighborCache, persists across agents and ticks */
-    float* dist;  /* nearestSqDistances (fresh per query)                   */
+    og_real* dist;  /* nearestSqDistances (fresh per query)                   */
     int* idx;
     int idx_cap;
     const og_v2* sort_pos;
@@ -139,7 +164,7 @@ og_kdtree* og_kdtree_create(int k)
     og_kdtree* t = (og_kdtree*)calloc(1, sizeof(og_kdtree));
     t->k = k;
     t->cache = (int*)calloc((size_t)k, sizeof(int)); /* std::vector<int>::resize -> 0 */
-    t->dist = (float*)malloc(sizeof(float) * (size_t)k);
+    t->dist = (og_real*)malloc(sizeof(og_real) * (size_t)k);
     return t;
 }
 
@@ -163,8 +188,8 @@ static void msort(int* a, int* tmp, int n, const og_v2* pos, int axis)
     msort(a + h, tmp, n - h, pos, axis);
     int i = 0, j = h, o = 0;
     while (i < h && j < n) {
-        float ka = axis ? pos[a[i]].y : pos[a[i]].x;
-        float kb = axis ? pos[a[j]].y : pos[a[j]].x;
+        og_real ka = axis ? pos[a[i]].y : pos[a[i]].x;
+        og_real kb = axis ? pos[a[j]].y : pos[a[j]].x;
         if (kb < ka) tmp[o++] = a[j++];
         else tmp[o++] = a[i++];
     }
@@ -216,16 +241,16 @@ static void kd_knn_rec(og_kdtree* t, const og_v2* pos, og_v2 target, int cur, in
     if (depth > t->max_depth) return;
     if (t->tree[cur] == -1) return;
     og_v2 cp = pos[t->tree[cur]];
-    float dx = cp.x - target.x, dy = cp.y - target.y;
-    float d = dx * dx + dy * dy;
+    og_real dx = cp.x - target.x, dy = cp.y - target.y;
+    og_real d = dx * dx + dy * dy;
     int* ni = t->cache;
-    float* nd = t->dist;
+    og_real* nd = t->dist;
     if (*kfound < k && d > OG_EPS) {
         ni[*kfound] = t->tree[cur];
         nd[*kfound] = d;
         (*kfound)++;
         if (*kfound == k) {
-            float largest = d;
+            og_real largest = d;
             int li = k - 1;
             for (int i = 0; i < k - 1; i++)
                 if (nd[i] > largest) { largest = nd[i]; li = i; }
@@ -239,7 +264,7 @@ static void kd_knn_rec(og_kdtree* t, const og_v2* pos, og_v2 target, int cur, in
         if (d < nd[0] && d > OG_EPS) {
             nd[0] = d;
             ni[0] = t->tree[cur];
-            float largest = d;
+            og_real largest = d;
             int li = 0;
             for (int i = 1; i < k; i++)
                 if (nd[i] > largest) { largest = nd[i]; li = i; }
@@ -249,15 +274,15 @@ static void kd_knn_rec(og_kdtree* t, const og_v2* pos, og_v2 target, int cur, in
             ni[li] = t->tree[cur];
         }
     }
-    float cv = depth % 2 == 0 ? cp.x : cp.y;
-    float tv = depth % 2 == 0 ? target.x : target.y;
+    og_real cv = depth % 2 == 0 ? cp.x : cp.y;
+    og_real tv = depth % 2 == 0 ? target.x : target.y;
     if (tv < cv) {
         kd_knn_rec(t, pos, target, cur * 2 + 1, k, kfound, depth + 1);
-        float db = tv - cv;
+        og_real db = tv - cv;
         if (db * db < nd[k - 1]) kd_knn_rec(t, pos, target, cur * 2 + 2, k, kfound, depth + 1);
     } else {
         kd_knn_rec(t, pos, target, cur * 2 + 2, k, kfound, depth + 1);
-        float db = tv - cv;
+        og_real db = tv - cv;
         if (db * db < nd[k - 1]) kd_knn_rec(t, pos, target, cur * 2 + 1, k, kfound, depth + 1);
     }
 }
@@ -266,7 +291,7 @@ static void kd_knn_rec(og_kdtree* t, const og_v2* pos, og_v2 target, int cur, in
 int og_kdtree_query(og_kdtree* t, const og_state* s, int agent, int* out_ids)
 {
     int k = t->k;
-    for (int i = 0; i < k; i++) t->dist[i] = FLT_MAX;
+    for (int i = 0; i < k; i++) t->dist[i] = OG_REAL_MAX;
     int kfound = 0;
     kd_knn_rec(t, s->pos, s->pos[agent], 0, k, &kfound, 0);
     if (out_ids)
@@ -277,16 +302,16 @@ int og_kdtree_query(og_kdtree* t, const og_state* s, int agent, int* out_ids)
 /* ---------------------------------------------------------------------------
  * Simulator::FindNearestObstacles (ECMAgentSimulator/Simulator.cpp:259-292)
  * ------------------------------------------------------------------------- */
-int og_find_obstacles(const og_obstacles* o, og_v2 pos, float range_sq, int* out, int cap, int libm)
+int og_find_obstacles(const og_obstacles* o, og_v2 pos, og_real range_sq, int* out, int cap, int libm)
 {
     int n = 0;
     for (int i = 0; i < o->n_verts; i++) {
         og_v2 a = o->p[i];
         og_v2 b = o->p[o->next[i]];
         /* LineLeftDistance (UtilityFunctions.cpp:28-31): Det(v1 - p, v2 - v1) */
-        float sld = vdet(vsub(a, pos), vsub(b, a));
-        float num = libm ? powf(sld, 2.0f) : sld * sld;
-        float sq = num / vsqdist(a, b);
+        og_real sld = vdet(vsub(a, pos), vsub(b, a));
+        og_real num = libm ? og_pow(sld, 2.0f) : sld * sld;
+        og_real sq = num / vsqdist(a, b);
         if (sq < range_sq) {
             if (sld < 0.0f) {
                 og_v2 c = closest_on_segment(pos, a, b);
@@ -305,7 +330,7 @@ int og_find_obstacles(const og_obstacles* o, og_v2 pos, float range_sq, int* out
  * A constraint is stored as 4 floats: point.x, point.y, normal.x, normal.y
  * (Constraint::Init, ORCA.h:29-47; slope/intercepts are unused by the LP).
  * ------------------------------------------------------------------------- */
-static inline int push_con(float* c, int n, int cap, og_v2 p, og_v2 nrm)
+static inline int push_con(og_real* c, int n, int cap, og_v2 p, og_v2 nrm)
 {
     if (n < cap) {
         c[4 * n + 0] = p.x;
@@ -318,14 +343,14 @@ static inline int push_con(float* c, int n, int cap, og_v2 p, og_v2 nrm)
 
 int og_generate_constraints(const og_obstacles* o, const og_state* s, const og_params* p, int agent,
                             const int* nbrs, int n_nbrs, const int* obst, int n_obst_cand,
-                            float* cons, int cap, int* out_n_obst)
+                            og_real* cons, int cap, int* out_n_obst)
 {
     og_v2 position = s->pos[agent];
     og_v2 velocity = s->vel[agent];
-    float clr = s->clear[agent];
+    og_real clr = s->clear[agent];
     int n = 0;
     const og_v2 zero = v2(0.0f, 0.0f);
-    const float inf = INFINITY;
+    const og_real inf = INFINITY;
 
     for (int i = 0; i < n_obst_cand; i++) {
         int L = obst[i];
@@ -333,12 +358,12 @@ int og_generate_constraints(const og_obstacles* o, const og_state* s, const og_p
         og_v2 rp1 = vsub(o->p[L], position);
         og_v2 rp2 = vsub(o->p[R], position);
         og_v2 seg = vsub(o->p[R], o->p[L]);
-        const float sparam = vdot(vmul(rp1, -1.0f), seg) / vlen2(seg);
-        const float distSqLine = vlen2(vsub(vmul(rp1, -1.0f), vmul(seg, sparam)));
-        const float distSq1 = vlen2(rp1);
-        const float distSq2 = vlen2(rp2);
+        const og_real sparam = vdot(vmul(rp1, -1.0f), seg) / vlen2(seg);
+        const og_real distSqLine = vlen2(vsub(vmul(rp1, -1.0f), vmul(seg, sparam)));
+        const og_real distSq1 = vlen2(rp1);
+        const og_real distSq2 = vlen2(rp2);
         seg = vnormalize(seg);
-        const float radiusSq = clr * clr;
+        const og_real radiusSq = clr * clr;
 
         if (sparam < 0.0f && distSq1 <= radiusSq) { /* ORCA.cpp:92-105 */
             if (o->convex[L]) n = push_con(cons, n, cap, zero, vnormalized(vmul(rp1, -1.0f)));
@@ -357,24 +382,24 @@ int og_generate_constraints(const og_obstacles* o, const og_state* s, const og_p
         if (sparam < 0.0f && distSqLine <= radiusSq) { /* ORCA.cpp:146-169 */
             if (!o->convex[L]) continue;
             R = L;
-            const float leg1 = sqrtf(distSq1 - radiusSq);
+            const og_real leg1 = og_sqrt(distSq1 - radiusSq);
             leftLeg = vdiv(v2(rp1.x * leg1 - rp1.y * clr, rp1.x * clr + rp1.y * leg1), distSq1);
             rightLeg = vdiv(v2(rp1.x * leg1 + rp1.y * clr, -rp1.x * clr + rp1.y * leg1), distSq1);
         } else if (sparam > 1.0f && distSqLine <= radiusSq) { /* ORCA.cpp:171-183 */
             if (!o->convex[R]) continue;
             L = R;
-            const float leg2 = sqrtf(distSq2 - radiusSq);
+            const og_real leg2 = og_sqrt(distSq2 - radiusSq);
             leftLeg = vdiv(v2(rp2.x * leg2 - rp2.y * clr, rp2.x * clr + rp2.y * leg2), distSq2);
             rightLeg = vdiv(v2(rp2.x * leg2 + rp2.y * clr, -rp2.x * clr + rp2.y * leg2), distSq2);
         } else { /* ORCA.cpp:186-212 */
             if (o->convex[L]) {
-                const float leg1 = sqrtf(distSq1 - radiusSq);
+                const og_real leg1 = og_sqrt(distSq1 - radiusSq);
                 leftLeg = vdiv(v2(rp1.x * leg1 - rp1.y * clr, rp1.x * clr + rp1.y * leg1), distSq1);
             } else {
                 leftLeg = vmul(seg, -1.0f);
             }
             if (o->convex[R]) {
-                const float leg2 = sqrtf(distSq2 - radiusSq);
+                const og_real leg2 = og_sqrt(distSq2 - radiusSq);
                 rightLeg = vdiv(v2(rp2.x * leg2 + rp2.y * clr, -rp2.x * clr + rp2.y * leg2), distSq2);
             } else {
                 rightLeg = seg;
@@ -396,13 +421,13 @@ int og_generate_constraints(const og_obstacles* o, const og_state* s, const og_p
         }
 
         /* cut-off, ORCA.cpp:241-332 */
-        float invT = 1.0f / p->tau_obst;
+        og_real invT = 1.0f / p->tau_obst;
         const og_v2 leftCutoff = vmul(vsub(o->p[L], position), invT);
         const og_v2 rightCutoff = vmul(vsub(o->p[R], position), invT);
         const og_v2 cutoffVec = vsub(rightCutoff, leftCutoff);
-        const float t = (L == R ? 0.5f : vdot(vsub(velocity, leftCutoff), cutoffVec) / vlen2(cutoffVec));
-        const float tLeft = vdot(vsub(velocity, leftCutoff), leftLeg);
-        const float tRight = vdot(vsub(velocity, rightCutoff), rightLeg);
+        const og_real t = (L == R ? 0.5f : vdot(vsub(velocity, leftCutoff), cutoffVec) / vlen2(cutoffVec));
+        const og_real tLeft = vdot(vsub(velocity, leftCutoff), leftLeg);
+        const og_real tRight = vdot(vsub(velocity, rightCutoff), rightLeg);
 
         if ((t < 0.0f && tLeft < 0.0f) || (L == R && tLeft < 0.0f && tRight < 0.0f)) {
             og_v2 unitW = vnormalized(vsub(velocity, leftCutoff));
@@ -416,10 +441,10 @@ int og_generate_constraints(const og_obstacles* o, const og_state* s, const og_p
             continue;
         }
 
-        const float distSqCutoff = ((t < 0.0f || t > 1.0f || L == R) ? inf
+        const og_real distSqCutoff = ((t < 0.0f || t > 1.0f || L == R) ? inf
                                     : vlen2(vsub(velocity, vadd(leftCutoff, vmul(cutoffVec, t)))));
-        const float distSqLeft = ((tLeft < 0.0f) ? inf : vlen2(vsub(velocity, vadd(leftCutoff, vmul(leftLeg, tLeft)))));
-        const float distSqRight = ((tRight < 0.0f) ? inf : vlen2(vsub(velocity, vadd(rightCutoff, vmul(rightLeg, tRight)))));
+        const og_real distSqLeft = ((tLeft < 0.0f) ? inf : vlen2(vsub(velocity, vadd(leftCutoff, vmul(leftLeg, tLeft)))));
+        const og_real distSqRight = ((tRight < 0.0f) ? inf : vlen2(vsub(velocity, vadd(rightCutoff, vmul(rightLeg, tRight)))));
 
         if (distSqCutoff <= distSqLeft && distSqCutoff <= distSqRight) {
             og_v2 normal = vleft(vmul(seg, -1.0f));
@@ -443,39 +468,39 @@ int og_generate_constraints(const og_obstacles* o, const og_state* s, const og_p
     *out_n_obst = n;
 
     /* agent constraints, ORCA.cpp:339-423 */
-    const float ta = p->tau_agent;
+    const og_real ta = p->tau_agent;
     for (int i = 0; i < n_nbrs; i++) {
         int nb = nbrs[i];
         og_v2 np = s->pos[nb];
         og_v2 nv = s->vel[nb];
-        float nc = s->clear[nb];
+        og_real nc = s->clear[nb];
         og_v2 VOPos = v2((np.x - position.x) / ta, (np.y - position.y) / ta);
-        float VOPosLength = vlen(VOPos);
-        float combinedRadius = nc + clr;
-        float VORadius = combinedRadius / ta;
+        og_real VOPosLength = vlen(VOPos);
+        og_real combinedRadius = nc + clr;
+        og_real VORadius = combinedRadius / ta;
         og_v2 relVel = v2(velocity.x - nv.x, velocity.y - nv.y);
         og_v2 relPos = v2(np.x - position.x, np.y - position.y);
-        float relPosLength = vlen(relPos);
+        og_real relPosLength = vlen(relPos);
 
         if (relPosLength < combinedRadius) { /* ORCA.cpp:356-372 */
             og_v2 w = vsub(relVel, vdiv(relPos, p->dt));
-            float wLength = vlen(w);
+            og_real wLength = vlen(w);
             og_v2 unitW = vdiv(w, wLength);
             og_v2 U = vmul(unitW, (combinedRadius / p->dt - wLength));
             n = push_con(cons, n, cap, vadd(velocity, vmul(U, 0.5f)), unitW);
             continue;
         }
 
-        float tanAngleFactor = VORadius / VOPosLength;
-        float tanHalfAngle = p->libm ? atanf(tanAngleFactor) : ecmg_atanf(tanAngleFactor);
+        og_real tanAngleFactor = VORadius / VOPosLength;
+        og_real tanHalfAngle = p->libm ? og_atan(tanAngleFactor) : ecmg_atanf(tanAngleFactor);
         og_v2 VOLeftLeg = rotate(VOPos, tanHalfAngle, p->libm);
         og_v2 VORightLeg = rotate(VOPos, -tanHalfAngle, p->libm);
-        float sqDistFromCircleCentre = vsqdist(VOPos, relVel);
+        og_real sqDistFromCircleCentre = vsqdist(VOPos, relVel);
         og_v2 bse = vsub(VOLeftLeg, VOPos), chk = vsub(relVel, VOPos);
         int liesBelow = bse.x * chk.y - bse.y * chk.x > 0; /* IsLeftOfVector */
 
         if (liesBelow) {
-            float distToEdge = VORadius - sqrtf(sqDistFromCircleCentre);
+            og_real distToEdge = VORadius - og_sqrt(sqDistFromCircleCentre);
             og_v2 lineNormal = vnormalize(vsub(relVel, VOPos));
             og_v2 pointOnLine = vadd(velocity, vmul(vmul(lineNormal, distToEdge), 0.5f));
             n = push_con(cons, n, cap, pointOnLine, lineNormal);
@@ -484,12 +509,12 @@ int og_generate_constraints(const og_obstacles* o, const og_state* s, const og_p
             int closerToLeft = vdot(leftPerp, relVel) >= 0;
             if (closerToLeft) {
                 og_v2 lln = vnormalized(VOLeftLeg);
-                float len = vdot(relVel, lln); /* GetClosestPointOnLineThroughOrigin */
+                og_real len = vdot(relVel, lln); /* GetClosestPointOnLineThroughOrigin */
                 og_v2 U = vsub(vmul(lln, len), relVel);
                 n = push_con(cons, n, cap, vadd(velocity, vmul(U, 0.5f)), vleft(lln));
             } else {
                 og_v2 rln = vnormalized(VORightLeg);
-                float len = vdot(relVel, rln);
+                og_real len = vdot(relVel, rln);
                 og_v2 U = vsub(vmul(rln, len), relVel);
                 n = push_con(cons, n, cap, vadd(velocity, vmul(U, 0.5f)), vright(rln));
             }
@@ -501,7 +526,7 @@ int og_generate_constraints(const og_obstacles* o, const og_state* s, const og_p
 /* ---------------------------------------------------------------------------
  * ORCA::RandomizedLP (ECMAgentSimulator/ORCA.cpp:428-587)
  * ------------------------------------------------------------------------- */
-int og_lp(const float* cons, int n, og_v2 opt, float maxSpeed, int useDirOpt, og_v2* out)
+int og_lp(const og_real* cons, int n, og_v2 opt, og_real maxSpeed, int useDirOpt, og_v2* out)
 {
     if (useDirOpt) {
         *out = vmul(opt, maxSpeed);
@@ -519,23 +544,23 @@ int og_lp(const float* cons, int n, og_v2 opt, float maxSpeed, int useDirOpt, og
         if (vdet(vright(N), vsub(P, *out)) <= 0.0f) continue;
 
         og_v2 dir = vright(N);
-        float dirPointDot = vdot(dir, P);
-        float discriminant = dirPointDot * dirPointDot + maxSpeed * maxSpeed - vdot(P, P);
+        og_real dirPointDot = vdot(dir, P);
+        og_real discriminant = dirPointDot * dirPointDot + maxSpeed * maxSpeed - vdot(P, P);
         if (discriminant <= 0.0f) return i;
 
-        float sq = sqrtf(discriminant);
-        float left = -dirPointDot - sq;
-        float right = -dirPointDot + sq;
+        og_real sq = og_sqrt(discriminant);
+        og_real left = -dirPointDot - sq;
+        og_real right = -dirPointDot + sq;
         for (int j = 0; j < i; j++) {
             og_v2 Pj = v2(cons[4 * j], cons[4 * j + 1]);
             og_v2 Nj = v2(cons[4 * j + 2], cons[4 * j + 3]);
-            float den = vdet(vright(N), vright(Nj));
-            float num = vdet(vright(Nj), vsub(P, Pj));
-            if (fabsf(den) <= OG_EPS) {
+            og_real den = vdet(vright(N), vright(Nj));
+            og_real num = vdet(vright(Nj), vsub(P, Pj));
+            if (og_fabs(den) <= OG_EPS) {
                 if (num < 0.0f) return i;
                 continue;
             }
-            const float t = num / den;
+            const og_real t = num / den;
             if (den >= 0.0f) right = (t < right) ? t : right; /* std::min(right, t) */
             else left = (left < t) ? t : left;                 /* std::max(left, t)  */
             if (left > right) return i;
@@ -544,7 +569,7 @@ int og_lp(const float* cons, int n, og_v2 opt, float maxSpeed, int useDirOpt, og
             if (vdot(opt, vright(N)) > 0) *out = vadd(P, vmul(vright(N), right));
             else *out = vadd(P, vmul(vright(N), left));
         } else {
-            float t = vdot(vright(N), vsub(opt, P));
+            og_real t = vdot(vright(N), vsub(opt, P));
             if (t < left) *out = vadd(P, vmul(vright(N), left));
             else if (t > right) *out = vadd(P, vmul(vright(N), right));
             else *out = vadd(P, vmul(vright(N), t));
@@ -556,10 +581,10 @@ int og_lp(const float* cons, int n, og_v2 opt, float maxSpeed, int useDirOpt, og
 /* ---------------------------------------------------------------------------
  * ORCA::RandomizedLP3D (ECMAgentSimulator/ORCA.cpp:592-669)
  * ------------------------------------------------------------------------- */
-void og_lp3d(const float* cons, int n, int nObst, float maxSpeed, int failed, og_v2* out)
+void og_lp3d(const og_real* cons, int n, int nObst, og_real maxSpeed, int failed, og_v2* out)
 {
-    float maxPen = 0.0f;
-    float* proj = (float*)malloc(sizeof(float) * 4 * (size_t)(n + 1));
+    og_real maxPen = 0.0f;
+    og_real* proj = (og_real*)malloc(sizeof(og_real) * 4 * (size_t)(n + 1));
     for (int i = failed; i < n; i++) {
         og_v2 Pi = v2(cons[4 * i], cons[4 * i + 1]);
         og_v2 Ni = v2(cons[4 * i + 2], cons[4 * i + 3]);
@@ -567,17 +592,17 @@ void og_lp3d(const float* cons, int n, int nObst, float maxSpeed, int failed, og
         if (vdet(dir, vsub(Pi, *out)) <= maxPen) continue;
 
         int m = 0;
-        for (int k = 0; k < nObst; k++, m++) memcpy(proj + 4 * m, cons + 4 * k, sizeof(float) * 4);
+        for (int k = 0; k < nObst; k++, m++) memcpy(proj + 4 * m, cons + 4 * k, sizeof(og_real) * 4);
         for (int j = nObst; j < i; j++) {
             og_v2 Pj = v2(cons[4 * j], cons[4 * j + 1]);
             og_v2 Nj = v2(cons[4 * j + 2], cons[4 * j + 3]);
-            float det = vdet(vright(Ni), vright(Nj));
+            og_real det = vdet(vright(Ni), vright(Nj));
             og_v2 newP;
-            if (fabsf(det) <= OG_EPS) {
+            if (og_fabs(det) <= OG_EPS) {
                 if (vdot(Ni, Nj) > 0) continue;
                 newP = vmul(vadd(Pi, Pj), 0.5f);
             } else {
-                float t = vdet(vright(Nj), vsub(Pi, Pj)) / det;
+                og_real t = vdet(vright(Nj), vsub(Pi, Pj)) / det;
                 newP = vadd(Pi, vmul(vright(Ni), t));
             }
             og_v2 nn = vnormalized(vsub(Nj, Ni));
@@ -599,8 +624,8 @@ int og_orca_velocity(const og_obstacles* o, const og_state* s, const og_params* 
                      int agent, const int* nbrs, int n_nbrs, og_v2 pref_vel,
                      og_v2* out_vel, int* out_n_obst, int* out_fail)
 {
-    float maxSpeed = p->max_speed > 0.0f ? p->max_speed : s->pref_speed[agent];
-    float range = p->tau_obst * maxSpeed + s->clear[agent];
+    og_real maxSpeed = p->max_speed > 0.0f ? p->max_speed : s->pref_speed[agent];
+    og_real range = p->tau_obst * maxSpeed + s->clear[agent];
     int cap_o = 64;
     int* ob = (int*)malloc(sizeof(int) * (size_t)cap_o);
     int no = og_find_obstacles(o, s->pos[agent], range * range, ob, cap_o, p->libm);
@@ -611,7 +636,7 @@ int og_orca_velocity(const og_obstacles* o, const og_state* s, const og_params* 
         no = og_find_obstacles(o, s->pos[agent], range * range, ob, cap_o, p->libm);
     }
     int cap = no + n_nbrs + 1;
-    float* cons = (float*)malloc(sizeof(float) * 4 * (size_t)cap);
+    og_real* cons = (og_real*)malloc(sizeof(og_real) * 4 * (size_t)cap);
     int nob = 0;
     int m = og_generate_constraints(o, s, p, agent, nbrs, n_nbrs, ob, no, cons, cap, &nob);
     int failed = og_lp(cons, m, pref_vel, maxSpeed, 0, out_vel);
@@ -635,10 +660,10 @@ static int contains_poly(og_v2 p, const og_v2* q, int nq)
         og_v2 a = q[s], b = q[(s + 1) % nq];
         if (vapprox(p, a)) return 0;
         if (vapprox(p, b)) return 0;
-        if (p.y > fminf(a.y, b.y)) {
-            if (p.y < fmaxf(a.y, b.y)) {
-                if (p.x < fmaxf(a.x, b.x)) {
-                    float xi = (p.y - a.y) * (b.x - a.x) / (b.y - a.y) + a.x;
+        if (p.y > og_fmin(a.y, b.y)) {
+            if (p.y < og_fmax(a.y, b.y)) {
+                if (p.x < og_fmax(a.x, b.x)) {
+                    og_real xi = (p.y - a.y) * (b.x - a.x) / (b.y - a.y) + a.x;
                     if (a.x == b.x || p.x < xi) inside = !inside;
                 }
             }
@@ -680,10 +705,10 @@ static int ray_segment(og_v2 o, og_v2 d, og_v2 p1, og_v2 p2, og_v2* out)
     og_v2 v1 = vsub(o, p1);
     og_v2 v2_ = vsub(p2, p1);
     og_v2 v3 = v2(-d.y, d.x);
-    float dot = vdot(v2_, v3);
-    if (fabsf(dot) < 0.000001) return 0;
-    float t1 = vdet(v2_, v1) / dot; /* Cross(v2, v1) */
-    float t2 = vdot(v1, v3) / dot;
+    og_real dot = vdot(v2_, v3);
+    if (og_fabs(dot) < 0.000001) return 0;
+    og_real t1 = vdet(v2_, v1) / dot; /* Cross(v2, v1) */
+    og_real t2 = vdot(v1, v3) / dot;
     if (t1 >= 0.0 && (t2 >= 0.0 && t2 <= 1.0)) {
         out->x = o.x + d.x * t1;
         out->y = o.y + d.y * t1;
@@ -733,8 +758,8 @@ int og_irm(const og_ecm* e, og_v2 pos, const og_v2* path, int n, og_v2* out)
     og_v2 oa = e->he_left[2 * ed];
     og_v2 ob = e->he_right[2 * ed + 1];
     og_v2 co = closest_on_segment(r, oa, ob);
-    float clearance = vlen(vsub(r, co));
-    float rcs = clearance * clearance;
+    og_real clearance = vlen(vsub(r, co));
+    og_real rcs = clearance * clearance;
     og_v2 goal = path[n - 1];
     og_v2 ptg = vsub(goal, r);
     if (vlen2(ptg) < rcs) { *out = goal; return 1; }
@@ -743,21 +768,21 @@ int og_irm(const og_ecm* e, og_v2 pos, const og_v2* path, int n, og_v2* out)
         og_v2 p1 = vsub(path[i], r);
         og_v2 p2 = vsub(path[i + 1], r);
         og_v2 ed2 = vsub(p2, p1);
-        float els = vlen2(ed2);
-        float det = vdet(p1, p2);
-        float disc = rcs * els - det * det;
+        og_real els = vlen2(ed2);
+        og_real det = vdet(p1, p2);
+        og_real disc = rcs * els - det * det;
         if (disc < OG_EPS) continue;
         success = 1;
         int dySign = ed2.y < 0.0f ? -1 : 1;
-        float sd = sqrtf(disc);
-        og_v2 i1 = v2((det * ed2.y + (float)dySign * ed2.x * sd) / els, (-det * ed2.x + fabsf(ed2.y) * sd) / els);
-        og_v2 i2 = v2((det * ed2.y - (float)dySign * ed2.x * sd) / els, (-det * ed2.x - fabsf(ed2.y) * sd) / els);
+        og_real sd = og_sqrt(disc);
+        og_v2 i1 = v2((det * ed2.y + (og_real)dySign * ed2.x * sd) / els, (-det * ed2.x + og_fabs(ed2.y) * sd) / els);
+        og_v2 i2 = v2((det * ed2.y - (og_real)dySign * ed2.x * sd) / els, (-det * ed2.x - og_fabs(ed2.y) * sd) / els);
         og_v2 g1 = vadd(p1, r), g2 = vadd(p2, r);
         og_v2 gi1 = vadd(i1, r), gi2 = vadd(i2, r);
         og_v2 edge = vsub(g2, g1);
-        float t1 = vdot(vsub(gi1, g1), edge) / els;
-        float t2 = vdot(vsub(gi2, g1), edge) / els;
-        float maxT = -1.0f;
+        og_real t1 = vdot(vsub(gi1, g1), edge) / els;
+        og_real t2 = vdot(vsub(gi2, g1), edge) / els;
+        og_real maxT = -1.0f;
         if (t1 >= 0.0f && t1 <= 1.0f) { *out = gi1; maxT = t1; }
         if (t2 >= 0.0f && t2 <= 1.0f) {
             if (t2 > maxT) *out = gi2;
@@ -786,8 +811,8 @@ static void orca_range(og_job* j)
     const og_params* p = j->p;
     int k = p->k;
     int* ids = (int*)malloc(sizeof(int) * (size_t)(k > 0 ? k : 1));
-    float* d2 = (float*)malloc(sizeof(float) * (size_t)(k > 0 ? k : 1));
-    float r2 = p->neighbor_dist * p->neighbor_dist;
+    og_real* d2 = (og_real*)malloc(sizeof(og_real) * (size_t)(k > 0 ? k : 1));
+    og_real r2 = p->neighbor_dist * p->neighbor_dist;
     for (int i = j->lo; i < j->hi; i++) {
         if (!j->alive[i]) continue;
         int nn = og_knn_exact(j->snap, i, k, r2, ids, d2);
@@ -822,14 +847,14 @@ static void* orca_thread(void* arg)
    returns 0, 1 when the agent is to be destroyed, 2 when it needs a replan */
 static int attract_one(const og_ecm* e, const og_state* s, const og_params* p, int i, og_v2* attr)
 {
-    const float delSq = p->delete_radius * p->delete_radius;
-    const float arrSq = p->arrival_radius * p->arrival_radius;
+    const og_real delSq = p->delete_radius * p->delete_radius;
+    const og_real arrSq = p->arrival_radius * p->arrival_radius;
     const og_v2* path = s->path_xy + s->path_off[i];
     int np = s->path_len[i];
     og_v2 pos = s->pos[i];
     og_v2 g = path[np - 1];
-    float dx = pos.x - g.x, dy = pos.y - g.y; /* SquareDistance(x0,y0,x1,y1) */
-    float dist = dx * dx + dy * dy;
+    og_real dx = pos.x - g.x, dy = pos.y - g.y; /* SquareDistance(x0,y0,x1,y1) */
+    og_real dist = dx * dx + dy * dy;
     if (dist < arrSq) {
         *attr = g;
         return dist < delSq ? 1 : 0;
@@ -945,11 +970,11 @@ int og_tick(const og_obstacles* o, const og_ecm* e, og_state* s, const og_params
 
     /* UpdateVelocitySystem (Simulator.cpp:619-635): force = vOrca - v
        (Simulator.cpp:676-677), v += F * (1/m) * dt */
-    const float massRecip = 1.0f / p->mass;
+    const og_real massRecip = 1.0f / p->mass;
     for (int i = 0; i <= last; i++) {
         if (!s->active[i]) continue;
-        float fx = vorca[i].x - s->vel[i].x;
-        float fy = vorca[i].y - s->vel[i].y;
+        og_real fx = vorca[i].x - s->vel[i].x;
+        og_real fy = vorca[i].y - s->vel[i].y;
         s->vel[i].x += fx * massRecip * p->dt;
         s->vel[i].y += fy * massRecip * p->dt;
     }
@@ -994,14 +1019,14 @@ static void* sample_thread(void* arg)
     const og_params* p = j->p;
     int k = p->k;
     int* ids = (int*)malloc(sizeof(int) * (size_t)k);
-    const float arrSq = p->arrival_radius * p->arrival_radius;
+    const og_real arrSq = p->arrival_radius * p->arrival_radius;
     for (int q = j->lo; q < j->hi; q++) {
         int i = j->sample[q];
         const og_v2* path = s->path_xy + s->path_off[i];
         int np = s->path_len[i];
         og_v2 pos = s->pos[i];
         og_v2 g = path[np - 1];
-        float dx = pos.x - g.x, dy = pos.y - g.y;
+        og_real dx = pos.x - g.x, dy = pos.y - g.y;
         og_v2 attr = s->attr[i];
         if (dx * dx + dy * dy < arrSq) attr = g;
         else {
@@ -1034,7 +1059,7 @@ int og_time_sample(const og_obstacles* o, const og_ecm* e, const og_state* s, co
         jobs[t].o = o; jobs[t].e = e; jobs[t].s = s; jobs[t].p = p;
         jobs[t].kd = *kd;
         jobs[t].kd.cache = (int*)calloc((size_t)p->k, sizeof(int));
-        jobs[t].kd.dist = (float*)malloc(sizeof(float) * (size_t)p->k);
+        jobs[t].kd.dist = (og_real*)malloc(sizeof(og_real) * (size_t)p->k);
         jobs[t].sample = sample;
         jobs[t].lo = t * span < n_sample ? t * span : n_sample;
         jobs[t].hi = (t + 1) * span < n_sample ? (t + 1) * span : n_sample;
@@ -1078,9 +1103,9 @@ static void* tick_sample_thread(void* arg)
     og_sample_out* out = j->out;
     int k = p->k;
     int* ids = (int*)malloc(sizeof(int) * (size_t)(k > 0 ? k : 1));
-    float* d2 = (float*)malloc(sizeof(float) * (size_t)(k > 0 ? k : 1));
-    const float r2 = p->neighbor_dist * p->neighbor_dist;
-    const float massRecip = 1.0f / p->mass;
+    og_real* d2 = (og_real*)malloc(sizeof(og_real) * (size_t)(k > 0 ? k : 1));
+    const og_real r2 = p->neighbor_dist * p->neighbor_dist;
+    const og_real massRecip = 1.0f / p->mass;
     for (int q = j->lo; q < j->hi; q++) {
         int i = j->sample[q];
         for (int c = 0; c < k; c++) out->nbr_ids[(size_t)q * k + c] = -1;
@@ -1107,8 +1132,8 @@ static void* tick_sample_thread(void* arg)
         out->v_orca[q] = v;
         /* UpdateVelocitySystem, UpdatePositionSystem */
         og_v2 vel = s->vel[i];
-        float fx = v.x - vel.x;
-        float fy = v.y - vel.y;
+        og_real fx = v.x - vel.x;
+        og_real fy = v.y - vel.y;
         vel.x += fx * massRecip * p->dt;
         vel.y += fy * massRecip * p->dt;
         og_v2 pos = s->pos[i];

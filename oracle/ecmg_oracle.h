@@ -25,7 +25,17 @@
 extern "C" {
 #endif
 
-typedef struct { float x, y; } og_v2;
+/* The arithmetic type.  float: the restatement (bit for bit the reference).
+   Built with -DOG_REAL_DOUBLE (liboracle64.so) the same code computes in
+   double with the host libm: the FP64 run that FP32 results are measured
+   against. */
+#ifdef OG_REAL_DOUBLE
+typedef double og_real;
+#else
+typedef float og_real;
+#endif
+
+typedef struct { og_real x, y; } og_v2;
 
 /* Static obstacles, flattened in the reference's global order
    (Environment::GetObstacles() obstacle by obstacle, vertex by vertex). */
@@ -41,7 +51,7 @@ typedef struct {
 typedef struct {
     int n_vertices;
     const og_v2* v_pos;     /* ECMVertex::position       */
-    const float* v_clear;   /* ECMVertex::clearance      */
+    const og_real* v_clear;   /* ECMVertex::clearance      */
     const int* v_idx;       /* ECMVertex::idx            */
     const int* v_halfedge;  /* ECMVertex::half_edge_idx  */
     int n_edges;
@@ -52,14 +62,14 @@ typedef struct {
 } og_ecm;
 
 typedef struct {
-    float dt;               /* Simulator::m_SimStepTime                      */
-    float tau_agent;        /* ORCA::m_lookAheadAgent                        */
-    float tau_obst;         /* ORCA::m_lookAheadObstacle                     */
-    float neighbor_dist;    /* kNN cut-off radius (exact-kNN mode only)      */
-    float max_speed;        /* <= 0: LP radius = preferred speed (Simulator.cpp:671) */
-    float mass;             /* Simulator.cpp:622                             */
-    float arrival_radius;   /* Simulator.cpp:543                             */
-    float delete_radius;    /* Simulator.cpp:542                             */
+    og_real dt;               /* Simulator::m_SimStepTime                      */
+    og_real tau_agent;        /* ORCA::m_lookAheadAgent                        */
+    og_real tau_obst;         /* ORCA::m_lookAheadObstacle                     */
+    og_real neighbor_dist;    /* kNN cut-off radius (exact-kNN mode only)      */
+    og_real max_speed;        /* <= 0: LP radius = preferred speed (Simulator.cpp:671) */
+    og_real mass;             /* Simulator.cpp:622                             */
+    og_real arrival_radius;   /* Simulator.cpp:543                             */
+    og_real delete_radius;    /* Simulator.cpp:542                             */
     int k;                  /* ORCA(numNeighbors)                            */
     int knn_mode;           /* 0 = exact kNN (d2,id) within neighbor_dist; 1 = kd-tree as the reference */
     int libm;               /* 1 = host libm transcendentals; 0 = ecmg_tmath.h */
@@ -75,8 +85,8 @@ typedef struct {
     og_v2* vel;
     og_v2* attr;            /* attraction points          */
     og_v2* pref_vel;
-    float* clear;
-    float* pref_speed;
+    og_real* clear;
+    og_real* pref_speed;
     unsigned char* active;
     int* path_off;          /* path CSR: agent i owns path_xy[path_off[i] .. +path_len[i]) */
     int* path_len;
@@ -109,9 +119,9 @@ void og_kdtree_build(og_kdtree* t, const og_state* s);
 int og_kdtree_query(og_kdtree* t, const og_state* s, int agent, int* out_ids);
 
 /* exact k nearest (d2, id) with EPSILON < d2 < r2; returns the count */
-int og_knn_exact(const og_state* s, int agent, int k, float r2, int* out_ids, float* out_d2);
+int og_knn_exact(const og_state* s, int agent, int k, og_real r2, int* out_ids, og_real* out_d2);
 
-int og_find_obstacles(const og_obstacles* o, og_v2 pos, float range_sq, int* out, int cap, int libm);
+int og_find_obstacles(const og_obstacles* o, og_v2 pos, og_real range_sq, int* out, int cap, int libm);
 
 /* ORCA constraints + LP + LP3D for one agent with the given neighbour list.
    Returns the number of constraints. */
@@ -120,11 +130,11 @@ int og_orca_velocity(const og_obstacles* o, const og_state* s, const og_params* 
                      og_v2* out_vel, int* out_n_obst, int* out_fail);
 
 /* half-plane LP of ORCA.cpp:428-587; constraints as (point, normal) quadruples */
-int og_lp(const float* cons, int n, og_v2 opt, float max_speed, int use_dir_opt, og_v2* out);
-void og_lp3d(const float* cons, int n, int n_obst, float max_speed, int failed, og_v2* out);
+int og_lp(const og_real* cons, int n, og_v2 opt, og_real max_speed, int use_dir_opt, og_v2* out);
+void og_lp3d(const og_real* cons, int n, int n_obst, og_real max_speed, int failed, og_v2* out);
 int og_generate_constraints(const og_obstacles* o, const og_state* s, const og_params* p, int agent,
                             const int* nbrs, int n_nbrs, const int* obst, int n_obst_cand,
-                            float* cons_out, int cap, int* out_n_obst);
+                            og_real* cons_out, int cap, int* out_n_obst);
 
 int og_point_location(const og_ecm* e, og_v2 p);
 int og_retract(const og_ecm* e, og_v2 p, og_v2* out, int* out_edge);

@@ -18,6 +18,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liboracle.so")
+PORT64_SO = os.path.join(HERE, "_build", "liboracle64.so")
 REF_SO = os.path.join(HERE, "_ref", "libecmref.so")
 
 F32, I32, U8 = np.float32, np.int32, np.uint8
@@ -55,6 +56,13 @@ class EcmS(C.Structure):
                 ("he_right", C.c_void_p)]
 
 
+class Params64(C.Structure):
+    _fields_ = [("dt", C.c_double), ("tau_agent", C.c_double), ("tau_obst", C.c_double),
+                ("neighbor_dist", C.c_double), ("max_speed", C.c_double), ("mass", C.c_double),
+                ("arrival_radius", C.c_double), ("delete_radius", C.c_double), ("k", C.c_int),
+                ("knn_mode", C.c_int), ("libm", C.c_int), ("threads", C.c_int)]
+
+
 class Params(C.Structure):
     _fields_ = [("dt", C.c_float), ("tau_agent", C.c_float), ("tau_obst", C.c_float),
                 ("neighbor_dist", C.c_float), ("max_speed", C.c_float), ("mass", C.c_float),
@@ -88,10 +96,12 @@ def _addr(a):
 class Port:
     """The C restatement.  Holds numpy-owned state mirrored to C structs."""
 
-    def __init__(self):
-        if not os.path.exists(PORT_SO):
+    REAL = F32
+
+    def __init__(self, so=PORT_SO):
+        if not os.path.exists(so):
             build()
-        self.lib = C.CDLL(PORT_SO)
+        self.lib = C.CDLL(so)
         L = self.lib
         L.og_tick.restype = C.c_int
         L.og_point_location.restype = C.c_int
@@ -115,17 +125,18 @@ class Port:
 
     # -- structs ---------------------------------------------------------
     def obstacles(self, scene):
-        keep = [np.ascontiguousarray(scene.obst_xy, F32), np.ascontiguousarray(scene.obst_next, I32),
+        keep = [np.ascontiguousarray(scene.obst_xy, self.REAL), np.ascontiguousarray(scene.obst_next, I32),
                 np.ascontiguousarray(scene.obst_prev, I32), np.ascontiguousarray(scene.obst_convex, U8)]
         o = Obst(int(keep[0].shape[0]), *[_addr(a) for a in keep])
         o._keep = keep
         return o
 
     def ecm(self, e):
-        keep = [np.ascontiguousarray(e.v_pos, F32), np.ascontiguousarray(e.v_clear, F32),
+        R = self.REAL
+        keep = [np.ascontiguousarray(e.v_pos, R), np.ascontiguousarray(e.v_clear, R),
                 np.ascontiguousarray(e.v_idx, I32), np.ascontiguousarray(e.v_halfedge, I32),
                 np.ascontiguousarray(e.he_target, I32), np.ascontiguousarray(e.he_next, I32),
-                np.ascontiguousarray(e.he_left, F32), np.ascontiguousarray(e.he_right, F32)]
+                np.ascontiguousarray(e.he_left, R), np.ascontiguousarray(e.he_right, R)]
         s = EcmS(e.n_vertices, _addr(keep[0]), _addr(keep[1]), _addr(keep[2]), _addr(keep[3]),
                  e.n_edges, _addr(keep[4]), _addr(keep[5]), _addr(keep[6]), _addr(keep[7]))
         s._keep = keep
@@ -184,10 +195,13 @@ class Port:
         s = self.state(st)
         n = st.n_slots
         k = params.k if k is None else k
-        res = dict(destroyed=np.zeros(n, I32), replan=np.zeros(n, I32), replan_pos=np.zeros((n, 2), F32))
+        R = self.REAL
+        for f in ("pos", "vel", "attr", "pref_vel", "clear", "pref_speed", "path_xy"):
+            assert getattr(st, f).dtype == R, f"state array {f} must be {np.dtype(R).name}"
+        res = dict(destroyed=np.zeros(n, I32), replan=np.zeros(n, I32), replan_pos=np.zeros((n, 2), R))
         if record:
             res.update(nbr_ids=np.full((n, max(k, 1)), -1, I32), nbr_count=np.zeros(n, I32),
-                       v_orca=np.zeros((n, 2), F32), n_constraints=np.zeros(n, I32),
+                       v_orca=np.zeros((n, 2), R), n_constraints=np.zeros(n, I32),
                        n_obst_constraints=np.zeros(n, I32), lp_fail=np.zeros(n, I32))
         out = TickOut(_addr(res["destroyed"]), 0, _addr(res["replan"]), _addr(res["replan_pos"]), 0,
                       _addr(res.get("nbr_ids")), _addr(res.get("nbr_count")), _addr(res.get("v_orca")),
@@ -234,6 +248,34 @@ class Port:
         L.og_time_sample(C.byref(obst_s), C.byref(ecm_s), C.byref(s), C.byref(params), _addr(sample),
                          int(sample.shape[0]), int(threads), C.byref(tb), C.byref(ta))
         return tb.value, ta.value
+
+
+class Port64(Port):
+    """The same restatement computing in double with the host libm
+    (liboracle64.so, built with -DOG_REAL_DOUBLE): the FP64 run that the FP32
+    tick is measured against.  Its states hold float64 arrays (as_f64)."""
+
+    REAL = np.float64
+
+    def __init__(self):
+        super().__init__(PORT64_SO)
+        self.lib.og_tick.argtypes = [C.POINTER(Obst), C.POINTER(EcmS), C.POINTER(State), C.POINTER(Params64),
+                                     C.c_void_p, C.POINTER(TickOut)]
+
+    @staticmethod
+    def params(**kw):
+        d = dict(dt=1.0 / 60.0, tau_agent=2.0, tau_obst=2.0, neighbor_dist=5.0, max_speed=0.0, mass=0.8,
+                 arrival_radius=20.0, delete_radius=2.0, k=10, knn_mode=0, libm=1, threads=1)
+        d.update(kw)
+        assert d["libm"] == 1, "the FP64 run uses the host libm"
+        return Params64(**d)
+
+    @staticmethod
+    def as_f64(st):
+        c = st.copy()
+        for f in ("pos", "vel", "attr", "pref_vel", "clear", "pref_speed", "path_xy"):
+            setattr(c, f, np.ascontiguousarray(getattr(c, f), np.float64))
+        return c
 
 
 class Ref:
