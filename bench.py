@@ -201,7 +201,7 @@ def apply_launch(plain, learned, args):
                 set_lp_mode(s_, "warp", grab)
             else:
                 set_launch(s_, r["block_size"], grab, r["grid_cell_scale"], r["occupancy_divisor"])
-                set_lp_mode(s_, "thread", 1)
+                set_lp_mode(s_, r["lp_mode"], 1)
         return r
     grab = 4 if args.lp_mode == "warp" else 32
     for s_ in (plain, learned):
@@ -401,11 +401,23 @@ def run_ours(args):
     # velocity, active flag, slot, neighbour count and k indices, and writes
     # pos and vel
     kern = {"k_neighbors": (main_t.tot["neighbors_ms"], 8 + 4 * k), "k_agents": (main_t.tot["orca_ms"], 57 + 4 * k)}
+    fused = launch.get("lp_mode") == "fused" and args.neighbors != "kdtree"
+    if fused:
+        # the search inside the per-agent kernel: the agent's state in and
+        # out (snapshot pos, vel, radius, speed, preferred velocity, active
+        # flag, slot in; pos, vel out); the lists it writes and reads back
+        # are intermediate
+        kern = {"k_agents_knn": (main_t.tot["orca_ms"], 53)}
     if args.neighbors == "kdtree":
         # the kd-tree pipeline (build, query, cache composition) in place of
         # k_neighbors; its algorithmic bytes per agent are derived in DESIGN
         kern = {"kd-tree pipeline": (main_t.tot["neighbors_ms"], KD_BYTES_PER_AGENT(k, (n + spawn_slots).bit_length())),
                 "k_agents": (main_t.tot["orca_ms"], 57 + 4 * k)}
+    kernel_ms = {"k_attract": main_t.tot["attract_ms"] / args.steps}
+    if not fused:
+        kernel_ms["k_neighbors"] = main_t.tot["neighbors_ms"] / args.steps
+    kernel_ms["features+k_mlp_infer"] = main_t.tot["proposal_ms"] / args.steps
+    kernel_ms["k_agents_knn" if fused else "k_agents"] = main_t.tot["orca_ms"] / args.steps
     kname = max(kern, key=lambda q: kern[q][0])
     kern_ms = kern[kname][0] / max(args.steps, 1)
     alg_bytes = kern[kname][1]
@@ -458,10 +470,7 @@ def run_ours(args):
                      "traffic": traffic, "kernel": kname, "kernel_ms": kern_ms, "alg_bytes_per_agent": alg_bytes,
                      "limiter": limiter,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
-                     "kernel_ms_per_tick": {"k_attract": main_t.tot["attract_ms"] / args.steps,
-                                            "k_neighbors": main_t.tot["neighbors_ms"] / args.steps,
-                                            "features+k_mlp_infer": main_t.tot["proposal_ms"] / args.steps,
-                                            "k_agents": main_t.tot["orca_ms"] / args.steps}},
+                     "kernel_ms_per_tick": kernel_ms},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "tick_stats": {"lp3d_per_tick": T["lp3d"] / args.steps, "replans_per_tick": T["replans"] / args.steps,
@@ -538,7 +547,7 @@ def main():
                     help="agents/s per spawn area, 4 spawn areas (UpdateSpawnAreas every tick); 0: none")
     ap.add_argument("--proposal", default=None, help="proposal weights (.npy)")
     ap.add_argument("--no-gate", action="store_true", help="keep the proposal model on every tick")
-    ap.add_argument("--lp-mode", default="tune", choices=["tune", "thread", "warp"],
+    ap.add_argument("--lp-mode", default="tune", choices=["tune", "thread", "warp", "fused"],
                     help="per-agent kernel layout (default: autotuned)")
     args = ap.parse_args()
     if args.warmup < 3:

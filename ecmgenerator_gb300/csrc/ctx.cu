@@ -207,7 +207,7 @@ struct ecmg_ctx {
     int block = 128;
     int tile = 32;
     float cell_scale = 0.4f;
-    int lp_mode = 0; /* 0: one thread per agent, 1: one warp per agent */
+    int lp_mode = 0; /* ECMG_LP_THREAD, ECMG_LP_WARP or ECMG_LP_THREAD_FUSED */
     int occ_div = 1; /* per-thread layout: resident blocks per SM divided by this */
     int wgrab = 4;   /* agents per work grab in warp mode */
 
@@ -1696,7 +1696,7 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t, bool use_model)
     t.slot_rank = c->rank.p;
     t.scenes = c->d_scenes.p;
     t.slot_scene = b.slot_scene;
-    t.tile = c->lp_mode ? c->wgrab : c->tile;
+    t.tile = c->lp_mode == ECMG_LP_WARP ? c->wgrab : c->tile;
     t.lp_mode = c->lp_mode;
     t.occ_div = c->occ_div;
     const ecmg_params& p = c->prm;
@@ -1853,6 +1853,8 @@ int ecmg_kernels_per_tick(const ecmg_ctx* c)
     if (c->nbr_mode == ECMG_NEIGHBORS_KDTREE) {
         const int L = c->kd.levels;
         n += -1 + 6 + 84 + 1 + 11 + (L - 1) + 5 * std::max(0, L - 2) + 2 + 4;
+    } else if (c->lp_mode == ECMG_LP_THREAD_FUSED && !c->model && !c->trace) {
+        n -= 1; /* the search runs inside the per-agent kernel */
     }
     return n;
 }
@@ -2154,9 +2156,16 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
                 st = trial(Launch{cell, 0, b, tl, dv, c->wgrab}, &better);
             }
     }
+    /* the per-thread layout fused with the neighbour search, at the best
+       per-thread launch (the kd-tree mode builds its lists separately) */
+    const Launch thr = bestL;
+    for (int dv : divs) {
+        if (st != ECMG_OK || c->nbr_mode == ECMG_NEIGHBORS_KDTREE) break;
+        st = trial(Launch{cell, ECMG_LP_THREAD_FUSED, thr.block, thr.tile, dv, c->wgrab}, &better);
+    }
     for (int w : wgrabs) {
         if (st != ECMG_OK || c->nbr_mode == ECMG_NEIGHBORS_KDTREE) break; /* one thread per agent there */
-        st = trial(Launch{cell, 1, bestL.block, bestL.tile, 1, w}, &better);
+        st = trial(Launch{cell, 1, thr.block, thr.tile, 1, w}, &better);
     }
     if (st != ECMG_OK) {
         c->replan_enabled = true;
@@ -2178,7 +2187,7 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
     sp.free_(); sv.free_(); sa.free_(); spv.free_(); sact.free_();
     if (out) {
         out->block_size = bb;
-        out->agents_per_warp_grab = bmode ? bw : bt;
+        out->agents_per_warp_grab = bmode == ECMG_LP_WARP ? bw : bt;
         out->lp_mode = bmode;
         out->grid_cell_scale = bs;
         out->best_tick_ms = best;
@@ -2230,7 +2239,8 @@ ecmg_status ecmg_set_neighbor_mode(ecmg_ctx* c, int mode)
 
 ecmg_status ecmg_set_lp_mode(ecmg_ctx* c, int mode, int agents_per_warp_grab)
 {
-    if (!c || (mode != ECMG_LP_THREAD && mode != ECMG_LP_WARP)) return ECMG_ERR_INVALID_ARG;
+    if (!c || (mode != ECMG_LP_THREAD && mode != ECMG_LP_WARP && mode != ECMG_LP_THREAD_FUSED))
+        return ECMG_ERR_INVALID_ARG;
     if (mode == ECMG_LP_WARP && c->nbr_mode == ECMG_NEIGHBORS_KDTREE)
         return fail(c, ECMG_ERR_STATE, "the kd-tree neighbour mode runs one thread per agent");
     if (mode == ECMG_LP_WARP && (agents_per_warp_grab < 1 || agents_per_warp_grab > 64)) return ECMG_ERR_INVALID_ARG;

@@ -5,9 +5,12 @@
  *   k_bin      bucket every active slot into the uniform agent grid
  *   k_scan_*   exclusive scan of the bucket counts
  *   k_scatter  tick-start snapshot of position/velocity/radius in grid order
- *   k_agents   one thread per agent: attraction point (IRM), preferred
- *              velocity, exact kNN on the grid, obstacle + agent ORCA
- *              half-planes, 2D LP (+3D LP), velocity and position update
+ *   k_attract  attraction point (IRM) and preferred velocity (second stream)
+ *   k_neighbors exact kNN on the grid
+ *   k_agents   one thread per agent: obstacle + agent ORCA half-planes,
+ *              2D LP (+3D LP), velocity and position update
+ *              (k_agents_warp: one warp per agent; k_agents_knn: the kNN and
+ *              the step in one persistent kernel)
  * The snapshot makes the tick Jacobi-exact: neighbours are read from the
  * tick-start copy while each thread writes its own slot, which is what the
  * reference's system order guarantees (velocities change only in
@@ -568,25 +571,29 @@ __device__ void orca_tick(const TickArgs& a, int t)
 /* neighbour lists of every grid-order agent of the tick (KNearestAgents,
    KDTree.cpp:85-202, as the exact (d2, slot) query of the grid) */
 template <int K>
+__device__ __forceinline__ void knn_agent(const TickArgs& a, int t, int slot)
+{
+    const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
+    Knn<K> nn;
+    knn_grid<K>(nn, a.k, a.s_pos[t], a.rnb, a.rnb2, a.s_pos, a.s_slot, a.cell_start + sc.bucket_base, sc.grid);
+    a.ncnt[t] = nn.cnt;
+    int* o = a.nbr + (size_t)t * a.k;
+#pragma unroll
+    for (int q2 = 0; q2 < K; q2++) {
+        const int q = q2 - (K - a.k);
+        if (q >= 0) {
+            const int sl = (int)(unsigned)nn.key[q2];
+            o[q] = q < nn.cnt ? a.cell_start[a.slot_bucket[sl]] + a.slot_rank[sl] : -1;
+        }
+    }
+}
+
+template <int K>
 __global__ void __launch_bounds__(128) k_neighbors(TickArgs a)
 {
     const int n = a.counters[C_NSORTED];
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int slot = a.s_slot[t];
-        const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
-        Knn<K> nn;
-        knn_grid<K>(nn, a.k, a.s_pos[t], a.rnb, a.rnb2, a.s_pos, a.s_slot, a.cell_start + sc.bucket_base, sc.grid);
-        a.ncnt[t] = nn.cnt;
-        int* o = a.nbr + (size_t)t * a.k;
-#pragma unroll
-        for (int q2 = 0; q2 < K; q2++) {
-            const int q = q2 - (K - a.k);
-            if (q >= 0) {
-                const int sl = (int)(unsigned)nn.key[q2];
-                o[q] = q < nn.cnt ? a.cell_start[a.slot_bucket[sl]] + a.slot_rank[sl] : -1;
-            }
-        }
-    }
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+        knn_agent<K>(a, t, a.s_slot[t]);
 }
 
 /* UpdateAttractionPointSystem + ApplySteeringForce for every agent */
@@ -665,6 +672,32 @@ __global__ void __launch_bounds__(256) k_agents(TickArgs a)
         for (int o = 0; o < a.tile; o += 32) {
             int t = base + o + lane;
             if (t < n) orca_tick<K>(a, t);
+        }
+    }
+}
+
+/* the per-thread layout fused with the neighbour search (ECMG_LP_THREAD_FUSED):
+   each thread finds its agent's k nearest, then runs the agent's step, so
+   that warps in the ALU-bound search and warps in the issue-bound LPs share
+   every SM.  Agents destroyed by the attraction kernel get no list (no later
+   stage of a plain tick reads it). */
+template <int K>
+__global__ void __launch_bounds__(256) k_agents_knn(TickArgs a)
+{
+    const int n = a.counters[C_NSORTED];
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&a.counters[C_WORK], a.tile);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        for (int o = 0; o < a.tile; o += 32) {
+            const int t = base + o + lane;
+            if (t >= n) continue;
+            const int slot = a.s_slot[t];
+            if (!a.active[slot]) continue;
+            knn_agent<K>(a, t, slot);
+            orca_tick<K>(a, t);
         }
     }
 }
@@ -1112,22 +1145,24 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
         if (e != cudaSuccess) return e;
     }
     if (ev) cudaEventRecordWithFlags(ev[1], s2, evflags);
+    /* the fused layout runs the neighbour search inside the per-agent kernel
+       (not with a learned proposal, whose features need every list first) */
+    const bool fused = t.lp_mode == 2 && !kd && !t.feat;
     if (kd) {
         /* the reference's kd-tree: build and per-member query beside the
            attraction kernel, the cache composition after it */
         e = kd_build_and_query(*kd, s, sms);
         if (e != cudaSuccess) return e;
-    } else if (t.k <= 8) {
-        k_neighbors<8><<<gk, 128, 0, s>>>(t);
-    } else if (t.k <= 16) {
-        k_neighbors<16><<<gk, 128, 0, s>>>(t);
-    } else {
-        k_neighbors<32><<<gk, 128, 0, s>>>(t);
+    } else if (!fused) {
+        if (t.k <= 8) k_neighbors<8><<<gk, 128, 0, s>>>(t);
+        else if (t.k <= 16) k_neighbors<16><<<gk, 128, 0, s>>>(t);
+        else k_neighbors<32><<<gk, 128, 0, s>>>(t);
     }
-    if (ev && !kd) cudaEventRecordWithFlags(ev[2], s, evflags);
+    if (ev && !kd && !fused) cudaEventRecordWithFlags(ev[2], s, evflags);
     e = cudaEventRecord(ev_join, s2);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_join, 0);
     if (e != cudaSuccess) return e;
+    if (ev && fused) cudaEventRecordWithFlags(ev[2], s, evflags);
     if (kd) {
         e = kd_finish(*kd, s, sms);
         if (e != cudaSuccess) return e;
@@ -1151,6 +1186,18 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
         } else {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_warp<32>, 256, 0);
             k_agents_warp<32><<<sms * (per_sm > 0 ? per_sm : 1), 256, 0, s>>>(t);
+        }
+    } else if (fused) {
+        const int div = t.occ_div > 1 ? t.occ_div : 1;
+        if (t.k <= 8) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_knn<8>, block, 0);
+            k_agents_knn<8><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
+        } else if (t.k <= 16) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_knn<16>, block, 0);
+            k_agents_knn<16><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
+        } else {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_knn<32>, block, 0);
+            k_agents_knn<32><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
         }
     } else {
         /* persistent grid: the resident blocks per SM, divided by occ_div

@@ -480,7 +480,7 @@ def autotune(sim: Simulator, ticks_per_trial: int = 2) -> dict:
     sim._ck(sim.L.ecmg_autotune(sim.h, int(ticks_per_trial), C.byref(r)))
     return dict(block_size=r.block_size, agents_per_warp_grab=r.agents_per_warp_grab,
                 grid_cell_scale=r.grid_cell_scale, best_tick_ms=r.best_tick_ms, trials=r.trials,
-                lp_mode=("warp" if r.lp_mode == 1 else "thread"), occupancy_divisor=r.occupancy_divisor)
+                lp_mode={0: "thread", 1: "warp", 2: "fused"}[r.lp_mode], occupancy_divisor=r.occupancy_divisor)
 
 
 def set_launch(sim: Simulator, block_size: int, agents_per_warp_grab: int, grid_cell_scale: float,
@@ -491,9 +491,10 @@ def set_launch(sim: Simulator, block_size: int, agents_per_warp_grab: int, grid_
 
 
 def set_lp_mode(sim: Simulator, mode: str = "warp", agents_per_warp_grab: int = 4):
-    """per-agent kernel layout: "thread" (one thread per agent) or "warp"
-    (one warp per agent); results are identical"""
-    m = {"thread": 0, "warp": 1}[mode]
+    """per-agent kernel layout: "thread" (one thread per agent), "warp"
+    (one warp per agent) or "fused" (one thread per agent, the neighbour
+    search in the same kernel); results are identical"""
+    m = {"thread": 0, "warp": 1, "fused": 2}[mode]
     sim._ck(sim.L.ecmg_set_lp_mode(sim.h, m, int(agents_per_warp_grab)))
 
 

@@ -326,7 +326,7 @@ typedef struct {
     float grid_cell_scale;
     float best_tick_ms;
     int trials;
-    int lp_mode;             /* ECMG_LP_THREAD or ECMG_LP_WARP */
+    int lp_mode;             /* ECMG_LP_THREAD, ECMG_LP_WARP or ECMG_LP_THREAD_FUSED */
     int occupancy_divisor;   /* per-thread layout: resident blocks per SM divided by this */
 } ecmg_tune_result;
 ecmg_status ecmg_set_launch(ecmg_ctx* ctx, int block_size, int agents_per_warp_grab, float grid_cell_scale);
@@ -334,13 +334,18 @@ ecmg_status ecmg_set_launch(ecmg_ctx* ctx, int block_size, int agents_per_warp_g
    grabs of agents_per_warp_grab from ecmg_set_launch).  ECMG_LP_WARP: one
    warp per agent -- the lanes build the constraints in parallel and share
    the inner loops of the LPs -- taking agents_per_warp_grab agents per work
-   grab (1..64).  Both give identical results. */
+   grab (1..64).  ECMG_LP_THREAD_FUSED: the per-thread layout with the
+   neighbour search in the same kernel (each thread finds its agent's k
+   nearest, then steps it; the separate search kernel is skipped; with a
+   learned proposal or the kd-tree neighbour mode the per-thread layout runs
+   instead).  All give identical results. */
 /* per-thread layout: run the persistent per-agent kernel with the resident
    blocks per SM divided by `divisor` (1..8; fewer resident warps leave more
    L1 to each thread's local constraint arrays) */
 ecmg_status ecmg_set_occupancy(ecmg_ctx* ctx, int divisor);
 #define ECMG_LP_THREAD 0
 #define ECMG_LP_WARP 1
+#define ECMG_LP_THREAD_FUSED 2
 ecmg_status ecmg_set_lp_mode(ecmg_ctx* ctx, int mode, int agents_per_warp_grab);
 /* Neighbour query of the tick.  ECMG_NEIGHBORS_EXACT (default): the exact k
    nearest within neighbor_dist, ordered by (d^2, index).

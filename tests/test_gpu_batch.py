@@ -20,13 +20,15 @@ def _scene(seed, n, w=60.0):
     return s, st, paths
 
 
-def test_batch_matches_oracle_per_scene(port):
-    from ecmgenerator_gb300.simulator import BatchSimulator
+@pytest.mark.parametrize("mode", ["thread", "fused"])
+def test_batch_matches_oracle_per_scene(port, mode):
+    from ecmgenerator_gb300.simulator import BatchSimulator, set_lp_mode
 
     specs = [(21, 120, 40.0), (22, 400, 60.0), (23, 37, 30.0)]
     data = [_scene(*sp) for sp in specs]
     caps = [d[1].n_slots for d in data]
     sim = BatchSimulator([d[0] for d in data], caps, 1.0 / 60.0, max_neighbors=10, **ORCA)
+    set_lp_mode(sim, mode, 1)
     sim.set_record(True)
     bases = []
     for i, (s, st, paths) in enumerate(data):

@@ -165,7 +165,7 @@ def _pair(n_agents=1000, ticks=30, mode=None):
     return a, b
 
 
-@pytest.mark.parametrize("mode", ["thread", "warp"])
+@pytest.mark.parametrize("mode", ["thread", "warp", "fused"])
 def test_true_classes_as_proposals_are_accepted_and_exact(lib, mode):
     torch = _torch()
     from ecmgenerator_gb300 import proposal as P
@@ -191,7 +191,7 @@ def test_true_classes_as_proposals_are_accepted_and_exact(lib, mode):
     b.close()
 
 
-@pytest.mark.parametrize("mode", ["thread", "warp"])
+@pytest.mark.parametrize("mode", ["thread", "warp", "fused"])
 def test_wrong_proposals_are_rejected_and_results_unchanged(lib, mode):
     torch = _torch()
 

@@ -79,6 +79,13 @@ def test_tick_bitexact_warp_layout(port, c1_small):
     _run(port, scene, st, paths, ticks=40, k=10, lp_mode="warp", grab=3)
 
 
+@pytest.mark.parametrize("k", [1, 5, 10, 16, 32])
+def test_tick_bitexact_fused_layout(port, c1_small, k):
+    """the neighbour search inside the per-agent kernel: the same bits"""
+    scene, st, paths = c1_small
+    _run(port, scene, st, paths, ticks=40 if k == 10 else 4, k=k, lp_mode="fused")
+
+
 @pytest.mark.parametrize("k", [1, 16, 32])
 def test_tick_bitexact_warp_k(port, c1_small, k):
     scene, st, paths = c1_small
@@ -96,7 +103,7 @@ def test_tick_bitexact_warp_dense(port):
     paths = Planner(scene).find_paths(st.pos, st.goal, st.clear)
     paths = [p if p is not None else np.stack([st.pos[i], st.goal[i]]) for i, p in enumerate(paths)]
     st.set_paths(paths)
-    for mode in ("thread", "warp"):
+    for mode in ("thread", "warp", "fused"):
         ev = _run(port, scene, st, paths, ticks=6, k=16, lp_mode=mode)
         assert ev > 1000
 
