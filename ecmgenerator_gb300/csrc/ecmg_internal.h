@@ -43,6 +43,7 @@ enum {
     C_PROPOSED = 8,    /* LPs that received a learned proposal */
     C_ACCEPTED = 9,    /* proposals that passed the exact check */
     C_REPLAN_DEV = 10, /* re-plans that fail at the start retraction (not listed) */
+    C_NBR_WORK = 11,   /* work counter of the persistent neighbour kernel */
     kCounters = 16
 };
 

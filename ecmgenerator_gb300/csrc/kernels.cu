@@ -588,12 +588,22 @@ __device__ __forceinline__ void knn_agent(const TickArgs& a, int t, int slot)
     }
 }
 
+/* persistent: a warp takes 32 consecutive grid-order agents per work grab
+   (neighbouring agents: their candidates share L1), so that warps whose
+   agents have more candidates do not leave the SMs' last wave ragged */
 template <int K>
 __global__ void __launch_bounds__(128) k_neighbors(TickArgs a)
 {
     const int n = a.counters[C_NSORTED];
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
-        knn_agent<K>(a, t, a.s_slot[t]);
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&a.counters[C_NBR_WORK], 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const int t = base + lane;
+        if (t < n) knn_agent<K>(a, t, a.s_slot[t]);
+    }
 }
 
 /* UpdateAttractionPointSystem + ApplySteeringForce for every agent */
@@ -1154,9 +1164,18 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
         e = kd_build_and_query(*kd, s, sms);
         if (e != cudaSuccess) return e;
     } else if (!fused) {
-        if (t.k <= 8) k_neighbors<8><<<gk, 128, 0, s>>>(t);
-        else if (t.k <= 16) k_neighbors<16><<<gk, 128, 0, s>>>(t);
-        else k_neighbors<32><<<gk, 128, 0, s>>>(t);
+        /* one resident wave of the persistent search */
+        int pn = 1;
+        if (t.k <= 8) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pn, k_neighbors<8>, 128, 0);
+            k_neighbors<8><<<sms * (pn > 0 ? pn : 1), 128, 0, s>>>(t);
+        } else if (t.k <= 16) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pn, k_neighbors<16>, 128, 0);
+            k_neighbors<16><<<sms * (pn > 0 ? pn : 1), 128, 0, s>>>(t);
+        } else {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pn, k_neighbors<32>, 128, 0);
+            k_neighbors<32><<<sms * (pn > 0 ? pn : 1), 128, 0, s>>>(t);
+        }
     }
     if (ev && !kd && !fused) cudaEventRecordWithFlags(ev[2], s, evflags);
     e = cudaEventRecord(ev_join, s2);
