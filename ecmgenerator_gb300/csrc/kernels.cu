@@ -592,7 +592,7 @@ __device__ __forceinline__ void knn_agent(const TickArgs& a, int t, int slot)
    (neighbouring agents: their candidates share L1), so that warps whose
    agents have more candidates do not leave the SMs' last wave ragged */
 template <int K>
-__global__ void __launch_bounds__(128) k_neighbors(TickArgs a)
+__global__ void __launch_bounds__(128, (K <= 16) ? 8 : 1) k_neighbors(TickArgs a)
 {
     const int n = a.counters[C_NSORTED];
     const int lane = threadIdx.x & 31;
