@@ -670,7 +670,7 @@ __global__ void __launch_bounds__(128) k_features(TickArgs a)
 /* persistent kernel: a warp takes `tile` consecutive grid-order agents per
    work grab (one atomic per grab) and runs them 32 at a time */
 template <int K>
-__global__ void __launch_bounds__(256) k_agents(TickArgs a)
+__global__ void __launch_bounds__(256, (K <= 16) ? 4 : 1) k_agents(TickArgs a)
 {
     const int n = a.counters[C_NSORTED];
     const int lane = threadIdx.x & 31;
