@@ -55,10 +55,10 @@ def dist_env():
     return rank, world, local
 
 
-def make_workload(name, seed):
+def make_workload(name, seed, planner="reference"):
     from ecmgenerator_gb300.workloads import make_workload as mk
 
-    return mk(name, seed)
+    return mk(name, seed, planner=planner)
 
 
 class ClockSampler:
@@ -285,7 +285,7 @@ def run_ours(args):
             sims.append(s_)
         spawn_slots = 0
     else:
-        cfg, scene, st, paths, k = make_workload(args.workload, args.seed)
+        cfg, scene, st, paths, k = make_workload(args.workload, args.seed, args.planner)
         n = st.num_agents
         scene_desc = f'{cfg["w"]:.0f}x{cfg["h"]:.0f} m, {cfg["boxes"]} boxes'
         sims = []
@@ -306,6 +306,11 @@ def run_ours(args):
             s_.push_spawn_random(stream)
         sims.append(s_)
     plain, learned = sims
+    if args.planner != "reference":
+        from ecmgenerator_gb300.simulator import set_planner_mode
+
+        for s_ in sims:
+            set_planner_mode(s_, args.planner)
     if args.neighbors == "kdtree":
         # the reference's kd-tree query (no learned proposal in this mode)
         from ecmgenerator_gb300.simulator import set_neighbor_mode
@@ -452,6 +457,7 @@ def run_ours(args):
                    "l2": "flushed before every timed tick (512 MB write)", "parallelism": f"replicas x{world}",
                    "seed": args.seed, "mode": "learned proposal" if model is not None else "plain",
                    "neighbors": args.neighbors,
+                   "planner": args.planner,
                    "launch": launch},
         "plain": {"value": plain_value, "ms_per_step": p_ms_all / args.steps,
                   "lp3d_per_tick": tp.tot["lp3d"] / args.steps,
@@ -545,6 +551,9 @@ def main():
                     help="exact kNN (default) or the reference's kd-tree query with its neighbour cache")
     ap.add_argument("--spawn-rate", type=float, default=0.0,
                     help="agents/s per spawn area, 4 spawn areas (UpdateSpawnAreas every tick); 0: none")
+    ap.add_argument("--planner", default="reference", choices=["reference", "fast"],
+                    help="host planner of the initial paths and re-plans: the reference's FindPath restated "
+                         "(default) or the opt-in fast A* (not the reference's paths)")
     ap.add_argument("--proposal", default=None, help="proposal weights (.npy)")
     ap.add_argument("--no-gate", action="store_true", help="keep the proposal model on every tick")
     ap.add_argument("--lp-mode", default="tune", choices=["tune", "thread", "warp", "fused"],

@@ -19,7 +19,7 @@ extern "C" {
 struct ecmg_planner {
     HostScene scene;
     GridCSR vis;
-    int mode = ECMG_PLANNER_FAST;
+    int mode = ECMG_PLANNER_REFERENCE;
 };
 
 ecmg_status ecmg_planner_create(const ecmg_obstacles* o, const ecmg_ecm* e, ecmg_planner** out)
@@ -118,26 +118,40 @@ ecmg_status ecmg_planner_locate(ecmg_planner* pl, int n, const float* xy, int* o
 
 /* Simulator::ValidSpawnLocation (Simulator.cpp:295-311) on the device state */
 
+}  // extern "C"
+
 /* ---------------------------------------------------------------------- */
-static AgentGrid knn_grid_of(float x0, float y0, float x1, float y1, float cell)
+/* The grid of the stand-alone kNN: cells of `cell` metres over the box with
+   one spare ring and one overflow bucket.  Sizes are computed in double and
+   refused (false) when the box or the cell is not finite or the grid would
+   exceed kKnnMaxCells cells, so that no int below overflows. */
+bool ecmg::knn_grid_of(float x0, float y0, float x1, float y1, float cell, AgentGrid* out)
 {
+    if (!std::isfinite(x0) || !std::isfinite(y0) || !std::isfinite(x1) || !std::isfinite(y1)) return false;
+    if (!(cell > 0.0f) || !std::isfinite(cell) || !(x1 >= x0) || !(y1 >= y0)) return false;
+    const double gw = std::ceil(((double)x1 - (double)x0) / (double)cell) + 3.0;
+    const double gh = std::ceil(((double)y1 - (double)y0) / (double)cell) + 3.0;
+    if (!(gw * gh <= (double)kKnnMaxCells)) return false;
     AgentGrid g;
     g.cell = cell;
     g.inv = 1.0f / cell;
     g.x0 = x0 - cell;
     g.y0 = y0 - cell;
-    g.gw = (int)std::ceil(std::max(0.0f, x1 - x0) / cell) + 3;
-    g.gh = (int)std::ceil(std::max(0.0f, y1 - y0) / cell) + 3;
+    g.gw = (int)gw;
+    g.gh = (int)gh;
     g.ncells = g.gw * g.gh;
-    return g;
+    *out = g;
+    return true;
 }
+
+extern "C" {
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 size_t ecmg_knn_scratch_bytes(int n, float min_x, float min_y, float max_x, float max_y, float cell)
 {
-    if (n < 0 || !(cell > 0.0f) || !(max_x >= min_x) || !(max_y >= min_y)) return 0;
-    AgentGrid g = knn_grid_of(min_x, min_y, max_x, max_y, cell);
+    AgentGrid g;
+    if (n < 0 || !knn_grid_of(min_x, min_y, max_x, max_y, cell, &g)) return 0;
     size_t nb = (size_t)g.ncells + 1;
     size_t b = 0;
     b += align256(sizeof(int) * (size_t)std::max(1, n)) * 3; /* key, rank, s_slot */
@@ -157,7 +171,8 @@ ecmg_status ecmg_knn(const float* dev_pos, const unsigned char* dev_active, int 
     if (!dev_pos || !dev_active || !dev_out_ids || !dev_out_count || !dev_scratch) return ECMG_ERR_INVALID_ARG;
     size_t need = ecmg_knn_scratch_bytes(n, min_x, min_y, max_x, max_y, cell);
     if (need == 0 || scratch_bytes < need) return ECMG_ERR_INVALID_ARG;
-    AgentGrid g = knn_grid_of(min_x, min_y, max_x, max_y, cell);
+    AgentGrid g;
+    if (!knn_grid_of(min_x, min_y, max_x, max_y, cell, &g)) return ECMG_ERR_INVALID_ARG;
     size_t nb = (size_t)g.ncells + 1;
     char* p = (char*)dev_scratch;
     auto take = [&](size_t bytes) { char* r = p; p += align256(bytes); return r; };

@@ -240,7 +240,7 @@ struct ecmg_ctx {
     void* plan_user = nullptr;
     PlanScratch scratch;
     HostPool pool; /* planner threads (built-in planner only: it is re-entrant) */
-    int planner_mode = ECMG_PLANNER_FAST;
+    int planner_mode = ECMG_PLANNER_REFERENCE; /* the reference's paths unless FAST is chosen */
     bool replan_enabled = true;
     bool spawn_enabled = true; /* off while the autotuner runs its trial ticks */
     /* per slot: the start edge from which the built-in planner's search

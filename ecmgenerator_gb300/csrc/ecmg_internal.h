@@ -142,6 +142,7 @@ struct BinArgs {
     const SceneDev* scenes;   /* batch: per-scene grid and bucket base */
     const int* slot_scene;
     int total_buckets;        /* sum over scenes of (cells + overflow) */
+    int n_fixed;              /* > 0: bin slots [0, n_fixed) (stand-alone kNN); 0: [0, counters[C_LAST]] */
 };
 
 /* kernels.cu; propose (may be null) runs between the feature kernel and the
@@ -161,6 +162,11 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
                         cudaStream_t s, cudaStream_t s2, cudaEvent_t ev_fork, cudaEvent_t ev_join,
                         const cudaEvent_t* ev, ProposeFn propose, void* propose_user,
                         HookFn after_attract, void* after_attract_user, const KdArgs* kd);
+/* api_host.cu: the checked grid of the stand-alone kNN (ecmg_knn,
+   ecmg_knn_noalloc); false for a non-finite box or cell, or more than
+   kKnnMaxCells cells */
+constexpr double kKnnMaxCells = 32.0e6;
+bool knn_grid_of(float x0, float y0, float x1, float y1, float cell, AgentGrid* out);
 cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k, float r, AgentGrid g,
                        int* key, int* rank, int* cell_count, int* cell_start, int* s_slot, V2* s_pos,
                        int* scan_tmp, int scan_blocks, int* out_ids, int* out_cnt, cudaStream_t s);

@@ -48,7 +48,7 @@ __device__ __forceinline__ int bucket_of(const AgentGrid& g, V2 p)
 
 __global__ void k_bin(BinArgs a)
 {
-    int last = a.counters[C_LAST];
+    const int last = a.n_fixed > 0 ? a.n_fixed - 1 : a.counters[C_LAST];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= last; i += gridDim.x * blockDim.x) {
         if (!a.active[i]) continue;
         int b;
@@ -65,7 +65,7 @@ __global__ void k_bin(BinArgs a)
 
 __global__ void k_scatter(BinArgs a)
 {
-    int last = a.counters[C_LAST];
+    const int last = a.n_fixed > 0 ? a.n_fixed - 1 : a.counters[C_LAST];
     if (blockIdx.x == 0 && threadIdx.x == 0) a.counters[C_NSORTED] = a.cell_start[a.total_buckets];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= last; i += gridDim.x * blockDim.x) {
         if (!a.active[i]) continue;
@@ -1249,10 +1249,9 @@ cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k,
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(out_cnt, 0, sizeof(int) * (size_t)n, s);
     if (e != cudaSuccess) return e;
-    int last = n - 1;
-    e = cudaMemcpyAsync(counters + C_LAST, &last, sizeof(int), cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return e;
+    /* the slot range is passed by value: the query queues no host-to-device copy */
     BinArgs b{};
+    b.n_fixed = n;
     b.pos = pos;
     b.active = active;
     b.key = key;

@@ -18,6 +18,11 @@
  * call's contents: the bucket counters that must start at zero are cleared by
  * every call, and calls that overlap on the GPU (different streams, or
  * different host threads on one device) race on it.
+ *
+ * The cached address belongs to the device's primary context, the one the
+ * CUDA runtime uses.  A caller that makes another context current through the
+ * driver API, or that resets the device (cudaDeviceReset) after the first
+ * call, is not supported: the cached address would not be valid there.
  */
 #include "../../include/ecmg.h"
 #include "ecmg_internal.h"
@@ -58,15 +63,9 @@ extern "C" ecmg_status ecmg_knn_noalloc(const float* dev_pos, const unsigned cha
         }
         base = g_addr[dev];
     }
-    /* the same partition of the scratch as ecmg_knn */
+    /* the same grid and partition of the scratch as ecmg_knn */
     AgentGrid g;
-    g.cell = cell;
-    g.inv = 1.0f / cell;
-    g.x0 = min_x - cell;
-    g.y0 = min_y - cell;
-    g.gw = (int)ceilf(fmaxf(0.0f, max_x - min_x) / cell) + 3;
-    g.gh = (int)ceilf(fmaxf(0.0f, max_y - min_y) / cell) + 3;
-    g.ncells = g.gw * g.gh;
+    if (!knn_grid_of(min_x, min_y, max_x, max_y, cell, &g)) return ECMG_ERR_INVALID_ARG;
     size_t nb = (size_t)g.ncells + 1;
     char* p = (char*)base;
     auto take = [&](size_t bytes) { char* r = p; p += a256(bytes); return r; };

@@ -27,9 +27,10 @@ def _ptr(x):
 class Planner:
     """Host-only ECM planner (ecmg_planner_*); needs no GPU."""
 
-    def __init__(self, scene, mode: str = "fast"):
-        """mode 'fast' (A* with landmark bounds, greedy shortening) or
-        'reference' (ECMPathPlanner::FindPath restated: the reference's paths)"""
+    def __init__(self, scene, mode: str = "reference"):
+        """mode 'reference' (default: ECMPathPlanner::FindPath restated, the
+        reference's paths) or 'fast' (opt-in: A* with landmark bounds and
+        greedy shortening, not the reference's paths)"""
         L = self.L = _lib.load()
         self._keep, o, e = _scene_structs(scene)
         h = C.c_void_p()
@@ -37,7 +38,7 @@ class Planner:
         if rc:
             raise EcmgError(rc, "ecmg_planner_create failed")
         self.h = h
-        if mode != "fast":
+        if mode != "reference":
             rc = L.ecmg_planner_set_mode(self.h, {"fast": 0, "reference": 1}[mode])
             if rc:
                 raise EcmgError(rc, "ecmg_planner_set_mode failed")
@@ -507,6 +508,6 @@ def set_neighbor_mode(sim: Simulator, mode: str = "kdtree"):
 
 
 def set_planner_mode(sim: Simulator, mode: str = "reference"):
-    """built-in planner of re-plans and spawns: 'fast' (default) or
-    'reference' (the reference planner's paths), ecmg_set_planner_mode"""
+    """built-in planner of re-plans and spawns: 'reference' (default, the
+    reference planner's paths) or 'fast' (opt-in), ecmg_set_planner_mode"""
     sim._ck(sim.L.ecmg_set_planner_mode(sim.h, {"fast": 0, "reference": 1}[mode]))

@@ -33,8 +33,10 @@ ORCA = dict(tau_agent=2.0, tau_obst=2.0, neighbor_dist=5.0)
 DT = 1.0 / 60.0
 
 
-def make_workload(name, seed, verbose=True):
-    """(cfg, scene, agent state with planned paths, paths, k)"""
+def make_workload(name, seed, verbose=True, planner="reference"):
+    """(cfg, scene, agent state with planned paths, paths, k); the initial
+    paths come from the reference planner (ECMPathPlanner::FindPath restated)
+    unless planner="fast"; an agent without a path walks straight to its goal"""
     from . import agents as ag
     from .simulator import Planner
 
@@ -43,13 +45,13 @@ def make_workload(name, seed, verbose=True):
     t0 = time.time()
     scene = ag.build_scene(cfg, seed)
     st = ag.spawn_agents(cfg, scene, seed)
-    pl = Planner(scene)
+    pl = Planner(scene, mode=planner)
     n = st.num_agents
     paths = []
     chunk = 100_000
     for a in range(0, n, chunk):
         b = min(n, a + chunk)
-        got = pl.find_paths(st.pos[a:b], st.goal[a:b], st.clear[a:b], threads=0, cap=64)
+        got = pl.find_paths(st.pos[a:b], st.goal[a:b], st.clear[a:b], threads=0, cap=256)
         for i, p in enumerate(got):
             if p is None:
                 p = np.stack([st.pos[a + i], st.goal[a + i]])
@@ -121,7 +123,7 @@ def _batch_scene(job):
     scene = ag.build_scene(cfg, seed)
     st = ag.spawn_agents(cfg, scene, seed)
     pl = Planner(scene)
-    got = pl.find_paths(st.pos[:n], st.goal[:n], st.clear[:n], threads=1, cap=64)
+    got = pl.find_paths(st.pos[:n], st.goal[:n], st.clear[:n], threads=1, cap=256)
     pl.close()
     paths = [np.asarray(p if p is not None else np.stack([st.pos[i], st.goal[i]]), np.float32)
              for i, p in enumerate(got)]

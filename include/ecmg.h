@@ -148,13 +148,14 @@ ecmg_status ecmg_set_obstacles(ecmg_ctx* ctx, const ecmg_obstacles* o);
 ecmg_status ecmg_set_ecm(ecmg_ctx* ctx, const ecmg_ecm* e);
 /* replaces the built-in A* planner (NULL restores it) */
 ecmg_status ecmg_set_planner(ecmg_ctx* ctx, ecmg_plan_fn fn, void* user);
-/* Built-in planner.  ECMG_PLANNER_FAST (default): A* over the ECM vertices
-   with the clearance filter (landmark lower bounds), then the polyline is
-   shortened greedily where a straight piece keeps the clearance.
-   ECMG_PLANNER_REFERENCE: ECMPathPlanner::FindPath restated
-   (ECMPathPlanner.cpp:22-411, AStar.cpp:44-210): the reference's A* --
-   its open list included --, corridor, portals and funnel, giving the
-   reference planner's paths. */
+/* Built-in planner.  ECMG_PLANNER_REFERENCE (default):
+   ECMPathPlanner::FindPath restated (ECMPathPlanner.cpp:22-411,
+   AStar.cpp:44-210): the reference's A* -- its open list included --,
+   corridor, portals and funnel, giving the reference planner's paths.
+   ECMG_PLANNER_FAST (opt-in, not the reference's paths): A* over the ECM
+   vertices with the clearance filter (landmark lower bounds), then the
+   polyline is shortened greedily where a straight piece keeps the
+   clearance. */
 #define ECMG_PLANNER_FAST 0
 #define ECMG_PLANNER_REFERENCE 1
 ecmg_status ecmg_set_planner_mode(ecmg_ctx* ctx, int mode);
@@ -189,7 +190,7 @@ ecmg_status ecmg_planner_destroy(ecmg_planner* p);
 ecmg_status ecmg_planner_find_paths(ecmg_planner* p, int n, const float* starts, const float* goals,
                                     const float* clearances, int threads, int cap_per_path,
                                     float* out_xy, int* out_n);
-/* ECMG_PLANNER_FAST (default) or ECMG_PLANNER_REFERENCE, as ecmg_set_planner_mode */
+/* ECMG_PLANNER_REFERENCE (default) or ECMG_PLANNER_FAST, as ecmg_set_planner_mode */
 ecmg_status ecmg_planner_set_mode(ecmg_planner* p, int mode);
 /* ECMGraph::FindCell for n points: cell index (2*edge + side) or -1 */
 ecmg_status ecmg_planner_locate(ecmg_planner* p, int n, const float* xy, int* out_cell);
@@ -394,8 +395,10 @@ ecmg_status ecmg_knn(const float* dev_pos, const unsigned char* dev_active, int 
    library until the process exits; a query needing more
    (ecmg_knn_scratch_bytes > the limit) returns ECMG_ERR_BOUND.  The first call
    on a device resolves the array's device address -- make it before any
-   stream capture.  Calls share the array: overlapping calls on one device
-   race.  Allocates nothing. */
+   stream capture.  The address is kept per device for its primary context:
+   other contexts made current through the driver API, and calls after a
+   cudaDeviceReset, are not supported.  Calls share the array: overlapping
+   calls on one device race.  Allocates nothing. */
 #define ECMG_KNN_STATIC_SCRATCH_BYTES (16u * 1024u * 1024u)
 ecmg_status ecmg_knn_noalloc(const float* dev_pos, const unsigned char* dev_active, int n, int k, float radius,
                              float min_x, float min_y, float max_x, float max_y, float cell,

@@ -24,12 +24,14 @@ REF_SO = os.path.join(HERE, "_ref", "libecmref.so")
 F32, I32, U8 = np.float32, np.int32, np.uint8
 
 
-def build(ref: bool = False) -> None:
-    """Compile the C restatement (and the reference, when its sources exist)."""
+def build(ref: bool = False, ref_tree: str | None = None) -> None:
+    """Compile the C restatement (and the reference, when its sources exist;
+    ref_tree overrides the Makefile's default location of the source tree)."""
     targets = ["oracle"]
     if ref:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+    extra = [f"REF={ref_tree}"] if ref and ref_tree else []
+    subprocess.run(["make", "-s", "-C", HERE] + targets + extra, check=True)
 
 
 def ref_available() -> bool:

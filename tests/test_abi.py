@@ -46,6 +46,19 @@ def test_knn_scratch_size(lib):
     assert lib.ecmg_knn_scratch_bytes(10, 0.0, 0.0, 1.0, 1.0, 0.0) == 0
 
 
+def test_knn_grid_too_large_is_refused_before_any_launch(lib):
+    """a box of 65,533 m with 1 m cells is a 65,536 x 65,536 grid: refused
+    (scratch size 0, invalid argument) rather than sized with a wrapped int;
+    also non-finite boxes.  Host-only: the calls return before any device
+    work, so fake non-null device pointers are never touched."""
+    fake = 4096
+    for box, cell in (((0.0, 0.0, 65533.0, 65533.0), 1.0), ((0.0, 0.0, float("inf"), 1.0), 1.0),
+                      ((float("nan"), 0.0, 1.0, 1.0), 1.0), ((0.0, 0.0, 1e30, 1e30), 1e-3)):
+        assert lib.ecmg_knn_scratch_bytes(1000, *box, cell) == 0
+        assert lib.ecmg_knn(fake, fake, 1000, 4, 1.0, *box, cell, fake, fake, fake, 1 << 30, None) == 1
+        assert lib.ecmg_knn_noalloc(fake, fake, 1000, 4, 1.0, *box, cell, fake, fake, None) == 1
+
+
 def test_planner_host_only(c1_small, port):
     from ecmgenerator_gb300.simulator import Planner
 

@@ -11,19 +11,24 @@ pytestmark = pytest.mark.gpu
 
 
 def test_knn_noalloc_matches_knn_twice(lib):
+    """two calls in a row with different sizes, boxes and cells: the second,
+    smaller call lays its grid out differently, so leftovers of the first in
+    the shared array would show up as differences"""
     import torch
 
     dev = torch.device("cuda:0")
     rng = np.random.default_rng(4)
-    n, k, r = 20000, 16, 3.0
-    box = (0.0, 0.0, 60.0, 60.0)
-    cell = 1.0
-    need = lib.ecmg_knn_scratch_bytes(n, *box, cell)
-    assert 0 < need <= 16 * 1024 * 1024
-    scratch = torch.empty(need, dtype=torch.uint8, device=dev)
-    for call in range(2):
-        pos = torch.from_numpy(rng.uniform(0, 60, (n, 2)).astype(np.float32)).to(dev)
-        act = torch.from_numpy((rng.uniform(0, 1, n) < (0.9 if call == 0 else 0.6)).astype(np.uint8)).to(dev)
+    calls = [dict(n=20000, k=16, r=3.0, box=(0.0, 0.0, 60.0, 60.0), cell=1.0, frac=0.9),
+             dict(n=7000, k=10, r=2.5, box=(-10.0, -5.0, 30.0, 40.0), cell=1.7, frac=0.6)]
+    for c in calls:
+        n, k, r, box, cell = c["n"], c["k"], c["r"], c["box"], c["cell"]
+        need = lib.ecmg_knn_scratch_bytes(n, *box, cell)
+        assert 0 < need <= 16 * 1024 * 1024
+        scratch = torch.empty(need, dtype=torch.uint8, device=dev)
+        # a few agents outside the box (the overflow bucket every query scans)
+        xy = np.stack([rng.uniform(box[0] - 2, box[2] + 2, n), rng.uniform(box[1] - 2, box[3] + 2, n)], 1)
+        pos = torch.from_numpy(xy.astype(np.float32)).to(dev)
+        act = torch.from_numpy((rng.uniform(0, 1, n) < c["frac"]).astype(np.uint8)).to(dev)
         ref_ids = torch.full((n, k), -5, dtype=torch.int32, device=dev)
         ref_cnt = torch.zeros(n, dtype=torch.int32, device=dev)
         assert lib.ecmg_knn(pos.data_ptr(), act.data_ptr(), n, k, r, *box, cell, ref_ids.data_ptr(),
@@ -36,6 +41,7 @@ def test_knn_noalloc_matches_knn_twice(lib):
         live = act.cpu().numpy() == 1
         assert np.array_equal(cnt.cpu().numpy(), ref_cnt.cpu().numpy())
         assert np.array_equal(ids.cpu().numpy()[live], ref_ids.cpu().numpy()[live])
+        assert ref_cnt.cpu().numpy()[live].mean() > 1.0
 
 
 def test_knn_noalloc_rejects_oversize(lib):
