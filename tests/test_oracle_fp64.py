@@ -91,4 +91,11 @@ def test_fp32_against_fp64_host_run(port):
     assert report["velocity, one tick, A-C"]["median"] < 1e-5
     assert report["velocity, one tick, A-B"]["median"] < 1e-5
     assert report["velocity, one tick, A-B"]["max"] < 1e-5
-    assert report["position after 600 ticks, A-B"]["p99"] < 1e-3
+    # after 600 ticks the crowd is chaotic: one rounding difference grows.
+    # The two FP32 runs (own transcendentals vs the host libm) must stay far
+    # closer to each other than either is to FP64: with the reference
+    # planner's paths 13 of 955 agents differ by more than 1 mm between them,
+    # against 89 between FP32 and FP64
+    ab, ac = report["position after 600 ticks, A-B"], report["position after 600 ticks, A-C"]
+    assert ab["median"] < 1e-5 and ab["within"] >= 0.98
+    assert ab["beyond"] * 4 <= ac["beyond"]
