@@ -452,13 +452,10 @@ def run_ours(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_all / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded scene, agents and paths)",
-        "config": {"workload": args.workload, "agents": n, "max_neighbors": k, "neighbor_dist_m": 5.0,
-                   "time_horizon_s": 2.0, "dt_s": DT, "scene": scene_desc,
-                   "l2": "flushed before every timed tick (512 MB write)", "parallelism": f"replicas x{world}",
-                   "seed": args.seed, "mode": "learned proposal" if model is not None else "plain",
-                   "neighbors": args.neighbors,
-                   "planner": args.planner,
-                   "launch": launch},
+        "config": workload_config(args, n, k, scene_desc, world),
+        "mode": "learned proposal" if model is not None else "plain",
+        "neighbors": "exact (d2, index)" if args.neighbors == "exact" else "kd-tree (the reference's query)",
+        "launch": launch,
         "plain": {"value": plain_value, "ms_per_step": p_ms_all / args.steps,
                   "lp3d_per_tick": tp.tot["lp3d"] / args.steps,
                   "graph_ms_per_tick": tp.tot["device_ms"] / args.steps,
@@ -497,7 +494,7 @@ def run_ours(args):
                                 "candidate locations tested on the device against all agents, spawned agents "
                                 "planned on the host; stage_ms includes the planning, check_ms the device test "
                                 "with its copies and wait"}
-        out["config"]["spawn_rate_per_area"] = args.spawn_rate
+        out["spawn_rate_per_area"] = args.spawn_rate
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(scene, st, k, threads=1, budget_s=args.cpu_budget)
     for s_ in sims:
@@ -510,29 +507,94 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def workload_config(args, n, k, scene_desc, world):
+    """the `config` object of both arms: the workload only"""
+    return {"workload": args.workload, "agents": n, "max_neighbors": k, "neighbor_dist_m": 5.0,
+            "time_horizon_s": 2.0, "dt_s": DT, "scene": scene_desc,
+            "l2": "inputs larger than L2 (agent state ~0.2 GB at 1M agents); the GPU arm also flushes L2 "
+                  "(512 MB write) before every timed tick",
+            "parallelism": f"replicas x{world}", "seed": args.seed, "planner": args.planner}
+
+
 def run_reference(args):
+    """The reference's CPU tick on the host cores: the C port of
+    Simulator::Update (pinned bit for bit to the reference's own sources on
+    x86-64) in the reference's kd-tree neighbour mode with the host libm,
+    whole ticks on every host thread (og_tick_mt), re-plans served inside the
+    timed tick by the port of ECMPathPlanner::FindPath.  Scene, agents and
+    initial paths are built without the product library (the oracle's planner
+    plans them), so nothing of the GPU library is loaded in this process."""
     rank, world, local = dist_env()
     if rank != 0:
         return
-    cfg, scene, st, paths, k = make_workload(args.workload, args.seed)
+    if WORKLOADS[args.workload].get("batch"):
+        raise SystemExit("the reference arm runs single-scene workloads")
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle as orc
+    from ecmgenerator_gb300.workloads import make_workload as mk
+
+    orc.build()
+    port = orc.Port()
     threads = os.cpu_count() or 1
-    vals = []
+    t0 = time.time()
+    holder = {}
+
+    def plan(scene, a_, b_, c_):
+        if "E" not in holder:
+            holder["E"] = port.ecm(scene.ecm)
+        return port.find_paths(holder["E"], a_, b_, c_, threads=threads, cap=256)
+
+    cfg, scene, st, paths, k = mk(args.workload, args.seed, planner="reference", plan=plan)
+    del paths
+    setup_s = time.time() - t0
+    n = st.num_agents
+    O, E = port.obstacles(scene), holder["E"]
+    P = port.params(k=k, libm=1, knn_mode=1, **ORCA)
+    kd = port.kdtree(k)
+    stats = dict(replans=0, replans_ok=0, destroyed=0, lp3d=0)
+
+    def tick():
+        agents = st.num_agents
+        destroyed, replan, rpos, nlp3d = port.tick_mt(O, E, st, P, kd, threads)
+        if replan.size:
+            # Simulator::UpdatePath from the tick-start position to the path's goal
+            got = port.find_paths(E, rpos, st.goals(replan), st.clear[replan], threads=threads, cap=256)
+            st.replace_paths(replan, got)
+            stats["replans_ok"] += sum(g_ is not None for g_ in got)
+        stats["replans"] += int(replan.size)
+        stats["destroyed"] += int(destroyed.size)
+        stats["lp3d"] += int(nlp3d)
+        return agents
+
     for _ in range(args.warmup):
-        cpu_baseline(scene, st, k, threads=threads, budget_s=2.0)
-    t0 = time.perf_counter()
+        tick()
+    for key in stats:
+        stats[key] = 0
+    times, steps = [], 0
     for _ in range(args.steps):
-        vals.append(cpu_baseline(scene, st, k, threads=threads, budget_s=min(args.cpu_budget / 2, 120.0 / args.steps)))
-    t1 = time.perf_counter()
-    v = float(np.median([x["value"] for x in vals]))
-    ms = 1e3 * st.num_agents / v
-    out = {"impl": "reference", "metric": "agent-steps/s at 1M agents: learned-proposal vs plain GPU ORCA; ms/tick", "value": v, "unit": "agent-steps/s",
-           "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene, agents and paths)",
-           "config": {"workload": args.workload, "agents": st.num_agents, "max_neighbors": k, "seed": args.seed},
-           "cpu_baseline": {"value": v, "unit": "agent-steps/s", "cores": threads, "kind": "port",
-                            "sample": vals[0]["sample"]},
+        t1 = time.perf_counter()
+        steps += tick()
+        times.append(time.perf_counter() - t1)
+    total = sum(times)
+    v = steps / total
+    one = cpu_baseline(scene, st, k, threads=1, budget_s=args.cpu_budget)
+    out = {"impl": "reference", "metric": "agent-steps/s at 1M agents: learned-proposal vs plain GPU ORCA; ms/tick",
+           "value": v, "unit": "agent-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic (seeded scene, agents and paths)",
+           "config": workload_config(args, n, k, f'{cfg["w"]:.0f}x{cfg["h"]:.0f} m, {cfg["boxes"]} boxes', world),
+           "neighbors": "kd-tree (the reference's KDTree query, neighbour cache per thread)",
+           "cpu_baseline": {"value": v, "unit": "agent-steps/s", "cores": threads,
+                            "kind": "port (C restatement of the reference, pinned bit for bit to the reference's "
+                                    "own sources on x86-64)",
+                            "sample": f"{args.steps} whole ticks of all {n} agents after {args.warmup} warm-up "
+                                      f"ticks, state advanced tick by tick, re-plans inside the timed ticks, "
+                                      f"{threads} host threads"},
+           "one_thread": one,
            "e2e": {"value": v, "unit": "agent-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-           "wall_s": t1 - t0}
+           "tick_ms": [round(1e3 * x, 1) for x in times],
+           "tick_stats": {k_: v_ / max(args.steps, 1) for k_, v_ in stats.items()},
+           "setup_s": setup_s}
     print(json.dumps(out), flush=True)
 
 

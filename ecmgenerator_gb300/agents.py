@@ -68,6 +68,24 @@ class AgentState:
         self.path_len[slot] = path.shape[0]
         self.path_xy = np.ascontiguousarray(np.concatenate([self.path_xy, path], 0), F32)
 
+    def replace_paths(self, slots, paths) -> None:
+        """replace_path for many slots with one append (None keeps a slot's path)"""
+        keep = [(int(s_), np.asarray(p, F32).reshape(-1, 2)) for s_, p in zip(slots, paths) if p is not None]
+        if not keep:
+            return
+        base = self.path_xy.shape[0]
+        lens = np.array([p.shape[0] for _, p in keep], I32)
+        offs = base + np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(I32)
+        idx = np.array([s_ for s_, _ in keep], np.int64)
+        self.path_off[idx] = offs
+        self.path_len[idx] = lens
+        self.path_xy = np.ascontiguousarray(np.concatenate([self.path_xy] + [p for _, p in keep], 0), F32)
+
+    def goals(self, slots) -> np.ndarray:
+        """the last point of each listed slot's path (its goal)"""
+        slots = np.asarray(slots, np.int64)
+        return self.path_xy[self.path_off[slots] + self.path_len[slots] - 1]
+
     def path(self, slot: int) -> np.ndarray:
         o, n = int(self.path_off[slot]), int(self.path_len[slot])
         return self.path_xy[o:o + n]

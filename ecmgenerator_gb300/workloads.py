@@ -33,31 +33,39 @@ ORCA = dict(tau_agent=2.0, tau_obst=2.0, neighbor_dist=5.0)
 DT = 1.0 / 60.0
 
 
-def make_workload(name, seed, verbose=True, planner="reference"):
+def make_workload(name, seed, verbose=True, planner="reference", plan=None):
     """(cfg, scene, agent state with planned paths, paths, k); the initial
-    paths come from the reference planner (ECMPathPlanner::FindPath restated)
-    unless planner="fast"; an agent without a path walks straight to its goal"""
+    paths come from the library's reference planner (ECMPathPlanner::FindPath
+    restated) unless planner="fast", or from plan(scene, starts, goals,
+    clearances) -> list of paths / None when given; an agent without a path
+    walks straight to its goal"""
     from . import agents as ag
-    from .simulator import Planner
 
     w = WORKLOADS[name]
     cfg = ag.scaled(w["cfg"], agents=w["agents"])
     t0 = time.time()
     scene = ag.build_scene(cfg, seed)
     st = ag.spawn_agents(cfg, scene, seed)
-    pl = Planner(scene, mode=planner)
+    if plan is None:
+        from .simulator import Planner
+
+        pl = Planner(scene, mode=planner)
+        plan = lambda sc, a_, b_, c_: pl.find_paths(a_, b_, c_, threads=0, cap=256)  # noqa: E731
+    else:
+        pl = None
     n = st.num_agents
     paths = []
     chunk = 100_000
     for a in range(0, n, chunk):
         b = min(n, a + chunk)
-        got = pl.find_paths(st.pos[a:b], st.goal[a:b], st.clear[a:b], threads=0, cap=256)
+        got = plan(scene, st.pos[a:b], st.goal[a:b], st.clear[a:b])
         for i, p in enumerate(got):
             if p is None:
                 p = np.stack([st.pos[a + i], st.goal[a + i]])
             paths.append(np.asarray(p, np.float32))
     st.set_paths(paths)
-    pl.close()
+    if pl is not None:
+        pl.close()
     if verbose:
         print(f"[workload] {name}: {n} agents, {scene.ecm.n_edges} ECM edges, setup {time.time() - t0:.1f}s",
               file=sys.stderr, flush=True)

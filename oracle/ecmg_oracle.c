@@ -24,6 +24,7 @@
 #define og_sin sin
 #define og_cos cos
 #define og_pow pow
+#define og_ceil ceil
 #define OG_REAL_MAX DBL_MAX
 #else
 #define og_sqrt sqrtf
@@ -34,6 +35,7 @@
 #define og_sin sinf
 #define og_cos cosf
 #define og_pow powf
+#define og_ceil ceilf
 #define OG_REAL_MAX FLT_MAX
 #endif
 
@@ -1166,5 +1168,553 @@ int og_tick_sample(const og_obstacles* o, const og_ecm* e, const og_state* s, co
     for (int t = 1; t < th; t++) pthread_join(tid[t], NULL);
     free(jobs);
     free(tid);
+    return 0;
+}
+
+/* ---------------------------------------------------------------------------
+ * Path planning: ECMPathPlanner::FindPath (ECMGenerator/ECMPathPlanner.cpp:22-136)
+ * ------------------------------------------------------------------------- */
+
+/* a growable array of fixed-size elements */
+typedef struct { void* p; int n, cap, esz; } og_vec;
+static void* vec_push(og_vec* v)
+{
+    if (v->n == v->cap) {
+        v->cap = v->cap ? 2 * v->cap : 64;
+        v->p = realloc(v->p, (size_t)v->cap * (size_t)v->esz);
+    }
+    return (char*)v->p + (size_t)v->n++ * (size_t)v->esz;
+}
+#define VEC_AT(v, T, i) (((T*)(v).p)[i])
+
+typedef struct { og_v2 p0, p1; } og_seg;
+
+struct og_planner {
+    const og_ecm* e;
+    /* AStar::m_Nodes (AStar.h:59-63): per vertex index g and f cost, parent,
+       visited flag; reset after every request (CleanRequestData) */
+    og_real* g;
+    og_real* f;
+    unsigned* parent;
+    unsigned char* visited;
+    og_vec heap, apath, rpath, hpath, centers, radii, lb, rb, lcb, rcb, curve, portals;
+};
+
+og_planner* og_planner_create(const og_ecm* e)
+{
+    og_planner* pl = (og_planner*)calloc(1, sizeof(og_planner));
+    const int V = e->n_vertices > 0 ? e->n_vertices : 1;
+    pl->e = e;
+    pl->g = (og_real*)malloc(sizeof(og_real) * (size_t)V);
+    pl->f = (og_real*)malloc(sizeof(og_real) * (size_t)V);
+    pl->parent = (unsigned*)malloc(sizeof(unsigned) * (size_t)V);
+    pl->visited = (unsigned char*)calloc((size_t)V, 1);
+    /* AStar::Initialize (AStar.cpp:9-31) */
+    for (int i = 0; i < V; i++) {
+        pl->g[i] = OG_REAL_MAX;
+        pl->f[i] = OG_REAL_MAX;
+        pl->parent[i] = (unsigned)e->n_vertices;
+    }
+    pl->heap.esz = pl->apath.esz = pl->rpath.esz = pl->hpath.esz = pl->curve.esz = sizeof(int);
+    pl->centers.esz = pl->lb.esz = pl->rb.esz = pl->lcb.esz = pl->rcb.esz = sizeof(og_v2);
+    pl->radii.esz = sizeof(og_real);
+    pl->portals.esz = sizeof(og_seg);
+    return pl;
+}
+
+void og_planner_destroy(og_planner* pl)
+{
+    if (!pl) return;
+    free(pl->g); free(pl->f); free(pl->parent); free(pl->visited);
+    og_vec* v[] = {&pl->heap, &pl->apath, &pl->rpath, &pl->hpath, &pl->centers, &pl->radii, &pl->lb, &pl->rb,
+                   &pl->lcb, &pl->rcb, &pl->curve, &pl->portals};
+    for (size_t i = 0; i < sizeof(v) / sizeof(v[0]); i++) free(v[i]->p);
+    free(pl);
+}
+
+/* MathUtility::Distance(p1, p2) (UtilityFunctions.cpp:15-22) */
+static og_real pl_dist(og_v2 p1, og_v2 p2)
+{
+    og_real dx = p2.x - p1.x, dy = p2.y - p1.y;
+    return og_sqrt(dx * dx + dy * dy);
+}
+/* Point::operator== (ECMDataTypes.h:99-103) */
+static int pl_eq(og_v2 a, og_v2 b)
+{
+    return a.x > b.x - OG_EPS && a.x < b.x + OG_EPS && a.y > b.y - OG_EPS && a.y < b.y + OG_EPS;
+}
+/* MathUtility::TriangleArea (UtilityFunctions.cpp:203-210) */
+static og_real pl_area(og_v2 p1, og_v2 p2, og_v2 p3)
+{
+    og_real ax = p2.x - p1.x, ay = p2.y - p1.y, bx = p3.x - p1.x, by = p3.y - p1.y;
+    return bx * ay - ax * by;
+}
+/* MathUtility::IsLeftOfSegment (UtilityFunctions.cpp:193-196) */
+static int pl_left(og_seg s, og_v2 p)
+{
+    return (s.p1.x - s.p0.x) * (p.y - s.p0.y) - (s.p1.y - s.p0.y) * (p.x - s.p0.x) > 0;
+}
+
+/* The open list of AStar::FindPath is a std::priority_queue of node pointers
+   ordered by AStarCompare (a->fCost > b->fCost, AStar.h:26-33) whose costs
+   change after they are pushed, so its pop order is that of the binary-heap
+   algorithm itself, restated here on vertex indices with the current f read
+   at every comparison: push = append + sift up; pop = move the last element
+   out, walk the hole from the root to a leaf along the child that does not
+   compare before its sibling, then sift the moved element up from there. */
+static int heap_before(const og_planner* pl, int a, int b) { return pl->f[a] > pl->f[b]; }
+static void heap_sift_up(og_planner* pl, long hole, long top, int value)
+{
+    int* h = (int*)pl->heap.p;
+    long parent = (hole - 1) / 2;
+    while (hole > top && heap_before(pl, h[parent], value)) {
+        h[hole] = h[parent];
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    h[hole] = value;
+}
+static void heap_push(og_planner* pl, int v)
+{
+    *(int*)vec_push(&pl->heap) = v;
+    heap_sift_up(pl, pl->heap.n - 1, 0, v);
+}
+static void heap_pop(og_planner* pl)
+{
+    int* h = (int*)pl->heap.p;
+    const long size = pl->heap.n;
+    if (size > 1) {
+        const long len = size - 1;
+        const int value = h[len];
+        h[len] = h[0];
+        long hole = 0, child = 0;
+        while (child < (len - 1) / 2) {
+            child = 2 * (child + 1);
+            if (heap_before(pl, h[child], h[child - 1])) child--;
+            h[hole] = h[child];
+            hole = child;
+        }
+        if ((len & 1) == 0 && child == (len - 2) / 2) {
+            child = 2 * (child + 1);
+            h[hole] = h[child - 1];
+            hole = child - 1;
+        }
+        heap_sift_up(pl, hole, 0, value);
+    }
+    pl->heap.n--;
+}
+
+/* AStar::CleanRequestData (AStar.cpp:162-175) */
+static void astar_clean(og_planner* pl)
+{
+    const int V = pl->e->n_vertices;
+    for (int i = 0; i < V; i++) {
+        pl->f[i] = OG_REAL_MAX;
+        pl->g[i] = OG_REAL_MAX;
+        pl->parent[i] = (unsigned)V;
+        pl->visited[i] = 0;
+    }
+}
+
+/* AStar::FindPath (AStar.cpp:44-160) with ConstructPath (AStar.cpp:183-210):
+   vertex indices into pl->apath */
+static int astar(og_planner* pl, og_v2 startLoc, og_v2 goalLoc, int startEdge, int goalEdge, og_real clearance)
+{
+    const og_ecm* e = pl->e;
+    const unsigned INVALID = (unsigned)e->n_vertices;
+    pl->heap.n = 0;
+    pl->apath.n = 0;
+    const int a = e->v_idx[e->he_target[2 * startEdge]], b = e->v_idx[e->he_target[2 * startEdge + 1]];
+    pl->g[a] = pl_dist(startLoc, e->v_pos[e->he_target[2 * startEdge]]);
+    pl->f[a] = pl->g[a] + pl_dist(e->v_pos[e->he_target[2 * startEdge]], goalLoc);
+    pl->g[b] = pl_dist(startLoc, e->v_pos[e->he_target[2 * startEdge + 1]]);
+    pl->f[b] = pl->g[b] + pl_dist(e->v_pos[e->he_target[2 * startEdge + 1]], goalLoc);
+    heap_push(pl, a);
+    heap_push(pl, b);
+    const int ga = e->he_target[2 * goalEdge], gb = e->he_target[2 * goalEdge + 1];
+    while (pl->heap.n > 0) {
+        while (pl->heap.n > 0 && pl->visited[VEC_AT(pl->heap, int, 0)]) heap_pop(pl);
+        if (pl->heap.n == 0) {
+            astar_clean(pl);
+            return 0;
+        }
+        const int cur = VEC_AT(pl->heap, int, 0);
+        heap_pop(pl);
+        pl->visited[cur] = 1;
+        if (e->v_clear[cur] < clearance) continue;
+        if (cur == ga || cur == gb) {
+            pl->rpath.n = 0;
+            *(int*)vec_push(&pl->rpath) = cur == ga ? gb : ga;
+            *(int*)vec_push(&pl->rpath) = cur == ga ? ga : gb;
+            for (unsigned nx = pl->parent[cur]; nx < INVALID; nx = pl->parent[nx]) *(int*)vec_push(&pl->rpath) = (int)nx;
+            for (int i = pl->rpath.n - 1; i >= 0; i--) *(int*)vec_push(&pl->apath) = VEC_AT(pl->rpath, int, i);
+            astar_clean(pl);
+            return 1;
+        }
+        /* neighbours: the targets of the half-edges from the vertex's first
+           outgoing one, following next_idx until the first target recurs */
+        int he = e->v_halfedge[cur];
+        if (he < 0) continue; /* an isolated vertex (the reference would read out of bounds) */
+        const int first = e->he_target[he];
+        int nb = first, guard = 0;
+        do {
+            if (!pl->visited[nb]) {
+                heap_push(pl, nb);
+                const og_v2 cp = e->v_pos[cur], np = e->v_pos[nb];
+                const og_real ng = pl->g[cur] + pl_dist(cp, np);
+                if (ng < pl->g[nb]) {
+                    const og_real nf = ng + pl_dist(np, goalLoc);
+                    pl->parent[nb] = (unsigned)cur;
+                    pl->f[nb] = nf;
+                    pl->g[nb] = ng;
+                }
+            }
+            he = e->he_next[he];
+            nb = e->he_target[he];
+        } while (nb != first && ++guard < 65536);
+    }
+    astar_clean(pl);
+    return 0;
+}
+
+/* SampleCorridorArc (ECMPathPlanner.cpp:255-276) */
+static void sample_arc(og_planner* pl, og_v2 p1, og_v2 p2, og_v2 o1, og_v2 o2, og_v2 c, og_real radius, int leftArc)
+{
+    const og_real maxLen = 10.0f;
+    og_seg* s = (og_seg*)vec_push(&pl->portals);
+    if (leftArc) { s->p0 = p1; s->p1 = o1; }
+    else { s->p0 = o1; s->p1 = p1; }
+    const og_v2 d = vsub(p2, p1);
+    const og_real edgeLength = og_sqrt(d.x * d.x + d.y * d.y);
+    const int numSamples = (int)og_ceil(edgeLength / maxLen);
+    const og_real sampleLength = edgeLength / (og_real)numSamples;
+    const og_v2 dir = vdiv(d, edgeLength);
+    for (int i = 0; i < numSamples; i++) {
+        og_v2 step = vmul(vmul(dir, sampleLength), (og_real)i);
+        og_v2 p = v2(p1.x + step.x, p1.y + step.y);
+        og_v2 a = vnormalize(vsub(p, c));
+        p = v2(c.x + a.x * radius, c.y + a.y * radius);
+        s = (og_seg*)vec_push(&pl->portals);
+        if (leftArc) { s->p0 = p; s->p1 = o2; }
+        else { s->p0 = o2; s->p1 = p; }
+    }
+}
+
+/* ECMPathPlanner::Funnel (ECMPathPlanner.cpp:321-411): the simple stupid
+   funnel algorithm; returns the number of points written (-2: more than cap) */
+static int funnel(const og_seg* portals, int np, og_v2 start, og_v2 goal, og_v2* out, int cap)
+{
+    og_v2 apex = start, pleft = start, pright = start;
+    int leftIdx = 0, rightIdx = 0, apexIdx = 0, n = 0;
+#define PL_EMIT(q) do { if (n >= cap) return -2; out[n++] = (q); } while (0)
+    PL_EMIT(start);
+    for (int i = 0; i < np; i++) {
+        const og_v2 left = portals[i].p0, right = portals[i].p1;
+        if (pl_area(apex, pright, right) <= 0.0f) {
+            if (vapprox(apex, pright) || pl_area(apex, pleft, right) > 0.0f) {
+                pright = right;
+                rightIdx = i;
+            } else {
+                PL_EMIT(pleft);
+                apex = pleft;
+                apexIdx = leftIdx;
+                pleft = apex;
+                pright = apex;
+                leftIdx = apexIdx;
+                rightIdx = apexIdx;
+                i = apexIdx;
+                continue;
+            }
+        }
+        if (pl_area(apex, pleft, left) >= 0.0f) {
+            if (vapprox(apex, pleft) || pl_area(apex, pright, left) < 0.0f) {
+                pleft = left;
+                leftIdx = i;
+            } else {
+                PL_EMIT(pright);
+                apex = pright;
+                apexIdx = rightIdx;
+                pleft = apex;
+                pright = apex;
+                leftIdx = apexIdx;
+                rightIdx = apexIdx;
+                i = apexIdx;
+                continue;
+            }
+        }
+    }
+    if (!vapprox(out[n - 1], goal)) PL_EMIT(goal);
+#undef PL_EMIT
+    return n;
+}
+
+int og_find_path(og_planner* pl, og_v2 start, og_v2 goal, og_real clearance, og_v2* out, int cap)
+{
+    const og_ecm* e = pl->e;
+    if (cap < 2) return -2;
+    /* clearance += preferredAdditionalClearance (0, Simulator.cpp:108) */
+    /* 1. FindCell of start and goal (ECM.cpp:191-194: the linear query) */
+    if (og_point_location(e, start) < 0 || og_point_location(e, goal) < 0) return -1;
+    /* 2. ECM::RetractPoint */
+    og_v2 rs, rg;
+    int es, eg;
+    if (!og_retract(e, start, &rs, &es)) return -1;
+    if (!og_retract(e, goal, &rg, &eg)) return -1;
+    if (es == eg) {
+        out[0] = start;
+        out[1] = goal;
+        return 2;
+    }
+    /* 3. A* on the medial axis */
+    if (!astar(pl, rs, rg, es, eg, clearance)) return -1;
+    /* the half-edge between consecutive vertices of the A* path */
+    pl->hpath.n = 0;
+    for (int i = 0; i + 1 < pl->apath.n; i++) {
+        const int a = VEC_AT(pl->apath, int, i), b = VEC_AT(pl->apath, int, i + 1);
+        const int h0 = e->v_halfedge[a];
+        if (h0 < 0) continue;
+        int h = h0, guard = 0;
+        do {
+            if (e->he_target[h] == b) {
+                *(int*)vec_push(&pl->hpath) = h;
+                break;
+            }
+            h = e->he_next[h];
+        } while (h != h0 && ++guard < 65536);
+    }
+    const int n = pl->hpath.n;
+    if (n == 0) return -1; /* the reference would read an empty corridor */
+    /* 4. CreateCorridor (ECMPathPlanner.cpp:144-156): the source vertex of
+       each half-edge (GetSource: the twin's target, ECM.h:71-84) */
+    pl->centers.n = pl->radii.n = pl->lb.n = pl->rb.n = pl->lcb.n = pl->rcb.n = pl->curve.n = 0;
+    for (int i = 0; i < n; i++) {
+        const int h = VEC_AT(pl->hpath, int, i);
+        const int src = e->he_target[h ^ 1];
+        *(og_v2*)vec_push(&pl->centers) = e->v_pos[src];
+        *(og_real*)vec_push(&pl->radii) = e->v_clear[src];
+        *(og_v2*)vec_push(&pl->lb) = e->he_left[h];
+        *(og_v2*)vec_push(&pl->rb) = e->he_right[h];
+    }
+    /* ShrinkCorridor (ECMPathPlanner.cpp:158-214) */
+    for (int i = 0; i < n; i++) {
+        const og_v2 c = VEC_AT(pl->centers, og_v2, i), l = VEC_AT(pl->lb, og_v2, i), r = VEC_AT(pl->rb, og_v2, i);
+        og_v2 lc, rc;
+        if (VEC_AT(pl->radii, og_real, i) < clearance) {
+            lc = c;
+            rc = c;
+        } else {
+            const og_v2 ml = vnormalize(vsub(c, l)), mr = vnormalize(vsub(c, r));
+            lc = v2(l.x + ml.x * clearance, l.y + ml.y * clearance);
+            rc = v2(r.x + mr.x * clearance, r.y + mr.y * clearance);
+        }
+        *(og_v2*)vec_push(&pl->lcb) = lc;
+        *(og_v2*)vec_push(&pl->rcb) = rc;
+        if (i + 1 < n) { /* CorridorBoundCurve: 0 LINEAR, 1 LEFT_ARC, 2 RIGHT_ARC */
+            int t = 0;
+            if (pl_eq(l, VEC_AT(pl->lb, og_v2, i + 1))) t = 1;
+            else if (pl_eq(r, VEC_AT(pl->rb, og_v2, i + 1))) t = 2;
+            *(int*)vec_push(&pl->curve) = t;
+        }
+    }
+    /* 5. TriangulateCorridor (ECMPathPlanner.cpp:216-253) */
+    pl->portals.n = 0;
+    const og_v2* L = (const og_v2*)pl->lcb.p;
+    const og_v2* R = (const og_v2*)pl->rcb.p;
+    for (int i = 0; i + 1 < n; i++) {
+        const int t = VEC_AT(pl->curve, int, i);
+        if (t == 0) {
+            og_seg* s = (og_seg*)vec_push(&pl->portals);
+            s->p0 = L[i]; s->p1 = R[i];
+            s = (og_seg*)vec_push(&pl->portals);
+            s->p0 = L[i + 1]; s->p1 = R[i];
+        } else if (t == 1) {
+            sample_arc(pl, L[i], L[i + 1], R[i], R[i + 1], VEC_AT(pl->lb, og_v2, i), clearance, 1);
+        } else {
+            sample_arc(pl, R[i], R[i + 1], L[i], L[i + 1], VEC_AT(pl->rb, og_v2, i), clearance, 0);
+        }
+    }
+    og_seg* last = (og_seg*)vec_push(&pl->portals);
+    last->p0 = L[n - 1];
+    last->p1 = R[n - 1];
+    /* FitPortalRange (ECMPathPlanner.cpp:278-318) */
+    og_seg* P = (og_seg*)pl->portals.p;
+    int np = pl->portals.n, first = 0;
+    for (int i = 0; i < np; i++)
+        if (!pl_left(P[i], start)) {
+            first = i;
+            break;
+        }
+    memmove(P, P + first, sizeof(og_seg) * (size_t)(np - first));
+    np -= first;
+    int lastIdx = np - 1;
+    for (int i = np - 1; i >= 0; i--)
+        if (pl_left(P[i], goal)) {
+            lastIdx = i;
+            break;
+        }
+    np -= np - lastIdx;
+    pl->portals.n = np;
+    og_seg* gs = (og_seg*)vec_push(&pl->portals);
+    gs->p0 = goal;
+    gs->p1 = goal;
+    /* 7. Funnel */
+    return funnel((const og_seg*)pl->portals.p, pl->portals.n, start, goal, out, cap);
+}
+
+typedef struct {
+    const og_ecm* e;
+    const og_v2 *starts, *goals;
+    const og_real* clr;
+    og_v2* out;
+    int* out_n;
+    int cap, lo, hi;
+} og_pjob;
+
+static void* plan_thread(void* arg)
+{
+    og_pjob* j = (og_pjob*)arg;
+    og_planner* pl = og_planner_create(j->e);
+    for (int i = j->lo; i < j->hi; i++)
+        j->out_n[i] = og_find_path(pl, j->starts[i], j->goals[i], j->clr[i], j->out + (size_t)i * j->cap, j->cap);
+    og_planner_destroy(pl);
+    return NULL;
+}
+
+int og_find_paths(const og_ecm* e, int n, const og_v2* starts, const og_v2* goals, const og_real* clr, int threads,
+                  int cap, og_v2* out, int* out_n)
+{
+    int th = threads > 1 ? threads : 1;
+    if (th > n) th = n > 0 ? n : 1;
+    og_pjob* jobs = (og_pjob*)calloc((size_t)th, sizeof(og_pjob));
+    pthread_t* tid = (pthread_t*)calloc((size_t)th, sizeof(pthread_t));
+    for (int t = 0; t < th; t++) {
+        jobs[t].e = e; jobs[t].starts = starts; jobs[t].goals = goals; jobs[t].clr = clr;
+        jobs[t].out = out; jobs[t].out_n = out_n; jobs[t].cap = cap;
+        jobs[t].lo = (int)((long long)n * t / th);
+        jobs[t].hi = (int)((long long)n * (t + 1) / th);
+    }
+    for (int t = 1; t < th; t++) pthread_create(&tid[t], NULL, plan_thread, &jobs[t]);
+    plan_thread(&jobs[0]);
+    for (int t = 1; t < th; t++) pthread_join(tid[t], NULL);
+    free(jobs);
+    free(tid);
+    return 0;
+}
+
+/* ---------------------------------------------------------------------------
+ * Whole tick on host threads (see ecmg_oracle.h)
+ * ------------------------------------------------------------------------- */
+typedef struct {
+    const og_obstacles* o;
+    const og_ecm* e;
+    og_state* s;
+    const og_state* snap;
+    const og_params* p;
+    og_kdtree kd;            /* shares the tree, owns its neighbour cache */
+    unsigned char* res;      /* attraction stage result per slot */
+    og_v2* vorca;
+    int stage, lo, hi, n_lp3d;
+} og_mjob;
+
+static void* mt_thread(void* arg)
+{
+    og_mjob* j = (og_mjob*)arg;
+    og_state* s = j->s;
+    const og_params* p = j->p;
+    if (j->stage == 0) {
+        /* UpdateAttractionPointSystem (Simulator.cpp:538-590), per slot */
+        for (int i = j->lo; i < j->hi; i++)
+            j->res[i] = s->active[i] ? (unsigned char)attract_one(j->e, s, p, i, &s->attr[i]) : 0;
+    } else if (j->stage == 1) {
+        /* ApplySteeringForce + ApplyObstacleAvoidanceForce (Simulator.cpp:638-686) */
+        int* ids = (int*)malloc(sizeof(int) * (size_t)(p->k > 0 ? p->k : 1));
+        for (int i = j->lo; i < j->hi; i++) {
+            if (!s->active[i]) continue;
+            s->pref_vel[i] = vmul(vnormalize(vsub(s->attr[i], s->pos[i])), s->pref_speed[i]);
+            int nn = og_kdtree_query(&j->kd, j->snap, i, ids);
+            int nob = 0, fail = 0;
+            int m = og_orca_velocity(j->o, s, p, i, ids, nn, s->pref_vel[i], &j->vorca[i], &nob, &fail);
+            if (fail < m) j->n_lp3d++;
+        }
+        free(ids);
+    } else {
+        /* UpdateVelocitySystem, UpdatePositionSystem (Simulator.cpp:592-635) */
+        const og_real massRecip = 1.0f / p->mass;
+        for (int i = j->lo; i < j->hi; i++) {
+            if (!s->active[i]) continue;
+            og_real fx = j->vorca[i].x - s->vel[i].x;
+            og_real fy = j->vorca[i].y - s->vel[i].y;
+            s->vel[i].x += fx * massRecip * p->dt;
+            s->vel[i].y += fy * massRecip * p->dt;
+            s->pos[i].x += (s->vel[i].x * p->dt);
+            s->pos[i].y += (s->vel[i].y * p->dt);
+        }
+    }
+    return NULL;
+}
+
+int og_tick_mt(const og_obstacles* o, const og_ecm* e, og_state* s, const og_params* p, og_kdtree* kd, int threads,
+               og_tick_out* out)
+{
+    /* UpdateMaxAgentIndex (Simulator.cpp:481-492) */
+    int empty = 0;
+    for (int i = s->last_idx; i >= 0; i--) {
+        if (s->active[i]) break;
+        empty++;
+    }
+    s->last_idx -= empty;
+    const int last = s->last_idx, n = s->n_slots;
+    unsigned char* act0 = (unsigned char*)malloc((size_t)(n > 0 ? n : 1));
+    memcpy(act0, s->active, (size_t)n);
+    og_state snap = *s;
+    snap.active = act0;
+    /* KDTree::Construct (KDTree.cpp:22-83) over the tick-start agents */
+    og_kdtree_build(kd, s);
+    const int th = threads > 1 ? threads : 1;
+    og_mjob* jobs = (og_mjob*)calloc((size_t)th, sizeof(og_mjob));
+    pthread_t* tid = (pthread_t*)calloc((size_t)th, sizeof(pthread_t));
+    unsigned char* res = (unsigned char*)calloc((size_t)(n > 0 ? n : 1), 1);
+    og_v2* vorca = (og_v2*)calloc((size_t)(n > 0 ? n : 1), sizeof(og_v2));
+    for (int t = 0; t < th; t++) {
+        jobs[t].o = o; jobs[t].e = e; jobs[t].s = s; jobs[t].snap = &snap; jobs[t].p = p;
+        jobs[t].kd = *kd;
+        jobs[t].kd.cache = (int*)calloc((size_t)p->k, sizeof(int));
+        jobs[t].kd.dist = (og_real*)malloc(sizeof(og_real) * (size_t)p->k);
+        jobs[t].res = res; jobs[t].vorca = vorca;
+        jobs[t].lo = (int)((long long)(last + 1) * t / th);
+        jobs[t].hi = (int)((long long)(last + 1) * (t + 1) / th);
+    }
+    for (int stage = 0; stage < 3; stage++) {
+        for (int t = 0; t < th; t++) jobs[t].stage = stage;
+        for (int t = 1; t < th; t++) pthread_create(&tid[t], NULL, mt_thread, &jobs[t]);
+        mt_thread(&jobs[0]);
+        for (int t = 1; t < th; t++) pthread_join(tid[t], NULL);
+        if (stage == 0) {
+            /* DestroyAgent (Simulator.cpp:202-208) and re-plan requests, in slot order */
+            if (out) { out->n_destroyed = 0; out->n_replan = 0; }
+            for (int i = 0; i <= last; i++) {
+                if (res[i] == 1) {
+                    s->num_agents--;
+                    s->active[i] = 0;
+                    if (out) {
+                        if (out->destroyed) out->destroyed[out->n_destroyed] = i;
+                        out->n_destroyed++;
+                    }
+                } else if (res[i] == 2 && out) {
+                    if (out->replan) out->replan[out->n_replan] = i;
+                    if (out->replan_pos) out->replan_pos[out->n_replan] = s->pos[i];
+                    out->n_replan++;
+                }
+            }
+        }
+    }
+    int n_lp3d = 0;
+    for (int t = 0; t < th; t++) {
+        n_lp3d += jobs[t].n_lp3d;
+        free(jobs[t].kd.cache);
+        free(jobs[t].kd.dist);
+    }
+    if (out) out->n_lp3d = n_lp3d;
+    free(jobs); free(tid); free(res); free(vorca); free(act0);
     return 0;
 }

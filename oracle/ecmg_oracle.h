@@ -175,6 +175,31 @@ typedef struct {
 int og_tick_sample(const og_obstacles* o, const og_ecm* e, const og_state* s, const og_params* p,
                    const int* sample, int n_sample, int threads, og_sample_out* out);
 
+/* ECMPathPlanner::FindPath (ECMGenerator/ECMPathPlanner.cpp:22-136) with
+   AStar::FindPath (AStar.cpp:44-210), as Simulator::UpdatePath calls it
+   (preferred additional clearance 0).  An og_planner holds one thread's A*
+   node arrays.  og_find_path writes at most cap points and returns their
+   count, -1 when the reference finds no path, -2 when the path has more than
+   cap points.  og_find_paths plans n requests on `threads` host threads (out
+   holds cap points per request). */
+typedef struct og_planner og_planner;
+og_planner* og_planner_create(const og_ecm* e);
+void og_planner_destroy(og_planner* pl);
+int og_find_path(og_planner* pl, og_v2 start, og_v2 goal, og_real clearance, og_v2* out, int cap);
+int og_find_paths(const og_ecm* e, int n, const og_v2* starts, const og_v2* goals, const og_real* clr, int threads,
+                  int cap, og_v2* out, int* out_n);
+
+/* One Simulator::Update in the reference's kd-tree neighbour mode
+   (p->knn_mode is ignored) with the per-agent stages split over `threads`
+   host threads: the timed CPU arm of the benchmark.  The kd-tree is built on
+   one thread as the reference does; each thread carries its own neighbour
+   cache (ORCA.h:100), so stale cache entries are those of its own agents
+   rather than of the previous agent in slot order; everything else is
+   og_tick's arithmetic.  Destroyed agents and re-plan requests are listed in
+   out in slot order; re-plans are left to the caller. */
+int og_tick_mt(const og_obstacles* o, const og_ecm* e, og_state* s, const og_params* p, og_kdtree* kd, int threads,
+               og_tick_out* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -221,6 +221,42 @@ class Port:
     def kdtree(self, k):
         return self.lib.og_kdtree_create(k)
 
+    def find_paths(self, ecm_s, starts, goals, clearances, threads=1, cap=256):
+        """ECMPathPlanner::FindPath restated (og_find_paths) for n requests on
+        `threads` host threads: a list of (m, 2) arrays, None where the
+        reference finds no path (or the path has more than cap points)."""
+        L = self.lib
+        L.og_find_paths.argtypes = [C.POINTER(EcmS), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                    C.c_int, C.c_void_p, C.c_void_p]
+        R = self.REAL
+        starts = np.ascontiguousarray(np.asarray(starts).reshape(-1, 2), R)
+        goals = np.ascontiguousarray(np.asarray(goals).reshape(-1, 2), R)
+        clr = np.ascontiguousarray(clearances, R)
+        n = starts.shape[0]
+        out = np.zeros((n, cap, 2), R)
+        cnt = np.zeros(n, I32)
+        L.og_find_paths(C.byref(ecm_s), n, _addr(starts), _addr(goals), _addr(clr), int(threads), int(cap),
+                        _addr(out), _addr(cnt))
+        return [out[i, :cnt[i]].copy() if cnt[i] > 0 else None for i in range(n)]
+
+    def tick_mt(self, obst_s, ecm_s, st, params, kd, threads):
+        """One Simulator::Update in the kd-tree mode on `threads` host threads
+        (og_tick_mt; ``st`` modified in place): destroyed slots and re-plan
+        requests (slots, positions)."""
+        L = self.lib
+        L.og_tick_mt.argtypes = [C.POINTER(Obst), C.POINTER(EcmS), C.POINTER(State), C.POINTER(Params),
+                                 C.c_void_p, C.c_int, C.POINTER(TickOut)]
+        s = self.state(st)
+        n = st.n_slots
+        res = dict(destroyed=np.zeros(n, I32), replan=np.zeros(n, I32), replan_pos=np.zeros((n, 2), self.REAL))
+        out = TickOut(_addr(res["destroyed"]), 0, _addr(res["replan"]), _addr(res["replan_pos"]), 0,
+                      None, None, None, None, None, None, 0)
+        L.og_tick_mt(C.byref(obst_s), C.byref(ecm_s), C.byref(s), C.byref(params), kd, int(threads), C.byref(out))
+        st.last_idx = s.last_idx
+        st.num_agents = s.num_agents
+        return (res["destroyed"][:out.n_destroyed].copy(), res["replan"][:out.n_replan].copy(),
+                res["replan_pos"][:out.n_replan].copy(), out.n_lp3d)
+
     def tick_sample(self, obst_s, ecm_s, st, params, sample, threads=1):
         """One exact-kNN tick for the listed slots only, from ``st`` (not
         modified); see og_tick_sample.  Returns a dict of per-sample arrays."""
