@@ -2132,7 +2132,7 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
     };
     /* stage 1: the agent-grid cell (mostly the neighbour search), default
        launch; stage 2: the per-agent kernel's launch at the best cell */
-    const float scales[] = {0.3f, 0.4f, 0.5f, 0.6f, 0.8f};
+    const float scales[] = {0.2f, 0.25f, 0.3f, 0.4f, 0.5f, 0.6f, 0.8f};
     const int blocks[] = {64, 128, 256};
     const int tiles[] = {32, 64, 128};
     const int divs[] = {1, 2, 3};

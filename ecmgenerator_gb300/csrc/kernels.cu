@@ -256,6 +256,148 @@ __device__ void knn_grid(Knn<K>& s, int k, V2 p, float rnb, float r2, const V2* 
 }
 
 /* ---------------------------------------------------------------------- */
+/* Fast path of the exact kNN: cells in ascending order of their distance.
+   The grid cells around an agent's cell (Chebyshev radius <= kTmplR) are
+   visited in ascending order of their smallest distance from the quarter of
+   the agent's cell that holds the agent (a table built at compile time for
+   the lower-left quarter and mirrored for the others), so the k nearest are
+   met early and few candidates enter the list only to be dropped again; the
+   walk stops at the first cell whose distance bound exceeds the current k-th
+   distance.  The list is kept as 32-bit float distances with the candidates'
+   grid-order indices beside them: a candidate enters when its d2 is strictly
+   below the k-th.  That equals the (d2, slot) order of the reference
+   definition unless two d2 are equal -- two listed ones, or a dropped one
+   equal to the k-th -- and the search then returns false and the caller runs
+   the 64-bit (d2, slot) search (knn_grid); likewise when the table ends
+   before the search could (sparse crowds) or the agent is outside the
+   grid. */
+constexpr int kTmplR = 6, kTmplCap = (2 * kTmplR + 1) * (2 * kTmplR + 1);
+/* bound per axis from the quarter [0, 1/2] of cell 0 to cell d, in half cells */
+constexpr int tmpl_half(int d) { return d >= 1 ? 2 * d - 1 : (d <= -1 ? 2 * (-d - 1) : 0); }
+/* the table holds the cells whose bound is at most kTmplR cells: every cell
+   outside it is at least kTmplR cells away, so a walk that stops inside the
+   table has passed every cell that can hold a closer agent */
+constexpr bool tmpl_in(int dx, int dy)
+{
+    return tmpl_half(dx) * tmpl_half(dx) + tmpl_half(dy) * tmpl_half(dy) <= 4 * kTmplR * kTmplR;
+}
+constexpr int tmpl_count()
+{
+    int n = 0;
+    for (int dy = -kTmplR; dy <= kTmplR; dy++)
+        for (int dx = -kTmplR; dx <= kTmplR; dx++) n += tmpl_in(dx, dy) ? 1 : 0;
+    return n;
+}
+constexpr int kTmplN = tmpl_count();
+struct KnnTemplate {
+    signed char dx[kTmplN], dy[kTmplN];
+    unsigned char hx[kTmplN], hy[kTmplN]; /* distance bound per axis in half cells */
+};
+constexpr KnnTemplate make_knn_template()
+{
+    KnnTemplate t{};
+    int key[kTmplN] = {};
+    int n = 0;
+    for (int dy = -kTmplR; dy <= kTmplR; dy++)
+        for (int dx = -kTmplR; dx <= kTmplR; dx++) {
+            if (!tmpl_in(dx, dy)) continue;
+            const int hx = tmpl_half(dx), hy = tmpl_half(dy);
+            /* squared bound, then the nearer cells first among equal bounds */
+            const int kk = (hx * hx + hy * hy) * 1024 + (dx < 0 ? -dx : dx) + (dy < 0 ? -dy : dy);
+            int i = n++;
+            while (i > 0 && key[i - 1] > kk) {
+                key[i] = key[i - 1];
+                t.dx[i] = t.dx[i - 1];
+                t.dy[i] = t.dy[i - 1];
+                t.hx[i] = t.hx[i - 1];
+                t.hy[i] = t.hy[i - 1];
+                i--;
+            }
+            key[i] = kk;
+            t.dx[i] = (signed char)dx;
+            t.dy[i] = (signed char)dy;
+            t.hx[i] = (unsigned char)hx;
+            t.hy[i] = (unsigned char)hy;
+        }
+    return t;
+}
+__constant__ KnnTemplate c_knn_tmpl = make_knn_template();
+
+/* d2 and grid index of one candidate into the sorted list (key, id); a
+   candidate it does not keep, or the entry it pushes out, lowers *rej */
+template <int K>
+__device__ __forceinline__ void knn_fast_consider(float* key, int* id, float* rej, int j, V2 p, const V2* s_pos)
+{
+    const V2 q = s_pos[j];
+    const float dx = q.x - p.x, dy = q.y - p.y;
+    float nk = dx * dx + dy * dy; /* KDTree.cpp:107-108 */
+    if (!(nk > kEps)) return;
+    if (nk < key[K - 1]) {
+        int ni = j;
+#pragma unroll
+        for (int q2 = 0; q2 < K; q2++) {
+            const bool c = nk < key[q2];
+            const float tk = key[q2];
+            const int ti = id[q2];
+            key[q2] = c ? nk : tk;
+            id[q2] = c ? ni : ti;
+            nk = c ? tk : nk;
+            ni = c ? ti : ni;
+        }
+    }
+    *rej = fminf(*rej, nk);
+}
+
+/* true: key[K-k .. K-1] / id[..] hold the exact list (count in *cnt) */
+template <int K>
+__device__ __forceinline__ bool knn_fast(float* key, int* id, int k, V2 p, float r2, const V2* s_pos,
+                                         const int* cell_start, const AgentGrid& g, int* cnt)
+{
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        key[q] = q < K - k ? 0.0f : r2; /* 0: below every candidate (d2 > kEps); r2: empty */
+        id[q] = -1;
+    }
+    float rej = INFINITY;
+    for (int j = cell_start[g.ncells]; j < cell_start[g.ncells + 1]; j++) knn_fast_consider<K>(key, id, &rej, j, p, s_pos);
+    const float fx = (p.x - g.x0) * g.inv, fy = (p.y - g.y0) * g.inv;
+    if (!(fx >= 0.0f && fy >= 0.0f && fx < (float)g.gw && fy < (float)g.gh)) return false;
+    const int cx = (int)fx, cy = (int)fy;
+    const int sx = fx - (float)cx < 0.5f ? 1 : -1, sy = fy - (float)cy < 0.5f ? 1 : -1;
+    const float half = 0.5f * g.cell;
+    int i = 0;
+    for (; i < kTmplN; i++) {
+        /* every later cell is at least this far from the agent (1 cm for the
+           rounding of the bucket assignment) */
+        const float bx = fmaxf((float)c_knn_tmpl.hx[i] * half - 0.01f, 0.0f);
+        const float by = fmaxf((float)c_knn_tmpl.hy[i] * half - 0.01f, 0.0f);
+        if (bx * bx + by * by > key[K - 1]) break;
+        const int x = cx + sx * (int)c_knn_tmpl.dx[i], y = cy + sy * (int)c_knn_tmpl.dy[i];
+        if (x < 0 || y < 0 || x >= g.gw || y >= g.gh) continue;
+        const float rx0 = g.x0 + (float)x * g.cell, ry0 = g.y0 + (float)y * g.cell;
+        const float ex = fmaxf(fmaxf(rx0 - p.x, p.x - (rx0 + g.cell)) - 0.01f, 0.0f);
+        const float ey = fmaxf(fmaxf(ry0 - p.y, p.y - (ry0 + g.cell)) - 0.01f, 0.0f);
+        if (ex * ex + ey * ey > key[K - 1]) continue;
+        const int c = y * g.gw + x;
+        const int j1 = cell_start[c + 1];
+        for (int j = cell_start[c]; j < j1; j++) knn_fast_consider<K>(key, id, &rej, j, p, s_pos);
+    }
+    if (i == kTmplN) return false; /* the neighbourhood reaches beyond the table */
+    int n = 0;
+    bool tie = false;
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        if (q >= K - k && key[q] < r2) {
+            n++;
+            if (q + 1 < K && key[q + 1] == key[q]) tie = true;
+        }
+    }
+    if (n == k && rej == key[K - 1]) tie = true;
+    *cnt = n;
+    return !tie;
+}
+
+/* ---------------------------------------------------------------------- */
 struct LocalGet {
     const Con* c;
     __device__ Con operator()(int i) const { return c[i]; }
@@ -568,12 +710,12 @@ __device__ void orca_tick(const TickArgs& a, int t)
     }
 }
 
-/* neighbour lists of every grid-order agent of the tick (KNearestAgents,
-   KDTree.cpp:85-202, as the exact (d2, slot) query of the grid) */
+/* the 64-bit (d2, slot) search of grid-order agent t (rare: equal
+   distances, sparse crowds, agents outside the grid); out of line so that it
+   does not take registers from the fast path */
 template <int K>
-__device__ __forceinline__ void knn_agent(const TickArgs& a, int t, int slot)
+__device__ __noinline__ void knn_agent_exact(const TickArgs& a, int t, const SceneDev& sc)
 {
-    const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
     Knn<K> nn;
     knn_grid<K>(nn, a.k, a.s_pos[t], a.rnb, a.rnb2, a.s_pos, a.s_slot, a.cell_start + sc.bucket_base, sc.grid);
     a.ncnt[t] = nn.cnt;
@@ -586,6 +728,27 @@ __device__ __forceinline__ void knn_agent(const TickArgs& a, int t, int slot)
             o[q] = q < nn.cnt ? a.cell_start[a.slot_bucket[sl]] + a.slot_rank[sl] : -1;
         }
     }
+}
+
+/* neighbour lists of every grid-order agent of the tick (KNearestAgents,
+   KDTree.cpp:85-202, as the exact (d2, slot) query of the grid) */
+template <int K>
+__device__ __forceinline__ void knn_agent(const TickArgs& a, int t, int slot)
+{
+    const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
+    float key[K];
+    int id[K], n = 0;
+    if (knn_fast<K>(key, id, a.k, a.s_pos[t], a.rnb2, a.s_pos, a.cell_start + sc.bucket_base, sc.grid, &n)) {
+        a.ncnt[t] = n;
+        int* o = a.nbr + (size_t)t * a.k;
+#pragma unroll
+        for (int q2 = 0; q2 < K; q2++) {
+            const int q = q2 - (K - a.k);
+            if (q >= 0) o[q] = q < n ? id[q2] : -1;
+        }
+        return;
+    }
+    knn_agent_exact<K>(a, t, sc);
 }
 
 /* persistent: a warp takes 32 consecutive grid-order agents per work grab

@@ -583,7 +583,15 @@ int og_lp(const og_real* cons, int n, og_v2 opt, og_real maxSpeed, int useDirOpt
 /* ---------------------------------------------------------------------------
  * ORCA::RandomizedLP3D (ECMAgentSimulator/ORCA.cpp:592-669)
  * ------------------------------------------------------------------------- */
+/* fp64 != 0: the bisector of two non-parallel lines is intersected in
+   double precision and rounded to og_real, as the GPU tick's lp3d_fp64 mode
+   does (the reference computes it in float) */
+static void lp3d_impl(const og_real* cons, int n, int nObst, og_real maxSpeed, int failed, og_v2* out, int fp64);
 void og_lp3d(const og_real* cons, int n, int nObst, og_real maxSpeed, int failed, og_v2* out)
+{
+    lp3d_impl(cons, n, nObst, maxSpeed, failed, out, 0);
+}
+static void lp3d_impl(const og_real* cons, int n, int nObst, og_real maxSpeed, int failed, og_v2* out, int fp64)
 {
     og_real maxPen = 0.0f;
     og_real* proj = (og_real*)malloc(sizeof(og_real) * 4 * (size_t)(n + 1));
@@ -603,9 +611,16 @@ void og_lp3d(const og_real* cons, int n, int nObst, og_real maxSpeed, int failed
             if (og_fabs(det) <= OG_EPS) {
                 if (vdot(Ni, Nj) > 0) continue;
                 newP = vmul(vadd(Pi, Pj), 0.5f);
-            } else {
+            } else if (!fp64) {
                 og_real t = vdet(vright(Nj), vsub(Pi, Pj)) / det;
                 newP = vadd(Pi, vmul(vright(Ni), t));
+            } else {
+                const double ax = (double)Nj.y, ay = -(double)Nj.x; /* Right(Nj) */
+                const double bx = (double)Pi.x - (double)Pj.x, by = (double)Pi.y - (double)Pj.y;
+                const double rx = (double)Ni.y, ry = -(double)Ni.x; /* Right(Ni) */
+                const double dd = rx * ay - ry * ax;
+                const double t = (ax * by - ay * bx) / dd;
+                newP = v2((og_real)((double)Pi.x + rx * t), (og_real)((double)Pi.y + ry * t));
             }
             og_v2 nn = vnormalized(vsub(Nj, Ni));
             proj[4 * m + 0] = newP.x;
@@ -642,7 +657,7 @@ int og_orca_velocity(const og_obstacles* o, const og_state* s, const og_params* 
     int nob = 0;
     int m = og_generate_constraints(o, s, p, agent, nbrs, n_nbrs, ob, no, cons, cap, &nob);
     int failed = og_lp(cons, m, pref_vel, maxSpeed, 0, out_vel);
-    if (failed < m) og_lp3d(cons, m, nob, maxSpeed, failed, out_vel);
+    if (failed < m) lp3d_impl(cons, m, nob, maxSpeed, failed, out_vel, p->lp3d_fp64);
     if (out_n_obst) *out_n_obst = nob;
     if (out_fail) *out_fail = failed;
     free(cons);

@@ -74,6 +74,7 @@ typedef struct {
     int knn_mode;           /* 0 = exact kNN (d2,id) within neighbor_dist; 1 = kd-tree as the reference */
     int libm;               /* 1 = host libm transcendentals; 0 = ecmg_tmath.h */
     int threads;            /* >1: split the per-agent stages over threads (exact-kNN mode only) */
+    int lp3d_fp64;          /* 1: 3D-LP bisector intersections in double (the GPU's lp3d_fp64 mode) */
 } og_params;
 
 /* Slot-indexed agent state (Simulator component arrays). */

@@ -62,14 +62,14 @@ class Params64(C.Structure):
     _fields_ = [("dt", C.c_double), ("tau_agent", C.c_double), ("tau_obst", C.c_double),
                 ("neighbor_dist", C.c_double), ("max_speed", C.c_double), ("mass", C.c_double),
                 ("arrival_radius", C.c_double), ("delete_radius", C.c_double), ("k", C.c_int),
-                ("knn_mode", C.c_int), ("libm", C.c_int), ("threads", C.c_int)]
+                ("knn_mode", C.c_int), ("libm", C.c_int), ("threads", C.c_int), ("lp3d_fp64", C.c_int)]
 
 
 class Params(C.Structure):
     _fields_ = [("dt", C.c_float), ("tau_agent", C.c_float), ("tau_obst", C.c_float),
                 ("neighbor_dist", C.c_float), ("max_speed", C.c_float), ("mass", C.c_float),
                 ("arrival_radius", C.c_float), ("delete_radius", C.c_float), ("k", C.c_int),
-                ("knn_mode", C.c_int), ("libm", C.c_int), ("threads", C.c_int)]
+                ("knn_mode", C.c_int), ("libm", C.c_int), ("threads", C.c_int), ("lp3d_fp64", C.c_int)]
 
 
 class State(C.Structure):
@@ -147,7 +147,7 @@ class Port:
     @staticmethod
     def params(**kw):
         d = dict(dt=1.0 / 60.0, tau_agent=2.0, tau_obst=2.0, neighbor_dist=5.0, max_speed=0.0, mass=0.8,
-                 arrival_radius=20.0, delete_radius=2.0, k=10, knn_mode=0, libm=0, threads=1)
+                 arrival_radius=20.0, delete_radius=2.0, k=10, knn_mode=0, libm=0, threads=1, lp3d_fp64=0)
         d.update(kw)
         return Params(**d)
 
