@@ -503,8 +503,21 @@ EG_HD Con agent_constraint(V2 position, V2 velocity, float clr, V2 np, V2 nv, fl
     }
     float tanAngleFactor = VORadius / VOPosLength;
     float tanHalfAngle = ecmg_atanf(tanAngleFactor);
-    V2 VOLeftLeg = rotate(VOPos, tanHalfAngle);
-    V2 VORightLeg = rotate(VOPos, -tanHalfAngle);
+    /* RotateVector(VOPos, +/-tanHalfAngle): ecmg_sincosf is odd / even
+       symmetric bit for bit on the nonzero angles of [-pi/2, pi/2] (the
+       range of the atan), so the rotation by -angle takes (-sin, cos) of the
+       same call; a zero or NaN angle (where the sign of a zero or of a NaN
+       could differ) calls it again */
+    float sn, cs, sn2, cs2;
+    ecmg_sincosf(tanHalfAngle, &sn, &cs);
+    if (tanHalfAngle != 0.0f && tanHalfAngle == tanHalfAngle) {
+        sn2 = -sn;
+        cs2 = cs;
+    } else {
+        ecmg_sincosf(-tanHalfAngle, &sn2, &cs2);
+    }
+    V2 VOLeftLeg = mk(VOPos.x * cs - VOPos.y * sn, VOPos.x * sn + VOPos.y * cs);
+    V2 VORightLeg = mk(VOPos.x * cs2 - VOPos.y * sn2, VOPos.x * sn2 + VOPos.y * cs2);
     float sqDistFromCircleCentre = sqdist(VOPos, relVel);
     V2 bse = VOLeftLeg - VOPos, chk = relVel - VOPos;
     bool liesBelow = bse.x * chk.y - bse.y * chk.x > 0; /* IsLeftOfVector */

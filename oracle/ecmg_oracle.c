@@ -1098,6 +1098,24 @@ int og_time_sample(const og_obstacles* o, const og_ecm* e, const og_state* s, co
 /* the shared transcendentals, exported for their accuracy tests */
 float og_test_atanf(float x) { return ecmg_atanf(x); }
 void og_test_sincosf(float a, float* s, float* c) { ecmg_sincosf(a, s, c); }
+/* number of a in (0, pi/2] (every step-th binary32 value) where
+   ecmg_sincosf(-a) is not (-sin a, cos a) bit for bit */
+long og_test_sincos_symmetry(unsigned step)
+{
+    const float top = 1.57079637050628662109375f;
+    unsigned top_bits;
+    memcpy(&top_bits, &top, 4);
+    long bad = 0;
+    for (unsigned u = 1; u <= top_bits; u += step) {
+        float a, s1, c1, s2, c2;
+        memcpy(&a, &u, 4);
+        ecmg_sincosf(a, &s1, &c1);
+        ecmg_sincosf(-a, &s2, &c2);
+        float ns1 = -s1;
+        if (memcmp(&ns1, &s2, 4) != 0 || memcmp(&c1, &c2, 4) != 0) bad++;
+    }
+    return bad;
+}
 
 /* ---------------------------------------------------------------------------
  * One tick for a sample of agents (see ecmg_oracle.h)

@@ -37,3 +37,15 @@ def _call_sincos(L, v):
     L.og_test_sincosf.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.og_test_sincosf(float(v), C.byref(s), C.byref(c))
     return s.value, c.value
+
+
+def test_sincos_is_odd_even_symmetric_bit_for_bit(port):
+    """the agent half-plane takes the rotation by -angle from the same
+    ecmg_sincosf call as the rotation by +angle (sin(-a) = -sin a,
+    cos(-a) = cos a): true bit for bit on every 29th binary32 value of
+    (0, pi/2], the range of the atan that produces the angle (a zero angle
+    calls it twice: sin(-0) rounds to +0)"""
+    L = port.lib
+    L.og_test_sincos_symmetry.restype = C.c_long
+    L.og_test_sincos_symmetry.argtypes = [C.c_uint]
+    assert L.og_test_sincos_symmetry(29) == 0
