@@ -163,6 +163,7 @@ def load(build_if_missing: bool = False):
         "ecmg_mlp_loss_grad": (C.c_int, [vp, vp, vp, C.c_int, fp, vp]),
         "ecmg_mlp_train": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_ulonglong, vp, vp]),
         "ecmg_mlp_predict": (C.c_int, [vp, vp, C.c_int, vp]),
+        "ecmg_mlp_set_wait_limit": (C.c_int, [vp, C.c_int]),
         "ecmg_set_proposal": (C.c_int, [vp, vp]),
         "ecmg_set_trace": (C.c_int, [vp, C.c_int]),
         "ecmg_set_proposal_gate": (C.c_int, [vp, C.c_float, C.c_int]),

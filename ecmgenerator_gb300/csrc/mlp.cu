@@ -59,23 +59,33 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 }
 
 /* ------------------------------------------------------------------------
- * Inference on the 5th-generation tensor cores (tcgen05).  One CTA of four
- * warps per SM, persistent over tiles of 128 agents; per tile three MMA
- * chains (M = 128, N = 128 / 128 / 160, K = 96 / 128 / 128 in steps of 16),
- * each issued by one thread and completed through an mbarrier, with the
- * accumulators in tensor memory (128 lanes x N fp32 columns).  Each warp
- * reads its 32 lanes (rows) back with tcgen05.ld for the fused epilogue:
- * bias + GELU + BF16 into the next layer's operand tile, or bias + argmax.
- * Operands sit in shared memory in the canonical K-major layout without
- * swizzle: 8-row x 16-byte core matrices; the row groups of one 8-column
- * chunk are adjacent (stride byte offset 128), chunks R x 16 bytes apart
- * (leading byte offset) for an operand of R rows.  One chunk of a 128-row
- * feature tile is then one 2 KB TMA box (8 columns x 128 rows), so the
- * tile arrives by 12 cp.async.bulk.tensor copies, prefetched for the next
- * tile while the hidden layers of this one run.
+ * Inference on the 5th-generation tensor cores (tcgen05).  One CTA of eight
+ * warps per SM, persistent over tiles of 128 agents, with two tiles in
+ * flight (slots 0 and 1): while the warps run the epilogue of one slot's
+ * layer, the tensor core runs the other slot's next MMA chain.  Per tile
+ * three chains (M = 128, N = 128 / 128 / 160, K = 96 / 128 / 128 in steps
+ * of 16), each issued by one thread and completed through the slot's
+ * mbarrier, with the slot's accumulator in its own 256 tensor-memory
+ * columns (128 lanes x N fp32).  Epilogue: warp w reads lanes
+ * 32 (w mod 4) .. +31 (rows) and half w / 4 of the columns with
+ * tcgen05.ld -- bias + GELU (tanh.approx) + BF16 into the slot's hidden
+ * tile, or bias + argmax for the output (the two column halves combined in
+ * shared memory, first maximum wins).  Operands sit in shared memory in the
+ * canonical K-major layout without swizzle: 8-row x 16-byte core matrices;
+ * the row groups of one 8-column chunk are adjacent (stride byte offset
+ * 128), chunks R x 16 bytes apart (leading byte offset) for an operand of R
+ * rows.  One chunk of a 128-row feature tile is one 2 KB TMA box (8 columns
+ * x 128 rows): a slot's next tile is requested as soon as its first layer
+ * has consumed the current one, four epilogues ahead of its use.  Every
+ * wait is bounded (spin limit); on a timeout the CTA sets the error bit,
+ * waits for its copies and MMAs in flight, frees its tensor memory and
+ * returns.
  * ---------------------------------------------------------------------- */
 constexpr int kTile = 128;      /* agents per tile (MMA M) */
-constexpr int kTmemCols = 256;  /* >= the widest accumulator (160), a power of 2 */
+constexpr int kSlotCols = 256;  /* tensor-memory columns per slot: >= the widest accumulator (160) */
+constexpr int kTmemCols = 2 * kSlotCols;
+constexpr int kInferThreads = 256;
+constexpr int kSpinDefault = 1 << 22;
 
 /* byte offset of element (r, k) of an [R x K] bf16 operand in that layout */
 __host__ __device__ constexpr int tc_off(int r, int k, int R)
@@ -86,7 +96,9 @@ __host__ __device__ constexpr int tc_off(int r, int k, int R)
 constexpr int kW1B = HID * IN * 2, kW2B = HID * HID * 2, kW3B = OUT * HID * 2; /* B operands: N rows x K */
 constexpr int kWB = kW1B + kW2B + kW3B;
 constexpr int kXB = kTile * IN * 2, kHB = kTile * HID * 2;
-constexpr size_t kInferSmem = (size_t)kWB + kXB + kHB + sizeof(float) * (2 * HID + OUT) + 32;
+/* weights, two feature tiles, two hidden tiles, biases, argmax exchange, barriers */
+constexpr size_t kInferSmem = (size_t)kWB + 2 * kXB + 2 * kHB + sizeof(float) * (2 * HID + OUT) +
+                              2 * kTile * (sizeof(float) + sizeof(int)) + 64;
 
 /* shared-memory matrix descriptor (no swizzle) */
 __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
@@ -129,16 +141,28 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar)
                  : "memory");
 }
 
-/* bounded wait for the mbarrier phase with the given parity: false on timeout */
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+/* bounded wait for the mbarrier phase with the given parity: false after
+   `limit` polls.  Limits of at least 1024 poll with try_wait (which may
+   suspend the thread for a while); smaller ones -- the diagnostic setting
+   of ecmg_mlp_set_wait_limit -- with the non-blocking test_wait, so that a
+   limit of one poll really gives up at once */
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, int limit = kSpinDefault)
 {
-    for (int it = 0; it < (1 << 22); it++) {
+    const bool blocking = limit >= 1024;
+    for (int it = 0; it < limit; it++) {
         uint32_t ok;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(ok)
-            : "r"(mbar), "r"(parity)
-            : "memory");
+        if (blocking)
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(ok)
+                : "r"(mbar), "r"(parity)
+                : "memory");
+        else
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(ok)
+                : "r"(mbar), "r"(parity)
+                : "memory");
         if (ok) return true;
     }
     return false;
@@ -181,33 +205,69 @@ __device__ __forceinline__ void tma_tile(const CUtensorMap* tm, uint32_t sdst, i
             : "memory");
 }
 
-/* class of every row of X [n, IN] (bf16, row-major); err |= errbit on a
-   timed-out tensor-core wait (the CTA then stops and frees its tensor memory) */
-__global__ void __launch_bounds__(128, 1) k_mlp_infer(const __grid_constant__ CUtensorMap tmX, const int* n_ptr,
-                                                      int n_fixed, const unsigned char* wpack, const float* bias,
-                                                      unsigned char* cls, int* err, int errbit)
+__device__ __forceinline__ float tanh_approx(float x)
+{
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+/* GELU (tanh form) for inference: the hardware tanh approximation (relative
+   error about 2^-11, below the BF16 rounding of the activations) */
+__device__ __forceinline__ float gelu_fast(float x)
+{
+    const float k0 = 0.7978845608028654f, k1 = 0.044715f;
+    const float u = k0 * __fmaf_rn(k1 * (x * x), x, x);
+    const float hx = 0.5f * x;
+    return __fmaf_rn(hx, tanh_approx(u), hx);
+}
+
+/* 32 consecutive fp32 columns of this thread's lane, one wait */
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+/* class of every row of X [n, IN] (bf16, row-major); err |= errbit when a
+   wait runs past `spin` polls (the CTA then drains and stops) */
+__global__ void __launch_bounds__(kInferThreads, 1)
+    k_mlp_infer(const __grid_constant__ CUtensorMap tmX, const int* n_ptr, int n_fixed, const unsigned char* wpack,
+                const float* bias, unsigned char* cls, int* err, int errbit, int spin)
 {
     extern __shared__ __align__(128) unsigned char sm[];
     unsigned char* sW1 = sm;
     unsigned char* sW2 = sW1 + kW1B;
     unsigned char* sW3 = sW2 + kW2B;
-    unsigned char* sX = sW3 + kW3B;
-    unsigned char* sH = sX + kXB;
-    float* sb = reinterpret_cast<float*>(sH + kHB);
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sb + 2 * HID + OUT);
-    uint64_t* s_mbar = reinterpret_cast<uint64_t*>(s_tmem + 2); /* [0] MMA done, [1] feature tile landed */
+    unsigned char* sX = sW3 + kW3B;  /* [2][kXB] */
+    unsigned char* sH = sX + 2 * kXB; /* [2][kHB] */
+    float* sb = reinterpret_cast<float*>(sH + 2 * kHB);
+    float* s_best = sb + 2 * HID + OUT; /* [kTile]: the second column half's maximum per row */
+    int* s_bidx = reinterpret_cast<int*>(s_best + kTile);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_bidx + kTile);
+    uint64_t* s_mbar = reinterpret_cast<uint64_t*>(
+        (reinterpret_cast<uintptr_t>(s_tmem + 2) + 7) & ~(uintptr_t)7); /* [0..1] MMA done, [2..3] tile landed */
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int quad = warp & 3, half = warp >> 2;
     const int n = n_ptr ? *n_ptr : n_fixed;
 
-    /* weights (packed in the operand layout) and biases, once per CTA */
     for (int i = tid; i < kWB / 16; i += blockDim.x)
         reinterpret_cast<uint4*>(sm)[i] = reinterpret_cast<const uint4*>(wpack)[i];
     for (int i = tid; i < 2 * HID + OUT; i += blockDim.x) sb[i] = bias[i];
-    const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(s_mbar);
-    const uint32_t mbar_x = mbar + 8;
+    const uint32_t mbar0 = (uint32_t)__cvta_generic_to_shared(s_mbar);
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_x) : "memory");
+        for (int b = 0; b < 4; b++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0 + 8u * b) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -222,88 +282,146 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(const __grid_constant__ CU
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *s_tmem;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16); /* this warp's 32 lanes */
-    const uint32_t aX = (uint32_t)__cvta_generic_to_shared(sX), aH = (uint32_t)__cvta_generic_to_shared(sH);
+    const uint32_t aX0 = (uint32_t)__cvta_generic_to_shared(sX), aH0 = (uint32_t)__cvta_generic_to_shared(sH);
     const uint32_t aW1 = (uint32_t)__cvta_generic_to_shared(sW1), aW2 = (uint32_t)__cvta_generic_to_shared(sW2),
                    aW3 = (uint32_t)__cvta_generic_to_shared(sW3);
-    const int row = warp * 32 + lane;
-    uint32_t phase = 0, phase_x = 0;
-    bool fail = false, x_pending = false;
+    const int row = quad * 32 + lane;
     const int ntiles = (n + kTile - 1) / kTile;
-    if ((int)blockIdx.x < ntiles) {
-        if (tid == 0) tma_tile(&tmX, aX, blockIdx.x * kTile, mbar_x);
-        x_pending = true;
-    }
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int r0 = tile * kTile;
-        /* this tile's features (rows beyond the tensor read as zeros) */
-        fail = __syncthreads_or(!mbar_wait(mbar_x, phase_x)) != 0;
-        phase_x ^= 1u;
-        x_pending = false;
-        if (fail) break;
-        /* three layers: D = A * W; hidden epilogues write the next A into sH */
-#pragma unroll 1
-        for (int layer = 0; layer < 3 && !fail; layer++) {
-            const int K = layer == 0 ? IN : HID, N = layer == 2 ? OUT : HID;
-            fence_async_smem();
-            tc_fence_before();
-            __syncthreads();
-            tc_fence_after();
-            if (tid == 0) {
-                tc_layer(tmem, layer == 0 ? aX : aH, layer == 0 ? aW1 : (layer == 1 ? aW2 : aW3), K, N);
-                tc_commit(mbar);
-            }
-            fail = __syncthreads_or(!mbar_wait(mbar, phase)) != 0;
-            phase ^= 1u;
-            tc_fence_after();
-            if (fail) break;
-            if (layer == 0 && tile + (int)gridDim.x < ntiles) {
-                /* sX has been read: bring in the next tile meanwhile */
-                if (tid == 0) tma_tile(&tmX, aX, (tile + (int)gridDim.x) * kTile, mbar_x);
-                x_pending = true;
-            }
-            const float* bl = sb + (layer == 0 ? 0 : (layer == 1 ? HID : 2 * HID));
-            if (layer < 2) {
-#pragma unroll 1
-                for (int c = 0; c < HID; c += 16) {
-                    float v[16];
-                    tmem_ld16(lane_base + (uint32_t)c, v);
-                    uint4 lo, hi;
-                    lo.x = pack_bf16(gelu(v[0] + bl[c + 0]), gelu(v[1] + bl[c + 1]));
-                    lo.y = pack_bf16(gelu(v[2] + bl[c + 2]), gelu(v[3] + bl[c + 3]));
-                    lo.z = pack_bf16(gelu(v[4] + bl[c + 4]), gelu(v[5] + bl[c + 5]));
-                    lo.w = pack_bf16(gelu(v[6] + bl[c + 6]), gelu(v[7] + bl[c + 7]));
-                    hi.x = pack_bf16(gelu(v[8] + bl[c + 8]), gelu(v[9] + bl[c + 9]));
-                    hi.y = pack_bf16(gelu(v[10] + bl[c + 10]), gelu(v[11] + bl[c + 11]));
-                    hi.z = pack_bf16(gelu(v[12] + bl[c + 12]), gelu(v[13] + bl[c + 13]));
-                    hi.w = pack_bf16(gelu(v[14] + bl[c + 14]), gelu(v[15] + bl[c + 15]));
-                    *reinterpret_cast<uint4*>(sH + tc_off(row, c, kTile)) = lo;
-                    *reinterpret_cast<uint4*>(sH + tc_off(row, c + 8, kTile)) = hi;
-                }
-            } else {
-                float best = -INFINITY;
-                int bi = 0;
-#pragma unroll 1
-                for (int c = 0; c < OUT; c += 16) {
-                    float v[16];
-                    tmem_ld16(lane_base + (uint32_t)c, v);
-#pragma unroll
-                    for (int i = 0; i < 16; i++) {
-                        const float z = v[i] + bl[c + i];
-                        if (z > best) { best = z; bi = c + i; }
-                    }
-                }
-                if (r0 + row < n) cls[r0 + row] = (unsigned char)bi;
-            }
+    /* slot s runs the tiles blockIdx.x + (2 j + s) gridDim.x, j = 0, 1, ... */
+    int tile[2] = {(int)blockIdx.x, (int)blockIdx.x + (int)gridDim.x};
+    uint32_t ph_mma[2] = {0u, 0u}, ph_x[2] = {0u, 0u};
+    bool mma_pending[2] = {false, false}, x_pending[2] = {false, false};
+    bool fail = false;
+
+    auto mbar_mma = [&](int s_) { return mbar0 + 8u * (uint32_t)s_; };
+    auto mbar_x = [&](int s_) { return mbar0 + 8u * (uint32_t)(2 + s_); };
+    auto issue_x = [&](int s_) { /* thread 0 */
+        tma_tile(&tmX, aX0 + (uint32_t)(s_ * kXB), tile[s_] * kTile, mbar_x(s_));
+    };
+    /* all threads: wait for slot s's MMA chain; false on timeout */
+    auto wait_mma = [&](int s_) {
+        const bool ok = mbar_wait(mbar_mma(s_), ph_mma[s_], spin);
+        fail = __syncthreads_or(!ok) != 0;
+        if (!fail) {
+            ph_mma[s_] ^= 1u;
+            mma_pending[s_] = false;
         }
-        if (fail) break;
-        /* the accumulator is read out before the next tile's MMAs overwrite it */
+        tc_fence_after();
+        return !fail;
+    };
+    /* one layer's MMA chain for slot s, after the operands written by the
+       threads are visible to the tensor core */
+    auto issue_mma = [&](int s_, int layer) {
+        fence_async_smem();
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
+        if (tid == 0) {
+            const uint32_t a = layer == 0 ? aX0 + (uint32_t)(s_ * kXB) : aH0 + (uint32_t)(s_ * kHB);
+            tc_layer(tmem + (uint32_t)(s_ * kSlotCols), a, layer == 0 ? aW1 : (layer == 1 ? aW2 : aW3),
+                     layer == 0 ? IN : HID, layer == 2 ? OUT : HID);
+            tc_commit(mbar_mma(s_));
+        }
+        mma_pending[s_] = true;
+    };
+    /* first layer of slot s's current tile: its features, then the chain */
+    auto start_tile = [&](int s_) {
+        const bool ok = mbar_wait(mbar_x(s_), ph_x[s_], spin);
+        fail = __syncthreads_or(!ok) != 0;
+        if (fail) return false;
+        ph_x[s_] ^= 1u;
+        x_pending[s_] = false;
+        issue_mma(s_, 0);
+        return true;
+    };
+    /* bias + GELU + BF16 of slot s's accumulator into its hidden tile */
+    auto epi_hidden = [&](int s_, int layer) {
+        const float* bl = sb + (layer == 0 ? 0 : HID);
+        unsigned char* h = sH + s_ * kHB;
+        const uint32_t lb = tmem + (uint32_t)(s_ * kSlotCols) + ((uint32_t)(quad * 32) << 16);
+#pragma unroll 1
+        for (int c = half * (HID / 2); c < (half + 1) * (HID / 2); c += 32) {
+            float v[32];
+            tmem_ld32(lb + (uint32_t)c, v);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                uint4 u;
+                u.x = pack_bf16(gelu_fast(v[8 * q + 0] + bl[c + 8 * q + 0]), gelu_fast(v[8 * q + 1] + bl[c + 8 * q + 1]));
+                u.y = pack_bf16(gelu_fast(v[8 * q + 2] + bl[c + 8 * q + 2]), gelu_fast(v[8 * q + 3] + bl[c + 8 * q + 3]));
+                u.z = pack_bf16(gelu_fast(v[8 * q + 4] + bl[c + 8 * q + 4]), gelu_fast(v[8 * q + 5] + bl[c + 8 * q + 5]));
+                u.w = pack_bf16(gelu_fast(v[8 * q + 6] + bl[c + 8 * q + 6]), gelu_fast(v[8 * q + 7] + bl[c + 8 * q + 7]));
+                *reinterpret_cast<uint4*>(h + tc_off(row, c + 8 * q, kTile)) = u;
+            }
+        }
+    };
+    /* bias + argmax of slot s's output accumulator; the first maximum wins */
+    auto epi_out = [&](int s_) {
+        const float* bl = sb + 2 * HID;
+        const uint32_t lb = tmem + (uint32_t)(s_ * kSlotCols) + ((uint32_t)(quad * 32) << 16);
+        float best = -INFINITY;
+        int bi = half * (OUT / 2);
+#pragma unroll 1
+        for (int c = half * (OUT / 2); c < (half + 1) * (OUT / 2); c += 16) {
+            float v[16];
+            tmem_ld16(lb + (uint32_t)c, v);
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                const float z = v[i] + bl[c + i];
+                if (z > best) { best = z; bi = c + i; }
+            }
+        }
+        if (half == 1) {
+            s_best[row] = best;
+            s_bidx[row] = bi;
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (half == 0) {
+            if (s_best[row] > best) bi = s_bidx[row];
+            const int r = tile[s_] * kTile + row;
+            if (r < n) cls[r] = (unsigned char)bi;
+        }
+    };
+
+    for (int s_ = 0; s_ < 2; s_++)
+        if (tile[s_] < ntiles) {
+            if (tid == 0) issue_x(s_);
+            x_pending[s_] = true;
+        }
+    for (int s_ = 0; s_ < 2 && !fail; s_++)
+        if (tile[s_] < ntiles) start_tile(s_);
+    while (!fail && (tile[0] < ntiles || tile[1] < ntiles)) {
+        /* layer 1 epilogues; a slot's features are consumed: request its next tile */
+        for (int s_ = 0; s_ < 2 && !fail; s_++) {
+            if (tile[s_] >= ntiles || !wait_mma(s_)) continue;
+            epi_hidden(s_, 0);
+            const int nxt = tile[s_] + 2 * (int)gridDim.x;
+            if (nxt < ntiles) {
+                if (tid == 0) tma_tile(&tmX, aX0 + (uint32_t)(s_ * kXB), nxt * kTile, mbar_x(s_));
+                x_pending[s_] = true;
+            }
+            issue_mma(s_, 1);
+        }
+        for (int s_ = 0; s_ < 2 && !fail; s_++) {
+            if (tile[s_] >= ntiles || !wait_mma(s_)) continue;
+            epi_hidden(s_, 1);
+            issue_mma(s_, 2);
+        }
+        for (int s_ = 0; s_ < 2 && !fail; s_++) {
+            if (tile[s_] >= ntiles || !wait_mma(s_)) continue;
+            epi_out(s_);
+            tile[s_] += 2 * (int)gridDim.x;
+            if (tile[s_] < ntiles) start_tile(s_);
+        }
     }
     if (fail && tid == 0) atomicOr(err, errbit);
-    if (x_pending) (void)mbar_wait(mbar_x, phase_x); /* no copy may land after the CTA ends */
+    /* nothing in flight may outlive the CTA: its copies and MMAs are waited
+       for (with the default bound) before the tensor memory is freed */
+    for (int s_ = 0; s_ < 2; s_++) {
+        if (x_pending[s_]) (void)mbar_wait(mbar_x(s_), ph_x[s_]);
+        if (mma_pending[s_]) (void)mbar_wait(mbar_mma(s_), ph_mma[s_]);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -476,6 +594,7 @@ struct ecmg_mlp {
     float* v = nullptr;     /* Adam second moment */
     unsigned char* pack = nullptr; /* BF16 weights in the tensor-core operand layout (inference) */
     int* derr = nullptr;           /* inference error flag (ecmg_mlp_predict) */
+    int spin = kSpinDefault;       /* polls of an mbarrier before the inference gives up */
     float* bias = nullptr;  /* b1 | b2 | b3 */
     int step = 0;
     bool packed = false;
@@ -558,7 +677,8 @@ cudaError_t ecmg::mlp_infer(ecmg_mlp* mm, const void* X, const int* n_dev, int n
     int tiles = (n_max + kTile - 1) / kTile;
     int grid = tiles < sms ? tiles : sms; /* one CTA per SM holds the weights once */
     if (grid < 1) grid = 1;
-    k_mlp_infer<<<grid, 128, kInferSmem, s>>>(tm, n_dev, n_max, mm->pack, mm->bias, cls, err, errbit);
+    k_mlp_infer<<<grid, kInferThreads, kInferSmem, s>>>(tm, n_dev, n_max, mm->pack, mm->bias, cls, err, errbit,
+                                                         mm->spin);
     return cudaGetLastError();
 }
 
@@ -753,6 +873,13 @@ ecmg_status ecmg_mlp_train(ecmg_mlp* mm, const void* dev_x, const unsigned char*
     }
     mm->packed = false;
     return cudaStreamSynchronize(mm->s) == cudaSuccess ? ECMG_OK : ECMG_ERR_CUDA;
+}
+
+ecmg_status ecmg_mlp_set_wait_limit(ecmg_mlp* mm, int polls)
+{
+    if (!mm || polls < 0) return ECMG_ERR_INVALID_ARG;
+    mm->spin = polls > 0 ? polls : kSpinDefault;
+    return ECMG_OK;
 }
 
 ecmg_status ecmg_mlp_predict(ecmg_mlp* mm, const void* dev_x, int n, unsigned char* dev_cls)

@@ -434,8 +434,15 @@ ecmg_status ecmg_mlp_loss_grad(ecmg_mlp* model, const void* dev_x, const unsigne
    from the n rows (seeded); per-step loss / accuracy to host arrays if given */
 ecmg_status ecmg_mlp_train(ecmg_mlp* model, const void* dev_x, const unsigned char* dev_y, int n, int steps,
                            int batch, float lr, unsigned long long seed, float* host_loss, float* host_acc);
-/* class of every row (argmax of the BF16 tensor-core forward) */
+/* class of every row (argmax of the BF16 tensor-core forward); returns
+   ECMG_ERR_BOUND when a bounded wait of the inference kernel gave up (the
+   kernel drains its copies and MMAs, frees its tensor memory and returns) */
 ecmg_status ecmg_mlp_predict(ecmg_mlp* model, const void* dev_x, int n, unsigned char* dev_cls);
+/* how many times the inference kernel polls an mbarrier (a feature-tile copy
+   or an MMA chain) before it gives up with ECMG_ERR_BOUND; 0 restores the
+   default (2^22).  A diagnostic of the device-side timeout path: a tiny
+   limit makes the first wait run out. */
+ecmg_status ecmg_mlp_set_wait_limit(ecmg_mlp* model, int polls);
 
 /* Learned mode for a context: model != NULL turns it on (the context does
    not own the model; keep it alive while it is set), NULL turns it off.

@@ -90,6 +90,44 @@ def test_mlp_predict_tensor_cores_matches_bf16_oracle(lib):
     m.close()
 
 
+def test_mlp_predict_pipelined_tiles_match_single_tiles(lib):
+    """many tiles per CTA (both pipeline slots, tiles that wait for their
+    features) give the classes that launches of a few tiles give"""
+    torch = _torch()
+    from ecmgenerator_gb300.proposal import ProposalModel
+
+    m = ProposalModel(seed=6)
+    n = 152 * 2 * 4 * 128 + 77
+    x = _bf16_rows(torch, n, 13)
+    full = m.predict(x).cpu()
+    parts = torch.cat([m.predict(x[i:i + 4096].contiguous()).cpu() for i in range(0, n, 4096)])
+    assert torch.equal(full, parts)
+    m.close()
+
+
+def test_inference_wait_bound_reports_a_timeout_and_recovers(lib):
+    """the inference kernel's bounded mbarrier waits: with a limit of one
+    poll the first wait (a feature-tile copy) runs out; the kernel waits for
+    its copies, frees its tensor memory and returns, the call reports
+    ECMG_ERR_BOUND, and the next call with the default limit gives the
+    normal classes"""
+    torch = _torch()
+    from ecmgenerator_gb300._lib import EcmgError
+    from ecmgenerator_gb300.proposal import ProposalModel
+
+    m = ProposalModel(seed=7)
+    x = _bf16_rows(torch, 70000, 14)
+    want = m.predict(x).cpu()
+    assert lib.ecmg_mlp_set_wait_limit(m.h, 1) == 0
+    with pytest.raises(EcmgError) as e:
+        m.predict(x)
+    assert e.value.status == 3  # ECMG_ERR_BOUND
+    assert lib.ecmg_mlp_set_wait_limit(m.h, 0) == 0
+    assert torch.equal(m.predict(x).cpu(), want)
+    assert lib.ecmg_mlp_set_wait_limit(m.h, -1) == 1
+    m.close()
+
+
 def test_mlp_training_learns_a_separable_task(lib):
     torch = _torch()
     from ecmgenerator_gb300.proposal import ProposalModel
