@@ -486,12 +486,19 @@ EG_HD Con agent_constraint(V2 position, V2 velocity, float clr, V2 np, V2 nv, fl
     Con c;
     const float rx = np.x - position.x, ry = np.y - position.y;
     V2 VOPos = inv_tau != 0.0f ? mk(rx * inv_tau, ry * inv_tau) : mk(rx / tau, ry / tau);
-    float VOPosLength = len(VOPos);
+    V2 relPos = mk(rx, ry);
+    float relPosLength = len(relPos);
+    /* with a power-of-two 1/tau every step of the length scales exactly
+       while all squares and sums stay normal numbers -- each component zero
+       or within [1e-12, 1e12] m and 1/tau within [2^-20, 2^20] -- so
+       |VOPos| = |relPos| / tau bit for bit and needs no second square root */
+    const float ax = fabsf(rx), ay = fabsf(ry);
+    const bool scaled = inv_tau >= 9.5367431640625e-07f && inv_tau <= 1048576.0f &&
+                        (ax == 0.0f || (ax >= 1e-12f && ax <= 1e12f)) && (ay == 0.0f || (ay >= 1e-12f && ay <= 1e12f));
+    float VOPosLength = scaled ? relPosLength * inv_tau : len(VOPos);
     float combinedRadius = nclr + clr;
     float VORadius = inv_tau != 0.0f ? combinedRadius * inv_tau : combinedRadius / tau;
     V2 relVel = mk(velocity.x - nv.x, velocity.y - nv.y);
-    V2 relPos = mk(np.x - position.x, np.y - position.y);
-    float relPosLength = len(relPos);
     if (relPosLength < combinedRadius) {
         V2 w = relVel - relPos / dt;
         float wLength = len(w);
