@@ -205,8 +205,10 @@ def apply_launch(plain, learned, args):
         return r
     grab = 4 if args.lp_mode == "warp" else 32
     for s_ in (plain, learned):
+        if args.grid_scale > 0:
+            set_launch(s_, 128, 32, args.grid_scale)
         set_lp_mode(s_, args.lp_mode, grab if args.lp_mode == "warp" else 1)
-    return {"lp_mode": args.lp_mode, "agents_per_warp_grab": grab}
+    return {"lp_mode": args.lp_mode, "agents_per_warp_grab": grab, "grid_cell_scale": args.grid_scale or None}
 
 
 class TickTimer:
@@ -620,6 +622,8 @@ def main():
     ap.add_argument("--no-gate", action="store_true", help="keep the proposal model on every tick")
     ap.add_argument("--lp-mode", default="tune", choices=["tune", "thread", "warp", "fused"],
                     help="per-agent kernel layout (default: autotuned)")
+    ap.add_argument("--grid-scale", type=float, default=0.0,
+                    help="with a fixed --lp-mode: agent-grid cell scale (cell = scale * sqrt(k / density))")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -4,6 +4,8 @@
                    four 250k groups spawned in 60 m bands along the sides,
                    goals in the opposite band (overlap allowed), k = 16
     crossing_100k  the same scene with 100,000 agents
+    crossing_250k  a quarter of the 1M crossing at its density: 200x200 m,
+                   50 boxes, 30 m bands, 250,000 agents (profiling case)
     boxes_100k     1000x1000 m, 4,000 boxes of side U[2,8] m, 100,000 agents
                    spawned without overlap, goals uniform in free space, k = 10
     boxes_1k       100x100 m, 40 boxes, 1,000 agents, k = 10
@@ -25,6 +27,7 @@ import numpy as np
 WORKLOADS = {
     "crossing_1m": dict(cfg="c3", agents=1_000_000, k=16),
     "crossing_100k": dict(cfg="c3", agents=100_000, k=16),
+    "crossing_250k": dict(cfg="c3", agents=250_000, k=16, over=dict(w=200.0, h=200.0, boxes=50, bands=30.0)),
     "boxes_100k": dict(cfg="c2", agents=100_000, k=10),
     "boxes_1k": dict(cfg="c1", agents=1_000, k=10),
     "batch_256": dict(batch=256, agents=1_300_000, k=10),
@@ -42,7 +45,7 @@ def make_workload(name, seed, verbose=True, planner="reference", plan=None):
     from . import agents as ag
 
     w = WORKLOADS[name]
-    cfg = ag.scaled(w["cfg"], agents=w["agents"])
+    cfg = ag.scaled(w["cfg"], agents=w["agents"], **w.get("over", {}))
     t0 = time.time()
     scene = ag.build_scene(cfg, seed)
     st = ag.spawn_agents(cfg, scene, seed)
