@@ -301,7 +301,7 @@ def run_ours(args):
         stream = np.random.default_rng(args.seed + 99).integers(
             0, 2147483647, 33 * (int(args.spawn_rate * DT) + 1) * 4 * 4000, dtype=np.int32)
     for _ in range(0 if batch else 2):
-        s_ = Simulator(scene, n + spawn_slots, DT, max_neighbors=k, **ORCA)
+        s_ = Simulator(scene, n + spawn_slots, DT, max_neighbors=k, lp3d_fp64=args.lp3d_fp64, **ORCA)
         s_.add_agents(st.pos[:n], st.clear[:n], st.pref_speed[:n], paths)
         if args.spawn_rate > 0:
             add_spawn_areas(s_, scene, args.spawn_rate)
@@ -373,6 +373,27 @@ def run_ours(args):
     value = steps_all / (ms_all / 1e3)
     p_ms_all, p_steps_all = reduce_over_ranks(tp.ms(), tp.steps, world, "cuda")
     plain_value = p_steps_all / (p_ms_all / 1e3)
+    no_gate = None
+    if model is not None and not args.no_gate:
+        # the learned tick with the model forced on every tick (no gate),
+        # K ticks after the timed blocks: what the model itself costs here
+        learned.set_proposal_gate(0.0, 0)
+        for _ in range(2):
+            learned.update()
+        tn = TickTimer(learned, flush)
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            tn.tick()
+        torch.cuda.synchronize()
+        n_ms, n_steps = reduce_over_ranks(tn.ms(), tn.steps, world, "cuda")
+        K_ = max(args.steps, 1)
+        no_gate = {"value": n_steps / (n_ms / 1e3), "ms_per_step": n_ms / K_,
+                   "vs_plain": (n_steps / (n_ms / 1e3)) / plain_value,
+                   "proposed_per_tick": tn.tot["proposed"] / K_, "accepted_per_tick": tn.tot["accepted"] / K_,
+                   "features_and_inference_ms_per_tick": tn.tot["proposal_ms"] / K_,
+                   "per_agent_kernel_ms_per_tick": tn.tot["orca_ms"] / K_,
+                   "note": "the learned tick with the gate open on every tick (model on), timed after the "
+                           "gated blocks; 2D LPs with a proposal are those the model did not class as other"}
     # e2e through the public API: update + positions/velocities back to host
     e2e = {}
     for name, sim in (("learned", learned), ("plain", plain)):
@@ -456,6 +477,7 @@ def run_ours(args):
         "dtype": "f32", "data": "synthetic (seeded scene, agents and paths)",
         "config": workload_config(args, n, k, scene_desc, world),
         "mode": "learned proposal" if model is not None else "plain",
+        "lp3d_projection": "fp64" if args.lp3d_fp64 else "fp32 (the reference's)",
         "neighbors": "exact (d2, index)" if args.neighbors == "exact" else "kd-tree (the reference's query)",
         "launch": launch,
         "plain": {"value": plain_value, "ms_per_step": p_ms_all / args.steps,
@@ -469,7 +491,7 @@ def run_ours(args):
             **model_info, "proposed_per_tick": T["proposed"] / args.steps,
             "accepted_per_tick": T["accepted"] / args.steps,
             "acceptance_rate": T["accepted"] / max(1, main_t.steps), "gated_ticks": T["gated"],
-            "trajectories_identical": same},
+            "trajectories_identical": same, "no_gate": no_gate},
         "e2e": e2e_main,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": kname, "kernel_ms": kern_ms, "alg_bytes_per_agent": alg_bytes,
@@ -622,6 +644,8 @@ def main():
     ap.add_argument("--no-gate", action="store_true", help="keep the proposal model on every tick")
     ap.add_argument("--lp-mode", default="tune", choices=["tune", "thread", "warp", "fused"],
                     help="per-agent kernel layout (default: autotuned)")
+    ap.add_argument("--lp3d-fp64", action="store_true",
+                    help="build the 3D-LP bisector intersections in FP64 (ecmg_params.lp3d_fp64)")
     ap.add_argument("--grid-scale", type=float, default=0.0,
                     help="with a fixed --lp-mode: agent-grid cell scale (cell = scale * sqrt(k / density))")
     args = ap.parse_args()

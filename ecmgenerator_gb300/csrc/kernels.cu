@@ -263,15 +263,20 @@ __device__ void knn_grid(Knn<K>& s, int k, V2 p, float rnb, float r2, const V2* 
    the lower-left quarter and mirrored for the others), so the k nearest are
    met early and few candidates enter the list only to be dropped again; the
    walk stops at the first cell whose distance bound exceeds the current k-th
-   distance.  The list is kept as 32-bit float distances with the candidates'
-   grid-order indices beside them: a candidate enters when its d2 is strictly
-   below the k-th.  That equals the (d2, slot) order of the reference
-   definition unless two d2 are equal -- two listed ones, or a dropped one
-   equal to the k-th -- and the search then returns false and the caller runs
-   the 64-bit (d2, slot) search (knn_grid); likewise when the table ends
-   before the search could (sparse crowds) or the agent is outside the
-   grid. */
-constexpr int kTmplR = 6, kTmplCap = (2 * kTmplR + 1) * (2 * kTmplR + 1);
+   distance.
+   The list holds packed keys: a candidate's d2 with its 12 low mantissa bits
+   replaced by a code of where it came from (table step, offset in its
+   cell), so that one float min / max pair per list position inserts it --
+   the ALU pipe's work -- and the code gives its grid index back at the end.
+   Packed keys order candidates by d2 except within a relative 2^-11 of each
+   other ("near ties"); those groups are re-sorted by the exact (d2, slot)
+   key afterwards.  The list keeps two entries beyond the k-th so that a near
+   tie at the k-th is resolved inside the list; when it may reach beyond it
+   (a dropped candidate with the same leading bits), when a cell holds more
+   than 32 agents, when the table ends before the search could (sparse
+   crowds) or when the agent is outside the grid, the search returns false
+   and the caller runs the 64-bit (d2, slot) search (knn_grid). */
+constexpr int kTmplR = 5, kTmplCap = (2 * kTmplR + 1) * (2 * kTmplR + 1);
 /* bound per axis from the quarter [0, 1/2] of cell 0 to cell d, in half cells */
 constexpr int tmpl_half(int d) { return d >= 1 ? 2 * d - 1 : (d <= -1 ? 2 * (-d - 1) : 0); }
 /* the table holds the cells whose bound is at most kTmplR cells: every cell
@@ -323,78 +328,152 @@ constexpr KnnTemplate make_knn_template()
 }
 __constant__ KnnTemplate c_knn_tmpl = make_knn_template();
 
-/* d2 and grid index of one candidate into the sorted list (key, id); a
-   candidate it does not keep, or the entry it pushes out, lowers *rej */
-template <int K>
-__device__ __forceinline__ void knn_fast_consider(float* key, int* id, float* rej, int j, V2 p, const V2* s_pos)
+constexpr unsigned kCodeMask = 0xFFFu;  /* low mantissa bits of a packed key */
+constexpr int kCodeOverflow = 127;       /* table step code of the overflow bucket */
+static_assert(kTmplN < kCodeOverflow, "table steps must fit 7 bits");
+
+__device__ __forceinline__ unsigned key_hi(float k) { return __float_as_uint(k) & ~kCodeMask; }
+
+/* one candidate (grid index j) into the packed list of KL entries; code =
+   table step << 5 | offset in the cell; a candidate not kept, or the entry
+   pushed out, lowers *rej */
+template <int KL>
+__device__ __forceinline__ void knn_pk_consider(float* key, float* rej, int j, unsigned code, V2 p, float r2,
+                                                const V2* s_pos)
 {
     const V2 q = s_pos[j];
     const float dx = q.x - p.x, dy = q.y - p.y;
-    float nk = dx * dx + dy * dy; /* KDTree.cpp:107-108 */
-    if (!(nk > kEps)) return;
-    if (nk < key[K - 1]) {
-        int ni = j;
+    const float d2 = dx * dx + dy * dy; /* KDTree.cpp:107-108 */
+    if (!(d2 > kEps) || !(d2 < r2)) return;
+    float nk = __uint_as_float((__float_as_uint(d2) & ~kCodeMask) | code);
+    if (nk < key[KL - 1]) {
 #pragma unroll
-        for (int q2 = 0; q2 < K; q2++) {
-            const bool c = nk < key[q2];
-            const float tk = key[q2];
-            const int ti = id[q2];
-            key[q2] = c ? nk : tk;
-            id[q2] = c ? ni : ti;
-            nk = c ? tk : nk;
-            ni = c ? ti : ni;
+        for (int q2 = 0; q2 < KL; q2++) {
+            const float a = key[q2];
+            key[q2] = fminf(a, nk);
+            nk = fmaxf(a, nk);
         }
     }
     *rej = fminf(*rej, nk);
 }
 
-/* true: key[K-k .. K-1] / id[..] hold the exact list (count in *cnt) */
-template <int K>
-__device__ __forceinline__ bool knn_fast(float* key, int* id, int k, V2 p, float r2, const V2* s_pos,
-                                         const int* cell_start, const AgentGrid& g, int* cnt)
+/* grid index of a packed key's candidate */
+__device__ __forceinline__ int knn_pk_index(float k, int cx, int cy, int sx, int sy, const int* cell_start,
+                                            const AgentGrid& g)
 {
-#pragma unroll
-    for (int q = 0; q < K; q++) {
-        key[q] = q < K - k ? 0.0f : r2; /* 0: below every candidate (d2 > kEps); r2: empty */
-        id[q] = -1;
+    const unsigned code = __float_as_uint(k) & kCodeMask;
+    const int i = (int)(code >> 5), off = (int)(code & 31u);
+    if (i == kCodeOverflow) return cell_start[g.ncells] + off;
+    const int x = cx + sx * (int)c_knn_tmpl.dx[i], y = cy + sy * (int)c_knn_tmpl.dy[i];
+    return cell_start[y * g.gw + x] + off;
+}
+
+/* where a packed list's codes point: the agent's cell and mirror signs */
+struct PkFrame {
+    int cx, cy, sx, sy;
+};
+
+/* the packed list of KL entries */
+template <int KL>
+struct PkList {
+    float key[KL];
+};
+
+/* near ties in the list (rare; out of line): the valid entries from lo on
+   decoded, re-sorted by the exact (d2, slot) key and the first k written to
+   o[0 .. k) (-1 beyond the count) */
+template <int KL>
+__device__ __noinline__ void knn_pk_write_exact(PkList<KL> L, int lo, int k, PkFrame f, V2 p, const V2* s_pos,
+                                                const int* s_slot, const int* cell_start, AgentGrid g, int* o)
+{
+    unsigned long long ek[KL];
+    int id[KL];
+    int n = 0;
+    for (int q = lo; q < KL; q++) {
+        if (!(L.key[q] < INFINITY)) break;
+        const int j = knn_pk_index(L.key[q], f.cx, f.cy, f.sx, f.sy, cell_start, g);
+        const V2 c = s_pos[j];
+        const float dx = c.x - p.x, dy = c.y - p.y;
+        const float d2 = dx * dx + dy * dy;
+        ek[n] = ((unsigned long long)__float_as_uint(d2) << 32) | (unsigned)s_slot[j];
+        id[n] = j;
+        n++;
     }
+    for (int q = 1; q < n; q++) {
+        for (int r = q; r > 0 && ek[r - 1] > ek[r]; r--) {
+            const unsigned long long t = ek[r];
+            ek[r] = ek[r - 1];
+            ek[r - 1] = t;
+            const int ti = id[r];
+            id[r] = id[r - 1];
+            id[r - 1] = ti;
+        }
+    }
+    for (int q = 0; q < k; q++) o[q] = q < n ? id[q] : -1;
+}
+
+/* 1: the packed list in *L is exact apart from near ties inside it (2: with
+   such ties); 0: the caller must run the 64-bit search.  *cnt = count. */
+template <int K>
+__device__ __forceinline__ int knn_fast(PkList<K + 2>* L, PkFrame* f, int k, V2 p, float r2, const V2* s_pos,
+                                        const int* cell_start, const AgentGrid& g, int* cnt)
+{
+    constexpr int KL = K + 2; /* two entries beyond the k-th */
+    float* key = L->key;
+#pragma unroll
+    for (int q = 0; q < KL; q++) key[q] = q < K - k ? 0.0f : INFINITY; /* 0: below every candidate */
     float rej = INFINITY;
-    for (int j = cell_start[g.ncells]; j < cell_start[g.ncells + 1]; j++) knn_fast_consider<K>(key, id, &rej, j, p, s_pos);
+    const int o0 = cell_start[g.ncells], o1 = cell_start[g.ncells + 1];
+    if (o1 - o0 > 32) return 0;
+    for (int j = o0; j < o1; j++)
+        knn_pk_consider<KL>(key, &rej, j, (unsigned)(kCodeOverflow << 5) | (unsigned)(j - o0), p, r2, s_pos);
     const float fx = (p.x - g.x0) * g.inv, fy = (p.y - g.y0) * g.inv;
-    if (!(fx >= 0.0f && fy >= 0.0f && fx < (float)g.gw && fy < (float)g.gh)) return false;
+    if (!(fx >= 0.0f && fy >= 0.0f && fx < (float)g.gw && fy < (float)g.gh)) return 0;
     const int cx = (int)fx, cy = (int)fy;
     const int sx = fx - (float)cx < 0.5f ? 1 : -1, sy = fy - (float)cy < 0.5f ? 1 : -1;
+    f->cx = cx;
+    f->cy = cy;
+    f->sx = sx;
+    f->sy = sy;
     const float half = 0.5f * g.cell;
+    bool crowded = false;
     int i = 0;
     for (; i < kTmplN; i++) {
+        /* the largest d2 the k-th entry can stand for */
+        const float kd = fminf(r2, __uint_as_float(__float_as_uint(key[K - 1]) | kCodeMask));
         /* every later cell is at least this far from the agent (1 cm for the
            rounding of the bucket assignment) */
         const float bx = fmaxf((float)c_knn_tmpl.hx[i] * half - 0.01f, 0.0f);
         const float by = fmaxf((float)c_knn_tmpl.hy[i] * half - 0.01f, 0.0f);
-        if (bx * bx + by * by > key[K - 1]) break;
+        if (bx * bx + by * by > kd) break;
         const int x = cx + sx * (int)c_knn_tmpl.dx[i], y = cy + sy * (int)c_knn_tmpl.dy[i];
         if (x < 0 || y < 0 || x >= g.gw || y >= g.gh) continue;
         const float rx0 = g.x0 + (float)x * g.cell, ry0 = g.y0 + (float)y * g.cell;
         const float ex = fmaxf(fmaxf(rx0 - p.x, p.x - (rx0 + g.cell)) - 0.01f, 0.0f);
         const float ey = fmaxf(fmaxf(ry0 - p.y, p.y - (ry0 + g.cell)) - 0.01f, 0.0f);
-        if (ex * ex + ey * ey > key[K - 1]) continue;
+        if (ex * ex + ey * ey > kd) continue;
         const int c = y * g.gw + x;
-        const int j1 = cell_start[c + 1];
-        for (int j = cell_start[c]; j < j1; j++) knn_fast_consider<K>(key, id, &rej, j, p, s_pos);
+        const int j0 = cell_start[c], j1 = cell_start[c + 1];
+        crowded |= j1 - j0 > 32;
+        const unsigned base = (unsigned)i << 5;
+        for (int j = j0; j < j1; j++) knn_pk_consider<KL>(key, &rej, j, base | (unsigned)(j - j0), p, r2, s_pos);
     }
-    if (i == kTmplN) return false; /* the neighbourhood reaches beyond the table */
+    if (i == kTmplN || crowded) return 0;
     int n = 0;
     bool tie = false;
 #pragma unroll
-    for (int q = 0; q < K; q++) {
-        if (q >= K - k && key[q] < r2) {
-            n++;
-            if (q + 1 < K && key[q + 1] == key[q]) tie = true;
-        }
+    for (int q = 0; q < KL; q++) {
+        if (q < K - k || !(key[q] < INFINITY)) continue;
+        if (q < K) n++;
+        if (q + 1 < KL && key[q + 1] < INFINITY && key_hi(key[q + 1]) == key_hi(key[q])) tie = true;
     }
-    if (n == k && rej == key[K - 1]) tie = true;
+    /* a dropped candidate may share the k-th entry's leading bits only when
+       the group reaches the list's last entry */
+    if (n == k && key[KL - 1] < INFINITY && key_hi(key[KL - 1]) == key_hi(key[K - 1]) &&
+        key_hi(rej) == key_hi(key[K - 1]))
+        return 0;
     *cnt = n;
-    return !tie;
+    return tie ? 2 : 1;
 }
 
 /* ---------------------------------------------------------------------- */
@@ -736,15 +815,23 @@ template <int K>
 __device__ __forceinline__ void knn_agent(const TickArgs& a, int t, int slot)
 {
     const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
-    float key[K];
-    int id[K], n = 0;
-    if (knn_fast<K>(key, id, a.k, a.s_pos[t], a.rnb2, a.s_pos, a.cell_start + sc.bucket_base, sc.grid, &n)) {
+    const int* cs = a.cell_start + sc.bucket_base;
+    const V2 p = a.s_pos[t];
+    PkList<K + 2> L;
+    PkFrame f;
+    int n = 0;
+    const int st = knn_fast<K>(&L, &f, a.k, p, a.rnb2, a.s_pos, cs, sc.grid, &n);
+    if (st != 0) {
         a.ncnt[t] = n;
         int* o = a.nbr + (size_t)t * a.k;
+        if (st == 1) {
 #pragma unroll
-        for (int q2 = 0; q2 < K; q2++) {
-            const int q = q2 - (K - a.k);
-            if (q >= 0) o[q] = q < n ? id[q2] : -1;
+            for (int q2 = 0; q2 < K; q2++) {
+                const int q = q2 - (K - a.k);
+                if (q >= 0) o[q] = q < n ? knn_pk_index(L.key[q2], f.cx, f.cy, f.sx, f.sy, cs, sc.grid) : -1;
+            }
+        } else {
+            knn_pk_write_exact<K + 2>(L, K - a.k, a.k, f, p, a.s_pos, a.s_slot, cs, sc.grid, o);
         }
         return;
     }
