@@ -197,10 +197,11 @@ def apply_launch(plain, learned, args):
         grab = r["agents_per_warp_grab"]
         for s_ in (plain, learned):
             if r["lp_mode"] == "warp":
-                set_launch(s_, 128, 32, r["grid_cell_scale"])
+                set_launch(s_, 128, 32, r["grid_cell_scale"], 1, r["neighbor_blocks_per_sm"])
                 set_lp_mode(s_, "warp", grab)
             else:
-                set_launch(s_, r["block_size"], grab, r["grid_cell_scale"], r["occupancy_divisor"])
+                set_launch(s_, r["block_size"], grab, r["grid_cell_scale"], r["occupancy_divisor"],
+                           r["neighbor_blocks_per_sm"])
                 set_lp_mode(s_, r["lp_mode"], 1)
         return r
     grab = 4 if args.lp_mode == "warp" else 32
@@ -376,7 +377,8 @@ def run_ours(args):
     no_gate = None
     if model is not None and not args.no_gate:
         # the learned tick with the model forced on every tick (no gate),
-        # K ticks after the timed blocks: what the model itself costs here
+        # K ticks after the timed blocks: what the model itself costs here;
+        # the gate is restored afterwards (the e2e run below uses it)
         learned.set_proposal_gate(0.0, 0)
         for _ in range(2):
             learned.update()
@@ -385,6 +387,7 @@ def run_ours(args):
         for _ in range(args.steps):
             tn.tick()
         torch.cuda.synchronize()
+        learned.set_proposal_gate(0.1, 64)
         n_ms, n_steps = reduce_over_ranks(tn.ms(), tn.steps, world, "cuda")
         K_ = max(args.steps, 1)
         no_gate = {"value": n_steps / (n_ms / 1e3), "ms_per_step": n_ms / K_,

@@ -58,7 +58,7 @@ class AreaInfo(C.Structure):
 class TuneResult(C.Structure):
     _fields_ = [("block_size", C.c_int), ("agents_per_warp_grab", C.c_int), ("grid_cell_scale", C.c_float),
                 ("best_tick_ms", C.c_float), ("trials", C.c_int), ("lp_mode", C.c_int),
-                ("occupancy_divisor", C.c_int)]
+                ("occupancy_divisor", C.c_int), ("neighbor_blocks_per_sm", C.c_int)]
 
 
 class Obstacles(C.Structure):
@@ -164,6 +164,7 @@ def load(build_if_missing: bool = False):
         "ecmg_mlp_train": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_ulonglong, vp, vp]),
         "ecmg_mlp_predict": (C.c_int, [vp, vp, C.c_int, vp]),
         "ecmg_mlp_set_wait_limit": (C.c_int, [vp, C.c_int]),
+        "ecmg_set_neighbor_blocks": (C.c_int, [vp, C.c_int]),
         "ecmg_set_proposal": (C.c_int, [vp, vp]),
         "ecmg_set_trace": (C.c_int, [vp, C.c_int]),
         "ecmg_set_proposal_gate": (C.c_int, [vp, C.c_float, C.c_int]),

@@ -209,6 +209,7 @@ struct ecmg_ctx {
     float cell_scale = 0.4f;
     int lp_mode = 0; /* ECMG_LP_THREAD, ECMG_LP_WARP or ECMG_LP_THREAD_FUSED */
     int occ_div = 1; /* per-thread layout: resident blocks per SM divided by this */
+    int knn_wide = 0; /* neighbour kernel register budget (TickArgs::knn_wide) */
     int wgrab = 4;   /* agents per work grab in warp mode */
 
     /* host mirrors (Simulator bookkeeping, Simulator.h:164-171) */
@@ -1699,6 +1700,7 @@ static void fill_args(ecmg_ctx* c, BinArgs& b, TickArgs& t, bool use_model)
     t.tile = c->lp_mode == ECMG_LP_WARP ? c->wgrab : c->tile;
     t.lp_mode = c->lp_mode;
     t.occ_div = c->occ_div;
+    t.knn_wide = c->knn_wide;
     const ecmg_params& p = c->prm;
     t.dt = p.dt;
     t.tau_a = p.tau_agent;
@@ -2097,9 +2099,9 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
     };
     struct Launch {
         float scale;
-        int mode, block, tile, occ_div, wgrab;
+        int mode, block, tile, occ_div, wgrab, knn_wide;
     };
-    Launch bestL{c->cell_scale, c->lp_mode, c->block, c->tile, c->occ_div, c->wgrab};
+    Launch bestL{c->cell_scale, c->lp_mode, c->block, c->tile, c->occ_div, c->wgrab, c->knn_wide};
     float best = 1e30f;
     int trials = 0;
     c->replan_enabled = false;
@@ -2114,6 +2116,7 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
         c->tile = L.tile;
         c->occ_div = L.occ_div;
         c->wgrab = L.wgrab;
+        c->knn_wide = L.knn_wide;
         c->graph_dirty = true;
         ecmg_tick_stats ts{};
         ecmg_status st = run_ticks(c, 1, &ts); /* warm-up and graph capture */
@@ -2143,17 +2146,19 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
     ecmg_status st = ECMG_OK;
     for (float sc : scales) {
         if (fixed_cell && sc != scales[0]) break;
-        st = trial(Launch{sc, 0, def_block, 32, 1, c->wgrab}, &better);
+        for (int kw = 0; kw < 2 && st == ECMG_OK; kw++)
+            st = trial(Launch{sc, 0, def_block, 32, 1, c->wgrab, kw}, &better);
         if (st != ECMG_OK) break;
     }
     const float cell = bestL.scale;
+    const int kw = bestL.knn_wide;
     for (int b : blocks) {
         if (st != ECMG_OK) break;
         if (c->prm.block_size && b != c->prm.block_size) continue;
         for (int tl : tiles)
             for (int dv : divs) {
                 if (st != ECMG_OK) break;
-                st = trial(Launch{cell, 0, b, tl, dv, c->wgrab}, &better);
+                st = trial(Launch{cell, 0, b, tl, dv, c->wgrab, kw}, &better);
             }
     }
     /* the per-thread layout fused with the neighbour search, at the best
@@ -2161,11 +2166,11 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
     const Launch thr = bestL;
     for (int dv : divs) {
         if (st != ECMG_OK || c->nbr_mode == ECMG_NEIGHBORS_KDTREE) break;
-        st = trial(Launch{cell, ECMG_LP_THREAD_FUSED, thr.block, thr.tile, dv, c->wgrab}, &better);
+        st = trial(Launch{cell, ECMG_LP_THREAD_FUSED, thr.block, thr.tile, dv, c->wgrab, kw}, &better);
     }
     for (int w : wgrabs) {
         if (st != ECMG_OK || c->nbr_mode == ECMG_NEIGHBORS_KDTREE) break; /* one thread per agent there */
-        st = trial(Launch{cell, 1, thr.block, thr.tile, 1, w}, &better);
+        st = trial(Launch{cell, 1, thr.block, thr.tile, 1, w, kw}, &better);
     }
     if (st != ECMG_OK) {
         c->replan_enabled = true;
@@ -2182,6 +2187,7 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
     c->lp_mode = bmode;
     c->wgrab = bw;
     c->cell_scale = bs;
+    c->knn_wide = bestL.knn_wide;
     for (auto& s : c->scenes) s->grid_ready = false;
     c->graph_dirty = true;
     sp.free_(); sv.free_(); sa.free_(); spv.free_(); sact.free_();
@@ -2193,6 +2199,7 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
         out->best_tick_ms = best;
         out->trials = trials;
         out->occupancy_divisor = bestL.occ_div;
+        out->neighbor_blocks_per_sm = bestL.knn_wide ? 6 : 8;
     }
     return ECMG_OK;
 }
@@ -2255,6 +2262,17 @@ ecmg_status ecmg_set_occupancy(ecmg_ctx* c, int divisor)
     if (!c || divisor < 1 || divisor > 8) return ECMG_ERR_INVALID_ARG;
     c->occ_div = divisor;
     c->graph_dirty = true;
+    return ECMG_OK;
+}
+
+ecmg_status ecmg_set_neighbor_blocks(ecmg_ctx* c, int blocks_per_sm)
+{
+    if (!c || (blocks_per_sm != 8 && blocks_per_sm != 6)) return ECMG_ERR_INVALID_ARG;
+    const int w = blocks_per_sm == 6 ? 1 : 0;
+    if (w != c->knn_wide) {
+        c->knn_wide = w;
+        c->graph_dirty = true;
+    }
     return ECMG_OK;
 }
 

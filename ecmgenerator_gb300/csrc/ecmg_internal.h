@@ -102,6 +102,7 @@ struct TickArgs {
     int tile;              /* agents a warp takes per work grab (per-thread mode: multiple of 32) */
     int lp_mode;           /* 0: one thread per agent, 1: one warp per agent */
     int occ_div;           /* per-thread layout: resident blocks per SM divided by this */
+    int knn_wide;          /* neighbour kernel: 0 = 8 blocks of 128 threads per SM (64 registers), 1 = 6 (80) */
     /* parameters */
     float dt, tau_a, tau_o, rnb, rnb2, max_speed, mass_recip, arr_sq, del_sq;
     float inv_tau_a;       /* 1 / tau_a when tau_a is a power of two (exact), else 0 */

@@ -841,8 +841,8 @@ __device__ __forceinline__ void knn_agent(const TickArgs& a, int t, int slot)
 /* persistent: a warp takes 32 consecutive grid-order agents per work grab
    (neighbouring agents: their candidates share L1), so that warps whose
    agents have more candidates do not leave the SMs' last wave ragged */
-template <int K>
-__global__ void __launch_bounds__(128, (K <= 16) ? 8 : 1) k_neighbors(TickArgs a)
+template <int K, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_neighbors(TickArgs a)
 {
     const int n = a.counters[C_NSORTED];
     const int lane = threadIdx.x & 31;
@@ -1415,16 +1415,24 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
         if (e != cudaSuccess) return e;
     } else if (!fused) {
         /* one resident wave of the persistent search */
+        /* two register budgets for k <= 16: 8 resident blocks per SM at
+           64 registers, or 6 at 80 (no spills); the autotuner picks */
         int pn = 1;
-        if (t.k <= 8) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pn, k_neighbors<8>, 128, 0);
-            k_neighbors<8><<<sms * (pn > 0 ? pn : 1), 128, 0, s>>>(t);
+        if (t.k <= 8 && !t.knn_wide) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pn, k_neighbors<8, 8>, 128, 0);
+            k_neighbors<8, 8><<<sms * (pn > 0 ? pn : 1), 128, 0, s>>>(t);
+        } else if (t.k <= 8) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pn, k_neighbors<8, 6>, 128, 0);
+            k_neighbors<8, 6><<<sms * (pn > 0 ? pn : 1), 128, 0, s>>>(t);
+        } else if (t.k <= 16 && !t.knn_wide) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pn, k_neighbors<16, 8>, 128, 0);
+            k_neighbors<16, 8><<<sms * (pn > 0 ? pn : 1), 128, 0, s>>>(t);
         } else if (t.k <= 16) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pn, k_neighbors<16>, 128, 0);
-            k_neighbors<16><<<sms * (pn > 0 ? pn : 1), 128, 0, s>>>(t);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pn, k_neighbors<16, 6>, 128, 0);
+            k_neighbors<16, 6><<<sms * (pn > 0 ? pn : 1), 128, 0, s>>>(t);
         } else {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pn, k_neighbors<32>, 128, 0);
-            k_neighbors<32><<<sms * (pn > 0 ? pn : 1), 128, 0, s>>>(t);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pn, k_neighbors<32, 1>, 128, 0);
+            k_neighbors<32, 1><<<sms * (pn > 0 ? pn : 1), 128, 0, s>>>(t);
         }
     }
     if (ev && !kd && !fused) cudaEventRecordWithFlags(ev[2], s, evflags);

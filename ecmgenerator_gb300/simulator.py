@@ -481,14 +481,16 @@ def autotune(sim: Simulator, ticks_per_trial: int = 2) -> dict:
     sim._ck(sim.L.ecmg_autotune(sim.h, int(ticks_per_trial), C.byref(r)))
     return dict(block_size=r.block_size, agents_per_warp_grab=r.agents_per_warp_grab,
                 grid_cell_scale=r.grid_cell_scale, best_tick_ms=r.best_tick_ms, trials=r.trials,
-                lp_mode={0: "thread", 1: "warp", 2: "fused"}[r.lp_mode], occupancy_divisor=r.occupancy_divisor)
+                lp_mode={0: "thread", 1: "warp", 2: "fused"}[r.lp_mode], occupancy_divisor=r.occupancy_divisor,
+                neighbor_blocks_per_sm=r.neighbor_blocks_per_sm)
 
 
 def set_launch(sim: Simulator, block_size: int, agents_per_warp_grab: int, grid_cell_scale: float,
-               occupancy_divisor: int = 1):
+               occupancy_divisor: int = 1, neighbor_blocks_per_sm: int = 8):
     sim._ck(sim.L.ecmg_set_launch(sim.h, int(block_size), int(agents_per_warp_grab), float(grid_cell_scale)))
     if occupancy_divisor != 1:
         sim._ck(sim.L.ecmg_set_occupancy(sim.h, int(occupancy_divisor)))
+    sim._ck(sim.L.ecmg_set_neighbor_blocks(sim.h, int(neighbor_blocks_per_sm)))
 
 
 def set_lp_mode(sim: Simulator, mode: str = "warp", agents_per_warp_grab: int = 4):

@@ -329,6 +329,7 @@ typedef struct {
     int trials;
     int lp_mode;             /* ECMG_LP_THREAD, ECMG_LP_WARP or ECMG_LP_THREAD_FUSED */
     int occupancy_divisor;   /* per-thread layout: resident blocks per SM divided by this */
+    int neighbor_blocks_per_sm; /* exact-kNN kernel (k <= 16): 8 resident blocks at 64 registers or 6 at 80 */
 } ecmg_tune_result;
 ecmg_status ecmg_set_launch(ecmg_ctx* ctx, int block_size, int agents_per_warp_grab, float grid_cell_scale);
 /* Per-agent kernel layout.  ECMG_LP_THREAD: one thread per agent (work
@@ -344,6 +345,9 @@ ecmg_status ecmg_set_launch(ecmg_ctx* ctx, int block_size, int agents_per_warp_g
    blocks per SM divided by `divisor` (1..8; fewer resident warps leave more
    L1 to each thread's local constraint arrays) */
 ecmg_status ecmg_set_occupancy(ecmg_ctx* ctx, int divisor);
+/* exact-kNN kernel for k <= 16: 8 resident blocks of 128 threads per SM
+   (64 registers) or 6 (80 registers, no spills); the autotuner picks one */
+ecmg_status ecmg_set_neighbor_blocks(ecmg_ctx* ctx, int blocks_per_sm);
 #define ECMG_LP_THREAD 0
 #define ECMG_LP_WARP 1
 #define ECMG_LP_THREAD_FUSED 2
