@@ -15,8 +15,9 @@
  * Inference: BF16 weights and activations on the 5th-generation tensor
  * cores (tcgen05.mma, FP32 accumulators in tensor memory), weights staged
  * once per CTA in shared memory in the MMA operand layout.  Training: FP32
- * master weights, FP32 forward/backward GEMMs on the CUDA cores, softmax
- * cross-entropy, Adam.
+ * master weights; every forward and backward GEMM on the tensor cores with
+ * BF16 operands and FP32 accumulation (k_tc_gemm), the elementwise steps,
+ * softmax cross-entropy and Adam in FP32.
  * This translation unit is not part of the parity-critical arithmetic.
  */
 #include "../../include/ecmg.h"
@@ -430,69 +431,160 @@ __global__ void __launch_bounds__(kInferThreads, 1)
 }
 
 /* ------------------------------------------------------------------------
- * Training (FP32 on the CUDA cores)
+ * Training GEMMs on the tensor cores.  C[M x N] = A[M x K] * B[N x K]^T with
+ * A and B BF16 row-major (K contiguous) in global memory, read by TMA in
+ * stages of 64 K columns (8 boxes of 8 columns x 128 rows for A, 8 boxes of
+ * 8 columns x N rows for B) into the canonical K-major layout, three stages
+ * in flight; one thread issues the tcgen05.mma chain (M = 128, N <= 256,
+ * K-steps of 16) into an FP32 accumulator in tensor memory; each warp reads
+ * its 32 rows back for the epilogue: a plain FP32 store, or an atomic add
+ * when the K range is split over CTAs (weight gradients, where K is the
+ * batch).  Rows or columns beyond the tensors read as zeros.  Bounded waits
+ * as in the inference kernel.
  * ---------------------------------------------------------------------- */
+constexpr int kGemmStages = 3;
+constexpr int kGemmKC = 64;                         /* K columns per stage */
+constexpr int kGemmAB = kTile * kGemmKC * 2;        /* A bytes per stage (16 KB) */
+constexpr int kGemmBB = 256 * kGemmKC * 2;          /* B bytes per stage, N <= 256 (32 KB) */
+constexpr int kGemmStageB = kGemmAB + kGemmBB;
+constexpr size_t kGemmSmem = (size_t)kGemmStages * kGemmStageB + 8 * (2 * kGemmStages + 1) + 16;
 
-/* C[M x N] (+)= op(A)[M x K] * op(B)[K x N]; row-major storage, lda/ldb/ldc
-   are row strides of the stored matrices.  With split > 1 the K range is cut
-   into `split` parts accumulated atomically (C must hold the initial value). */
-template <bool TA, bool TB>
-__global__ void k_gemm(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
-                       int split, int accumulate)
+__device__ __forceinline__ void tma_box(const CUtensorMap* tm, uint32_t sdst, int x, int y, uint32_t mbar)
 {
-    __shared__ float sa[32][33], sb[32][33];
-    int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
-    int tx = threadIdx.x & 31, ty = threadIdx.x >> 5; /* 32 x 8 threads, 4 rows each */
-    int kchunk = (K + split - 1) / split;
-    int k0 = bz * kchunk, k1 = min(K, k0 + kchunk);
-    float acc[4] = {0, 0, 0, 0};
-    for (int kk = k0; kk < k1; kk += 32) {
-        /* sa[m][k], sb[k][n]; consecutive threads read consecutive addresses */
-        for (int r = ty; r < 32; r += 8) {
-            if (TA) {
-                int m = by * 32 + tx, k = kk + r;
-                sa[tx][r] = (m < M && k < k1) ? A[(size_t)k * lda + m] : 0.0f;
-            } else {
-                int m = by * 32 + r, k = kk + tx;
-                sa[r][tx] = (m < M && k < k1) ? A[(size_t)m * lda + k] : 0.0f;
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(sdst), "l"(tm), "r"(x), "r"(y), "r"(mbar)
+        : "memory");
+}
+
+__global__ void __launch_bounds__(128, 1)
+    k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
+              int kper, float* C, int ldc, int atomic, int* err, int spin)
+{
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * kTile;
+    const int k0 = blockIdx.y * kper, k1 = min(K, k0 + kper);
+    const int nch = k1 > k0 ? (k1 - k0 + kGemmKC - 1) / kGemmKC : 0;
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
+    const uint32_t bar0 = sbase + (uint32_t)(kGemmStages * kGemmStageB);
+    auto full = [&](int st) { return bar0 + 8u * (uint32_t)st; };
+    auto empty = [&](int st) { return bar0 + 8u * (uint32_t)(kGemmStages + st); };
+    const uint32_t done = bar0 + 8u * (uint32_t)(2 * kGemmStages);
+    if (tid == 0) {
+        for (int b = 0; b < 2 * kGemmStages + 1; b++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8u * b) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_fail = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(&s_tmem)),
+                     "r"(256)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s_tmem;
+    if (tid == 0 && nch > 0) {
+        uint32_t fph[kGemmStages] = {}, eph[kGemmStages] = {};
+        bool xpend[kGemmStages] = {};
+        const uint32_t bytes = (uint32_t)(kGemmAB + N * kGemmKC * 2);
+        const uint32_t id = tc_idesc(kTile, N);
+        auto load = [&](int c) {
+            const int st = c % kGemmStages;
+            const uint32_t a = sbase + (uint32_t)(st * kGemmStageB), b = a + (uint32_t)kGemmAB;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full(st)), "r"(bytes)
+                         : "memory");
+#pragma unroll 1
+            for (int kc = 0; kc < kGemmKC / 8; kc++) {
+                const int x = k0 + c * kGemmKC + kc * 8;
+                tma_box(&tmA, a + (uint32_t)(kc * kTile * 16), x, m0, full(st));
+                tma_box(&tmB, b + (uint32_t)(kc * N * 16), x, 0, full(st));
             }
-            if (TB) {
-                int nb = bx * 32 + r, kb = kk + tx;
-                sb[tx][r] = (kb < k1 && nb < N) ? B[(size_t)nb * ldb + kb] : 0.0f;
-            } else {
-                int kb = kk + r, nb = bx * 32 + tx;
-                sb[r][tx] = (kb < k1 && nb < N) ? B[(size_t)kb * ldb + nb] : 0.0f;
-            }
-        }
-        __syncthreads();
-#pragma unroll 8
-        for (int q = 0; q < 32; q++) {
-            float b = sb[q][tx];
+            xpend[st] = true;
+        };
+        for (int c = 0; c < nch && c < kGemmStages; c++) load(c);
+        bool fail = false;
+        for (int c = 0; c < nch && !fail; c++) {
+            const int st = c % kGemmStages;
+            if (!mbar_wait(full(st), fph[st], spin)) { fail = true; break; }
+            fph[st] ^= 1u;
+            xpend[st] = false;
+            tc_fence_after();
+            const uint32_t a = sbase + (uint32_t)(st * kGemmStageB), b = a + (uint32_t)kGemmAB;
 #pragma unroll
-            for (int i = 0; i < 4; i++) acc[i] += sa[ty + 8 * i][q] * b;
+            for (int ks = 0; ks < kGemmKC / 16; ks++) {
+                const uint64_t ad = tc_sdesc(a + (uint32_t)(ks * 2 * kTile * 16), kTile * 16, 128);
+                const uint64_t bd = tc_sdesc(b + (uint32_t)(ks * 2 * N * 16), (uint32_t)N * 16, 128);
+                const uint32_t acc = (c > 0 || ks > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(id), "r"(acc));
+            }
+            tc_commit(empty(st));
+            /* refill the previous stage once its MMAs have read it */
+            const int pc = c - 1;
+            if (pc >= 0 && pc + kGemmStages < nch) {
+                const int ps = pc % kGemmStages;
+                if (!mbar_wait(empty(ps), eph[ps], spin)) { fail = true; break; }
+                eph[ps] ^= 1u;
+                load(pc + kGemmStages);
+            }
         }
-        __syncthreads();
-    }
-    for (int i = 0; i < 4; i++) {
-        int m = by * 32 + ty + 8 * i, nn = bx * 32 + tx;
-        if (m < M && nn < N) {
-            float* c = C + (size_t)m * ldc + nn;
-            if (split > 1) atomicAdd(c, acc[i]);
-            else *c = accumulate ? *c + acc[i] : acc[i];
+        /* every MMA issued so far completes on `done` (also after a timeout:
+           nothing may be in flight when the CTA frees its tensor memory) */
+        tc_commit(done);
+        if (fail) {
+            for (int st = 0; st < kGemmStages; st++)
+                if (xpend[st]) (void)mbar_wait(full(st), fph[st]);
+            (void)mbar_wait(done, 0u);
+            s_fail = 1;
         }
     }
+    __syncthreads();
+    bool fail = s_fail != 0;
+    if (!fail && nch > 0) {
+        const bool ok = mbar_wait(done, 0u, spin);
+        fail = __syncthreads_or(!ok) != 0;
+        if (fail && tid == 0) (void)mbar_wait(done, 0u);
+    }
+    tc_fence_after();
+    if (!fail && nch > 0) {
+        const int row = m0 + warp * 32 + lane;
+        const uint32_t lb = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+        for (int c = 0; c < N; c += 32) {
+            float v[32];
+            tmem_ld32(lb + (uint32_t)c, v);
+            if (row < M) {
+                float* out = C + (size_t)row * ldc + c;
+                if (atomic) {
+#pragma unroll
+                    for (int i = 0; i < 32; i++) atomicAdd(out + i, v[i]);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(out + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                }
+            }
+        }
+    }
+    if (fail && tid == 0) atomicOr(err, 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256) : "memory");
 }
 
-template <bool TA, bool TB>
-static void gemm(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc, int split,
-                 int accumulate, cudaStream_t s)
-{
-    dim3 grid((N + 31) / 32, (M + 31) / 32, split);
-    k_gemm<TA, TB><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, split, accumulate);
-}
-
+/* the minibatch: rows of X (BF16) gathered by idx or by a seeded hash */
 __global__ void k_gather(const __nv_bfloat16* X, const unsigned char* y, int n, int B, unsigned long long seed,
-                         const int* idx, float* xb, int* yb)
+                         const int* idx, __nv_bfloat16* xb, int* yb)
 {
     int r = blockIdx.x;
     if (r >= B) return;
@@ -505,8 +597,63 @@ __global__ void k_gather(const __nv_bfloat16* X, const unsigned char* y, int n, 
         z ^= z >> 31;
         src = (int)(z % (unsigned long long)n);
     }
-    for (int c = threadIdx.x; c < IN; c += blockDim.x) xb[(size_t)r * IN + c] = __bfloat162float(X[(size_t)src * IN + c]);
+    for (int c = threadIdx.x; c < IN; c += blockDim.x) xb[(size_t)r * IN + c] = X[(size_t)src * IN + c];
     if (threadIdx.x == 0) yb[r] = y[src];
+}
+
+/* elementwise steps between the GEMMs, in 32 x 32 tiles so that the
+   transposed BF16 copy (the operand of a weight-gradient GEMM, [cols][ldT])
+   is written coalesced as well:
+     kPostGelu  Z += bias (kept for the backward pass), out = gelu(Z)
+     kPostBack  D *= gelu'(Zs) (kept in place for the bias gradient), out = D
+     kPostCopy  out = D (FP32 or BF16 input)
+   out (BF16 row-major) and outT (BF16 transposed) may be null */
+enum { kPostGelu = 0, kPostBack = 1, kPostCopy = 2 };
+template <class TIn>
+__global__ void k_post(TIn* D, const float* Zs, const float* bias, int rows, int cols, int mode, __nv_bfloat16* out,
+                       __nv_bfloat16* outT, int ldT)
+{
+    __shared__ float tile[32][33];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int r = r0 + ty + 8 * i, c = c0 + tx;
+        float v = 0.0f;
+        if (r < rows && c < cols) {
+            const size_t o = (size_t)r * cols + c;
+            v = (float)D[o];
+            if (mode == kPostGelu) {
+                v += bias[c];
+                D[o] = (TIn)v;
+                v = gelu(v);
+            } else if (mode == kPostBack) {
+                v *= gelu_grad(Zs[o]);
+                D[o] = (TIn)v;
+            }
+            if (out) out[o] = __float2bfloat16_rn(v);
+        }
+        tile[ty + 8 * i][tx] = v;
+    }
+    if (!outT) return;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int c = c0 + ty + 8 * i, r = r0 + tx;
+        if (r < rows && c < cols) outT[(size_t)c * ldT + r] = __float2bfloat16_rn(tile[tx][ty + 8 * i]);
+    }
+}
+
+/* BF16 copies of the master weights for the GEMM operands: W^T ([N][K],
+   forward) and W as stored ([K][N] = the backward B operand) */
+__global__ void k_wconv(const float* W, int K, int N, __nv_bfloat16* WT, __nv_bfloat16* Wn)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K * N; i += gridDim.x * blockDim.x) {
+        const int k = i / N, n = i % N;
+        const __nv_bfloat16 v = __float2bfloat16_rn(W[i]);
+        if (WT) WT[(size_t)n * K + k] = v;
+        if (Wn) Wn[i] = v;
+    }
 }
 
 __global__ void k_bias_act(float* Z, float* Aout, const float* b, int rows, int cols, int act)
@@ -562,12 +709,6 @@ __global__ void k_colsum(const float* dZ, int rows, int cols, float* db)
     atomicAdd(&db[c], s);
 }
 
-__global__ void k_gelu_back(float* dA, const float* Z, size_t total)
-{
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
-        dA[i] *= gelu_grad(Z[i]);
-}
-
 __global__ void k_adam(float* w, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps,
                        float c1, float c2)
 {
@@ -598,11 +739,14 @@ struct ecmg_mlp {
     float* bias = nullptr;  /* b1 | b2 | b3 */
     int step = 0;
     bool packed = false;
-    /* training scratch for batch B */
-    int cap = 0;
-    float *xb = nullptr, *z1 = nullptr, *a1 = nullptr, *z2 = nullptr, *a2 = nullptr, *z3 = nullptr, *dz3 = nullptr,
-          *d2 = nullptr, *d1 = nullptr, *loss = nullptr;
-    int *yb = nullptr, *correct = nullptr;
+    /* training scratch for batch B (transposed copies have rows of capT) */
+    int cap = 0, capT = 0;
+    float *z1 = nullptr, *z2 = nullptr, *z3 = nullptr, *dz3 = nullptr, *d2 = nullptr, *d1 = nullptr, *loss = nullptr;
+    __nv_bfloat16 *xb = nullptr, *xT = nullptr, *a1 = nullptr, *a1T = nullptr, *a2 = nullptr, *a2T = nullptr,
+                  *dz3h = nullptr, *dz3T = nullptr, *d2h = nullptr, *d2T = nullptr, *d1T = nullptr;
+    /* BF16 operand copies of the weights: W^T for the forward GEMMs, W for the backward ones */
+    __nv_bfloat16 *w1T = nullptr, *w2T = nullptr, *w3T = nullptr, *w2n = nullptr, *w3n = nullptr;
+    int *yb = nullptr, *correct = nullptr, *gerr = nullptr;
     cudaStream_t s = nullptr;
 };
 
@@ -736,10 +880,14 @@ ecmg_status ecmg_mlp_destroy(ecmg_mlp* mm)
 {
     if (!mm) return ECMG_ERR_INVALID_ARG;
     if (mm->s) cudaStreamSynchronize(mm->s);
-    float* fs[] = {mm->p, mm->g, mm->m, mm->v, mm->bias, mm->xb, mm->z1, mm->a1, mm->z2, mm->a2, mm->z3, mm->dz3,
-                   mm->d2, mm->d1, mm->loss};
+    float* fs[] = {mm->p, mm->g, mm->m, mm->v, mm->bias, mm->z1, mm->z2, mm->z3, mm->dz3, mm->d2, mm->d1, mm->loss};
     for (float* f : fs)
         if (f) cudaFree(f);
+    __nv_bfloat16* hs[] = {mm->xb, mm->xT, mm->a1, mm->a1T, mm->a2, mm->a2T, mm->dz3h, mm->dz3T, mm->d2h, mm->d2T,
+                           mm->d1T, mm->w1T, mm->w2T, mm->w3T, mm->w2n, mm->w3n};
+    for (__nv_bfloat16* h : hs)
+        if (h) cudaFree(h);
+    if (mm->gerr) cudaFree(mm->gerr);
     if (mm->pack) cudaFree(mm->pack);
     if (mm->derr) cudaFree(mm->derr);
     if (mm->yb) cudaFree(mm->yb);
@@ -773,60 +921,124 @@ ecmg_status ecmg_mlp_set_params(ecmg_mlp* mm, const float* host_in)
 static ecmg_status ensure_batch(ecmg_mlp* mm, int B)
 {
     if (B <= mm->cap) return ECMG_OK;
-    float** fs[] = {&mm->xb, &mm->z1, &mm->a1, &mm->z2, &mm->a2, &mm->z3, &mm->dz3, &mm->d2, &mm->d1};
+    float** fs[] = {&mm->z1, &mm->z2, &mm->z3, &mm->dz3, &mm->d2, &mm->d1};
     for (float** f : fs)
         if (*f) { cudaFree(*f); *f = nullptr; }
+    __nv_bfloat16** hs[] = {&mm->xb, &mm->xT, &mm->a1, &mm->a1T, &mm->a2, &mm->a2T, &mm->dz3h, &mm->dz3T, &mm->d2h,
+                            &mm->d2T, &mm->d1T};
+    for (__nv_bfloat16** h : hs)
+        if (*h) { cudaFree(*h); *h = nullptr; }
     if (mm->yb) { cudaFree(mm->yb); mm->yb = nullptr; }
-    size_t b = (size_t)B;
-    bool ok = cudaMalloc(&mm->xb, sizeof(float) * b * IN) == cudaSuccess &&
-              cudaMalloc(&mm->z1, sizeof(float) * b * HID) == cudaSuccess &&
-              cudaMalloc(&mm->a1, sizeof(float) * b * HID) == cudaSuccess &&
-              cudaMalloc(&mm->z2, sizeof(float) * b * HID) == cudaSuccess &&
-              cudaMalloc(&mm->a2, sizeof(float) * b * HID) == cudaSuccess &&
-              cudaMalloc(&mm->z3, sizeof(float) * b * OUT) == cudaSuccess &&
-              cudaMalloc(&mm->dz3, sizeof(float) * b * OUT) == cudaSuccess &&
-              cudaMalloc(&mm->d2, sizeof(float) * b * HID) == cudaSuccess &&
-              cudaMalloc(&mm->d1, sizeof(float) * b * HID) == cudaSuccess &&
-              cudaMalloc(&mm->yb, sizeof(int) * b) == cudaSuccess;
+    const size_t b = (size_t)B, bt = (size_t)((B + 7) & ~7); /* 16-byte rows of the transposed copies */
+    auto fa = [](float** p, size_t n) { return cudaMalloc(p, sizeof(float) * n) == cudaSuccess; };
+    auto ha = [](__nv_bfloat16** p, size_t n) { return cudaMalloc(p, 2 * n) == cudaSuccess; };
+    bool ok = fa(&mm->z1, b * HID) && fa(&mm->z2, b * HID) && fa(&mm->z3, b * OUT) && fa(&mm->dz3, b * OUT) &&
+              fa(&mm->d2, b * HID) && fa(&mm->d1, b * HID) && ha(&mm->xb, b * IN) && ha(&mm->xT, bt * IN) &&
+              ha(&mm->a1, b * HID) && ha(&mm->a1T, bt * HID) && ha(&mm->a2, b * HID) && ha(&mm->a2T, bt * HID) &&
+              ha(&mm->dz3h, b * OUT) && ha(&mm->dz3T, bt * OUT) && ha(&mm->d2h, b * HID) && ha(&mm->d2T, bt * HID) &&
+              ha(&mm->d1T, bt * HID) && cudaMalloc(&mm->yb, sizeof(int) * b) == cudaSuccess;
+    if (ok && !mm->w1T)
+        ok = ha(&mm->w1T, (size_t)IN * HID) && ha(&mm->w2T, (size_t)HID * HID) && ha(&mm->w3T, (size_t)HID * OUT) &&
+             ha(&mm->w2n, (size_t)HID * HID) && ha(&mm->w3n, (size_t)HID * OUT) &&
+             cudaMalloc(&mm->gerr, sizeof(int)) == cudaSuccess && cudaMemset(mm->gerr, 0, sizeof(int)) == cudaSuccess;
+    /* outside any stream capture: the GEMM kernel's shared memory limit */
+    if (ok) ok = cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem) ==
+                 cudaSuccess;
     if (!ok) return ECMG_ERR_CUDA;
     mm->cap = B;
+    mm->capT = (int)bt;
     return ECMG_OK;
 }
 
+/* [rows x cols] BF16 row-major with `ld` elements per row as a 2D tensor;
+   boxes of 8 columns x box_rows rows, reads beyond the tensor give zeros */
+static cudaError_t bf16_map(CUtensorMap* tm, const void* p, int rows, int cols, int ld, int box_rows)
+{
+    EncodeTiledFn enc = tensor_map_encoder();
+    if (!enc) return cudaErrorNotSupported;
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {8, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(p), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+/* C[M x N] (+)= A[M x K] B[N x K]^T on the tensor cores (k_tc_gemm); A has
+   lda, B ldb elements per row; split > 1 cuts K over CTAs, added atomically
+   into C (which must hold the initial value) */
+static cudaError_t tc_gemm(ecmg_mlp* mm, int M, int N, int K, const __nv_bfloat16* A, int lda,
+                           const __nv_bfloat16* B, int ldb, float* C, int ldc, int split)
+{
+    CUtensorMap ta, tb;
+    cudaError_t e = bf16_map(&ta, A, M, K, lda, kTile);
+    if (e == cudaSuccess) e = bf16_map(&tb, B, N, K, ldb, N);
+    if (e != cudaSuccess) return e;
+    int kper = (K + split - 1) / split;
+    kper = (kper + kGemmKC - 1) / kGemmKC * kGemmKC;
+    const dim3 grid((M + kTile - 1) / kTile, (K + kper - 1) / kper);
+    k_tc_gemm<<<grid, 128, kGemmSmem, mm->s>>>(ta, tb, M, N, K, kper, C, ldc, split > 1 ? 1 : 0, mm->gerr, mm->spin);
+    return cudaGetLastError();
+}
+
 /* forward + backward on B rows (gathered by idx, or sampled with seed);
-   leaves gradients in mm->g and the summed loss in mm->loss */
-static void fwd_bwd(ecmg_mlp* mm, const void* X, const unsigned char* y, int n, int B, unsigned long long seed,
-                    const int* idx)
+   leaves gradients in mm->g and the summed loss in mm->loss.  Every GEMM
+   takes BF16 operands on the tensor cores and accumulates in FP32; the
+   elementwise steps and the master weights stay FP32. */
+static cudaError_t fwd_bwd(ecmg_mlp* mm, const void* X, const unsigned char* y, int n, int B, unsigned long long seed,
+                           const int* idx)
 {
     cudaStream_t s = mm->s;
     const float* P = mm->p;
     float* G = mm->g;
+    const int T = mm->capT;
+    const dim3 pb(32, 8);
+    auto pg = [](int rows, int cols) { return dim3((cols + 31) / 32, (rows + 31) / 32); };
     cudaMemsetAsync(mm->loss, 0, sizeof(float), s);
     cudaMemsetAsync(mm->correct, 0, sizeof(int), s);
+    k_wconv<<<64, 256, 0, s>>>(P + OW1, IN, HID, mm->w1T, nullptr);
+    k_wconv<<<64, 256, 0, s>>>(P + OW2, HID, HID, mm->w2T, mm->w2n);
+    k_wconv<<<64, 256, 0, s>>>(P + OW3, HID, OUT, mm->w3T, mm->w3n);
     k_gather<<<B, 96, 0, s>>>((const __nv_bfloat16*)X, y, n, B, seed, idx, mm->xb, mm->yb);
-    gemm<false, false>(B, HID, IN, mm->xb, IN, P + OW1, HID, mm->z1, HID, 1, 0, s);
-    k_bias_act<<<1024, 256, 0, s>>>(mm->z1, mm->a1, P + OB1, B, HID, 1);
-    gemm<false, false>(B, HID, HID, mm->a1, HID, P + OW2, HID, mm->z2, HID, 1, 0, s);
-    k_bias_act<<<1024, 256, 0, s>>>(mm->z2, mm->a2, P + OB2, B, HID, 1);
-    gemm<false, false>(B, OUT, HID, mm->a2, HID, P + OW3, OUT, mm->z3, OUT, 1, 0, s);
+    k_post<__nv_bfloat16><<<pg(B, IN), pb, 0, s>>>(mm->xb, nullptr, nullptr, B, IN, kPostCopy, nullptr, mm->xT, T);
+    cudaError_t e;
+    /* forward */
+    if ((e = tc_gemm(mm, B, HID, IN, mm->xb, IN, mm->w1T, IN, mm->z1, HID, 1)) != cudaSuccess) return e;
+    k_post<float><<<pg(B, HID), pb, 0, s>>>(mm->z1, nullptr, P + OB1, B, HID, kPostGelu, mm->a1, mm->a1T, T);
+    if ((e = tc_gemm(mm, B, HID, HID, mm->a1, HID, mm->w2T, HID, mm->z2, HID, 1)) != cudaSuccess) return e;
+    k_post<float><<<pg(B, HID), pb, 0, s>>>(mm->z2, nullptr, P + OB2, B, HID, kPostGelu, mm->a2, mm->a2T, T);
+    if ((e = tc_gemm(mm, B, OUT, HID, mm->a2, HID, mm->w3T, HID, mm->z3, OUT, 1)) != cudaSuccess) return e;
     k_bias_act<<<1024, 256, 0, s>>>(mm->z3, nullptr, P + OB3, B, OUT, 0);
     k_softmax_ce<<<(B + 3) / 4, dim3(32, 4), 0, s>>>(mm->z3, mm->yb, B, mm->dz3, mm->loss, mm->correct);
-    int split = B >= 4096 ? 32 : 1;
-    int csplit = B >= 4096 ? 256 : 1;
+    k_post<float><<<pg(B, OUT), pb, 0, s>>>(mm->dz3, nullptr, nullptr, B, OUT, kPostCopy, mm->dz3h, mm->dz3T, T);
+    /* backward: weight gradients reduce over the batch, split over CTAs */
+    const int split = std::max(1, std::min(128, B / 512));
+    const int csplit = B >= 4096 ? 256 : 1;
     cudaMemsetAsync(G, 0, sizeof(float) * NPARAM, s);
-    /* layer 3 */
-    gemm<true, false>(HID, OUT, B, mm->a2, HID, mm->dz3, OUT, G + OW3, OUT, split, 0, s);
+    if ((e = tc_gemm(mm, HID, OUT, B, mm->a2T, T, mm->dz3T, T, G + OW3, OUT, split)) != cudaSuccess) return e;
     k_colsum<<<dim3((OUT + 127) / 128, csplit), 128, 0, s>>>(mm->dz3, B, OUT, G + OB3);
-    gemm<false, true>(B, HID, OUT, mm->dz3, OUT, P + OW3, OUT, mm->d2, HID, 1, 0, s);
-    k_gelu_back<<<1024, 256, 0, s>>>(mm->d2, mm->z2, (size_t)B * HID);
-    /* layer 2 */
-    gemm<true, false>(HID, HID, B, mm->a1, HID, mm->d2, HID, G + OW2, HID, split, 0, s);
+    if ((e = tc_gemm(mm, B, HID, OUT, mm->dz3h, OUT, mm->w3n, OUT, mm->d2, HID, 1)) != cudaSuccess) return e;
+    k_post<float><<<pg(B, HID), pb, 0, s>>>(mm->d2, mm->z2, nullptr, B, HID, kPostBack, mm->d2h, mm->d2T, T);
+    if ((e = tc_gemm(mm, HID, HID, B, mm->a1T, T, mm->d2T, T, G + OW2, HID, split)) != cudaSuccess) return e;
     k_colsum<<<dim3((HID + 127) / 128, csplit), 128, 0, s>>>(mm->d2, B, HID, G + OB2);
-    gemm<false, true>(B, HID, HID, mm->d2, HID, P + OW2, HID, mm->d1, HID, 1, 0, s);
-    k_gelu_back<<<1024, 256, 0, s>>>(mm->d1, mm->z1, (size_t)B * HID);
-    /* layer 1 */
-    gemm<true, false>(IN, HID, B, mm->xb, IN, mm->d1, HID, G + OW1, HID, split, 0, s);
+    if ((e = tc_gemm(mm, B, HID, HID, mm->d2h, HID, mm->w2n, HID, mm->d1, HID, 1)) != cudaSuccess) return e;
+    k_post<float><<<pg(B, HID), pb, 0, s>>>(mm->d1, mm->z1, nullptr, B, HID, kPostBack, nullptr, mm->d1T, T);
+    if ((e = tc_gemm(mm, IN, HID, B, mm->xT, T, mm->d1T, T, G + OW1, HID, split)) != cudaSuccess) return e;
     k_colsum<<<dim3((HID + 127) / 128, csplit), 128, 0, s>>>(mm->d1, B, HID, G + OB1);
+    return cudaGetLastError();
+}
+
+/* a tensor-core wait of the training GEMMs timed out (flag cleared) */
+static bool gemm_timed_out(ecmg_mlp* mm)
+{
+    int h = 0;
+    if (cudaMemcpyAsync(&h, mm->gerr, sizeof(int), cudaMemcpyDeviceToHost, mm->s) != cudaSuccess ||
+        cudaStreamSynchronize(mm->s) != cudaSuccess)
+        return true;
+    if (h) cudaMemsetAsync(mm->gerr, 0, sizeof(int), mm->s);
+    return h != 0;
 }
 
 ecmg_status ecmg_mlp_loss_grad(ecmg_mlp* mm, const void* dev_x, const unsigned char* dev_y, int n, float* loss,
@@ -839,10 +1051,11 @@ ecmg_status ecmg_mlp_loss_grad(ecmg_mlp* mm, const void* dev_x, const unsigned c
     int* didx = nullptr;
     if (cudaMalloc(&didx, sizeof(int) * n) != cudaSuccess) return ECMG_ERR_CUDA;
     cudaMemcpy(didx, idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
-    fwd_bwd(mm, dev_x, dev_y, n, n, 0, didx);
-    cudaError_t e = cudaStreamSynchronize(mm->s);
+    cudaError_t e = fwd_bwd(mm, dev_x, dev_y, n, n, 0, didx);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(mm->s);
     cudaFree(didx);
     if (e != cudaSuccess) return ECMG_ERR_CUDA;
+    if (gemm_timed_out(mm)) return ECMG_ERR_BOUND;
     float l = 0;
     cudaMemcpy(&l, mm->loss, sizeof(float), cudaMemcpyDeviceToHost);
     if (loss) *loss = l / (float)n;
@@ -857,7 +1070,9 @@ ecmg_status ecmg_mlp_train(ecmg_mlp* mm, const void* dev_x, const unsigned char*
     if (ensure_batch(mm, batch) != ECMG_OK) return ECMG_ERR_CUDA;
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     for (int it = 0; it < steps; it++) {
-        fwd_bwd(mm, dev_x, dev_y, n, batch, seed + 0x51ED27ull * (unsigned long long)(mm->step + 1), nullptr);
+        if (fwd_bwd(mm, dev_x, dev_y, n, batch, seed + 0x51ED27ull * (unsigned long long)(mm->step + 1), nullptr) !=
+            cudaSuccess)
+            return ECMG_ERR_CUDA;
         mm->step++;
         float c1 = 1.0f - powf(b1, (float)mm->step), c2 = 1.0f - powf(b2, (float)mm->step);
         k_adam<<<(NPARAM + 255) / 256, 256, 0, mm->s>>>(mm->p, mm->g, mm->m, mm->v, NPARAM, lr, b1, b2, eps, c1, c2);
@@ -872,7 +1087,8 @@ ecmg_status ecmg_mlp_train(ecmg_mlp* mm, const void* dev_x, const unsigned char*
         }
     }
     mm->packed = false;
-    return cudaStreamSynchronize(mm->s) == cudaSuccess ? ECMG_OK : ECMG_ERR_CUDA;
+    if (cudaStreamSynchronize(mm->s) != cudaSuccess) return ECMG_ERR_CUDA;
+    return gemm_timed_out(mm) ? ECMG_ERR_BOUND : ECMG_OK;
 }
 
 ecmg_status ecmg_mlp_set_wait_limit(ecmg_mlp* mm, int polls)

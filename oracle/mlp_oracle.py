@@ -1,7 +1,9 @@
 """FP64 numpy restatement of the proposal MLP's loss and gradient.
 
 Test infrastructure only: it checks the library's CUDA forward/backward
-kernels (ecmg_mlp_loss_grad) and never runs on the product path.  The network
+kernels (ecmg_mlp_loss_grad) and never runs on the product path; with
+bf16_operands it rounds the matrix-product operands as the library's
+tensor-core GEMMs do.  The network
 has no reference counterpart; the layer sizes, the tanh form of GELU and the
 parameter layout follow include/ecmg.h:
 
@@ -60,12 +62,25 @@ def forward(flat, x):
     return z1, a1, z2, a2, z3
 
 
-def loss_grad(flat, x, y):
-    """mean cross-entropy and its gradient (flat, float64)"""
+def _bf16(a):
+    """float64 -> float32 -> bf16 (round to nearest even) -> float64"""
+    return bf16_to_f64(f32_to_bf16(np.asarray(a, np.float32)))
+
+
+def loss_grad(flat, x, y, bf16_operands=False):
+    """mean cross-entropy and its gradient (flat, float64).  With
+    bf16_operands every matrix-product operand is rounded to BF16 as the
+    library's tensor-core GEMMs take it (weights, activations between layers,
+    the backward deltas); sums, biases and elementwise steps stay wide."""
     x = np.asarray(x, np.float64)
     y = np.asarray(y, np.int64)
+    r = _bf16 if bf16_operands else (lambda a: a)
     W1, b1, W2, b2, W3, b3 = split(flat)
-    z1, a1, z2, a2, z3 = forward(flat, x)
+    z1 = r(x) @ r(W1) + b1
+    a1 = gelu(z1)
+    z2 = r(a1) @ r(W2) + b2
+    a2 = gelu(z2)
+    z3 = r(a2) @ r(W3) + b3
     B = x.shape[0]
     m = z3.max(axis=1, keepdims=True)
     e = np.exp(z3 - m)
@@ -75,13 +90,13 @@ def loss_grad(flat, x, y):
     dz3 = e / se
     dz3[np.arange(B), y] -= 1.0
     dz3 /= B
-    gW3 = a2.T @ dz3
+    gW3 = r(a2).T @ r(dz3)
     gb3 = dz3.sum(0)
-    d2 = (dz3 @ W3.T) * gelu_grad(z2)
-    gW2 = a1.T @ d2
+    d2 = (r(dz3) @ r(W3).T) * gelu_grad(z2)
+    gW2 = r(a1).T @ r(d2)
     gb2 = d2.sum(0)
-    d1 = (d2 @ W2.T) * gelu_grad(z1)
-    gW1 = x.T @ d1
+    d1 = (r(d2) @ r(W2).T) * gelu_grad(z1)
+    gW1 = r(x).T @ r(d1)
     gb1 = d1.sum(0)
     return loss, np.concatenate([g.ravel() for g in (gW1, gb1, gW2, gb2, gW3, gb3)])
 
