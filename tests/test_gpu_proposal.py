@@ -296,7 +296,7 @@ def test_trained_model_gains_over_untrained_and_constant(lib):
     r_const, d3 = run(lambda s: s.set_proposal_classes(
         torch.full((s.max_agents,), major, dtype=torch.uint8, device="cuda")))
     print(f"acceptance trained {r_trained:.3f} untrained {r_untrained:.3f} constant {r_const:.3f}; classes {hist}")
-    assert max(d1, d2, d3) <= 1e-3
+    assert max(d1, d2, d3) == 0.0  # accepted proposals give the plain LP's bits
     assert r_trained > r_untrained + 0.1
     assert r_trained > r_const + 0.05
     model.close()
