@@ -571,20 +571,9 @@ EG_HD int lp2d(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2
     else if (len(opt) > maxSpeed) *out = normalized(opt) * maxSpeed;
     else *out = opt;
     if (n == 0) return n;
-    /* the loop over i (ORCA.cpp:452) written as "advance to the next
-       constraint that does not contain the current point, then move onto its
-       line": the same operations in the same order per thread, and on the GPU
-       the lanes of a warp reach their own next violated constraint before
-       they update together, instead of taking turns at each index */
-    int i = 0;
-    for (;;) {
-        while (i < n) {
-            const Con c = get(i);
-            if (!(det(right(c.n), c.p - *out) <= 0.0f)) break; /* Constraint::Contains */
-            i++;
-        }
-        if (i >= n) break;
+    for (int i = 0; i < n; i++) {
         Con h = get(i);
+        if (det(right(h.n), h.p - *out) <= 0.0f) continue; /* Constraint::Contains */
         V2 dir = right(h.n);
         float dirPointDot = dot(dir, h.p);
         float disc = dirPointDot * dirPointDot + maxSpeed * maxSpeed - dot(h.p, h.p);
@@ -627,7 +616,6 @@ EG_HD int lp2d(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2
                 if (TRACE) { tr->h = i; tr->src = 0; tr->j = -1; }
             }
         }
-        i++;
     }
     return n;
 }
@@ -649,18 +637,10 @@ template <class Get>
 EG_HD void lp3d(const Get& get, int n, int nObst, float maxSpeed, int failed, V2* out, Con* proj, bool fp64)
 {
     float maxPen = 0.0f;
-    /* as in lp2d: advance to the next constraint whose penetration exceeds
-       the running maximum, then re-solve (same order per thread) */
-    int i = failed;
-    for (;;) {
-        while (i < n) {
-            const Con c = get(i);
-            if (!(det(right(c.n), c.p - *out) <= maxPen)) break;
-            i++;
-        }
-        if (i >= n) break;
+    for (int i = failed; i < n; i++) {
         Con ci = get(i);
         V2 dir = right(ci.n);
+        if (det(dir, ci.p - *out) <= maxPen) continue;
         int m = 0;
         for (int j = nObst; j < i; j++) {
             Con cj = get(j);
@@ -689,7 +669,6 @@ EG_HD void lp3d(const Get& get, int n, int nObst, float maxSpeed, int failed, V2
         Lp3dProj<Get> pg{&get, proj, nObst};
         if (lp2d(pg, nObst + m, ci.n, maxSpeed, true, out) < nObst + m) *out = temp;
         maxPen = det(dir, ci.p - *out);
-        i++;
     }
 }
 
