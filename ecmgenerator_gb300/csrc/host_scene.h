@@ -59,6 +59,7 @@ struct RefPlanScratch {
     std::vector<int> parent;
     std::vector<unsigned char> visited;
     std::vector<int> heap;
+    std::vector<int> touched; /* nodes whose g was set by the current search */
 };
 
 struct PlanScratch {

@@ -127,16 +127,25 @@ bool ref_astar(const HostScene& s, RefPlanScratch& r, V2 startLoc, V2 goalLoc, i
         r.f.assign(V, kMaxF);
         r.parent.assign(V, INVALID);
         r.visited.assign(V, 0);
+        r.touched.clear();
     }
-    auto clean = [&]() { /* CleanRequestData (AStar.cpp:162-175) */
-        std::fill(r.g.begin(), r.g.end(), kMaxF);
-        std::fill(r.f.begin(), r.f.end(), kMaxF);
-        std::fill(r.parent.begin(), r.parent.end(), INVALID);
-        std::fill(r.visited.begin(), r.visited.end(), 0);
+    /* CleanRequestData (AStar.cpp:162-175) resets every node; resetting the
+       nodes this search wrote (g, f or parent set, or visited) leaves the
+       same state */
+    auto clean = [&]() {
+        for (int v : r.touched) {
+            r.g[v] = kMaxF;
+            r.f[v] = kMaxF;
+            r.parent[v] = INVALID;
+            r.visited[v] = 0;
+        }
+        r.touched.clear();
     };
     OpenList open{r.heap, r.f};
     r.heap.clear();
     const int sa = s.he_target[2 * startEdge], sb = s.he_target[2 * startEdge + 1];
+    r.touched.push_back(sa);
+    r.touched.push_back(sb);
     r.g[sa] = r_dist(startLoc, s.v_pos[sa]);
     r.f[sa] = r.g[sa] + r_dist(s.v_pos[sa], goalLoc);
     r.g[sb] = r_dist(startLoc, s.v_pos[sb]);
@@ -182,6 +191,7 @@ bool ref_astar(const HostScene& s, RefPlanScratch& r, V2 startLoc, V2 goalLoc, i
                 const V2 cp = s.v_pos[cur], np = s.v_pos[nb];
                 const float ng = r.g[cur] + r_dist(cp, np);
                 if (ng < r.g[nb]) {
+                    if (r.g[nb] == kMaxF) r.touched.push_back(nb);
                     r.parent[nb] = cur;
                     r.f[nb] = ng + r_dist(np, goalLoc);
                     r.g[nb] = ng;
