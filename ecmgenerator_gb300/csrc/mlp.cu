@@ -61,26 +61,26 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 
 /* ------------------------------------------------------------------------
  * Inference on the 5th-generation tensor cores (tcgen05).  One CTA of eight
- * warps per SM, persistent over tiles of 128 agents, with two tiles in
- * flight (slots 0 and 1): while the warps run the epilogue of one slot's
- * layer, the tensor core runs the other slot's next MMA chain.  Per tile
- * three chains (M = 128, N = 128 / 128 / 160, K = 96 / 128 / 128 in steps
- * of 16), each issued by one thread and completed through the slot's
- * mbarrier, with the slot's accumulator in its own 256 tensor-memory
- * columns (128 lanes x N fp32).  Epilogue: warp w reads lanes
- * 32 (w mod 4) .. +31 (rows) and half w / 4 of the columns with
- * tcgen05.ld -- bias + GELU (tanh.approx) + BF16 into the slot's hidden
- * tile, or bias + argmax for the output (the two column halves combined in
- * shared memory, first maximum wins).  Operands sit in shared memory in the
- * canonical K-major layout without swizzle: 8-row x 16-byte core matrices;
- * the row groups of one 8-column chunk are adjacent (stride byte offset
- * 128), chunks R x 16 bytes apart (leading byte offset) for an operand of R
- * rows.  One chunk of a 128-row feature tile is one 2 KB TMA box (8 columns
- * x 128 rows): a slot's next tile is requested as soon as its first layer
- * has consumed the current one, four epilogues ahead of its use.  Every
- * wait is bounded (spin limit); on a timeout the CTA sets the error bit,
- * waits for its copies and MMAs in flight, frees its tensor memory and
- * returns.
+ * warps per SM, persistent over tiles of 128 agents, as two independent
+ * pipelines: warps 0-3 run the tiles of slot 0, warps 4-7 those of slot 1,
+ * each with its own feature and hidden tiles in shared memory, its own 256
+ * tensor-memory columns and its own named barrier, so that one group's
+ * epilogue runs while the other group's MMA chain occupies the tensor core.
+ * Per tile three chains (M = 128, N = 128 / 128 / 160, K = 96 / 128 / 128
+ * in steps of 16), each issued by the group's first thread and completed
+ * through the group's mbarrier (FP32 accumulators, 128 lanes x N columns).
+ * Epilogue: warp w reads lanes 32 (w mod 4) .. +31 (its rows) with
+ * tcgen05.ld -- bias + GELU (tanh.approx) + BF16 into the group's hidden
+ * tile, or bias + argmax over the 160 outputs (first maximum wins).
+ * Operands sit in shared memory in the canonical K-major layout without
+ * swizzle: 8-row x 16-byte core matrices; the row groups of one 8-column
+ * chunk are adjacent (stride byte offset 128), chunks R x 16 bytes apart
+ * (leading byte offset) for an operand of R rows.  One chunk of a 128-row
+ * feature tile is one 2 KB TMA box (8 columns x 128 rows): a group's next
+ * tile is requested as soon as its first layer has consumed the current
+ * one.  Every wait is bounded (spin limit); on a timeout the group sets the
+ * error bit, waits for its copy and MMA chain in flight, and the CTA frees
+ * its tensor memory and returns.
  * ---------------------------------------------------------------------- */
 constexpr int kTile = 128;      /* agents per tile (MMA M) */
 constexpr int kSlotCols = 256;  /* tensor-memory columns per slot: >= the widest accumulator (160) */
@@ -97,9 +97,8 @@ __host__ __device__ constexpr int tc_off(int r, int k, int R)
 constexpr int kW1B = HID * IN * 2, kW2B = HID * HID * 2, kW3B = OUT * HID * 2; /* B operands: N rows x K */
 constexpr int kWB = kW1B + kW2B + kW3B;
 constexpr int kXB = kTile * IN * 2, kHB = kTile * HID * 2;
-/* weights, two feature tiles, two hidden tiles, biases, argmax exchange, barriers */
-constexpr size_t kInferSmem = (size_t)kWB + 2 * kXB + 2 * kHB + sizeof(float) * (2 * HID + OUT) +
-                              2 * kTile * (sizeof(float) + sizeof(int)) + 64;
+/* weights, two feature tiles, two hidden tiles, biases, barriers */
+constexpr size_t kInferSmem = (size_t)kWB + 2 * kXB + 2 * kHB + sizeof(float) * (2 * HID + OUT) + 64;
 
 /* shared-memory matrix descriptor (no swizzle) */
 __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
@@ -240,6 +239,20 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+/* barrier of one 4-warp group (ids 1 and 2; 0 is the CTA barrier) */
+__device__ __forceinline__ void group_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+/* barrier of one group that also ORs a flag over its threads */
+__device__ __forceinline__ bool group_any(bool v, int id)
+{
+    unsigned r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.u32 p, %1, 0;\nbar.red.or.pred q, %2, 128, p;\nselp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((unsigned)v), "r"(id)
+        : "memory");
+    return r != 0;
+}
+
 /* class of every row of X [n, IN] (bf16, row-major); err |= errbit when a
    wait runs past `spin` polls (the CTA then drains and stops) */
 __global__ void __launch_bounds__(kInferThreads, 1)
@@ -253,13 +266,12 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     unsigned char* sX = sW3 + kW3B;  /* [2][kXB] */
     unsigned char* sH = sX + 2 * kXB; /* [2][kHB] */
     float* sb = reinterpret_cast<float*>(sH + 2 * kHB);
-    float* s_best = sb + 2 * HID + OUT; /* [kTile]: the second column half's maximum per row */
-    int* s_bidx = reinterpret_cast<int*>(s_best + kTile);
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_bidx + kTile);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sb + 2 * HID + OUT);
     uint64_t* s_mbar = reinterpret_cast<uint64_t*>(
         (reinterpret_cast<uintptr_t>(s_tmem + 2) + 7) & ~(uintptr_t)7); /* [0..1] MMA done, [2..3] tile landed */
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int quad = warp & 3, half = warp >> 2;
+    const int g = warp >> 2, quad = warp & 3, gt = tid & 127; /* group = slot, TMEM lane quarter, thread in group */
+    const int bar_id = 1 + g;
     const int n = n_ptr ? *n_ptr : n_fixed;
 
     for (int i = tid; i < kWB / 16; i += blockDim.x)
@@ -282,68 +294,50 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *s_tmem;
-    const uint32_t aX0 = (uint32_t)__cvta_generic_to_shared(sX), aH0 = (uint32_t)__cvta_generic_to_shared(sH);
+    /* from here on the two groups run independent pipelines */
+    const uint32_t tmem = *s_tmem + (uint32_t)(g * kSlotCols);
+    const uint32_t lane_base = tmem + ((uint32_t)(quad * 32) << 16);
+    const uint32_t aX = (uint32_t)__cvta_generic_to_shared(sX + g * kXB);
+    const uint32_t aH = (uint32_t)__cvta_generic_to_shared(sH + g * kHB);
+    unsigned char* hbuf = sH + g * kHB;
     const uint32_t aW1 = (uint32_t)__cvta_generic_to_shared(sW1), aW2 = (uint32_t)__cvta_generic_to_shared(sW2),
                    aW3 = (uint32_t)__cvta_generic_to_shared(sW3);
+    const uint32_t mb_mma = mbar0 + 8u * (uint32_t)g, mb_x = mbar0 + 8u * (uint32_t)(2 + g);
     const int row = quad * 32 + lane;
     const int ntiles = (n + kTile - 1) / kTile;
-    /* slot s runs the tiles blockIdx.x + (2 j + s) gridDim.x, j = 0, 1, ... */
-    int tile[2] = {(int)blockIdx.x, (int)blockIdx.x + (int)gridDim.x};
-    uint32_t ph_mma[2] = {0u, 0u}, ph_x[2] = {0u, 0u};
-    bool mma_pending[2] = {false, false}, x_pending[2] = {false, false};
-    bool fail = false;
+    int tile = (int)blockIdx.x + g * (int)gridDim.x; /* slot g: tiles blockIdx.x + (2 j + g) gridDim.x */
+    uint32_t ph_mma = 0u, ph_x = 0u;
+    bool mma_pending = false, x_pending = false, fail = false;
 
-    auto mbar_mma = [&](int s_) { return mbar0 + 8u * (uint32_t)s_; };
-    auto mbar_x = [&](int s_) { return mbar0 + 8u * (uint32_t)(2 + s_); };
-    auto issue_x = [&](int s_) { /* thread 0 */
-        tma_tile(&tmX, aX0 + (uint32_t)(s_ * kXB), tile[s_] * kTile, mbar_x(s_));
-    };
-    /* all threads: wait for slot s's MMA chain; false on timeout */
-    auto wait_mma = [&](int s_) {
-        const bool ok = mbar_wait(mbar_mma(s_), ph_mma[s_], spin);
-        fail = __syncthreads_or(!ok) != 0;
+    auto wait = [&](uint32_t mb, uint32_t& ph, bool& pending) {
+        const bool ok = mbar_wait(mb, ph, spin);
+        fail = group_any(!ok, bar_id);
         if (!fail) {
-            ph_mma[s_] ^= 1u;
-            mma_pending[s_] = false;
+            ph ^= 1u;
+            pending = false;
         }
         tc_fence_after();
         return !fail;
     };
-    /* one layer's MMA chain for slot s, after the operands written by the
-       threads are visible to the tensor core */
-    auto issue_mma = [&](int s_, int layer) {
+    /* the operands the group's threads wrote are visible to the tensor core,
+       then the leader issues one layer's chain */
+    auto mma = [&](uint32_t a, uint32_t w, int K, int N) {
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
+        group_sync(bar_id);
         tc_fence_after();
-        if (tid == 0) {
-            const uint32_t a = layer == 0 ? aX0 + (uint32_t)(s_ * kXB) : aH0 + (uint32_t)(s_ * kHB);
-            tc_layer(tmem + (uint32_t)(s_ * kSlotCols), a, layer == 0 ? aW1 : (layer == 1 ? aW2 : aW3),
-                     layer == 0 ? IN : HID, layer == 2 ? OUT : HID);
-            tc_commit(mbar_mma(s_));
+        if (gt == 0) {
+            tc_layer(tmem, a, w, K, N);
+            tc_commit(mb_mma);
         }
-        mma_pending[s_] = true;
+        mma_pending = true;
     };
-    /* first layer of slot s's current tile: its features, then the chain */
-    auto start_tile = [&](int s_) {
-        const bool ok = mbar_wait(mbar_x(s_), ph_x[s_], spin);
-        fail = __syncthreads_or(!ok) != 0;
-        if (fail) return false;
-        ph_x[s_] ^= 1u;
-        x_pending[s_] = false;
-        issue_mma(s_, 0);
-        return true;
-    };
-    /* bias + GELU + BF16 of slot s's accumulator into its hidden tile */
-    auto epi_hidden = [&](int s_, int layer) {
-        const float* bl = sb + (layer == 0 ? 0 : HID);
-        unsigned char* h = sH + s_ * kHB;
-        const uint32_t lb = tmem + (uint32_t)(s_ * kSlotCols) + ((uint32_t)(quad * 32) << 16);
+    /* bias + GELU + BF16 of the accumulator into the group's hidden tile */
+    auto epi_hidden = [&](const float* bl) {
 #pragma unroll 1
-        for (int c = half * (HID / 2); c < (half + 1) * (HID / 2); c += 32) {
+        for (int c = 0; c < HID; c += 32) {
             float v[32];
-            tmem_ld32(lb + (uint32_t)c, v);
+            tmem_ld32(lane_base + (uint32_t)c, v);
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 uint4 u;
@@ -351,83 +345,63 @@ __global__ void __launch_bounds__(kInferThreads, 1)
                 u.y = pack_bf16(gelu_fast(v[8 * q + 2] + bl[c + 8 * q + 2]), gelu_fast(v[8 * q + 3] + bl[c + 8 * q + 3]));
                 u.z = pack_bf16(gelu_fast(v[8 * q + 4] + bl[c + 8 * q + 4]), gelu_fast(v[8 * q + 5] + bl[c + 8 * q + 5]));
                 u.w = pack_bf16(gelu_fast(v[8 * q + 6] + bl[c + 8 * q + 6]), gelu_fast(v[8 * q + 7] + bl[c + 8 * q + 7]));
-                *reinterpret_cast<uint4*>(h + tc_off(row, c + 8 * q, kTile)) = u;
+                *reinterpret_cast<uint4*>(hbuf + tc_off(row, c + 8 * q, kTile)) = u;
             }
         }
     };
-    /* bias + argmax of slot s's output accumulator; the first maximum wins */
-    auto epi_out = [&](int s_) {
+
+    if (tile < ntiles) {
+        if (gt == 0) tma_tile(&tmX, aX, tile * kTile, mb_x);
+        x_pending = true;
+    }
+    while (!fail && tile < ntiles) {
+        if (!wait(mb_x, ph_x, x_pending)) break;
+        mma(aX, aW1, IN, HID);
+        if (!wait(mb_mma, ph_mma, mma_pending)) break;
+        /* the features are consumed: request the group's next tile */
+        const int nxt = tile + 2 * (int)gridDim.x;
+        if (nxt < ntiles) {
+            if (gt == 0) tma_tile(&tmX, aX, nxt * kTile, mb_x);
+            x_pending = true;
+        }
+        epi_hidden(sb);
+        mma(aH, aW2, HID, HID);
+        if (!wait(mb_mma, ph_mma, mma_pending)) break;
+        epi_hidden(sb + HID);
+        mma(aH, aW3, HID, OUT);
+        if (!wait(mb_mma, ph_mma, mma_pending)) break;
+        /* bias + argmax over the 160 outputs; the first maximum wins */
         const float* bl = sb + 2 * HID;
-        const uint32_t lb = tmem + (uint32_t)(s_ * kSlotCols) + ((uint32_t)(quad * 32) << 16);
         float best = -INFINITY;
-        int bi = half * (OUT / 2);
+        int bi = 0;
 #pragma unroll 1
-        for (int c = half * (OUT / 2); c < (half + 1) * (OUT / 2); c += 16) {
-            float v[16];
-            tmem_ld16(lb + (uint32_t)c, v);
+        for (int c = 0; c < OUT; c += 32) {
+            float v[32];
+            tmem_ld32(lane_base + (uint32_t)c, v);
 #pragma unroll
-            for (int i = 0; i < 16; i++) {
+            for (int i = 0; i < 32; i++) {
                 const float z = v[i] + bl[c + i];
                 if (z > best) { best = z; bi = c + i; }
             }
         }
-        if (half == 1) {
-            s_best[row] = best;
-            s_bidx[row] = bi;
-        }
+        const int r = tile * kTile + row;
+        if (r < n) cls[r] = (unsigned char)bi;
+        /* the accumulator is read out before the next tile's chain */
         tc_fence_before();
-        __syncthreads();
+        group_sync(bar_id);
         tc_fence_after();
-        if (half == 0) {
-            if (s_best[row] > best) bi = s_bidx[row];
-            const int r = tile[s_] * kTile + row;
-            if (r < n) cls[r] = (unsigned char)bi;
-        }
-    };
-
-    for (int s_ = 0; s_ < 2; s_++)
-        if (tile[s_] < ntiles) {
-            if (tid == 0) issue_x(s_);
-            x_pending[s_] = true;
-        }
-    for (int s_ = 0; s_ < 2 && !fail; s_++)
-        if (tile[s_] < ntiles) start_tile(s_);
-    while (!fail && (tile[0] < ntiles || tile[1] < ntiles)) {
-        /* layer 1 epilogues; a slot's features are consumed: request its next tile */
-        for (int s_ = 0; s_ < 2 && !fail; s_++) {
-            if (tile[s_] >= ntiles || !wait_mma(s_)) continue;
-            epi_hidden(s_, 0);
-            const int nxt = tile[s_] + 2 * (int)gridDim.x;
-            if (nxt < ntiles) {
-                if (tid == 0) tma_tile(&tmX, aX0 + (uint32_t)(s_ * kXB), nxt * kTile, mbar_x(s_));
-                x_pending[s_] = true;
-            }
-            issue_mma(s_, 1);
-        }
-        for (int s_ = 0; s_ < 2 && !fail; s_++) {
-            if (tile[s_] >= ntiles || !wait_mma(s_)) continue;
-            epi_hidden(s_, 1);
-            issue_mma(s_, 2);
-        }
-        for (int s_ = 0; s_ < 2 && !fail; s_++) {
-            if (tile[s_] >= ntiles || !wait_mma(s_)) continue;
-            epi_out(s_);
-            tile[s_] += 2 * (int)gridDim.x;
-            if (tile[s_] < ntiles) start_tile(s_);
-        }
+        tile = nxt;
     }
-    if (fail && tid == 0) atomicOr(err, errbit);
-    /* nothing in flight may outlive the CTA: its copies and MMAs are waited
-       for (with the default bound) before the tensor memory is freed */
-    for (int s_ = 0; s_ < 2; s_++) {
-        if (x_pending[s_]) (void)mbar_wait(mbar_x(s_), ph_x[s_]);
-        if (mma_pending[s_]) (void)mbar_wait(mbar_mma(s_), ph_mma[s_]);
-    }
+    if (fail && gt == 0) atomicOr(err, errbit);
+    /* nothing in flight may outlive the CTA: the group's copy and MMA chain
+       are waited for (with the default bound) before tensor memory is freed */
+    if (x_pending) (void)mbar_wait(mb_x, ph_x);
+    if (mma_pending) (void)mbar_wait(mb_mma, ph_mma);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*s_tmem), "r"(kTmemCols) : "memory");
 }
 
 /* ------------------------------------------------------------------------
