@@ -498,6 +498,8 @@ def run_ours(args):
         "e2e": e2e_main,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": kname, "kernel_ms": kern_ms, "alg_bytes_per_agent": alg_bytes,
+                     "compute_frac": (limiter or {}).get("compute_frac"),
+                     "compute_pipe": (limiter or {}).get("compute_pipe"),
                      "limiter": limiter,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
                      "kernel_ms_per_tick": kernel_ms},
