@@ -426,7 +426,6 @@ ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
 #define CKC(x) do { if ((x) != cudaSuccess) { ecmg_destroy(c); return ECMG_ERR_CUDA; } } while (0)
-    CKC(kernels_init());
     CKC(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CKC(cudaEventCreate(&c->ev_t0));
     CKC(cudaEventCreate(&c->ev_t1));

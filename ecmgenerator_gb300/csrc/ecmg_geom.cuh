@@ -620,30 +620,21 @@ EG_HD int lp2d(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2
     return n;
 }
 
-/* where RandomizedLP3D keeps its bisectors: a plain array, or every
-   stride-th entry of one (a thread's column of a block-wide shared array) */
-struct ProjStore {
-    Con* p;
-    int stride;
-    EG_HD Con get(int i) const { return p[i * stride]; }
-    EG_HD void set(int i, const Con& c) { p[i * stride] = c; }
-};
-
 /* the projected lines of RandomizedLP3D: the obstacle constraints (read in
    place), then the bisectors in proj */
 template <class Get>
 struct Lp3dProj {
     const Get* get;
-    ProjStore proj;
+    const Con* proj;
     int nObst;
-    EG_HD Con operator()(int q) const { return q < nObst ? (*get)(q) : proj.get(q - nObst); }
+    EG_HD Con operator()(int q) const { return q < nObst ? (*get)(q) : proj[q - nObst]; }
 };
 
 /* ORCA::RandomizedLP3D (ORCA.cpp:592-669).  proj must hold n - nObst
    constraints.  With fp64 the bisector lines are intersected in double
    precision (the reference computes them in float). */
 template <class Get>
-EG_HD void lp3d(const Get& get, int n, int nObst, float maxSpeed, int failed, V2* out, ProjStore proj, bool fp64)
+EG_HD void lp3d(const Get& get, int n, int nObst, float maxSpeed, int failed, V2* out, Con* proj, bool fp64)
 {
     float maxPen = 0.0f;
     for (int i = failed; i < n; i++) {
@@ -672,7 +663,7 @@ EG_HD void lp3d(const Get& get, int n, int nObst, float maxSpeed, int failed, V2
             Con nc;
             nc.p = np_;
             nc.n = normalized(cj.n - ci.n);
-            proj.set(m++, nc);
+            proj[m++] = nc;
         }
         V2 temp = *out;
         Lp3dProj<Get> pg{&get, proj, nObst};

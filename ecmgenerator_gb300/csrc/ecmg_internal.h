@@ -172,8 +172,6 @@ cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k,
                        int* key, int* rank, int* cell_count, int* cell_start, int* s_slot, V2* s_pos,
                        int* scan_tmp, int scan_blocks, int* out_ids, int* out_cnt, cudaStream_t s);
 int scan_tmp_ints(int n);
-/* kernels.cu: one-time kernel attributes (call outside any stream capture) */
-cudaError_t kernels_init();
 
 /* spawn.cu: Simulator::ValidSpawnLocation (Simulator.cpp:295-311) for a batch
    of candidate locations.  Candidates of one spawn area share a clearance;

@@ -616,20 +616,13 @@ __device__ __noinline__ Con agent_constraint_ni(V2 position, V2 velocity, float 
     return agent_constraint(position, velocity, clr, np, nv, nclr, tau, dt, inv_tau);
 }
 
-/* RandomizedLP3D of one thread; its bisectors (at most the neighbour
-   constraints) in the thread's column of the block's shared array when the
-   kernel has one (sproj, stride = block size), else in local memory */
 template <int MC>
 __device__ __noinline__ void lp3d_local(const Con* cons, int m, int nObst, float maxSpeed, int failed, V2* v,
-                                        bool fp64, Con* sproj, int stride)
+                                        bool fp64)
 {
+    Con proj[MC - kMaxObstCons]; /* bisectors: at most the neighbour constraints */
     LocalGet get{cons};
-    if (sproj) {
-        lp3d(get, m, nObst, maxSpeed, failed, v, ProjStore{sproj, stride}, fp64);
-    } else {
-        Con proj[MC - kMaxObstCons];
-        lp3d(get, m, nObst, maxSpeed, failed, v, ProjStore{proj, 1}, fp64);
-    }
+    lp3d(get, m, nObst, maxSpeed, failed, v, proj, fp64);
 }
 
 /* attraction point and preferred velocity of grid-order agent t */
@@ -690,7 +683,7 @@ __device__ void attract_tick(const TickArgs& a, int t)
 /* ApplyObstacleAvoidanceForce + UpdateVelocitySystem + UpdatePositionSystem
    of grid-order agent t (agents destroyed this tick are skipped) */
 template <int K>
-__device__ void orca_tick(const TickArgs& a, int t, Con* sproj = nullptr)
+__device__ void orca_tick(const TickArgs& a, int t)
 {
     const int slot = a.s_slot[t];
     if (!a.active[slot]) return;
@@ -771,7 +764,7 @@ __device__ void orca_tick(const TickArgs& a, int t, Con* sproj = nullptr)
             failed = lp2d(get, m, pv, maxSpeed, false, &v);
         }
         if (failed < m) {
-            lp3d_local<MC>(cons, m, nObst, maxSpeed, failed, &v, a.lp3d_fp64 != 0, sproj, (int)blockDim.x);
+            lp3d_local<MC>(cons, m, nObst, maxSpeed, failed, &v, a.lp3d_fp64 != 0);
             need3d = true;
         }
     }
@@ -926,24 +919,11 @@ __global__ void __launch_bounds__(128) k_features(TickArgs a)
 
 /* persistent kernel: a warp takes `tile` consecutive grid-order agents per
    work grab (one atomic per grab) and runs them 32 at a time */
-/* dynamic shared memory of the per-thread agent kernels: for k <= 16 the
-   3D LP's bisectors, one column of K entries per thread (entry j of thread
-   t at j * blockDim + t, so a warp's lanes read consecutive entries) */
-extern __shared__ __align__(16) unsigned char g_agent_smem[];
-template <int K>
-__device__ __forceinline__ Con* agent_proj_column()
-{
-    return K <= 16 ? reinterpret_cast<Con*>(g_agent_smem) + threadIdx.x : nullptr;
-}
-template <int K>
-constexpr size_t agent_smem_bytes(int block) { return K <= 16 ? (size_t)block * K * sizeof(Con) : 0; }
-
 template <int K>
 __global__ void __launch_bounds__(256, (K <= 16) ? 4 : 1) k_agents(TickArgs a)
 {
     const int n = a.counters[C_NSORTED];
     const int lane = threadIdx.x & 31;
-    Con* sproj = agent_proj_column<K>();
     while (true) {
         int base = 0;
         if (lane == 0) base = atomicAdd(&a.counters[C_WORK], a.tile);
@@ -951,7 +931,7 @@ __global__ void __launch_bounds__(256, (K <= 16) ? 4 : 1) k_agents(TickArgs a)
         if (base >= n) break;
         for (int o = 0; o < a.tile; o += 32) {
             int t = base + o + lane;
-            if (t < n) orca_tick<K>(a, t, sproj);
+            if (t < n) orca_tick<K>(a, t);
         }
     }
 }
@@ -966,7 +946,6 @@ __global__ void __launch_bounds__(256) k_agents_knn(TickArgs a)
 {
     const int n = a.counters[C_NSORTED];
     const int lane = threadIdx.x & 31;
-    Con* sproj = agent_proj_column<K>();
     while (true) {
         int base = 0;
         if (lane == 0) base = atomicAdd(&a.counters[C_WORK], a.tile);
@@ -978,7 +957,7 @@ __global__ void __launch_bounds__(256) k_agents_knn(TickArgs a)
             const int slot = a.s_slot[t];
             if (!a.active[slot]) continue;
             knn_agent<K>(a, t, slot);
-            orca_tick<K>(a, t, sproj);
+            orca_tick<K>(a, t);
         }
     }
 }
@@ -1488,44 +1467,32 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
     } else if (fused) {
         const int div = t.occ_div > 1 ? t.occ_div : 1;
         if (t.k <= 8) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_knn<8>, block, agent_smem_bytes<8>(block));
-            k_agents_knn<8><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, agent_smem_bytes<8>(block), s>>>(t);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_knn<8>, block, 0);
+            k_agents_knn<8><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
         } else if (t.k <= 16) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_knn<16>, block, agent_smem_bytes<16>(block));
-            k_agents_knn<16><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, agent_smem_bytes<16>(block), s>>>(t);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_knn<16>, block, 0);
+            k_agents_knn<16><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
         } else {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_knn<32>, block, agent_smem_bytes<32>(block));
-            k_agents_knn<32><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, agent_smem_bytes<32>(block), s>>>(t);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_knn<32>, block, 0);
+            k_agents_knn<32><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
         }
     } else {
         /* persistent grid: the resident blocks per SM, divided by occ_div
            (fewer resident warps leave each more L1 for its local arrays) */
         const int div = t.occ_div > 1 ? t.occ_div : 1;
         if (t.k <= 8) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<8>, block, agent_smem_bytes<8>(block));
-            k_agents<8><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, agent_smem_bytes<8>(block), s>>>(t);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<8>, block, 0);
+            k_agents<8><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
         } else if (t.k <= 16) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<16>, block, agent_smem_bytes<16>(block));
-            k_agents<16><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, agent_smem_bytes<16>(block), s>>>(t);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<16>, block, 0);
+            k_agents<16><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
         } else {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<32>, block, agent_smem_bytes<32>(block));
-            k_agents<32><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, agent_smem_bytes<32>(block), s>>>(t);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<32>, block, 0);
+            k_agents<32><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
         }
     }
     if (ev) cudaEventRecordWithFlags(ev[4], s, evflags);
     return cudaGetLastError();
-}
-
-/* once per context, outside any stream capture: the dynamic shared memory
-   limit of the per-thread agent kernels (up to 256 threads x 16 bisectors) */
-cudaError_t kernels_init()
-{
-    const int lim = (int)agent_smem_bytes<16>(256);
-    cudaError_t e = cudaFuncSetAttribute(k_agents<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_agents<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_agents_knn<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_agents_knn<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    return e;
 }
 
 cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k, float r, AgentGrid g,
