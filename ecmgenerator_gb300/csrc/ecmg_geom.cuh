@@ -578,6 +578,9 @@ EG_HD int lp2d(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2
         float dirPointDot = dot(dir, h.p);
         float disc = dirPointDot * dirPointDot + maxSpeed * maxSpeed - dot(h.p, h.p);
         if (disc <= 0.0f) return i;
+        /* a NaN discriminant takes neither branch of ORCA.cpp:498-506: the
+           constraint is passed over */
+        if (!(disc > 0.0f)) continue;
         float sq = sqrtf(disc);
         float lo = -dirPointDot - sq;
         float hi = -dirPointDot + sq;

@@ -549,6 +549,9 @@ int og_lp(const og_real* cons, int n, og_v2 opt, og_real maxSpeed, int useDirOpt
         og_real dirPointDot = vdot(dir, P);
         og_real discriminant = dirPointDot * dirPointDot + maxSpeed * maxSpeed - vdot(P, P);
         if (discriminant <= 0.0f) return i;
+        /* a NaN discriminant takes neither branch (ORCA.cpp:498-506): the
+           constraint is passed over */
+        if (!(discriminant > 0.0f)) continue;
 
         og_real sq = og_sqrt(discriminant);
         og_real left = -dirPointDot - sq;

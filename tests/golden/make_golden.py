@@ -14,6 +14,10 @@ Outputs (numpy .npz, committed):
   units.npz       known answers of RandomizedLP / RandomizedLP3D on random
                   half-plane sets, point location, retraction, IRM attraction
                   points and FindNearestObstacles on the c1 scene
+  lp_nan.npz      RandomizedLP on half-plane sets with NaN rows
+
+    python tests/golden/make_golden.py [tick_c1 tick_dense units lp_nan]
+writes the named fixtures (all of them by default).
 """
 from __future__ import annotations
 
@@ -216,25 +220,69 @@ def units(s, st):
     return out
 
 
-def main():
+def lp_nan():
+    """RandomizedLP (ORCA.cpp:428-587) on constraint sets with NaN rows -- the
+    half-plane of an agent with itself (0 / 0), which the kd-tree neighbour
+    cache can hand to GenerateConstraints: a NaN discriminant takes neither
+    branch at ORCA.cpp:498-506, so the constraint is passed over"""
+    rng = np.random.default_rng(7)
+    s = sc.make_scene(20.0, 20.0, np.array([[10.0, 10.0, 1.0, 1.0]]))
+    s.ecm = sc.build_ecm_exact(s, h=0.1)
+    ref = orc.Ref(s, 8, ORCA["dt"], 10, ORCA["tau_agent"], ORCA["tau_obst"])  # its LP entry points only
+    cons_l, meta, outs = [], [], []
+    for c in range(200):
+        m = int(rng.integers(2, 20))
+        pts = rng.normal(0, 0.8, (m, 2))
+        ang = rng.uniform(0, 2 * np.pi, m)
+        cons = np.concatenate([pts, np.stack([np.cos(ang), np.sin(ang)], 1)], 1).astype(F32)
+        nan_rows = rng.choice(m, int(rng.integers(1, 3)), replace=False)
+        cons[nan_rows] = np.nan
+        opt = rng.normal(0, 1.2, 2).astype(F32)
+        ms = np.float32(rng.uniform(0.8, 2.0))
+        use_dir = int(c % 4 == 0)
+        if use_dir:
+            opt = (opt / np.linalg.norm(opt)).astype(F32)
+        f, v = ref.lp(cons, opt, ms, use_dir)
+        cons_l.append(cons)
+        meta.append((m, opt[0], opt[1], ms, use_dir, f))
+        outs.append(v)
+    ref.close()
+    return dict(lp_len=np.array([x[0] for x in meta], I32), lp_opt=np.array([(x[1], x[2]) for x in meta], F32),
+                lp_ms=np.array([x[3] for x in meta], F32), lp_dir=np.array([x[4] for x in meta], I32),
+                lp_fail=np.array([x[5] for x in meta], I32), lp_cons=np.concatenate(cons_l, 0),
+                lp_out=np.array(outs, F32))
+
+
+def main(names):
     if not orc.ref_available():
         orc.build(ref=True)
     cfg = ag.scaled("c1", agents=400)
-    s = ag.build_scene(cfg, seed=3)
-    st = ag.spawn_agents(cfg, s, seed=3)
-    d = scene_arrays(s)
-    d.update(record_ticks(s, st, 10, 12))
-    np.savez_compressed(os.path.join(HERE, "tick_c1.npz"), **d)
-    sd, std_ = dense_scene(4)
-    d = scene_arrays(sd)
-    d.update(record_ticks(sd, std_, 16, 12))
-    np.savez_compressed(os.path.join(HERE, "tick_dense.npz"), **d)
-    d = scene_arrays(s)
-    d.update(units(s, st))
-    np.savez_compressed(os.path.join(HERE, "units.npz"), **d)
-    for f in ("tick_c1.npz", "tick_dense.npz", "units.npz"):
+    written = []
+    if {"tick_c1", "units"} & names:
+        s = ag.build_scene(cfg, seed=3)
+        st = ag.spawn_agents(cfg, s, seed=3)
+    if "tick_c1" in names:
+        d = scene_arrays(s)
+        d.update(record_ticks(s, st, 10, 12))
+        np.savez_compressed(os.path.join(HERE, "tick_c1.npz"), **d)
+        written.append("tick_c1.npz")
+    if "tick_dense" in names:
+        sd, std_ = dense_scene(4)
+        d = scene_arrays(sd)
+        d.update(record_ticks(sd, std_, 16, 12))
+        np.savez_compressed(os.path.join(HERE, "tick_dense.npz"), **d)
+        written.append("tick_dense.npz")
+    if "units" in names:
+        d = scene_arrays(s)
+        d.update(units(s, st))
+        np.savez_compressed(os.path.join(HERE, "units.npz"), **d)
+        written.append("units.npz")
+    if "lp_nan" in names:
+        np.savez_compressed(os.path.join(HERE, "lp_nan.npz"), **lp_nan())
+        written.append("lp_nan.npz")
+    for f in written:
         print(f, os.path.getsize(os.path.join(HERE, f)))
 
 
 if __name__ == "__main__":
-    main()
+    main(set(sys.argv[1:]) or {"tick_c1", "tick_dense", "units", "lp_nan"})

@@ -106,3 +106,21 @@ def test_oracle_units(port):
         ids = port.find_obstacles(O, float(u["ob_q"][i, 0]), float(u["ob_q"][i, 1]), float(u["ob_r2"][i]), libm=1)
         assert np.array_equal(ids, u["ob_ids"][off:off + n])
         off += n
+
+
+def test_oracle_lp_passes_over_nan_constraints(port):
+    """RandomizedLP with NaN half-planes (an agent's own entry in the kd-tree
+    neighbour cache gives one): the reference passes over a constraint whose
+    discriminant is NaN (ORCA.cpp:498-506); the oracle does the same, bit for
+    bit, on the reference's own answers"""
+    u = goldens.load("lp_nan")
+    off = passed_over = 0
+    for c in range(u["lp_len"].shape[0]):
+        m = int(u["lp_len"][c])
+        cons = u["lp_cons"][off:off + m]
+        off += m
+        f, v = port.lp(cons, tuple(u["lp_opt"][c]), float(u["lp_ms"][c]), int(u["lp_dir"][c]))
+        assert f == u["lp_fail"][c], c
+        assert np.array_equal(np.array(v, np.float32), u["lp_out"][c], equal_nan=True), c
+        passed_over += int(f == m and np.isfinite(u["lp_out"][c]).all())
+    assert passed_over > 20  # feasible results although a NaN row was met
