@@ -347,12 +347,14 @@ __device__ __forceinline__ void knn_pk_consider(float* key, float* rej, int j, u
     if (!(d2 > kEps) || !(d2 < r2)) return;
     float nk = __uint_as_float((__float_as_uint(d2) & ~kCodeMask) | code);
     if (nk < key[KL - 1]) {
+        /* every entry from the old list alone (no chain through the list):
+           entry q becomes min(old q, max(old q-1, nk)); the entry pushed out
+           is max(old last, nk) */
+        const float out = fmaxf(key[KL - 1], nk);
 #pragma unroll
-        for (int q2 = 0; q2 < KL; q2++) {
-            const float a = key[q2];
-            key[q2] = fminf(a, nk);
-            nk = fmaxf(a, nk);
-        }
+        for (int q2 = KL - 1; q2 > 0; q2--) key[q2] = fminf(key[q2], fmaxf(key[q2 - 1], nk));
+        key[0] = fminf(key[0], nk);
+        nk = out;
     }
     *rej = fminf(*rej, nk);
 }
@@ -544,7 +546,7 @@ __device__ __noinline__ bool verify_proposal(const Get& get, int m, int nObst, i
     V2 dir = right(H.n);
     float dpd = dot(dir, H.p);
     float disc = dpd * dpd + maxSpeed * maxSpeed - dot(H.p, H.p);
-    if (disc <= 0.0f) return false;
+    if (!(disc > 0.0f)) return false;
     float sq = sqrtf(disc);
     float lo = -dpd - sq, hi = -dpd + sq;
     int lo_src = -1, hi_src = -1;
@@ -681,8 +683,11 @@ __device__ void attract_tick(const TickArgs& a, int t)
 }
 
 /* ApplyObstacleAvoidanceForce + UpdateVelocitySystem + UpdatePositionSystem
-   of grid-order agent t (agents destroyed this tick are skipped) */
-template <int K>
+   of grid-order agent t (agents destroyed this tick are skipped).  FULL
+   keeps the learned proposal's check, the trace labels and the recording of
+   the step; the plain tick's kernel is compiled without them (smaller code,
+   the same arithmetic). */
+template <int K, bool FULL = true>
 __device__ void orca_tick(const TickArgs& a, int t)
 {
     const int slot = a.s_slot[t];
@@ -732,8 +737,14 @@ __device__ void orca_tick(const TickArgs& a, int t)
     for (int q = 0; q < ncnt; q++) {
         const int j = nbr[q];
         if (j >= 0) {
-            cons[m++] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
-                                            a.inv_tau_a);
+            /* inline in the plain kernel (no other callers compete for the
+               instruction cache there), out of line in the full one */
+            if (FULL)
+                cons[m++] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
+                                                a.inv_tau_a);
+            else
+                cons[m++] = agent_constraint(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
+                                             a.inv_tau_a);
         } else {
             /* kd-tree mode: a cache entry left by an earlier agent that is
                not in this tick's grid; its slot is not written this tick */
@@ -747,7 +758,7 @@ __device__ void orca_tick(const TickArgs& a, int t)
     V2 v;
     LocalGet get{cons};
     int failed = -1;
-    if (a.cls || a.cls_slot) { /* learned proposal: accepted only when the exact check passes */
+    if (FULL && (a.cls || a.cls_slot)) { /* learned proposal: accepted only when the exact check passes */
         const int c = a.cls_slot ? a.cls_slot[slot] : a.cls[t];
         bool ok = c != kClsOther && verify_proposal(get, m, nObst, ncnt, pv, maxSpeed, c, &v);
         if (ok) failed = m;
@@ -756,7 +767,7 @@ __device__ void orca_tick(const TickArgs& a, int t)
     }
     bool need3d = false;
     if (failed < 0) {
-        if (a.label) {
+        if (FULL && a.label) {
             LpTrace tr;
             failed = lp2d<LocalGet, true>(get, m, pv, maxSpeed, false, &v, &tr);
             a.label[t] = (unsigned char)label_of(tr, failed, m, nObst);
@@ -778,7 +789,7 @@ __device__ void orca_tick(const TickArgs& a, int t)
     a.vel[slot] = nv;
     a.pos[slot] = npos;
 
-    if (a.rec_cnt) {
+    if (FULL && a.rec_cnt) {
         a.rec_cnt[slot] = ncnt;
         for (int q = 0; q < a.k; q++)
             a.rec_nbr[slot * a.k + q] = q < ncnt ? (nbr[q] >= 0 ? a.s_slot[nbr[q]] : -nbr[q] - 1) : -1;
@@ -919,7 +930,7 @@ __global__ void __launch_bounds__(128) k_features(TickArgs a)
 
 /* persistent kernel: a warp takes `tile` consecutive grid-order agents per
    work grab (one atomic per grab) and runs them 32 at a time */
-template <int K>
+template <int K, bool FULL>
 __global__ void __launch_bounds__(256, (K <= 16) ? 4 : 1) k_agents(TickArgs a)
 {
     const int n = a.counters[C_NSORTED];
@@ -931,7 +942,7 @@ __global__ void __launch_bounds__(256, (K <= 16) ? 4 : 1) k_agents(TickArgs a)
         if (base >= n) break;
         for (int o = 0; o < a.tile; o += 32) {
             int t = base + o + lane;
-            if (t < n) orca_tick<K>(a, t);
+            if (t < n) orca_tick<K, FULL>(a, t);
         }
     }
 }
@@ -941,7 +952,7 @@ __global__ void __launch_bounds__(256, (K <= 16) ? 4 : 1) k_agents(TickArgs a)
    that warps in the ALU-bound search and warps in the issue-bound LPs share
    every SM.  Agents destroyed by the attraction kernel get no list (no later
    stage of a plain tick reads it). */
-template <int K>
+template <int K, bool FULL>
 __global__ void __launch_bounds__(256) k_agents_knn(TickArgs a)
 {
     const int n = a.counters[C_NSORTED];
@@ -957,7 +968,7 @@ __global__ void __launch_bounds__(256) k_agents_knn(TickArgs a)
             const int slot = a.s_slot[t];
             if (!a.active[slot]) continue;
             knn_agent<K>(a, t, slot);
-            orca_tick<K>(a, t);
+            orca_tick<K, FULL>(a, t);
         }
     }
 }
@@ -1046,6 +1057,7 @@ __device__ int lp2d_warp(const Get& get, int n, V2 opt, float maxSpeed, bool use
         const float dpd = dot(dir, h.p);
         const float disc = dpd * dpd + maxSpeed * maxSpeed - dot(h.p, h.p);
         if (disc <= 0.0f) { *out = v; return i; }
+        if (!(disc > 0.0f)) continue; /* NaN: passed over (ORCA.cpp:498-506) */
         const float sq = sqrtf(disc);
         float lo = -dpd - sq, hi = -dpd + sq;
         int lo_src = -1, hi_src = -1;
@@ -1161,7 +1173,7 @@ __device__ __noinline__ bool verify_proposal_warp(const Con* cons, int m, int nO
     const V2 dir = right(H.n);
     const float dpd = dot(dir, H.p);
     const float disc = dpd * dpd + maxSpeed * maxSpeed - dot(H.p, H.p);
-    if (disc <= 0.0f) return false;
+    if (!(disc > 0.0f)) return false;
     const float sq = sqrtf(disc);
     float lo = -dpd - sq, hi = -dpd + sq;
     int lo_src = -1, hi_src = -1;
@@ -1466,30 +1478,26 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
         }
     } else if (fused) {
         const int div = t.occ_div > 1 ? t.occ_div : 1;
-        if (t.k <= 8) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_knn<8>, block, 0);
-            k_agents_knn<8><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
-        } else if (t.k <= 16) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_knn<16>, block, 0);
-            k_agents_knn<16><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
-        } else {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents_knn<32>, block, 0);
-            k_agents_knn<32><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
-        }
+        const bool full = t.cls || t.cls_slot || t.label || t.rec_cnt;
+        auto go = [&](auto kern) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0);
+            kern<<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
+        };
+        if (t.k <= 8) full ? go(k_agents_knn<8, true>) : go(k_agents_knn<8, false>);
+        else if (t.k <= 16) full ? go(k_agents_knn<16, true>) : go(k_agents_knn<16, false>);
+        else full ? go(k_agents_knn<32, true>) : go(k_agents_knn<32, false>);
     } else {
         /* persistent grid: the resident blocks per SM, divided by occ_div
            (fewer resident warps leave each more L1 for its local arrays) */
         const int div = t.occ_div > 1 ? t.occ_div : 1;
-        if (t.k <= 8) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<8>, block, 0);
-            k_agents<8><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
-        } else if (t.k <= 16) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<16>, block, 0);
-            k_agents<16><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
-        } else {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agents<32>, block, 0);
-            k_agents<32><<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
-        }
+        const bool full = t.cls || t.cls_slot || t.label || t.rec_cnt;
+        auto go = [&](auto kern) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0);
+            kern<<<sms * (per_sm / div > 0 ? per_sm / div : 1), block, 0, s>>>(t);
+        };
+        if (t.k <= 8) full ? go(k_agents<8, true>) : go(k_agents<8, false>);
+        else if (t.k <= 16) full ? go(k_agents<16, true>) : go(k_agents<16, false>);
+        else full ? go(k_agents<32, true>) : go(k_agents<32, false>);
     }
     if (ev) cudaEventRecordWithFlags(ev[4], s, evflags);
     return cudaGetLastError();
