@@ -129,7 +129,14 @@ def build_scene(cfg: dict, seed: int) -> sc.Scene:
     rng = np.random.default_rng(seed)
     boxes = sc.gen_boxes(rng, cfg["w"], cfg["h"], cfg["boxes"], *cfg["side"])
     s = sc.make_scene(cfg["w"], cfg["h"], boxes)
-    s.ecm = sc.build_ecm(s, h=cfg.get("h_ecm", 0.2))
+    # cfg["ecm"]: "sampled" (default: chains of the sampled diagram split
+    # where they bend, so curved bisectors are followed closely) or "exact"
+    # (one straight edge per Voronoi edge between exact vertices, the graph
+    # the reference builds from Boost's diagram)
+    if cfg.get("ecm", "sampled") == "exact":
+        s.ecm = sc.build_ecm_exact(s, h=cfg.get("h_ecm", 0.2))
+    else:
+        s.ecm = sc.build_ecm(s, h=cfg.get("h_ecm", 0.2))
     s.meta = dict(seed=seed, boxes=int(boxes.shape[0]))
     return s
 

@@ -1,9 +1,9 @@
-"""Seeded synthetic scenes and a host ECM builder.
+"""Seeded synthetic scenes and the host ECM builders.
 
 The reference builds its scene in ``Environment`` (ECMGenerator/Environment.cpp:188-229)
 and its Explicit Corridor Map with Boost.Polygon's segment Voronoi diagram
-(ECMGenerator/ECMGenerator.cpp:60-256).  Boost is not available, so this module
-builds the ECM from a point-sampled Voronoi diagram (scipy / Qhull):
+(ECMGenerator/ECMGenerator.cpp:60-256).  Boost is not available; both builders
+here start from a point-sampled Voronoi diagram (scipy / Qhull):
 
 * every obstacle segment (walkable-area border and box sides) is sampled at
   spacing ``h``; every segment interior and every corner is one *feature*;
@@ -11,11 +11,18 @@ builds the ECM from a point-sampled Voronoi diagram (scipy / Qhull):
   are not a segment and its own end point (those ridges are the "secondary"
   edges that ECMGenerator.cpp:157 skips with ``is_primary()``), and both of its
   vertices lie in free space (ECMGenerator.cpp:107-130);
-* chains of ridges that separate the same pair of features are merged into one
-  ECM edge, split again where the chain leaves its chord by more than ``tol``;
-* each half-edge stores the closest obstacle points at its source vertex, left
-  and right of its direction, as ECMGenerator.cpp:173-195 does
-  (``closest_left/right`` of half-edge 0 at vertex0, of half-edge 1 at vertex1).
+* chains of ridges that separate the same pair of features, from junction to
+  junction, are the diagram's edges.
+
+``build_ecm_exact`` (``cfg["ecm"] = "exact"``) turns every chain into one
+straight edge between exact Voronoi vertices, each solved as the point
+equidistant from the features that meet there -- the graph the reference builds
+from Boost's diagram.  ``build_ecm`` (the workloads' default) keeps the
+sampled vertices and splits chains where they leave their chord by more than
+``tol``, so that a curved bisector is followed to within ``tol``.  Each half-edge
+stores the closest obstacle points at its source vertex, left and right of its
+direction, as ECMGenerator.cpp:173-195 does (``closest_left/right`` of
+half-edge 0 at vertex0, of half-edge 1 at vertex1).
 
 The graph is returned as flat arrays in the layout of ``ECMGraph``
 (ECMGenerator/ECM.h:20-116): half-edge ``2e+h`` of edge ``e``.  Construction is
@@ -41,6 +48,7 @@ class Ecm:
     he_next: np.ndarray      # (2E,) i32
     he_left: np.ndarray      # (2E,2) f32 closest_left
     he_right: np.ndarray     # (2E,2) f32 closest_right
+    meta: dict = field(default_factory=dict)
 
     @property
     def n_vertices(self) -> int:
@@ -280,110 +288,153 @@ def _closest_on_seg(p, a, b):
     return a + t * d
 
 
-def build_ecm(scene: Scene, h: float = 0.2, tol: float = 0.3) -> Ecm:
-    from scipy.spatial import Voronoi
+class _Diagram:
+    """The point-sampled Voronoi diagram of an obstacle union, reduced to
+    chains: maximal runs of kept ridges that separate the same two features
+    (segment interiors 0..S-1, corner points S..S+C-1), from junction to
+    junction."""
 
-    segs = _segments(scene)
-    S = segs.shape[0]
-    # corner features: unique segment end points
-    ends = np.concatenate([segs[:, 0:2], segs[:, 2:4]], 0)
-    key = np.round(ends * 1e4).astype(np.int64)
-    uniq, inv = np.unique(key, axis=0, return_inverse=True)
-    inv = inv.reshape(-1)
-    corner_pt = np.zeros((uniq.shape[0], 2))
-    corner_pt[inv] = ends
-    seg_c0 = inv[:S]
-    seg_c1 = inv[S:]
-    C = uniq.shape[0]
-    # sites
-    pts = [corner_pt]
-    feat = [S + np.arange(C)]
-    for s in range(S):
-        a, b = segs[s, 0:2], segs[s, 2:4]
-        L = float(np.hypot(*(b - a)))
-        m = max(1, int(math.ceil(L / h)))
-        t = (np.arange(1, m) / m)[:, None]
-        if t.size:
-            pts.append(a + t * (b - a))
-            feat.append(np.full(t.shape[0], s))
-    P = np.concatenate(pts, 0)
-    Fe = np.concatenate(feat, 0).astype(np.int64)
-    vor = Voronoi(P)
-    V = vor.vertices
-    rp = vor.ridge_points
-    rv = np.array(vor.ridge_vertices, dtype=np.int64)
-    fa, fb = Fe[rp[:, 0]], Fe[rp[:, 1]]
-    keep = (rv[:, 0] >= 0) & (rv[:, 1] >= 0) & (fa != fb)
-    # secondary ridges: a segment and its own end point
-    def is_secondary(f1, f2):
+    def __init__(self, scene: Scene, h: float, segs: np.ndarray, end_eps: float = 0.0):
+        """segs: the obstacle union; h: sample spacing; end_eps > 0 adds a
+        sample that far from each end of every segment, so that the boundary
+        between a corner's cell and its own segment's cell (the segment's
+        normal through the corner) is placed to within end_eps / 2"""
+        from scipy.spatial import Voronoi
+
+        self.segs = segs
+        S = self.S = segs.shape[0]
+        # corner features: unique segment end points
+        ends = np.concatenate([segs[:, 0:2], segs[:, 2:4]], 0)
+        key = np.round(ends * 1e4).astype(np.int64)
+        uniq, inv = np.unique(key, axis=0, return_inverse=True)
+        inv = inv.reshape(-1)
+        corner_pt = np.zeros((uniq.shape[0], 2))
+        corner_pt[inv] = ends
+        self.corner_pt = corner_pt
+        self.seg_c0 = seg_c0 = inv[:S]
+        self.seg_c1 = seg_c1 = inv[S:]
+        C = uniq.shape[0]
+        # sites
+        pts = [corner_pt]
+        feat = [S + np.arange(C)]
+        for s in range(S):
+            a, b = segs[s, 0:2], segs[s, 2:4]
+            L = float(np.hypot(*(b - a)))
+            m = max(1, int(math.ceil(L / h)))
+            t = np.arange(1, m) / m
+            if end_eps > 0.0 and L > 4.0 * end_eps:
+                t = np.concatenate([[end_eps / L], t, [1.0 - end_eps / L]])
+            t = t[:, None]
+            if t.size:
+                pts.append(a + t * (b - a))
+                feat.append(np.full(t.shape[0], s))
+        P = np.concatenate(pts, 0)
+        Fe = np.concatenate(feat, 0).astype(np.int64)
+        vor = Voronoi(P)
+        self.V = V = vor.vertices
+        rp = vor.ridge_points
+        rv = np.array(vor.ridge_vertices, dtype=np.int64)
+        fa, fb = Fe[rp[:, 0]], Fe[rp[:, 1]]
+        finite = (rv[:, 0] >= 0) & (rv[:, 1] >= 0)
+        # the features whose sites generate each Voronoi vertex (every ridge
+        # around it, kept or not)
+        gv = np.concatenate([rv[:, 0], rv[:, 0], rv[:, 1], rv[:, 1]])
+        gf = np.concatenate([fa, fb, fa, fb])
+        self._gen_v, self._gen_f = gv[gv >= 0], gf[gv >= 0]
+        keep = finite & (fa != fb)
+        keep &= ~self.is_secondary(fa, fb)
+        # free-space test of Voronoi vertices
+        bidx = BoxIndex(scene)
+        vfree = np.zeros(V.shape[0], bool)
+        used = np.unique(rv[keep].reshape(-1))
+        cl = bidx.clearance(V[used, 0], V[used, 1], reach=4.0)
+        vfree[used] = cl > 1e-6
+        keep &= vfree[rv[:, 0]] & vfree[rv[:, 1]]
+        rv, fa, fb, rp = rv[keep], fa[keep], fb[keep], rp[keep]
+        # orient each ridge: left site of v0 -> v1
+        d = V[rv[:, 1]] - V[rv[:, 0]]
+        s0 = P[rp[:, 0]] - V[rv[:, 0]]
+        left_is_a = (d[:, 0] * s0[:, 1] - d[:, 1] * s0[:, 0]) > 0
+        fl = np.where(left_is_a, fa, fb)
+        fr = np.where(left_is_a, fb, fa)
+        self.chains = self._chains(rv, fl, fr)
+
+    def is_secondary(self, f1, f2):
+        """a segment and its own end point (ECMGenerator.cpp:157 skips these
+        edges with is_primary())"""
+        S = self.S
         seg_f = np.where(f1 < S, f1, f2)
         cor_f = np.where(f1 < S, f2, f1) - S
         one_seg = (f1 < S) != (f2 < S)
         segc = np.clip(seg_f, 0, S - 1)
-        return one_seg & ((seg_c0[segc] == cor_f) | (seg_c1[segc] == cor_f))
-    keep &= ~is_secondary(fa, fb)
-    # free-space test of Voronoi vertices
-    bidx = BoxIndex(scene)
-    vfree = np.zeros(V.shape[0], bool)
-    used = np.unique(rv[keep].reshape(-1))
-    cl = bidx.clearance(V[used, 0], V[used, 1], reach=4.0)
-    vfree[used] = cl > 1e-6
-    keep &= vfree[rv[:, 0]] & vfree[rv[:, 1]]
-    rv, fa, fb, rp = rv[keep], fa[keep], fb[keep], rp[keep]
-    # orient each ridge: left site of v0 -> v1
-    d = V[rv[:, 1]] - V[rv[:, 0]]
-    s0 = P[rp[:, 0]] - V[rv[:, 0]]
-    left_is_a = (d[:, 0] * s0[:, 1] - d[:, 1] * s0[:, 0]) > 0
-    fl = np.where(left_is_a, fa, fb)
-    fr = np.where(left_is_a, fb, fa)
-    # adjacency
-    R = rv.shape[0]
-    adj: dict[int, list[int]] = {}
-    for r in range(R):
-        adj.setdefault(int(rv[r, 0]), []).append(r)
-        adj.setdefault(int(rv[r, 1]), []).append(r)
+        return one_seg & ((self.seg_c0[segc] == cor_f) | (self.seg_c1[segc] == cor_f))
 
-    def pair(r):
-        return (min(fl[r], fr[r]), max(fl[r], fr[r]))
+    def generators(self, v: int) -> list[int]:
+        """distinct features of the sites around sampled vertex v"""
+        if not hasattr(self, "_gen"):
+            order = np.argsort(self._gen_v, kind="stable")
+            gv, gf = self._gen_v[order], self._gen_f[order]
+            b = np.searchsorted(gv, np.arange(self.V.shape[0] + 1))
+            self._gen = (gf, b)
+        gf, b = self._gen
+        return sorted(set(int(f) for f in gf[b[v]:b[v + 1]]))
 
-    junction = set()
-    for v, rs in adj.items():
-        if len(rs) != 2 or pair(rs[0]) != pair(rs[1]):
-            junction.add(v)
-    visited = np.zeros(R, bool)
-    chains = []  # (vertex list, left feature, right feature)
+    @staticmethod
+    def _chains(rv, fl, fr):
+        R = rv.shape[0]
+        adj: dict[int, list[int]] = {}
+        for r in range(R):
+            adj.setdefault(int(rv[r, 0]), []).append(r)
+            adj.setdefault(int(rv[r, 1]), []).append(r)
 
-    def walk(v_start, r0):
-        verts = [v_start]
-        r = r0
-        v = v_start
-        # orientation of the first ridge relative to the walk
-        if rv[r, 0] == v:
-            left, right = fl[r], fr[r]
-        else:
-            left, right = fr[r], fl[r]
-        while True:
-            visited[r] = True
-            nv = int(rv[r, 1] if rv[r, 0] == v else rv[r, 0])
-            verts.append(nv)
-            v = nv
-            if v in junction:
-                break
-            nr = [q for q in adj[v] if not visited[q]]
-            if not nr:
-                break
-            r = nr[0]
-        return verts, left, right
+        def pair(r):
+            return (min(fl[r], fr[r]), max(fl[r], fr[r]))
 
-    for v in sorted(junction):
-        for r in adj[v]:
+        junction = set()
+        for v, rs in adj.items():
+            if len(rs) != 2 or pair(rs[0]) != pair(rs[1]):
+                junction.add(v)
+        visited = np.zeros(R, bool)
+        chains = []  # (vertex list, left feature, right feature)
+
+        def walk(v_start, r0):
+            verts = [v_start]
+            r = r0
+            v = v_start
+            # orientation of the first ridge relative to the walk
+            if rv[r, 0] == v:
+                left, right = fl[r], fr[r]
+            else:
+                left, right = fr[r], fl[r]
+            while True:
+                visited[r] = True
+                nv = int(rv[r, 1] if rv[r, 0] == v else rv[r, 0])
+                verts.append(nv)
+                v = nv
+                if v in junction:
+                    break
+                nr = [q for q in adj[v] if not visited[q]]
+                if not nr:
+                    break
+                r = nr[0]
+            return verts, int(left), int(right)
+
+        for v in sorted(junction):
+            for r in adj[v]:
+                if not visited[r]:
+                    chains.append(walk(v, r))
+        for r in range(R):  # closed loops without junctions
             if not visited[r]:
+                v = int(rv[r, 0])
+                junction.add(v)
                 chains.append(walk(v, r))
-    for r in range(R):  # closed loops without junctions
-        if not visited[r]:
-            v = int(rv[r, 0])
-            junction.add(v)
-            chains.append(walk(v, r))
+        return chains
+
+
+def build_ecm(scene: Scene, h: float = 0.2, tol: float = 0.3) -> Ecm:
+    segs = _segments(scene)
+    D = _Diagram(scene, h, segs)
+    S, V, corner_pt, seg_c0, seg_c1, chains = D.S, D.V, D.corner_pt, D.seg_c0, D.seg_c1, D.chains
 
     # split chains that bend away from their chord (Douglas-Peucker)
     def split(vs):
@@ -414,45 +465,34 @@ def build_ecm(scene: Scene, h: float = 0.2, tol: float = 0.3) -> Ecm:
         for piece in split(vs):
             if piece[0] != piece[-1]:
                 edges.append((piece[0], piece[-1], l, r))
-    # compact vertex ids, spatially ordered (Morton-like) for locality
-    vids = sorted({e[0] for e in edges} | {e[1] for e in edges})
-    vpos64 = V[vids]
-    order = np.lexsort((vpos64[:, 0], np.floor(vpos64[:, 1] / 8.0)))
-    remap = {vids[o]: i for i, o in enumerate(order)}
-    vpos = vpos64[order]
-    nV = vpos.shape[0]
-    edges = [(remap[a], remap[b], l, r) for a, b, l, r in edges]
-    mid = np.array([(vpos[a] + vpos[b]) * 0.5 for a, b, _, _ in edges]).reshape(-1, 2)
-    eorder = np.lexsort((mid[:, 0], np.floor(mid[:, 1] / 8.0))) if len(edges) else np.zeros(0, np.int64)
-    edges = [edges[i] for i in eorder]
-    E = len(edges)
-
-    # A vertex where a corner's wedge meets the cell of one of that corner's
-    # own segments lies, in the exact diagram, on the segment's normal through
-    # the corner.  The sampled diagram puts it within ~h of that line; moving
-    # it onto the line makes the spoke to the corner perpendicular to the
-    # segment, so the corner triangle and the segment quad share one spoke and
-    # retraction rays (perpendicular to the segment) stay inside the quad.
-    vfeat: dict[int, set] = {}
-    for a_, b_, l_, r_ in edges:
-        for v_ in (a_, b_):
-            vfeat.setdefault(v_, set()).update((l_, r_))
-    for v_, fs in vfeat.items():
-        for f in fs:
-            if f < S:
-                continue
-            c = corner_pt[f - S]
-            for sg in fs:
-                if sg >= S or (seg_c0[sg] != f - S and seg_c1[sg] != f - S):
+    def snap(vpos, edges):
+        # A vertex where a corner's wedge meets the cell of one of that
+        # corner's own segments lies, in the exact diagram, on the segment's
+        # normal through the corner.  The sampled diagram puts it within ~h of
+        # that line; moving it onto the line makes the spoke to the corner
+        # perpendicular to the segment, so the corner triangle and the segment
+        # quad share one spoke and retraction rays (perpendicular to the
+        # segment) stay inside the quad.
+        vfeat: dict[int, set] = {}
+        for a_, b_, l_, r_ in edges:
+            for v_ in (a_, b_):
+                vfeat.setdefault(v_, set()).update((l_, r_))
+        for v_, fs in vfeat.items():
+            for f in fs:
+                if f < S:
                     continue
-                d = segs[sg, 2:4] - segs[sg, 0:2]
-                L2 = float(d @ d)
-                if L2 == 0.0:
-                    continue
-                t = float((vpos[v_] - c) @ d) / L2
-                if abs(t) * math.sqrt(L2) < 2.0 * h:
-                    vpos[v_] = vpos[v_] - t * d
-                break
+                c = corner_pt[f - S]
+                for sg in fs:
+                    if sg >= S or (seg_c0[sg] != f - S and seg_c1[sg] != f - S):
+                        continue
+                    d = segs[sg, 2:4] - segs[sg, 0:2]
+                    L2 = float(d @ d)
+                    if L2 == 0.0:
+                        continue
+                    t = float((vpos[v_] - c) @ d) / L2
+                    if abs(t) * math.sqrt(L2) < 2.0 * h:
+                        vpos[v_] = vpos[v_] - t * d
+                    break
 
     def feat_point(f, p):
         if f >= S:
@@ -465,6 +505,168 @@ def build_ecm(scene: Scene, h: float = 0.2, tol: float = 0.3) -> Ecm:
             if math.hypot(*(q - c)) < 1.5 * h:
                 return c.copy()
         return q
+
+    return _assemble(V, edges, feat_point, snap)
+
+
+def _solve_vertex(D: _Diagram, feats: list, x0: np.ndarray, h: float):
+    """The point equidistant from the features `feats` (segment interiors as
+    lines, corners as points) nearest the sampled vertex x0 (Newton on the
+    differences of the distances, least squares beyond three features).
+    Returns (point, ok)."""
+    S, segs = D.S, D.segs
+    # a corner together with two of its own segments: the corner itself (a
+    # walkable-area corner, where the border's two bisected sides meet)
+    for f in feats:
+        if f >= S:
+            c = f - S
+            own = [g for g in feats if g < S and (D.seg_c0[g] == c or D.seg_c1[g] == c)]
+            if len(own) >= 2:
+                return D.corner_pt[c].copy(), True
+    lines = {}
+    for f in feats:
+        if f < S:
+            a, b = segs[f, 0:2], segs[f, 2:4]
+            t = b - a
+            n = np.array([-t[1], t[0]]) / math.hypot(t[0], t[1])
+            if float(n @ (x0 - a)) < 0.0:
+                n = -n
+            lines[f] = (a, n)
+    x = np.array(x0, np.float64)
+    ok = False
+    for _ in range(60):
+        ds, gs = [], []
+        for f in feats:
+            if f >= S:
+                d = x - D.corner_pt[f - S]
+                r = math.hypot(d[0], d[1])
+                ds.append(r)
+                gs.append(d / r if r > 0.0 else np.zeros(2))
+            else:
+                a, n = lines[f]
+                ds.append(float(n @ (x - a)))
+                gs.append(n)
+        A = np.array([gs[i] - gs[0] for i in range(1, len(feats))])
+        res = np.array([ds[i] - ds[0] for i in range(1, len(feats))])
+        dx = np.linalg.lstsq(A, -res, rcond=None)[0]
+        x = x + dx
+        if math.hypot(dx[0], dx[1]) <= 1e-12 * max(1.0, math.hypot(x[0], x[1])):
+            ok = True
+            break
+    if ok:
+        ds = [math.hypot(*(x - D.corner_pt[f - S])) if f >= S else float(lines[f][1] @ (x - lines[f][0]))
+              for f in feats]
+        ok = min(ds) > 0.0 and max(ds) - min(ds) <= 1e-9 * max(1.0, max(ds)) and math.hypot(*(x - x0)) < 4.0 * h
+    return x, ok
+
+
+def build_ecm_exact(scene: Scene, h: float = 0.2, int_sites: bool = False) -> Ecm:
+    """The ECM of the exact segment Voronoi diagram of the obstacle union, the
+    graph ECMGenerator::ConstructECMGraph (ECMGenerator.cpp:60-232) builds
+    from Boost.Polygon's diagram: one straight edge per primary Voronoi edge
+    in free space, between its two Voronoi vertices, curved edges included.
+
+    The topology comes from the point-sampled diagram (`_Diagram`: which
+    features meet at which vertex, which two features each edge separates);
+    every vertex is then solved exactly as the point equidistant from its
+    generating features, so vertex positions and clearances are those of the
+    segment diagram (to double precision) rather than of the samples, and a
+    bisector between two features is one edge however curved.  The samples
+    must be dense enough to separate the vertices (spacing h well below the
+    shortest Voronoi edge that matters).  With int_sites the diagram is built
+    on the coordinates truncated to integers, as construct_voronoi sees them
+    through the reference's int point_traits (ECMGenerator.cpp:37-44); closest
+    points and the free-space test use the scene's own coordinates
+    (ECMGenerator.cpp:84-105, 259-277)."""
+    segs = _segments(scene)
+    site = np.trunc(segs) if int_sites else segs
+    D = _Diagram(scene, h, site, end_eps=1e-4)
+    S = D.S
+    cache: dict[int, np.ndarray | None] = {}
+
+    def vert(v):
+        if v not in cache:
+            feats = D.generators(v)
+            x = None
+            if len(feats) >= 3:
+                x, ok = _solve_vertex(D, feats, D.V[v], h)
+                if not ok:
+                    x = None
+            cache[v] = x
+        return cache[v]
+
+    pts: list[np.ndarray] = []
+    ids: dict[tuple[int, int], int] = {}
+
+    def vid(x):
+        k = (int(round(x[0] * 1e6)), int(round(x[1] * 1e6)))  # one micrometre
+        if k not in ids:
+            ids[k] = len(pts)
+            pts.append(x)
+        return ids[k]
+
+    bidx = BoxIndex(scene)
+    edges, seen = [], set()
+    dropped = 0
+    for vs, l, r in D.chains:
+        xa, xb = vert(vs[0]), vert(vs[-1])
+        if xa is None or xb is None:
+            dropped += 1
+            continue
+        a, b = vid(xa), vid(xb)
+        if a == b or (a, b, l, r) in seen or (b, a, r, l) in seen:
+            continue
+        seen.add((a, b, l, r))
+        edges.append((a, b, l, r))
+    P = np.array(pts, np.float64).reshape(-1, 2)
+    # vertices strictly inside an obstacle are not ECM vertices
+    # (ECMGenerator.cpp:84-87); corners of the walkable area are
+    inside = np.zeros(P.shape[0], bool)
+    if P.shape[0] and scene.boxes.shape[0]:
+        b = scene.boxes
+        for i in range(P.shape[0]):
+            dx = np.abs(P[i, 0] - b[:, 0]) - b[:, 2]
+            dy = np.abs(P[i, 1] - b[:, 1]) - b[:, 3]
+            inside[i] = bool(np.any((dx < 0) & (dy < 0)))
+    edges = [e for e in edges if not inside[e[0]] and not inside[e[1]]]
+    # a corner's own point: the corner of the scene's segment it belongs to
+    corner_src = np.zeros((D.corner_pt.shape[0], 2))
+    corner_src[D.seg_c1] = segs[:, 2:4]
+    corner_src[D.seg_c0] = segs[:, 0:2]
+
+    def feat_point(f, p):
+        """GetClosestPointsToSource (ECMGenerator.cpp:259-277)"""
+        if f >= S:
+            return corner_src[f - S].copy()
+        return _closest_on_seg(p, segs[f, 0:2], segs[f, 2:4])
+
+    e = _assemble(P, edges, feat_point)
+    e.meta = dict(builder="exact segment Voronoi", h=h, int_sites=int_sites, unresolved_chains=dropped)
+    return e
+
+
+def _assemble(V: np.ndarray, edges: list, feat_point, adjust=None) -> Ecm:
+    """ECM arrays from straight edges (a, b, left feature, right feature)
+    between rows of V: vertices and edges in a spatial order, half-edge 2e
+    from a to b and 2e+1 back, each with the closest obstacle points left and
+    right of its direction at its source vertex (ECMGenerator.cpp:173-195),
+    and the rotation order of the half-edges around every vertex
+    (ECMGenerator.cpp:211-255).  adjust(vpos, edges) may move vertices after
+    the renumbering."""
+    # compact vertex ids, spatially ordered (Morton-like) for locality
+    vids = sorted({e[0] for e in edges} | {e[1] for e in edges})
+    vpos64 = V[vids] if vids else np.zeros((0, 2))
+    order = np.lexsort((vpos64[:, 0], np.floor(vpos64[:, 1] / 8.0)))
+    remap = {vids[o]: i for i, o in enumerate(order)}
+    vpos = vpos64[order].copy()
+    nV = vpos.shape[0]
+    edges = [(remap[a], remap[b], l, r) for a, b, l, r in edges]
+    mid = np.array([(vpos[a] + vpos[b]) * 0.5 for a, b, _, _ in edges]).reshape(-1, 2)
+    eorder = np.lexsort((mid[:, 0], np.floor(mid[:, 1] / 8.0))) if len(edges) else np.zeros(0, np.int64)
+    edges = [edges[i] for i in eorder]
+    E = len(edges)
+    if adjust is not None:
+        adjust(vpos, edges)
 
     he_target = np.zeros(2 * E, np.int32)
     he_left = np.zeros((2 * E, 2), np.float64)

@@ -102,14 +102,17 @@ def test_custom_transcendentals_divergence(port, c1_ref):
 
 
 @pytest.mark.ref
-def test_mode_a_ticks_bitexact_vs_unmodified_update(port):
+@pytest.mark.parametrize("ecm", ["sampled", "exact"])
+def test_mode_a_ticks_bitexact_vs_unmodified_update(port, ecm):
     """The oracle's kd-tree mode (knn_mode 1: KDTree::Construct and
     KNearestAgents_R with the neighbour cache carried across agents and ticks)
     against the unmodified Simulator::Update, tick by tick.  Re-plans happen
     inside the reference's Update with its own planner; the oracle takes the
     same paths afterwards (a failed re-plan keeps the old path on both
-    sides, where the reference would read path.x[-1])."""
-    cfg = ag.scaled("c1")
+    sides, where the reference would read path.x[-1]).  On the exact
+    segment-Voronoi ECM an agent meets its own cache entry and a NaN
+    half-plane, which the LP must pass over as the reference does."""
+    cfg = ag.scaled("c1", ecm=ecm)
     s = ag.build_scene(cfg, seed=2)
     st = ag.spawn_agents(cfg, s, seed=2)
     ref = orc.Ref(s, st.n_slots, 1.0 / 60.0, cfg["k"], 2.0, 2.0)
