@@ -355,9 +355,11 @@ struct Con {
 };
 
 /* obstacle part of ORCA::GenerateConstraints (ORCA.cpp:70-333) for one
-   candidate edge L; returns true and fills *c when a constraint is emitted */
-EG_NI bool obstacle_constraint(const ObstView& o, int L, V2 position, V2 velocity, float clr,
-                               float tau_obst, Con* c)
+   candidate edge L; returns true and fills *c when a constraint is emitted.
+   Inline for the plain tick's kernel; obstacle_constraint is the out-of-line
+   copy for the larger kernels. */
+EG_HD bool obstacle_constraint_inl(const ObstView& o, int L, V2 position, V2 velocity, float clr,
+                                   float tau_obst, Con* c)
 {
     int R = o.next[L];
     V2 pL = o.p[L], pR = o.p[R];
@@ -474,6 +476,12 @@ EG_NI bool obstacle_constraint(const ObstView& o, int L, V2 position, V2 velocit
         c->n = normal;
         return true;
     }
+}
+
+EG_NI bool obstacle_constraint(const ObstView& o, int L, V2 position, V2 velocity, float clr,
+                               float tau_obst, Con* c)
+{
+    return obstacle_constraint_inl(o, L, position, velocity, clr, tau_obst, c);
 }
 
 /* agent part of ORCA::GenerateConstraints (ORCA.cpp:339-423) for one

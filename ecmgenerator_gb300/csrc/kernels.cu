@@ -727,7 +727,8 @@ __device__ void orca_tick(const TickArgs& a, int t)
             int L = items ? items[q] : q;
             if (!obstacle_in_range(o, L, pos, rsq)) continue;
             Con c;
-            if (obstacle_constraint(o, L, pos, vel, clr, a.tau_o, &c)) {
+            if (FULL ? obstacle_constraint(o, L, pos, vel, clr, a.tau_o, &c)
+                     : obstacle_constraint_inl(o, L, pos, vel, clr, a.tau_o, &c)) {
                 if (m < MC - K) cons[m++] = c;
                 else overflow = true;
             }
