@@ -568,66 +568,82 @@ struct LpTrace {
     int j = -1;
 };
 
-/* ORCA::RandomizedLP (ORCA.cpp:428-587).  The constraint at index i is
-   fetched through get(i) so that callers may keep constraints in registers,
-   shared or local memory.  With TRACE the last update is recorded in *tr
-   (bookkeeping only; the arithmetic is the same). */
+/* the starting point of ORCA::RandomizedLP (ORCA.cpp:438-453) */
+EG_HD V2 lp2d_start(V2 opt, float maxSpeed, bool useDirOpt)
+{
+    if (useDirOpt) return opt * maxSpeed;
+    if (len(opt) > maxSpeed) return normalized(opt) * maxSpeed;
+    return opt;
+}
+
+/* step i of ORCA::RandomizedLP (ORCA.cpp:459-583): half-plane h (the
+   constraint at index i) against the solution *out of the steps before it;
+   the earlier constraints are fetched through get(j), j < i.  Returns false
+   when the LP fails at i (*out is then the solution before the step).  With
+   TRACE the update is recorded in *tr (bookkeeping only). */
+template <class Get, bool TRACE = false>
+EG_HD bool lp2d_step(const Get& get, int i, const Con& h, V2 opt, float maxSpeed, bool useDirOpt, V2* out,
+                     LpTrace* tr = nullptr)
+{
+    if (det(right(h.n), h.p - *out) <= 0.0f) return true; /* Constraint::Contains */
+    V2 dir = right(h.n);
+    float dirPointDot = dot(dir, h.p);
+    float disc = dirPointDot * dirPointDot + maxSpeed * maxSpeed - dot(h.p, h.p);
+    if (disc <= 0.0f) return false;
+    /* a NaN discriminant takes neither branch of ORCA.cpp:498-506: the
+       constraint is passed over */
+    if (!(disc > 0.0f)) return true;
+    float sq = sqrtf(disc);
+    float lo = -dirPointDot - sq;
+    float hi = -dirPointDot + sq;
+    int lo_src = -1, hi_src = -1;
+    for (int j = 0; j < i; j++) {
+        Con g = get(j);
+        float den = det(right(h.n), right(g.n));
+        float num = det(right(g.n), h.p - g.p);
+        if (fabsf(den) <= kEps) {
+            if (num < 0.0f) return false;
+            continue;
+        }
+        const float t = num / den;
+        if (den >= 0.0f) { /* std::min(right, t) */
+            if (TRACE && t < hi) hi_src = j;
+            hi = (t < hi) ? t : hi;
+        } else { /* std::max(left, t) */
+            if (TRACE && lo < t) lo_src = j;
+            lo = (lo < t) ? t : lo;
+        }
+        if (lo > hi) return false;
+    }
+    if (useDirOpt) {
+        if (dot(opt, right(h.n)) > 0) *out = h.p + right(h.n) * hi;
+        else *out = h.p + right(h.n) * lo;
+    } else {
+        float t = dot(right(h.n), opt - h.p);
+        if (t < lo) {
+            *out = h.p + right(h.n) * lo;
+            if (TRACE) { tr->h = i; tr->src = lo_src < 0 ? 1 : 2; tr->j = lo_src; }
+        } else if (t > hi) {
+            *out = h.p + right(h.n) * hi;
+            if (TRACE) { tr->h = i; tr->src = hi_src < 0 ? 1 : 2; tr->j = hi_src; }
+        } else {
+            *out = h.p + right(h.n) * t;
+            if (TRACE) { tr->h = i; tr->src = 0; tr->j = -1; }
+        }
+    }
+    return true;
+}
+
+/* ORCA::RandomizedLP (ORCA.cpp:428-587): its steps over the constraints
+   0 .. n-1 in order; returns the failing index or n.  The constraint at index
+   i is fetched through get(i) so that callers may keep constraints in
+   registers, shared or local memory. */
 template <class Get, bool TRACE = false>
 EG_HD int lp2d(const Get& get, int n, V2 opt, float maxSpeed, bool useDirOpt, V2* out, LpTrace* tr = nullptr)
 {
-    if (useDirOpt) *out = opt * maxSpeed;
-    else if (len(opt) > maxSpeed) *out = normalized(opt) * maxSpeed;
-    else *out = opt;
-    if (n == 0) return n;
-    for (int i = 0; i < n; i++) {
-        Con h = get(i);
-        if (det(right(h.n), h.p - *out) <= 0.0f) continue; /* Constraint::Contains */
-        V2 dir = right(h.n);
-        float dirPointDot = dot(dir, h.p);
-        float disc = dirPointDot * dirPointDot + maxSpeed * maxSpeed - dot(h.p, h.p);
-        if (disc <= 0.0f) return i;
-        /* a NaN discriminant takes neither branch of ORCA.cpp:498-506: the
-           constraint is passed over */
-        if (!(disc > 0.0f)) continue;
-        float sq = sqrtf(disc);
-        float lo = -dirPointDot - sq;
-        float hi = -dirPointDot + sq;
-        int lo_src = -1, hi_src = -1;
-        for (int j = 0; j < i; j++) {
-            Con g = get(j);
-            float den = det(right(h.n), right(g.n));
-            float num = det(right(g.n), h.p - g.p);
-            if (fabsf(den) <= kEps) {
-                if (num < 0.0f) return i;
-                continue;
-            }
-            const float t = num / den;
-            if (den >= 0.0f) { /* std::min(right, t) */
-                if (TRACE && t < hi) hi_src = j;
-                hi = (t < hi) ? t : hi;
-            } else { /* std::max(left, t) */
-                if (TRACE && lo < t) lo_src = j;
-                lo = (lo < t) ? t : lo;
-            }
-            if (lo > hi) return i;
-        }
-        if (useDirOpt) {
-            if (dot(opt, right(h.n)) > 0) *out = h.p + right(h.n) * hi;
-            else *out = h.p + right(h.n) * lo;
-        } else {
-            float t = dot(right(h.n), opt - h.p);
-            if (t < lo) {
-                *out = h.p + right(h.n) * lo;
-                if (TRACE) { tr->h = i; tr->src = lo_src < 0 ? 1 : 2; tr->j = lo_src; }
-            } else if (t > hi) {
-                *out = h.p + right(h.n) * hi;
-                if (TRACE) { tr->h = i; tr->src = hi_src < 0 ? 1 : 2; tr->j = hi_src; }
-            } else {
-                *out = h.p + right(h.n) * t;
-                if (TRACE) { tr->h = i; tr->src = 0; tr->j = -1; }
-            }
-        }
-    }
+    *out = lp2d_start(opt, maxSpeed, useDirOpt);
+    for (int i = 0; i < n; i++)
+        if (!lp2d_step<Get, TRACE>(get, i, get(i), opt, maxSpeed, useDirOpt, out, tr)) return i;
     return n;
 }
 
@@ -652,8 +668,17 @@ EG_HD void lp3d(const Get& get, int n, int nObst, float maxSpeed, int failed, V2
         Con ci = get(i);
         V2 dir = right(ci.n);
         if (det(dir, ci.p - *out) <= maxPen) continue;
+        /* RandomizedLP over the projected lines -- the obstacle constraints,
+           then the bisectors in order -- taking each bisector as soon as it
+           is built: the same steps as building them all first, and the
+           bisectors after a failing line are never read */
+        const V2 temp = *out;
+        Lp3dProj<Get> pg{&get, proj, nObst};
+        *out = lp2d_start(ci.n, maxSpeed, true);
+        bool ok = true;
+        for (int q = 0; q < nObst && ok; q++) ok = lp2d_step(pg, q, get(q), ci.n, maxSpeed, true, out);
         int m = 0;
-        for (int j = nObst; j < i; j++) {
+        for (int j = nObst; j < i && ok; j++) {
             Con cj = get(j);
             float dt = det(right(ci.n), right(cj.n));
             V2 np_;
@@ -674,11 +699,11 @@ EG_HD void lp3d(const Get& get, int n, int nObst, float maxSpeed, int failed, V2
             Con nc;
             nc.p = np_;
             nc.n = normalized(cj.n - ci.n);
-            proj[m++] = nc;
+            proj[m] = nc;
+            ok = lp2d_step(pg, nObst + m, nc, ci.n, maxSpeed, true, out);
+            m++;
         }
-        V2 temp = *out;
-        Lp3dProj<Get> pg{&get, proj, nObst};
-        if (lp2d(pg, nObst + m, ci.n, maxSpeed, true, out) < nObst + m) *out = temp;
+        if (!ok) *out = temp; /* ORCA.cpp:658-664 */
         maxPen = det(dir, ci.p - *out);
     }
 }

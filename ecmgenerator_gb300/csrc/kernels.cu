@@ -276,7 +276,7 @@ __device__ void knn_grid(Knn<K>& s, int k, V2 p, float rnb, float r2, const V2* 
    than 32 agents, when the table ends before the search could (sparse
    crowds) or when the agent is outside the grid, the search returns false
    and the caller runs the 64-bit (d2, slot) search (knn_grid). */
-constexpr int kTmplR = 5, kTmplCap = (2 * kTmplR + 1) * (2 * kTmplR + 1);
+constexpr int kTmplR = 5;
 /* bound per axis from the quarter [0, 1/2] of cell 0 to cell d, in half cells */
 constexpr int tmpl_half(int d) { return d >= 1 ? 2 * d - 1 : (d <= -1 ? 2 * (-d - 1) : 0); }
 /* the table holds the cells whose bound is at most kTmplR cells: every cell
@@ -706,6 +706,11 @@ __device__ void orca_tick(const TickArgs& a, int t)
     const int* nbr = a.nbr + (size_t)t * a.k;
     constexpr int MC = K + kMaxObstCons; /* constraint capacity */
     Con cons[MC];
+    LocalGet get{cons};
+    /* the plain tick takes each constraint into RandomizedLP as soon as it is
+       built (the LP's steps in the same order as over the finished list) */
+    V2 v = lp2d_start(pv, maxSpeed, false);
+    int failed2 = -1;
     int m = 0;
     bool overflow = false;
     const float range = a.tau_o * maxSpeed + clr;
@@ -729,8 +734,13 @@ __device__ void orca_tick(const TickArgs& a, int t)
             Con c;
             if (FULL ? obstacle_constraint(o, L, pos, vel, clr, a.tau_o, &c)
                      : obstacle_constraint_inl(o, L, pos, vel, clr, a.tau_o, &c)) {
-                if (m < MC - K) cons[m++] = c;
-                else overflow = true;
+                if (m < MC - K) {
+                    cons[m] = c;
+                    if (!FULL && failed2 < 0 && !lp2d_step(get, m, c, pv, maxSpeed, false, &v)) failed2 = m;
+                    m++;
+                } else {
+                    overflow = true;
+                }
             }
         }
     }
@@ -741,23 +751,23 @@ __device__ void orca_tick(const TickArgs& a, int t)
             /* inline in the plain kernel (no other callers compete for the
                instruction cache there), out of line in the full one */
             if (FULL)
-                cons[m++] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
-                                                a.inv_tau_a);
+                cons[m] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
+                                              a.inv_tau_a);
             else
-                cons[m++] = agent_constraint(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
-                                             a.inv_tau_a);
+                cons[m] = agent_constraint(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
+                                           a.inv_tau_a);
         } else {
             /* kd-tree mode: a cache entry left by an earlier agent that is
                not in this tick's grid; its slot is not written this tick */
             const int sl = -j - 1;
-            cons[m++] = agent_constraint_ni(pos, vel, clr, a.pos[sl], a.vel[sl], a.clear[sl], a.tau_a, a.dt,
-                                            a.inv_tau_a);
+            cons[m] = agent_constraint_ni(pos, vel, clr, a.pos[sl], a.vel[sl], a.clear[sl], a.tau_a, a.dt,
+                                          a.inv_tau_a);
         }
+        if (!FULL && failed2 < 0 && !lp2d_step(get, m, cons[m], pv, maxSpeed, false, &v)) failed2 = m;
+        m++;
     }
     if (overflow) atomicOr(&a.counters[C_ERROR], ECMG_DEV_ERR_CONSTRAINTS);
 
-    V2 v;
-    LocalGet get{cons};
     int failed = -1;
     if (FULL && (a.cls || a.cls_slot)) { /* learned proposal: accepted only when the exact check passes */
         const int c = a.cls_slot ? a.cls_slot[slot] : a.cls[t];
@@ -772,8 +782,10 @@ __device__ void orca_tick(const TickArgs& a, int t)
             LpTrace tr;
             failed = lp2d<LocalGet, true>(get, m, pv, maxSpeed, false, &v, &tr);
             a.label[t] = (unsigned char)label_of(tr, failed, m, nObst);
-        } else {
+        } else if (FULL) {
             failed = lp2d(get, m, pv, maxSpeed, false, &v);
+        } else {
+            failed = failed2 < 0 ? m : failed2;
         }
         if (failed < m) {
             lp3d_local<MC>(cons, m, nObst, maxSpeed, failed, &v, a.lp3d_fp64 != 0);
