@@ -56,3 +56,50 @@ def test_knn_noalloc_rejects_oversize(lib):
     rc = lib.ecmg_knn_noalloc(pos.data_ptr(), act.data_ptr(), n, 4, 1.0, 0.0, 0.0, 100.0, 100.0, 1.0,
                               out.data_ptr(), out.data_ptr(), None)
     assert rc == 3  # ECMG_ERR_BOUND, before any device work
+
+
+def test_knn_noalloc_captured_in_a_cuda_graph(lib):
+    """after a first call outside capture (which resolves the array's device
+    address), a call captured into a CUDA graph replays correctly: the query
+    makes no host-to-device copy and no allocation, so the graph holds only
+    its memsets and kernels and recomputes from the current positions"""
+    import torch
+
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(9)
+    n, k, r, box, cell = 12000, 12, 2.5, (0.0, 0.0, 50.0, 50.0), 1.2
+
+    def fresh():
+        return torch.from_numpy(rng.uniform(-1.0, 51.0, (n, 2)).astype(np.float32)).to(dev)
+
+    pos = fresh()
+    act = torch.from_numpy((rng.uniform(0, 1, n) < 0.8).astype(np.uint8)).to(dev)
+    ids = torch.full((n, k), -9, dtype=torch.int32, device=dev)
+    cnt = torch.full((n,), -9, dtype=torch.int32, device=dev)
+    s = torch.cuda.Stream()
+    args = lambda: (pos.data_ptr(), act.data_ptr(), n, k, r, *box, cell, ids.data_ptr(), cnt.data_ptr(),  # noqa: E731
+                    s.cuda_stream)
+    assert lib.ecmg_knn_noalloc(*args()) == 0
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s, capture_error_mode="thread_local"):
+        rc = lib.ecmg_knn_noalloc(*args())
+    assert rc == 0
+    need = lib.ecmg_knn_scratch_bytes(n, *box, cell)
+    scratch = torch.empty(need, dtype=torch.uint8, device=dev)
+    for _ in range(2):
+        pos.copy_(fresh())
+        ids.fill_(-9)
+        cnt.fill_(-9)
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        ref_ids = torch.full((n, k), -5, dtype=torch.int32, device=dev)
+        ref_cnt = torch.zeros(n, dtype=torch.int32, device=dev)
+        assert lib.ecmg_knn(pos.data_ptr(), act.data_ptr(), n, k, r, *box, cell, ref_ids.data_ptr(),
+                            ref_cnt.data_ptr(), scratch.data_ptr(), need, None) == 0
+        torch.cuda.synchronize()
+        live = act.cpu().numpy() == 1
+        assert np.array_equal(cnt.cpu().numpy(), ref_cnt.cpu().numpy())
+        assert np.array_equal(ids.cpu().numpy()[live], ref_ids.cpu().numpy()[live])
+        assert ref_cnt.cpu().numpy()[live].mean() > 1.0
