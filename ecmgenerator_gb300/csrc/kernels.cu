@@ -732,8 +732,7 @@ __device__ void orca_tick(const TickArgs& a, int t)
             int L = items ? items[q] : q;
             if (!obstacle_in_range(o, L, pos, rsq)) continue;
             Con c;
-            if (FULL ? obstacle_constraint(o, L, pos, vel, clr, a.tau_o, &c)
-                     : obstacle_constraint_inl(o, L, pos, vel, clr, a.tau_o, &c)) {
+            if (obstacle_constraint_inl(o, L, pos, vel, clr, a.tau_o, &c)) {
                 if (m < MC - K) {
                     cons[m] = c;
                     if (!FULL && failed2 < 0 && !lp2d_step(get, m, c, pv, maxSpeed, false, &v)) failed2 = m;
@@ -750,12 +749,8 @@ __device__ void orca_tick(const TickArgs& a, int t)
         if (j >= 0) {
             /* inline in the plain kernel (no other callers compete for the
                instruction cache there), out of line in the full one */
-            if (FULL)
-                cons[m] = agent_constraint_ni(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
-                                              a.inv_tau_a);
-            else
-                cons[m] = agent_constraint(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
-                                           a.inv_tau_a);
+            cons[m] = agent_constraint(pos, vel, clr, a.s_pos[j], a.s_vel[j], a.s_clear[j], a.tau_a, a.dt,
+                                       a.inv_tau_a);
         } else {
             /* kd-tree mode: a cache entry left by an earlier agent that is
                not in this tick's grid; its slot is not written this tick */
