@@ -195,7 +195,7 @@ EG_HD int special_index(const EcmView& e, float y)
    contain p is listed in p's grid cell or, when p.y is the height of a quad
    corner, in that height's list; both lists are ascending, so the smaller of
    their first hits is the linear scan's first hit. */
-EG_NI int point_location(const EcmView& e, V2 p)
+EG_HD int point_location_inl(const EcmView& e, V2 p)
 {
     V2 q[4];
     int best = -1;
@@ -220,6 +220,10 @@ EG_NI int point_location(const EcmView& e, V2 p)
     return best;
 }
 
+/* the out-of-line copy of point_location_inl for the callers that only
+   need it now and then */
+EG_NI int point_location(const EcmView& e, V2 p) { return point_location_inl(e, p); }
+
 /* MathUtility::GetRayToLineSegmentIntersection (UtilityFunctions.cpp:323-349) */
 EG_HD bool ray_segment(V2 o, V2 d, V2 p1, V2 p2, V2* out)
 {
@@ -239,9 +243,10 @@ EG_HD bool ray_segment(V2 o, V2 d, V2 p1, V2 p2, V2* out)
 }
 
 /* ECM::RetractPoint (ECMGenerator/ECM.cpp:20-96) */
-EG_HD bool retract(const EcmView& e, V2 loc, V2* out, int* out_edge)
+/* cell: loc's point location when the caller has it already (-2: look it up) */
+EG_HD bool retract(const EcmView& e, V2 loc, V2* out, int* out_edge, int cell = -2)
 {
-    int c = point_location(e, loc);
+    int c = cell == -2 ? point_location(e, loc) : cell;
     if (c < 0) return false;
     int ed = c >> 1;
     int ip1 = e.he_target[2 * ed + 1], ip2 = e.he_target[2 * ed];
@@ -270,11 +275,11 @@ EG_HD bool retract(const EcmView& e, V2 loc, V2* out, int* out_edge)
    *out is written only where the reference writes outPoint; *no_retract is
    set when the failure is the retraction of pos itself. */
 EG_NI bool irm(const EcmView& e, V2 pos, const V2* path, int n, V2* out, bool* no_retract = nullptr,
-               int* edge = nullptr)
+               int* edge = nullptr, int cell = -2)
 {
     V2 r;
     int ed;
-    if (!retract(e, pos, &r, &ed)) {
+    if (!retract(e, pos, &r, &ed, cell)) {
         if (no_retract) *no_retract = true;
         return false;
     }

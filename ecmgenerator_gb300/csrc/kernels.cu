@@ -633,6 +633,9 @@ __device__ void attract_tick(const TickArgs& a, int t)
     const int slot = a.s_slot[t];
     const V2 pos = a.s_pos[t];
     const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
+    /* the point location of the retraction, issued before the path loads
+       (independent chains of dependent loads); unused when the agent arrives */
+    const int cell = point_location_inl(sc.ecm, pos);
 
     /* UpdateAttractionPointSystem (Simulator.cpp:538-590) */
     const int off = a.path_off[slot], np = a.path_len[slot];
@@ -656,7 +659,7 @@ __device__ void attract_tick(const TickArgs& a, int t)
         V2 ap = mk(0.0f, 0.0f); /* Point attractionPoint; (0,0) */
         bool no_retract = false;
         int red = -1;
-        if (irm(sc.ecm, pos, path, np, &ap, &no_retract, &red)) {
+        if (irm(sc.ecm, pos, path, np, &ap, &no_retract, &red, cell)) {
             attr = ap;
             a.attr[slot] = attr;
         } else if (a.replan_dev_fail && (no_retract || (red >= 0 && a.fail_edge[slot] == red))) {
@@ -1419,7 +1422,10 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
     e = cudaEventRecord(ev_fork, s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, ev_fork, 0);
     if (e != cudaSuccess) return e;
-    k_attract<<<gk, 128, 0, s2>>>(t);
+    int ao = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ao, k_attract, 128, 0);
+    const int ga = ao > 0 && gk > sms * ao ? sms * ao : gk; /* one wave, grid-stride */
+    k_attract<<<ga, 128, 0, s2>>>(t);
     if (after_attract) {
         e = after_attract(after_attract_user, s2, evflags);
         if (e != cudaSuccess) return e;
