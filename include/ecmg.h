@@ -399,7 +399,8 @@ ecmg_status ecmg_knn(const float* dev_pos, const unsigned char* dev_active, int 
    library until the process exits; a query needing more
    (ecmg_knn_scratch_bytes > the limit) returns ECMG_ERR_BOUND.  The first call
    on a device resolves the array's device address -- make it before any
-   stream capture.  The address is kept per device for its primary context:
+   stream capture; later calls may be captured into a CUDA graph (a query
+   enqueues only memsets and kernels, no host copies).  The address is kept per device for its primary context:
    other contexts made current through the driver API, and calls after a
    cudaDeviceReset, are not supported.  Calls share the array: overlapping
    calls on one device race.  Allocates nothing. */
