@@ -127,6 +127,7 @@ def load(build_if_missing: bool = False):
         "ecmg_planner_locate": (C.c_int, [vp, C.c_int, vp, vp]),
         "ecmg_planner_set_mode": (C.c_int, [vp, C.c_int]),
         "ecmg_set_planner_mode": (C.c_int, [vp, C.c_int]),
+        "ecmg_set_replan_overlap": (C.c_int, [vp, C.c_int]),
         "ecmg_save_state": (C.c_int, [vp, C.c_char_p]),
         "ecmg_load_state": (C.c_int, [vp, C.c_char_p]),
         "ecmg_tick": (C.c_int, [vp, C.c_int, C.POINTER(TickStats)]),

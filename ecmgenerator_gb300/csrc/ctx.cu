@@ -248,6 +248,27 @@ struct ecmg_ctx {
        failed for the slot's current goal and clearance (-1: none) */
     std::vector<int> fail_edge;
     DBuf<int> d_fail_edge;
+    /* re-plans whose searches run on a helper thread (built-in planner)
+       while the next tick's graph runs: that tick marks their agents pending
+       and steps them in k_fixup once the paths are in (ecmg_set_replan_overlap) */
+    struct PlanBatch {
+        std::vector<int> slot; /* ascending */
+        std::vector<V2> start, goal;
+        std::vector<float> clr;
+        std::vector<std::vector<V2>> res;
+        std::vector<char> ok;
+        std::vector<int> fe;
+        /* a persistent helper thread that drives the planner pool */
+        std::thread th;
+        std::mutex mu;
+        std::condition_variable cv, cv_done;
+        bool work = false, stop = false;
+        std::atomic<bool> done{true};
+        bool active = false; /* started and not yet applied (calling thread only) */
+    } batch;
+    int replan_overlap = 1; /* 0 off, 1 when a search outlasts its tick, 2 always */
+    long long batch_failed = 0; /* failed searches applied outside a tick, counted with the next one */
+    DBuf<int> d_pend;
     /* recording */
     bool record = false;
     DBuf<int> rec_nbr, rec_cnt, rec_fail, rec_ncons, rec_nobst;
@@ -353,6 +374,18 @@ static bool finite2(float a, float b) { return std::isfinite(a) && std::isfinite
 
 extern "C" {
 
+/* applies the re-plans still in flight (defined with the tick's re-plan
+   helpers); entry points that read or change paths, agents, the scene or the
+   planner call it first */
+static ecmg_status drain(ecmg_ctx* c);
+static void batch_stop(ecmg_ctx* c);
+#define DRAIN(c)                                            \
+    do {                                                    \
+        ecmg_status drain_status_ = drain(c);               \
+        if (drain_status_ != ECMG_OK) return drain_status_; \
+    } while (0)
+
+
 void ecmg_default_params(ecmg_params* p)
 {
     if (!p) return;
@@ -439,6 +472,7 @@ ecmg_status ecmg_create_batch(const ecmg_params* p, int n_scenes, const int* max
     CKC(c->d_clear.alloc(N)); CKC(c->d_speed.alloc(N)); CKC(c->d_active.alloc(N));
     CKC(c->path_off.alloc(N)); CKC(c->path_len.alloc(N)); CKC(c->key.alloc(N)); CKC(c->rank.alloc(N));
     CKC(c->destroyed_list.alloc(N)); CKC(c->replan_list.alloc(N)); CKC(c->replan_pos.alloc(N));
+    CKC(c->d_pend.alloc(N));
     CKC(c->s_slot.alloc(N)); CKC(c->s_pos.alloc(N)); CKC(c->s_vel.alloc(N)); CKC(c->s_clear.alloc(N));
     CKC(c->d_slot_scene.alloc(N));
     CKC(c->nbr.alloc(N * (size_t)prm.max_neighbors));
@@ -489,13 +523,14 @@ ecmg_status ecmg_create(const ecmg_params* p, int max_agents, ecmg_ctx** out)
 ecmg_status ecmg_destroy(ecmg_ctx* c)
 {
     if (!c) return ECMG_ERR_INVALID_ARG;
+    batch_stop(c); /* searches in flight are waited for; their results are not needed */
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto& g : c->graph)
         if (g) cudaGraphExecDestroy(g);
     DBuf<V2>* v2s[] = {&c->pos, &c->vel, &c->attr, &c->pref_vel, &c->replan_pos, &c->path_xy, &c->s_pos, &c->s_vel,
                        &c->rec_vorca};
     for (auto* b : v2s) b->free_();
-    DBuf<int>* is[] = {&c->path_off, &c->path_len, &c->key, &c->rank, &c->destroyed_list, &c->replan_list,
+    DBuf<int>* is[] = {&c->d_pend, &c->path_off, &c->path_len, &c->key, &c->rank, &c->destroyed_list, &c->replan_list,
                        &c->d_slot_scene, &c->nbr, &c->ncnt, &c->d_fail_edge, &c->s_slot, &c->cell_count, &c->cell_start, &c->scan_tmp, &c->counters,
                        &c->rec_nbr, &c->rec_cnt, &c->rec_fail, &c->rec_ncons, &c->rec_nobst};
     for (auto* b : is) b->free_();
@@ -558,6 +593,7 @@ static SceneState* scene_at(ecmg_ctx* c, int scene)
 
 ecmg_status ecmg_scene_set_obstacles(ecmg_ctx* c, int scene, const ecmg_obstacles* o)
 {
+    DRAIN(c);
     SceneState* sc = scene_at(c, scene);
     if (!sc || !o) return fail(c, ECMG_ERR_INVALID_ARG, "null argument or bad scene");
     if (o->n_obstacles < 0 || (o->n_obstacles > 0 && (!o->ring_offsets || !o->xy)))
@@ -590,6 +626,7 @@ ecmg_status ecmg_scene_set_obstacles(ecmg_ctx* c, int scene, const ecmg_obstacle
 
 ecmg_status ecmg_scene_set_ecm(ecmg_ctx* c, int scene, const ecmg_ecm* e)
 {
+    DRAIN(c);
     SceneState* sc = scene_at(c, scene);
     if (!sc || !e) return fail(c, ECMG_ERR_INVALID_ARG, "null argument or bad scene");
     if (e->n_vertices < 0 || e->n_edges < 0) return fail(c, ECMG_ERR_INVALID_ARG, "negative sizes");
@@ -660,6 +697,7 @@ ecmg_status ecmg_set_ecm(ecmg_ctx* c, const ecmg_ecm* e) { return ecmg_scene_set
 ecmg_status ecmg_set_planner_mode(ecmg_ctx* c, int mode)
 {
     if (!c || (mode != ECMG_PLANNER_FAST && mode != ECMG_PLANNER_REFERENCE)) return ECMG_ERR_INVALID_ARG;
+    DRAIN(c);
     if (mode != c->planner_mode) {
         c->planner_mode = mode;
         /* the failed-search memo belongs to the planner that made it */
@@ -669,9 +707,19 @@ ecmg_status ecmg_set_planner_mode(ecmg_ctx* c, int mode)
     return ECMG_OK;
 }
 
+ecmg_status ecmg_set_replan_overlap(ecmg_ctx* c, int on)
+{
+    if (!c) return ECMG_ERR_INVALID_ARG;
+    DRAIN(c);
+    if (on < 0 || on > 2) return fail(c, ECMG_ERR_INVALID_ARG, "overlap mode %d", on);
+    c->replan_overlap = on;
+    return ECMG_OK;
+}
+
 ecmg_status ecmg_set_planner(ecmg_ctx* c, ecmg_plan_fn fn, void* user)
 {
     if (!c) return ECMG_ERR_INVALID_ARG;
+    DRAIN(c);
     if ((fn == nullptr) != (c->plan_fn == nullptr)) c->graph_dirty = true; /* TickArgs::replan_dev_fail */
     c->plan_fn = fn;
     c->plan_user = user;
@@ -776,6 +824,7 @@ ecmg_status ecmg_scene_add_agents(ecmg_ctx* c, int scene, int n, const float* po
                                   const float* pref_speed, const int* path_off, const int* path_len,
                                   const float* path_xy, int* out_slots)
 {
+    DRAIN(c);
     SceneState* sc = scene_at(c, scene);
     if (!sc) return fail(c, ECMG_ERR_INVALID_ARG, "bad scene");
     if (n < 0 || (n > 0 && (!pos || !clearance || !pref_speed || !path_off || !path_len || !path_xy)))
@@ -914,6 +963,155 @@ ecmg_status ecmg_find_path(ecmg_ctx* c, float sx, float sy, float gx, float gy, 
 }
 
 /* page-locked and device tables of the location checks (spawn.cu) */
+/* ---- re-plans of a tick (Simulator::UpdatePath, Simulator.cpp:97-124) ----
+   From the tick-start position, served in slot order.  When no path is
+   found the agent keeps its previous path (the reference would keep an empty
+   one and index path.x[-1]).  The built-in planner is re-entrant, so the
+   searches of a tick run on several host threads. */
+
+/* applies search results in slot order: the new path uploaded behind the
+   queued device work, or the failed-search edge remembered */
+static ecmg_status apply_plans(ecmg_ctx* c, const std::vector<int>& slot, std::vector<std::vector<V2>>& res,
+                               const std::vector<char>& ok, const std::vector<int>& fe, long long* failed)
+{
+    for (size_t i = 0; i < slot.size(); i++) {
+        const int sl = slot[i];
+        if (ok[i]) {
+            c->paths[sl] = std::move(res[i]);
+            ecmg_status ps = upload_path(c, sl);
+            if (ps != ECMG_OK) return ps;
+        } else {
+            (*failed)++;
+            if (fe[i] >= 0 && c->fail_edge[sl] != fe[i]) {
+                c->fail_edge[sl] = fe[i];
+                ecmg_status fs = stage_copy(c, c->d_fail_edge.p + sl, &fe[i], sizeof(int));
+                if (fs != ECMG_OK) return fs;
+            }
+        }
+    }
+    return ECMG_OK;
+}
+
+/* the re-plans of `slot` (ascending) from `start`, now: on the planner
+   threads, or on the calling thread while a batch holds them */
+static ecmg_status plan_now(ecmg_ctx* c, const std::vector<int>& slot, const std::vector<V2>& start,
+                            long long* failed)
+{
+    const int m = (int)slot.size();
+    std::vector<std::vector<V2>> res(m);
+    std::vector<char> ok(m, 0);
+    std::vector<int> fe(m, -1);
+    auto one = [&](int i, PlanScratch& scr) {
+        const int sl = slot[i];
+        SceneState* sc = c->scenes[c->slot_scene[sl]].get();
+        ok[i] = plan(c, sc, start[i], c->paths[sl].back(), c->clear[sl], res[i], scr, &fe[i]) == ECMG_OK &&
+                !res[i].empty();
+    };
+    if (c->batch.active) {
+        for (int i = 0; i < m; i++) one(i, c->scratch);
+    } else {
+        plan_jobs(c, m, one);
+    }
+    return apply_plans(c, slot, res, ok, fe, failed);
+}
+
+/* the searches of the current batch (on the helper thread) */
+static void batch_run(ecmg_ctx* c)
+{
+    ecmg_ctx::PlanBatch& b = c->batch;
+    const int m = (int)b.slot.size();
+    auto one = [&](int i, PlanScratch& scr) {
+        SceneState* sc = c->scenes[c->slot_scene[b.slot[i]]].get();
+        b.ok[i] = plan(c, sc, b.start[i], b.goal[i], b.clr[i], b.res[i], scr, &b.fe[i]) == ECMG_OK &&
+                  !b.res[i].empty();
+    };
+    if (c->pool.size() == 0) {
+        PlanScratch scr;
+        for (int i = 0; i < m; i++) one(i, scr);
+    } else {
+        c->pool.run(m, [&](int i, int w) { one(i, c->pool.scratch[w]); });
+    }
+}
+
+/* the re-plans of `slot` (ascending) on the helper thread, which drives the
+   pool of planner threads; goals and clearances are taken now */
+static void batch_start(ecmg_ctx* c, const std::vector<int>& slot, const std::vector<V2>& start)
+{
+    ecmg_ctx::PlanBatch& b = c->batch;
+    const int m = (int)slot.size();
+    b.slot = slot;
+    b.start = start;
+    b.goal.resize(m);
+    b.clr.resize(m);
+    for (int i = 0; i < m; i++) {
+        b.goal[i] = c->paths[slot[i]].back();
+        b.clr[i] = c->clear[slot[i]];
+    }
+    b.res.assign(m, {});
+    b.ok.assign(m, 0);
+    b.fe.assign(m, -1);
+    c->pool.start(std::min(15, (int)std::max(1u, std::thread::hardware_concurrency()) - 1));
+    if (!b.th.joinable())
+        b.th = std::thread([c] {
+            ecmg_ctx::PlanBatch& b = c->batch;
+            for (;;) {
+                {
+                    std::unique_lock<std::mutex> l(b.mu);
+                    b.cv.wait(l, [&] { return b.work || b.stop; });
+                    if (b.stop) return;
+                    b.work = false;
+                }
+                batch_run(c);
+                {
+                    std::lock_guard<std::mutex> l(b.mu);
+                    b.done.store(true);
+                }
+                b.cv_done.notify_all();
+            }
+        });
+    b.active = true;
+    {
+        std::lock_guard<std::mutex> l(b.mu);
+        b.done.store(false);
+        b.work = true;
+    }
+    b.cv.notify_one();
+}
+
+/* waits for the helper's searches and applies them */
+static ecmg_status batch_apply(ecmg_ctx* c, long long* failed)
+{
+    ecmg_ctx::PlanBatch& b = c->batch;
+    if (!b.active) return ECMG_OK;
+    {
+        std::unique_lock<std::mutex> l(b.mu);
+        b.cv_done.wait(l, [&] { return b.done.load(); });
+    }
+    b.active = false;
+    return apply_plans(c, b.slot, b.res, b.ok, b.fe, failed);
+}
+
+/* stops the helper thread (the context is going away) */
+static void batch_stop(ecmg_ctx* c)
+{
+    ecmg_ctx::PlanBatch& b = c->batch;
+    if (!b.th.joinable()) return;
+    {
+        std::lock_guard<std::mutex> l(b.mu);
+        b.stop = true;
+    }
+    b.cv.notify_all();
+    b.th.join();
+    b.active = false;
+}
+
+/* every re-plan in flight applied: before anything that reads or changes
+   paths, agents, the scene or the planner between ticks */
+static ecmg_status drain(ecmg_ctx* c)
+{
+    return c ? batch_apply(c, &c->batch_failed) : ECMG_OK;
+}
+
 static cudaError_t ensure_check_buffers(ecmg_ctx* c)
 {
     if (c->h_cand) return cudaSuccess;
@@ -961,6 +1159,7 @@ ecmg_status ecmg_spawn_agent(ecmg_ctx* c, float sx, float sy, float gx, float gy
                              int* out_slot)
 {
     if (!c || !out_slot) return ECMG_ERR_INVALID_ARG;
+    DRAIN(c);
     *out_slot = -1;
     SceneState* sc = c->scenes[0].get();
     if (!finite2(sx, sy) || !finite2(gx, gy) || !std::isfinite(clearance) || !std::isfinite(pref_speed))
@@ -1474,6 +1673,7 @@ ecmg_status ecmg_spawn_random_pending(const ecmg_ctx* c, long long* n)
 ecmg_status ecmg_update_spawn_areas(ecmg_ctx* c, ecmg_tick_stats* stats)
 {
     if (!c) return ECMG_ERR_INVALID_ARG;
+    DRAIN(c);
     ecmg_tick_stats st{};
     auto h0 = std::chrono::steady_clock::now();
     CK(cudaStreamSynchronize(c->stream));
@@ -1501,6 +1701,7 @@ ecmg_status ecmg_get_spawned(const ecmg_ctx* c, int* slots, float* start_xy, flo
 ecmg_status ecmg_destroy_agent(ecmg_ctx* c, int slot)
 {
     if (!c || slot < 0 || slot >= c->max_agents) return fail(c, ECMG_ERR_INVALID_ARG, "bad slot");
+    DRAIN(c);
     if (!c->active[slot]) return fail(c, ECMG_ERR_INVALID_ARG, "slot %d is not active", slot);
     SceneState* sc = c->scenes[c->slot_scene[slot]].get();
     sc->num_agents--;
@@ -1515,6 +1716,7 @@ ecmg_status ecmg_destroy_agent(ecmg_ctx* c, int slot)
 ecmg_status ecmg_reset(ecmg_ctx* c)
 {
     if (!c) return ECMG_ERR_INVALID_ARG;
+    DRAIN(c);
     for (auto& scp : c->scenes) { /* Simulator.cpp:327-332 */
         SceneState* sc = scp.get();
         for (int i = sc->slot_base; i <= sc->last_idx; i++)
@@ -1533,6 +1735,7 @@ ecmg_status ecmg_reset(ecmg_ctx* c)
 ecmg_status ecmg_set_path(ecmg_ctx* c, int slot, const float* xy, int n)
 {
     if (!c || slot < 0 || slot >= c->max_agents || n < 1 || !xy) return fail(c, ECMG_ERR_INVALID_ARG, "bad path argument");
+    DRAIN(c);
     for (int i = 0; i < n; i++)
         if (!finite2(xy[2 * i], xy[2 * i + 1])) return fail(c, ECMG_ERR_INVALID_ARG, "non-finite path point");
     c->paths[slot].assign((const V2*)xy, (const V2*)(xy + 2 * (size_t)n));
@@ -1542,6 +1745,7 @@ ecmg_status ecmg_set_path(ecmg_ctx* c, int slot, const float* xy, int n)
 ecmg_status ecmg_get_path(ecmg_ctx* c, int slot, float* out_xy, int cap, int* out_n)
 {
     if (!c || slot < 0 || slot >= c->max_agents || !out_n) return ECMG_ERR_INVALID_ARG;
+    DRAIN(c);
     const auto& p = c->paths[slot];
     *out_n = (int)p.size();
     for (int i = 0; i < (int)p.size() && i < cap; i++) { out_xy[2 * i] = p[i].x; out_xy[2 * i + 1] = p[i].y; }
@@ -1876,6 +2080,17 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             while (sc->last_idx >= sc->slot_base && !c->active[sc->last_idx]) sc->last_idx--;
         }
         st.ticks++;
+        bool spawning = false;
+        for (auto& scp : c->scenes) spawning |= c->spawn_enabled && !scp->spawn_areas.empty();
+        /* re-plans of the last tick still in flight: their agents are marked
+           pending for this tick and stepped by k_fixup after it (the spawn
+           stage needs the planner threads and the paths: apply them first) */
+        if (c->batch.active && (spawning || c->global_last() < 0)) {
+            ecmg_status ds = batch_apply(c, &st.replans_failed);
+            if (ds != ECMG_OK) return ds;
+        }
+        st.replans_failed += c->batch_failed;
+        c->batch_failed = 0;
         if (c->spawn_enabled) { /* UpdateSpawnAreas (Simulator.cpp:317) */
             auto s0 = std::chrono::steady_clock::now();
             ecmg_status ss = spawn_stage(c, st);
@@ -1888,12 +2103,21 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         if (gs != ECMG_OK) return gs;
         std::memset(c->h_counters, 0, sizeof(int) * kCounters);
         c->h_counters[C_LAST] = last;
-        st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - hs).count();
         const bool use_model = c->model && c->gate_left == 0;
         if (c->model && !use_model) {
             c->gate_left--;
             st.gated++;
         }
+        const int npend = c->batch.active ? (int)c->batch.slot.size() : 0;
+        if (npend > 0) {
+            ecmg_status ps = stage_copy(c, c->d_pend.p, c->batch.slot.data(), sizeof(int) * (size_t)npend);
+            if (ps != ECMG_OK) return ps;
+            BinArgs bm;
+            TickArgs tm;
+            fill_args(c, bm, tm, use_model);
+            CK(launch_mark_pending(tm, c->d_pend.p, npend, c->stream));
+        }
+        st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - hs).count();
         if (c->prm.use_graph) {
             /* a graph bakes in launch sizes covering slots [0, max_agents) */
             if (c->graph_dirty) {
@@ -1922,21 +2146,36 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             CK(enqueue_tick(c, last + 1, use_model));
         }
         CK(cudaEventRecord(c->ev_t1, c->stream));
-        /* the lists are final after k_attract: bookkeeping and re-plans run
-           on the host while the rest of the tick runs on the device; path
-           uploads are queued behind the tick */
+        if (npend > 0) {
+            auto hb = std::chrono::steady_clock::now();
+            /* the last tick's searches, their paths queued behind this tick's
+               kernels, then the pending agents' step of this tick */
+            ecmg_status bs = batch_apply(c, &st.replans_failed);
+            if (bs != ECMG_OK) return bs;
+            BinArgs bf;
+            TickArgs tf;
+            fill_args(c, bf, tf, use_model);
+            CK(launch_fixup(tf, c->d_pend.p, npend, c->stream));
+            CK(cudaMemcpyAsync(c->h_counters + kCounters, c->counters.p, sizeof(int) * kCounters,
+                               cudaMemcpyDeviceToHost, c->stream));
+            st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - hb).count();
+        }
+        /* the lists of the attraction kernel are final after it: bookkeeping
+           and re-plans run on the host while the rest of the tick runs on the
+           device; path uploads are queued behind the tick */
         CK(cudaEventSynchronize(c->ev_mid));
         auto h0 = std::chrono::steady_clock::now();
         const int* mid = c->h_counters + 2 * kCounters;
-        int nd = mid[C_DESTROYED], nr = mid[C_REPLAN];
-        st.destroyed += nd;
-        st.replans += nr + mid[C_REPLAN_DEV];
+        const int nd_mid = mid[C_DESTROYED], nr = mid[C_REPLAN];
         st.replans_host += nr;
-        st.replans_failed += mid[C_REPLAN_DEV];
-        if (nd > 0) {
+        /* the destroys of a tick with a fix-up are known only after it */
+        auto destroy = [&](int nd) -> ecmg_status {
+            if (nd <= 0) return ECMG_OK;
             std::vector<int> d(std::min(nd, c->max_agents));
-            if ((int)d.size() <= ecmg_ctx::kListStage) std::memcpy(d.data(), c->h_lists, sizeof(int) * d.size());
-            else CK(cudaMemcpy(d.data(), c->destroyed_list.p, sizeof(int) * d.size(), cudaMemcpyDeviceToHost));
+            if ((int)d.size() <= ecmg_ctx::kListStage && npend == 0)
+                std::memcpy(d.data(), c->h_lists, sizeof(int) * d.size());
+            else
+                CK(cudaMemcpy(d.data(), c->destroyed_list.p, sizeof(int) * d.size(), cudaMemcpyDeviceToHost));
             std::sort(d.begin(), d.end()); /* DestroyAgent order: slot order of the loop */
             for (int s : d) {
                 SceneState* sc = c->scenes[c->slot_scene[s]].get();
@@ -1945,54 +2184,81 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
                 c->active[s] = 0;
                 sc->free_stack.push_back(s);
             }
+            return ECMG_OK;
+        };
+        if (npend == 0) {
+            ecmg_status ds = destroy(nd_mid);
+            if (ds != ECMG_OK) return ds;
         }
-        if (nr > 0 && c->replan_enabled) {
-            int m = std::min(nr, c->max_agents);
-            std::vector<int> r(m);
-            std::vector<V2> rp(m);
-            if (m <= ecmg_ctx::kListStage) {
-                std::memcpy(r.data(), c->h_lists + ecmg_ctx::kListStage, sizeof(int) * m);
-                std::memcpy(rp.data(), c->h_lists + 2 * ecmg_ctx::kListStage, sizeof(V2) * m);
+        /* the re-plan list [from, to) (ascending slots with their positions) */
+        auto replans = [&](int from, int to, std::vector<int>& r, std::vector<V2>& rp) -> ecmg_status {
+            to = std::min(to, c->max_agents);
+            const int m = to - from;
+            if (m <= 0) return ECMG_OK;
+            std::vector<int> r0(m);
+            std::vector<V2> p0(m);
+            if (to <= ecmg_ctx::kListStage && from == 0) {
+                std::memcpy(r0.data(), c->h_lists + ecmg_ctx::kListStage, sizeof(int) * m);
+                std::memcpy(p0.data(), c->h_lists + 2 * ecmg_ctx::kListStage, sizeof(V2) * m);
             } else {
-                CK(cudaMemcpy(r.data(), c->replan_list.p, sizeof(int) * m, cudaMemcpyDeviceToHost));
-                CK(cudaMemcpy(rp.data(), c->replan_pos.p, sizeof(V2) * m, cudaMemcpyDeviceToHost));
+                CK(cudaMemcpy(r0.data(), c->replan_list.p + from, sizeof(int) * m, cudaMemcpyDeviceToHost));
+                CK(cudaMemcpy(p0.data(), c->replan_pos.p + from, sizeof(V2) * m, cudaMemcpyDeviceToHost));
             }
             std::vector<int> order(m);
             for (int i = 0; i < m; i++) order[i] = i;
-            std::sort(order.begin(), order.end(), [&](int a, int b) { return r[a] < r[b]; });
-            /* Simulator::UpdatePath (Simulator.cpp:97-124) from the tick-start
-               position, served in slot order.  When no path is found the agent
-               keeps its previous path (the reference would keep an empty one and
-               index path.x[-1]).  The built-in planner is re-entrant, so the
-               searches of a tick run on several host threads. */
-            std::vector<std::vector<V2>> res(m);
-            std::vector<char> ok(m, 0);
-            std::vector<int> fe(m, -1);
-            plan_jobs(c, m, [&](int i, PlanScratch& scr) {
-                int q = order[i], sl = r[q];
-                SceneState* sc = c->scenes[c->slot_scene[sl]].get();
-                V2 goal = c->paths[sl].back();
-                ok[i] = plan(c, sc, rp[q], goal, c->clear[sl], res[i], scr, &fe[i]) == ECMG_OK && !res[i].empty();
-            });
+            std::sort(order.begin(), order.end(), [&](int x, int y) { return r0[x] < r0[y]; });
+            r.resize(m);
+            rp.resize(m);
             for (int i = 0; i < m; i++) {
-                int sl = r[order[i]];
-                if (ok[i]) {
-                    c->paths[sl] = res[i];
-                    ecmg_status ps = upload_path(c, sl);
-                    if (ps != ECMG_OK) return ps;
-                } else {
-                    st.replans_failed++;
-                    if (fe[i] >= 0 && c->fail_edge[sl] != fe[i]) {
-                        c->fail_edge[sl] = fe[i];
-                        ecmg_status fs = stage_copy(c, c->d_fail_edge.p + sl, &fe[i], sizeof(int));
-                        if (fs != ECMG_OK) return fs;
-                    }
-                }
+                r[i] = r0[order[i]];
+                rp[i] = p0[order[i]];
+            }
+            return ECMG_OK;
+        };
+        /* searches overlap the next tick when the built-in planner serves them
+           and no spawn stage needs the planner threads first */
+        const bool overlap = c->replan_overlap != 0 && !c->plan_fn && !spawning;
+        if (nr > 0 && c->replan_enabled) {
+            std::vector<int> r;
+            std::vector<V2> rp;
+            ecmg_status rs = replans(0, nr, r, rp);
+            if (rs != ECMG_OK) return rs;
+            if (overlap) {
+                batch_start(c, r, rp);
+            } else {
+                rs = plan_now(c, r, rp, &st.replans_failed);
+                if (rs != ECMG_OK) return rs;
             }
         }
         st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - h0).count();
         CK(cudaStreamSynchronize(c->stream));
         c->h_up_used = 0; /* every queued upload has been applied */
+        const int* fin = c->h_counters + kCounters;
+        if (npend > 0) {
+            /* the fix-up's destroys join the tick's; its re-plans (an agent whose
+               new path already fails) are served now */
+            ecmg_status ds = destroy(fin[C_DESTROYED]);
+            if (ds != ECMG_OK) return ds;
+            if (fin[C_REPLAN] > nr && c->replan_enabled) {
+                std::vector<int> r;
+                std::vector<V2> rp;
+                ecmg_status rs = replans(nr, fin[C_REPLAN], r, rp);
+                if (rs == ECMG_OK) rs = plan_now(c, r, rp, &st.replans_failed);
+                if (rs != ECMG_OK) return rs;
+                st.replans_host += fin[C_REPLAN] - nr;
+                CK(cudaStreamSynchronize(c->stream));
+                c->h_up_used = 0;
+            }
+        }
+        st.destroyed += fin[C_DESTROYED];
+        st.replans += fin[C_REPLAN] + fin[C_REPLAN_DEV];
+        st.replans_failed += fin[C_REPLAN_DEV];
+        /* searches that ended while the tick's kernels ran are applied now, as
+           re-plans served inside the tick; the others overlap the next tick */
+        if (c->batch.active && c->batch.done.load() && c->replan_overlap != 2) {
+            ecmg_status bs = batch_apply(c, &st.replans_failed);
+            if (bs != ECMG_OK) return bs;
+        }
         auto h1 = std::chrono::steady_clock::now();
         /* attraction and neighbour kernels run side by side: both are timed
            from their common start */
@@ -2058,6 +2324,7 @@ ecmg_status ecmg_tick(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
 ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* out)
 {
     if (!c || ticks_per_trial < 1) return ECMG_ERR_INVALID_ARG;
+    DRAIN(c);
     if (c->num_agents == 0) return fail(c, ECMG_ERR_STATE, "autotune needs agents");
     size_t N = (size_t)c->max_agents;
     DBuf<V2> sp, sv, sa, spv;
@@ -2207,6 +2474,7 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
 ecmg_status ecmg_set_neighbor_mode(ecmg_ctx* c, int mode)
 {
     if (!c || (mode != ECMG_NEIGHBORS_EXACT && mode != ECMG_NEIGHBORS_KDTREE)) return ECMG_ERR_INVALID_ARG;
+    DRAIN(c);
     if (mode == c->nbr_mode) return ECMG_OK;
     if (mode == ECMG_NEIGHBORS_KDTREE) {
         if (c->model || c->trace || c->cls_override)
@@ -2340,6 +2608,7 @@ ecmg_status ecmg_host_view(ecmg_ctx* c, int field, const void** out)
 ecmg_status ecmg_set_state(ecmg_ctx* c, int field, const void* src)
 {
     if (!c || !src) return ECMG_ERR_INVALID_ARG;
+    DRAIN(c);
     size_t N = (size_t)c->max_agents;
     CK(cudaStreamSynchronize(c->stream));
     switch (field) {
@@ -2408,6 +2677,7 @@ extern "C" {
 ecmg_status ecmg_save_state(ecmg_ctx* c, const char* path)
 {
     if (!c || !path) return ECMG_ERR_INVALID_ARG;
+    DRAIN(c);
     CK(cudaStreamSynchronize(c->stream));
     const size_t N = (size_t)c->max_agents;
     std::vector<V2> pos(N), vel(N), attr(N), pv(N);
@@ -2481,6 +2751,7 @@ ecmg_status ecmg_save_state(ecmg_ctx* c, const char* path)
 ecmg_status ecmg_load_state(ecmg_ctx* c, const char* path)
 {
     if (!c || !path) return ECMG_ERR_INVALID_ARG;
+    DRAIN(c);
     FILE* f = fopen(path, "rb");
     if (!f) return fail(c, ECMG_ERR_INVALID_ARG, "cannot read %s", path);
     SnapReader r{f};

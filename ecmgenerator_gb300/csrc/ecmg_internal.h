@@ -17,6 +17,11 @@ namespace ecmg {
 constexpr int kMaxObstCons = 24;
 constexpr int kMaxK = 32;
 
+/* device active flag: bit 0 active; kActivePending marks an active agent
+   whose re-plan from the previous tick is still being computed on the host
+   when the tick starts (its attraction and ORCA step come from k_fixup) */
+constexpr unsigned char kActivePending = 2;
+
 /* Learned active-set proposal (mlp.cu).  Features: 16 neighbours x 5 + 2,
    zero-padded to kMlpIn.  Classes of an agent's 2D LP result, in terms of
    its neighbour half-planes q (constraint index nObst + q):
@@ -172,6 +177,11 @@ cudaError_t launch_knn(const V2* pos, const unsigned char* active, int n, int k,
                        int* key, int* rank, int* cell_count, int* cell_start, int* s_slot, V2* s_pos,
                        int* scan_tmp, int scan_blocks, int* out_ids, int* out_cnt, cudaStream_t s);
 int scan_tmp_ints(int n);
+/* kernels.cu: mark the agents of `list` pending (before the tick's graph);
+   after the graph and the upload of their paths, their attraction and ORCA
+   step of the tick (k_fixup) */
+cudaError_t launch_mark_pending(const TickArgs& t, const int* list, int n, cudaStream_t s);
+cudaError_t launch_fixup(const TickArgs& t, const int* list, int n, cudaStream_t s);
 
 /* spawn.cu: Simulator::ValidSpawnLocation (Simulator.cpp:295-311) for a batch
    of candidate locations.  Candidates of one spawn area share a clearance;

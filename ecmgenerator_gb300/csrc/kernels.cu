@@ -631,6 +631,7 @@ __device__ __noinline__ void lp3d_local(const Con* cons, int m, int nObst, float
 __device__ void attract_tick(const TickArgs& a, int t)
 {
     const int slot = a.s_slot[t];
+    if (a.active[slot] & kActivePending) return; /* done by k_fixup once its new path is in */
     const V2 pos = a.s_pos[t];
     const SceneDev& sc = a.scenes[a.slot_scene ? a.slot_scene[slot] : 0];
     /* the point location of the retraction, issued before the path loads
@@ -694,7 +695,7 @@ template <int K, bool FULL = true>
 __device__ void orca_tick(const TickArgs& a, int t)
 {
     const int slot = a.s_slot[t];
-    if (!a.active[slot]) return;
+    if (a.active[slot] != 1) return; /* inactive, or waiting for its re-plan (k_fixup) */
     const V2 pos = a.s_pos[t];
     const V2 vel = a.s_vel[t];
     const float clr = a.s_clear[t];
@@ -883,6 +884,32 @@ __global__ void __launch_bounds__(128) k_attract(TickArgs a)
 {
     const int n = a.counters[C_NSORTED];
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) attract_tick(a, t);
+}
+
+/* agents whose re-plan is still being computed on the host when the tick
+   starts: the tick's attraction and ORCA kernels skip them */
+__global__ void k_mark_pending(TickArgs a, const int* list, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        a.active[list[i]] |= kActivePending;
+}
+
+/* the skipped step of those agents, after the tick's kernels and the upload
+   of their new paths: UpdateAttractionPointSystem with the new path, then
+   ApplyObstacleAvoidanceForce and the integration on the tick's snapshot and
+   neighbour lists (still in place until the next tick's binning) -- the
+   same functions on the same inputs as the tick's own kernels */
+template <int K, bool FULL>
+__global__ void __launch_bounds__(128) k_fixup(TickArgs a, const int* list, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int slot = list[i];
+        if (!(a.active[slot] & kActivePending)) continue;
+        a.active[slot] = 1;
+        const int t = a.cell_start[a.slot_bucket[slot]] + a.slot_rank[slot];
+        attract_tick(a, t);
+        orca_tick<K, FULL>(a, t);
+    }
 }
 
 /* proposal features of every grid-order agent (zeros for agents destroyed
@@ -1239,7 +1266,7 @@ __device__ void orca_warp(const TickArgs& a, int t, int lane, Con* cons, Con* bi
 {
     constexpr int MC = K + kMaxObstCons;
     const int slot = a.s_slot[t];
-    if (!a.active[slot]) return;
+    if (a.active[slot] != 1) return;
     const V2 pos = a.s_pos[t];
     const V2 vel = a.s_vel[t];
     const float clr = a.s_clear[t];
@@ -1514,6 +1541,24 @@ cudaError_t launch_tick(const BinArgs& b, const TickArgs& t, int max_slots, int*
         else full ? go(k_agents<32, true>) : go(k_agents<32, false>);
     }
     if (ev) cudaEventRecordWithFlags(ev[4], s, evflags);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mark_pending(const TickArgs& t, const int* list, int n, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    k_mark_pending<<<(n + 127) / 128, 128, 0, s>>>(t, list, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fixup(const TickArgs& t, const int* list, int n, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const bool full = t.cls || t.cls_slot || t.label || t.rec_cnt;
+    const int g = (n + 127) / 128;
+    if (t.k <= 8) full ? k_fixup<8, true><<<g, 128, 0, s>>>(t, list, n) : k_fixup<8, false><<<g, 128, 0, s>>>(t, list, n);
+    else if (t.k <= 16) full ? k_fixup<16, true><<<g, 128, 0, s>>>(t, list, n) : k_fixup<16, false><<<g, 128, 0, s>>>(t, list, n);
+    else full ? k_fixup<32, true><<<g, 128, 0, s>>>(t, list, n) : k_fixup<32, false><<<g, 128, 0, s>>>(t, list, n);
     return cudaGetLastError();
 }
 

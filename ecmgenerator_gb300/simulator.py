@@ -509,6 +509,13 @@ def set_neighbor_mode(sim: Simulator, mode: str = "kdtree"):
     sim._ck(sim.L.ecmg_set_neighbor_mode(sim.h, m))
 
 
+def set_replan_overlap(sim: Simulator, mode=1):
+    """re-plan searches overlapping the next tick (ecmg_set_replan_overlap;
+    same results in every mode): 1 (default) when a search outlasts its
+    tick, 2 always, 0 / False never"""
+    sim._ck(sim.L.ecmg_set_replan_overlap(sim.h, int(mode)))
+
+
 def set_planner_mode(sim: Simulator, mode: str = "reference"):
     """built-in planner of re-plans and spawns: 'reference' (default, the
     reference planner's paths) or 'fast' (opt-in), ecmg_set_planner_mode"""

@@ -159,6 +159,19 @@ ecmg_status ecmg_set_planner(ecmg_ctx* ctx, ecmg_plan_fn fn, void* user);
 #define ECMG_PLANNER_FAST 0
 #define ECMG_PLANNER_REFERENCE 1
 ecmg_status ecmg_set_planner_mode(ecmg_ctx* ctx, int mode);
+/* Re-plans overlapping the next tick (the built-in planner only, and not
+   while spawn areas need the planner at the start of a tick).  The searches
+   of a tick's re-plans start on host threads while the tick's neighbour and
+   ORCA kernels run.  Mode 1 (default): searches that end with the tick are
+   applied then, as re-plans served inside the tick; longer ones keep running
+   after ecmg_tick returns, and the next tick skips those agents in its
+   attraction and ORCA kernels and steps them, with their new paths, in a
+   small launch after its own kernels -- the same inputs and functions, so the
+   same results, the searches overlapping a whole tick of device work.
+   Mode 2: every search is carried into the next tick that way.  Mode 0: the
+   tick waits for its searches.  Every entry point that reads or changes
+   paths, agents, the scene or the planner waits for the searches first. */
+ecmg_status ecmg_set_replan_overlap(ecmg_ctx* ctx, int mode);
 
 /* Simulator::SpawnAgent (Simulator.cpp:168-200): ValidSpawnLocation, then a
    planned path.  *out_slot = slot, or -1 with ECMG_ERR_NO_SLOT /

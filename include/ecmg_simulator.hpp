@@ -105,6 +105,9 @@ public:
         m_Dirty = 0x7fu;
     }
     void SetPlanner(ecmg_plan_fn fn, void* user) { check(ecmg_set_planner(m_Ctx, fn, user), "ecmg_set_planner"); }
+    /* re-plan searches overlapping the next Update (ecmg_set_replan_overlap:
+       1 default, when a search outlasts its tick; 2 always; 0 never) */
+    void SetReplanOverlap(int mode) { check(ecmg_set_replan_overlap(m_Ctx, mode), "ecmg_set_replan_overlap"); }
 
     /* spawn / goal areas (Simulator.h:92-104); Update() runs their spawn stage */
     int AddSpawnArea(const Point& position, const Vec2& halfSize, const SpawnConfiguration& config, int ID = -1)

@@ -178,7 +178,7 @@ def test_failed_search_is_settled_on_the_device(c1_small, lib, port):
     """A re-plan whose search failed from an ECM edge fails again from that
     edge (same goal and clearance): the next failure is settled on the device,
     with the same outcome (the agent keeps its path)."""
-    from ecmgenerator_gb300.simulator import Planner, Simulator
+    from ecmgenerator_gb300.simulator import Planner, Simulator, set_replan_overlap
 
     scene, st, paths = c1_small
     pl = Planner(scene)
@@ -200,13 +200,24 @@ def test_failed_search_is_settled_on_the_device(c1_small, lib, port):
     assert pick is not None
     p0, goal = pick
     far = np.stack([goal + np.float32(0.5), goal]).astype(np.float32)
-    sim = Simulator(scene, 4, 1.0 / 60.0, max_neighbors=10, **ORCA)
-    slot = int(sim.add_agents(p0[None], [clr], [1.3], [far])[0])
-    s1 = sim.update()
-    assert (s1.replans, s1.replans_failed, s1.replans_host) == (1, 1, 1)
-    s2 = sim.update(ticks=5)
-    assert s2.replans == 5 and s2.replans_failed == 5 and s2.replans_host < 5
-    assert np.array_equal(sim.get_path(slot), far)
+    # with the searches overlapping the next tick, a failed search is counted
+    # in the tick that applies it; the totals are the same
+    totals = []
+    for overlap in (0, 2):
+        sim = Simulator(scene, 4, 1.0 / 60.0, max_neighbors=10, **ORCA)
+        set_replan_overlap(sim, overlap)
+        slot = int(sim.add_agents(p0[None], [clr], [1.3], [far])[0])
+        s1 = sim.update()
+        s2 = sim.update(ticks=5)
+        if not overlap:
+            assert (s1.replans, s1.replans_failed, s1.replans_host) == (1, 1, 1)
+            assert s2.replans == 5 and s2.replans_failed == 5 and s2.replans_host < 5
+        assert np.array_equal(sim.get_path(slot), far)
+        totals.append((s1.replans + s2.replans, s1.replans_failed + s2.replans_failed,
+                       s1.replans_host + s2.replans_host))
+        if not overlap:
+            sim.close()
+    assert totals[0] == totals[1]
     # a caller-supplied planner is always asked
     sim.set_planner(lambda *a: None)
     s3 = sim.update(ticks=3)
