@@ -133,6 +133,7 @@ def load(build_if_missing: bool = False):
         "ecmg_tick": (C.c_int, [vp, C.c_int, C.POINTER(TickStats)]),
         "ecmg_get_state": (C.c_int, [vp, C.c_int, vp]),
         "ecmg_host_view": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
+        "ecmg_set_host_mirror": (C.c_int, [vp, C.c_int]),
         "ecmg_set_state": (C.c_int, [vp, C.c_int, vp]),
         "ecmg_get_counts": (C.c_int, [vp, ip, ip, ip]),
         "ecmg_get_path": (C.c_int, [vp, C.c_int, vp, C.c_int, ip]),

@@ -293,6 +293,11 @@ struct ecmg_ctx {
     /* pinned staging */
     int* h_counters = nullptr; /* [3 * kCounters]: in, out, after k_attract */
     void* hview[4] = {nullptr, nullptr, nullptr, nullptr}; /* ecmg_host_view of the float2 fields */
+    /* ecmg_set_host_mirror: every tick ends with a copy of the slots it may
+       have moved into hview[position] and hview[velocity] (device addresses
+       below); stale after any other write of positions or velocities */
+    bool mirror = false, mirror_stale = true;
+    V2* mirror_dev[2] = {nullptr, nullptr};
     /* the first kListStage entries of the destroyed / re-plan lists, copied
        back by every tick (no extra copy when a tick's lists fit) */
     static constexpr int kListStage = 1024;
@@ -868,6 +873,7 @@ ecmg_status ecmg_scene_add_agents(ecmg_ctx* c, int scene, int n, const float* po
         std::vector<unsigned char> one((size_t)cnt, 1);
         CK(cudaMemcpy(c->pos.p + s0, pos + 2 * (size_t)i, sizeof(V2) * cnt, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(c->vel.p + s0, z.data(), sizeof(V2) * cnt, cudaMemcpyHostToDevice));
+        c->mirror_stale = true;
         CK(cudaMemcpy(c->pref_vel.p + s0, z.data(), sizeof(V2) * cnt, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(c->d_clear.p + s0, clearance + i, sizeof(float) * cnt, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(c->d_speed.p + s0, pref_speed + i, sizeof(float) * cnt, cudaMemcpyHostToDevice));
@@ -2160,6 +2166,11 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
                                cudaMemcpyDeviceToHost, c->stream));
             st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - hb).count();
         }
+        /* the getters' host arrays: slots [0, last] are all this tick can
+           have moved (spawns included); the copy runs while the host does
+           the tick's bookkeeping */
+        if (c->mirror && !c->mirror_stale)
+            CK(launch_mirror(c->pos.p, c->vel.p, c->mirror_dev[0], c->mirror_dev[1], last + 1, c->sms, c->stream));
         /* the lists of the attraction kernel are final after it: bookkeeping
            and re-plans run on the host while the rest of the tick runs on the
            device; path uploads are queued behind the tick */
@@ -2350,6 +2361,7 @@ ecmg_status ecmg_autotune(ecmg_ctx* c, int ticks_per_trial, ecmg_tune_result* ou
     auto restore = [&]() -> ecmg_status {
         CK(cudaMemcpy(c->pos.p, sp.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
         CK(cudaMemcpy(c->vel.p, sv.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
+        c->mirror_stale = true;
         CK(cudaMemcpy(c->attr.p, sa.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
         CK(cudaMemcpy(c->pref_vel.p, spv.p, sizeof(V2) * N, cudaMemcpyDeviceToDevice));
         CK(cudaMemcpy(c->d_active.p, sact.p, N, cudaMemcpyDeviceToDevice));
@@ -2591,8 +2603,19 @@ ecmg_status ecmg_host_view(ecmg_ctx* c, int field, const void** out)
     case ECMG_FIELD_VELOCITY:
     case ECMG_FIELD_PREF_VELOCITY:
     case ECMG_FIELD_ATTRACTION: {
+        if (c->mirror && field <= ECMG_FIELD_VELOCITY) {
+            /* kept by the ticks; refreshed here after any other write */
+            if (c->mirror_stale) {
+                CK(cudaMemcpyAsync(c->hview[0], c->pos.p, sizeof(V2) * N, cudaMemcpyDeviceToHost, c->stream));
+                CK(cudaMemcpyAsync(c->hview[1], c->vel.p, sizeof(V2) * N, cudaMemcpyDeviceToHost, c->stream));
+                CK(cudaStreamSynchronize(c->stream));
+                c->mirror_stale = false;
+            }
+            *out = c->hview[field];
+            return ECMG_OK;
+        }
         void*& h = c->hview[field];
-        if (!h) CK(cudaHostAlloc(&h, sizeof(V2) * N, cudaHostAllocDefault));
+        if (!h) CK(cudaHostAlloc(&h, sizeof(V2) * N, cudaHostAllocMapped));
         const V2* src = field == ECMG_FIELD_POSITION ? c->pos.p
                         : field == ECMG_FIELD_VELOCITY ? c->vel.p
                         : field == ECMG_FIELD_PREF_VELOCITY ? c->pref_vel.p : c->attr.p;
@@ -2605,6 +2628,26 @@ ecmg_status ecmg_host_view(ecmg_ctx* c, int field, const void** out)
     }
 }
 
+ecmg_status ecmg_set_host_mirror(ecmg_ctx* c, int on)
+{
+    if (!c || (on != 0 && on != 1)) return ECMG_ERR_INVALID_ARG;
+    if ((on != 0) == c->mirror) return ECMG_OK;
+    CK(cudaStreamSynchronize(c->stream));
+    if (on) {
+        const size_t N = (size_t)c->max_agents;
+        for (int f = 0; f < 2; f++) {
+            if (!c->hview[f]) CK(cudaHostAlloc(&c->hview[f], sizeof(V2) * N, cudaHostAllocMapped));
+            void* d = nullptr;
+            CK(cudaHostGetDevicePointer(&d, c->hview[f], 0));
+            c->mirror_dev[f] = (V2*)d;
+        }
+    }
+    c->mirror = on != 0;
+    c->mirror_stale = true;
+    c->graph_dirty = true; /* TickArgs::h_pos / h_vel */
+    return ECMG_OK;
+}
+
 ecmg_status ecmg_set_state(ecmg_ctx* c, int field, const void* src)
 {
     if (!c || !src) return ECMG_ERR_INVALID_ARG;
@@ -2612,8 +2655,14 @@ ecmg_status ecmg_set_state(ecmg_ctx* c, int field, const void* src)
     size_t N = (size_t)c->max_agents;
     CK(cudaStreamSynchronize(c->stream));
     switch (field) {
-    case ECMG_FIELD_POSITION: CK(cudaMemcpy(c->pos.p, src, sizeof(V2) * N, cudaMemcpyHostToDevice)); break;
-    case ECMG_FIELD_VELOCITY: CK(cudaMemcpy(c->vel.p, src, sizeof(V2) * N, cudaMemcpyHostToDevice)); break;
+    case ECMG_FIELD_POSITION:
+        CK(cudaMemcpy(c->pos.p, src, sizeof(V2) * N, cudaMemcpyHostToDevice));
+        c->mirror_stale = true;
+        break;
+    case ECMG_FIELD_VELOCITY:
+        CK(cudaMemcpy(c->vel.p, src, sizeof(V2) * N, cudaMemcpyHostToDevice));
+        c->mirror_stale = true;
+        break;
     case ECMG_FIELD_PREF_VELOCITY: CK(cudaMemcpy(c->pref_vel.p, src, sizeof(V2) * N, cudaMemcpyHostToDevice)); break;
     case ECMG_FIELD_ATTRACTION: CK(cudaMemcpy(c->attr.p, src, sizeof(V2) * N, cudaMemcpyHostToDevice)); break;
     case ECMG_FIELD_CLEARANCE:
@@ -2822,6 +2871,7 @@ ecmg_status ecmg_load_state(ecmg_ctx* c, const char* path)
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaMemcpy(c->pos.p, pos.data(), sizeof(V2) * N, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->vel.p, vel.data(), sizeof(V2) * N, cudaMemcpyHostToDevice));
+    c->mirror_stale = true;
     CK(cudaMemcpy(c->attr.p, attr.data(), sizeof(V2) * N, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->pref_vel.p, pv.data(), sizeof(V2) * N, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->d_clear.p, clear.data(), sizeof(float) * N, cudaMemcpyHostToDevice));

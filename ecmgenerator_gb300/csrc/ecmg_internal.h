@@ -181,6 +181,9 @@ int scan_tmp_ints(int n);
    after the graph and the upload of their paths, their attraction and ORCA
    step of the tick (k_fixup) */
 cudaError_t launch_mark_pending(const TickArgs& t, const int* list, int n, cudaStream_t s);
+/* pos / vel of slots [0, n) into page-locked host memory (device addresses
+   of it): 16-byte loads and stores, coalesced on both sides */
+cudaError_t launch_mirror(const V2* pos, const V2* vel, V2* h_pos, V2* h_vel, int n, int sms, cudaStream_t s);
 cudaError_t launch_fixup(const TickArgs& t, const int* list, int n, cudaStream_t s);
 
 /* spawn.cu: Simulator::ValidSpawnLocation (Simulator.cpp:295-311) for a batch

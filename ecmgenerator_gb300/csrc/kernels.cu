@@ -1551,6 +1551,32 @@ cudaError_t launch_mark_pending(const TickArgs& t, const int* list, int n, cudaS
     return cudaGetLastError();
 }
 
+__global__ void k_mirror(const float4* __restrict__ pos, const float4* __restrict__ vel, float4* h_pos,
+                         float4* h_vel, int n2, const V2* __restrict__ pos_tail, const V2* __restrict__ vel_tail,
+                         V2* h_pos_tail, V2* h_vel_tail)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+        const float4 p = pos[i], v = vel[i];
+        h_pos[i] = p;
+        h_vel[i] = v;
+    }
+    if (pos_tail && blockIdx.x == 0 && threadIdx.x == 0) {
+        *h_pos_tail = *pos_tail;
+        *h_vel_tail = *vel_tail;
+    }
+}
+
+cudaError_t launch_mirror(const V2* pos, const V2* vel, V2* h_pos, V2* h_vel, int n, int sms, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const int n2 = n / 2; /* pairs of slots as 16-byte words (the arrays are 256-byte aligned) */
+    const bool odd = n & 1;
+    const int g = std::max(1, std::min((n2 + 255) / 256, sms * 4));
+    k_mirror<<<g, 256, 0, s>>>((const float4*)pos, (const float4*)vel, (float4*)h_pos, (float4*)h_vel, n2,
+                               odd ? pos + n - 1 : nullptr, odd ? vel + n - 1 : nullptr, h_pos + n - 1, h_vel + n - 1);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_fixup(const TickArgs& t, const int* list, int n, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;

@@ -315,11 +315,18 @@ class Simulator:
         self._ck(self.L.ecmg_get_state(self.h, FIELD[field], _ptr(out)))
         return out
 
+    def set_host_mirror(self, on: bool = True):
+        """ecmg_set_host_mirror: every tick ends by writing the host views of
+        the positions and velocities (view() of those fields then returns
+        without a copy, and the arrays change with every tick)"""
+        self._ck(self.L.ecmg_set_host_mirror(self.h, 1 if on else 0))
+
     def view(self, field: str):
         """Read-only numpy view of the library's host copy of a field
         (ecmg_host_view), as the reference's getters return pointers into the
         Simulator's arrays: refreshed by this call, overwritten by the next
-        view of the same field."""
+        view of the same field (and by every tick for the positions and
+        velocities while set_host_mirror is on)."""
         p = C.c_void_p()
         self._ck(self.L.ecmg_host_view(self.h, FIELD[field], C.byref(p)))
         n = self.max_agents

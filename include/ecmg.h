@@ -290,6 +290,18 @@ ecmg_status ecmg_get_state(ecmg_ctx* ctx, int field, void* host_dst);
    this call).  The pointer stays valid until ecmg_destroy; its contents are
    those of this call until the next ecmg_host_view of the same field. */
 ecmg_status ecmg_host_view(ecmg_ctx* ctx, int field, const void** out);
+/* Host mirror of the positions and velocities (no reference counterpart:
+   the reference's getters point into arrays that Update itself writes).
+   on = 1: every tick ends by writing the positions and velocities of the
+   slots it may have moved into the page-locked host views of
+   ECMG_FIELD_POSITION and ECMG_FIELD_VELOCITY (a device-side copy that runs
+   while the host finishes the tick), so that ecmg_host_view of those fields
+   returns without a copy (it copies once after anything other than a tick
+   changed them: adding, spawning through ecmg_spawn_agent, ecmg_set_state,
+   ecmg_load_state, ecmg_autotune).  The two views are then rewritten by every
+   tick, as the reference's arrays are by Update.  on = 0 (default):
+   ecmg_host_view copies on every call. */
+ecmg_status ecmg_set_host_mirror(ecmg_ctx* ctx, int on);
 /* Overwrite slot-indexed state from the host (float[2*n] for the 2-vectors);
    used to start a tick from a given state. */
 ecmg_status ecmg_set_state(ecmg_ctx* ctx, int field, const void* host_src);

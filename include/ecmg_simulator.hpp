@@ -108,6 +108,9 @@ public:
     /* re-plan searches overlapping the next Update (ecmg_set_replan_overlap:
        1 default, when a search outlasts its tick; 2 always; 0 never) */
     void SetReplanOverlap(int mode) { check(ecmg_set_replan_overlap(m_Ctx, mode), "ecmg_set_replan_overlap"); }
+    /* positions and velocities written to the getters' host arrays by every
+       Update (ecmg_set_host_mirror) */
+    void SetHostMirror(bool on) { check(ecmg_set_host_mirror(m_Ctx, on ? 1 : 0), "ecmg_set_host_mirror"); }
 
     /* spawn / goal areas (Simulator.h:92-104); Update() runs their spawn stage */
     int AddSpawnArea(const Point& position, const Vec2& halfSize, const SpawnConfiguration& config, int ID = -1)
