@@ -60,32 +60,38 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 }
 
 /* ------------------------------------------------------------------------
- * Inference on the 5th-generation tensor cores (tcgen05).  One CTA of eight
- * warps per SM, persistent over tiles of 128 agents, as two independent
- * pipelines: warps 0-3 run the tiles of slot 0, warps 4-7 those of slot 1,
- * each with its own feature and hidden tiles in shared memory, its own 256
- * tensor-memory columns and its own named barrier, so that one group's
- * epilogue runs while the other group's MMA chain occupies the tensor core.
- * Per tile three chains (M = 128, N = 128 / 128 / 160, K = 96 / 128 / 128
- * in steps of 16), each issued by the group's first thread and completed
- * through the group's mbarrier (FP32 accumulators, 128 lanes x N columns).
- * Epilogue: warp w reads lanes 32 (w mod 4) .. +31 (its rows) with
- * tcgen05.ld -- bias + GELU (tanh.approx) + BF16 into the group's hidden
- * tile, or bias + argmax over the 160 outputs (first maximum wins).
- * Operands sit in shared memory in the canonical K-major layout without
- * swizzle: 8-row x 16-byte core matrices; the row groups of one 8-column
- * chunk are adjacent (stride byte offset 128), chunks R x 16 bytes apart
- * (leading byte offset) for an operand of R rows.  One chunk of a 128-row
- * feature tile is one 2 KB TMA box (8 columns x 128 rows): a group's next
- * tile is requested as soon as its first layer has consumed the current
- * one.  Every wait is bounded (spin limit); on a timeout the group sets the
- * error bit, waits for its copy and MMA chain in flight, and the CTA frees
- * its tensor memory and returns.
+ * Inference on the 5th-generation tensor cores (tcgen05).  One CTA of
+ * sixteen warps per SM, persistent over tiles of 128 agents, as four
+ * independent pipelines: warps 4g .. 4g+3 run the tiles of pipeline g, each
+ * with its own operand tile in shared memory, its own 128 tensor-memory
+ * columns and its own named barrier, so that the epilogues of some
+ * pipelines run while another's MMA chain occupies the tensor core (the
+ * epilogues, not the tensor core, bound the kernel).  Per tile four chains
+ * (M = 128; N = 128 / 128 / 128 + 32, layer 3 in two chains over the same
+ * columns; K = 96 / 128 / 128 in steps of 16), each issued by the
+ * pipeline's first thread and completed through its mbarrier (FP32
+ * accumulators, 128 lanes x N columns).  Epilogue: warp w reads lanes
+ * 32 (w mod 4) .. +31 (its rows) with tcgen05.ld, the load of the next 16
+ * columns in flight while the current ones are used -- bias + GELU
+ * (tanh.approx) + BF16 into the operand tile, or bias + argmax over the 160
+ * outputs (first maximum wins).  The operand tile holds the features (one
+ * TMA copy), then each hidden layer over the operand the previous chain has
+ * finished reading; the next tile's copy is requested when the last chain
+ * of a tile has completed.  Operands sit in shared memory in the canonical
+ * K-major layout without swizzle: 8-row x 16-byte core matrices; the row
+ * groups of one 8-column chunk are adjacent (stride byte offset 128), chunks
+ * R x 16 bytes apart (leading byte offset) for an operand of R rows.  One
+ * chunk of a 128-row feature tile is one 2 KB TMA box (8 columns x 128
+ * rows).  Every wait is bounded (spin limit); on a timeout the pipeline sets
+ * the error bit, waits for its copy and MMA chain in flight, and the CTA
+ * frees its tensor memory and returns.
  * ---------------------------------------------------------------------- */
 constexpr int kTile = 128;      /* agents per tile (MMA M) */
-constexpr int kSlotCols = 256;  /* tensor-memory columns per slot: >= the widest accumulator (160) */
-constexpr int kTmemCols = 2 * kSlotCols;
-constexpr int kInferThreads = 256;
+constexpr int kGroups = 4;      /* independent pipelines per CTA */
+constexpr int kSlotCols = 128;  /* tensor-memory columns per pipeline (layer 3 runs as N = 128 + 32) */
+constexpr int kTmemCols = kGroups * kSlotCols;
+constexpr int kInferThreads = 128 * kGroups;
+constexpr int kOutA = 128;      /* layer-3 outputs of the first chain */
 constexpr int kSpinDefault = 1 << 22;
 
 /* byte offset of element (r, k) of an [R x K] bf16 operand in that layout */
@@ -97,8 +103,11 @@ __host__ __device__ constexpr int tc_off(int r, int k, int R)
 constexpr int kW1B = HID * IN * 2, kW2B = HID * HID * 2, kW3B = OUT * HID * 2; /* B operands: N rows x K */
 constexpr int kWB = kW1B + kW2B + kW3B;
 constexpr int kXB = kTile * IN * 2, kHB = kTile * HID * 2;
-/* weights, two feature tiles, two hidden tiles, biases, barriers */
-constexpr size_t kInferSmem = (size_t)kWB + 2 * kXB + 2 * kHB + sizeof(float) * (2 * HID + OUT) + 64;
+/* weights, one operand tile per pipeline (the feature tile, then each hidden
+   tile over it), biases, tensor-memory address and barriers */
+constexpr size_t kInferSmem = (size_t)kWB + kGroups * kHB + sizeof(float) * (2 * HID + OUT) + 128;
+static_assert(kXB <= kHB, "a feature tile fits the pipeline's operand tile");
+static_assert(kInferSmem <= 232448, "shared memory of one CTA");
 
 /* shared-memory matrix descriptor (no swizzle) */
 __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
@@ -120,13 +129,15 @@ __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence:
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-/* D[tmem] (+)= A[M x K] * B[K x N], K-steps of 16 (two chunks), one thread */
-__device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_saddr, uint32_t b_saddr, int K, int N)
+/* D[tmem] (+)= A[M x K] * B[K x N], K-steps of 16 (two chunks), one thread;
+   B is N rows of an operand packed with R rows (R = N, or a row block of a
+   taller operand: chunks R x 16 bytes apart) */
+__device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_saddr, uint32_t b_saddr, int K, int N, int R)
 {
     const uint32_t id = tc_idesc(kTile, N);
     for (int ks = 0; ks < K / 16; ks++) {
         const uint64_t ad = tc_sdesc(a_saddr + ks * 2 * (kTile * 16), kTile * 16, 128);
-        const uint64_t bd = tc_sdesc(b_saddr + ks * 2 * (N * 16), N * 16, 128);
+        const uint64_t bd = tc_sdesc(b_saddr + ks * 2 * (R * 16), R * 16, 128);
         const uint32_t acc = ks > 0 ? 1u : 0u;
         asm volatile(
             "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
@@ -168,18 +179,44 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, int li
     return false;
 }
 
-/* 16 consecutive fp32 columns of this thread's lane */
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
+/* 16 fp32 columns of this thread's lane, issued without waiting; the
+   registers are valid after tmem_wait16 on them (the wait takes them as
+   operands, so that no use is scheduled before it) */
+__device__ __forceinline__ void tmem_issue16(uint32_t taddr, uint32_t (&r)[16])
 {
-    uint32_t r[16];
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait16(uint32_t (&r)[16])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15])
+                 :
+                 : "memory");
+}
+/* f(registers, column) over `cols` columns (a multiple of 32) in chunks of
+   16, the load of each chunk in flight while the previous one is used */
+template <class F>
+__device__ __forceinline__ void tmem_chunks(uint32_t taddr, int cols, F&& f)
+{
+    uint32_t ra[16], rb[16];
+    tmem_issue16(taddr, ra);
+    tmem_wait16(ra);
+#pragma unroll 1
+    for (int c = 0; c < cols; c += 32) {
+        tmem_issue16(taddr + (uint32_t)(c + 16), rb);
+        f(ra, c);
+        tmem_wait16(rb);
+        const bool more = c + 32 < cols;
+        if (more) tmem_issue16(taddr + (uint32_t)(c + 32), ra);
+        f(rb, c + 16);
+        if (more) tmem_wait16(ra);
+    }
 }
 
 /* W [K x N] row-major FP32 -> BF16 B operand (N rows x K) in the tc layout */
@@ -234,7 +271,14 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
           "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
           "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                   "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
+                   "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+                 :
+                 : "memory"); /* the registers are tied to the wait: no use before it */
 #pragma unroll
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
@@ -263,14 +307,13 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     unsigned char* sW1 = sm;
     unsigned char* sW2 = sW1 + kW1B;
     unsigned char* sW3 = sW2 + kW2B;
-    unsigned char* sX = sW3 + kW3B;  /* [2][kXB] */
-    unsigned char* sH = sX + 2 * kXB; /* [2][kHB] */
-    float* sb = reinterpret_cast<float*>(sH + 2 * kHB);
+    unsigned char* sT = sW3 + kW3B; /* [kGroups][kHB] operand tiles */
+    float* sb = reinterpret_cast<float*>(sT + kGroups * kHB);
     uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sb + 2 * HID + OUT);
     uint64_t* s_mbar = reinterpret_cast<uint64_t*>(
-        (reinterpret_cast<uintptr_t>(s_tmem + 2) + 7) & ~(uintptr_t)7); /* [0..1] MMA done, [2..3] tile landed */
+        (reinterpret_cast<uintptr_t>(s_tmem + 2) + 7) & ~(uintptr_t)7); /* [g] MMA done, [kGroups + g] tile landed */
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int g = warp >> 2, quad = warp & 3, gt = tid & 127; /* group = slot, TMEM lane quarter, thread in group */
+    const int g = warp >> 2, quad = warp & 3, gt = tid & 127; /* pipeline, TMEM lane quarter, thread in group */
     const int bar_id = 1 + g;
     const int n = n_ptr ? *n_ptr : n_fixed;
 
@@ -279,7 +322,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     for (int i = tid; i < 2 * HID + OUT; i += blockDim.x) sb[i] = bias[i];
     const uint32_t mbar0 = (uint32_t)__cvta_generic_to_shared(s_mbar);
     if (tid == 0) {
-        for (int b = 0; b < 4; b++)
+        for (int b = 0; b < 2 * kGroups; b++)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0 + 8u * b) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -294,18 +337,17 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    /* from here on the two groups run independent pipelines */
+    /* from here on the groups run independent pipelines */
     const uint32_t tmem = *s_tmem + (uint32_t)(g * kSlotCols);
     const uint32_t lane_base = tmem + ((uint32_t)(quad * 32) << 16);
-    const uint32_t aX = (uint32_t)__cvta_generic_to_shared(sX + g * kXB);
-    const uint32_t aH = (uint32_t)__cvta_generic_to_shared(sH + g * kHB);
-    unsigned char* hbuf = sH + g * kHB;
+    const uint32_t aT = (uint32_t)__cvta_generic_to_shared(sT + g * kHB);
+    unsigned char* tbuf = sT + g * kHB;
     const uint32_t aW1 = (uint32_t)__cvta_generic_to_shared(sW1), aW2 = (uint32_t)__cvta_generic_to_shared(sW2),
                    aW3 = (uint32_t)__cvta_generic_to_shared(sW3);
-    const uint32_t mb_mma = mbar0 + 8u * (uint32_t)g, mb_x = mbar0 + 8u * (uint32_t)(2 + g);
+    const uint32_t mb_mma = mbar0 + 8u * (uint32_t)g, mb_x = mbar0 + 8u * (uint32_t)(kGroups + g);
     const int row = quad * 32 + lane;
     const int ntiles = (n + kTile - 1) / kTile;
-    int tile = (int)blockIdx.x + g * (int)gridDim.x; /* slot g: tiles blockIdx.x + (2 j + g) gridDim.x */
+    int tile = (int)blockIdx.x + g * (int)gridDim.x; /* group g: tiles blockIdx.x + (kGroups j + g) gridDim.x */
     uint32_t ph_mma = 0u, ph_x = 0u;
     bool mma_pending = false, x_pending = false, fail = false;
 
@@ -319,78 +361,86 @@ __global__ void __launch_bounds__(kInferThreads, 1)
         tc_fence_after();
         return !fail;
     };
-    /* the operands the group's threads wrote are visible to the tensor core,
-       then the leader issues one layer's chain */
-    auto mma = [&](uint32_t a, uint32_t w, int K, int N) {
+    /* the operands the group's threads wrote are visible to the tensor core
+       and the accumulator has been read out; then the leader issues one
+       chain */
+    auto mma = [&](uint32_t w, int K, int N, int R) {
         fence_async_smem();
         tc_fence_before();
         group_sync(bar_id);
         tc_fence_after();
         if (gt == 0) {
-            tc_layer(tmem, a, w, K, N);
+            tc_layer(tmem, aT, w, K, N, R);
             tc_commit(mb_mma);
         }
         mma_pending = true;
     };
-    /* bias + GELU + BF16 of the accumulator into the group's hidden tile */
+    /* bias + GELU + BF16 of the accumulator into the group's operand tile
+       (the chain that read it has completed) */
     auto epi_hidden = [&](const float* bl) {
-#pragma unroll 1
-        for (int c = 0; c < HID; c += 32) {
-            float v[32];
-            tmem_ld32(lane_base + (uint32_t)c, v);
+        tmem_chunks(lane_base, HID, [&](uint32_t (&r)[16], int c) {
+            const float4* b4 = reinterpret_cast<const float4*>(bl + c); /* 16-byte aligned */
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
+            for (int q = 0; q < 2; q++) {
+                const float4 ba = b4[2 * q], bb = b4[2 * q + 1];
+                const float* v = reinterpret_cast<const float*>(r) + 8 * q;
                 uint4 u;
-                u.x = pack_bf16(gelu_fast(v[8 * q + 0] + bl[c + 8 * q + 0]), gelu_fast(v[8 * q + 1] + bl[c + 8 * q + 1]));
-                u.y = pack_bf16(gelu_fast(v[8 * q + 2] + bl[c + 8 * q + 2]), gelu_fast(v[8 * q + 3] + bl[c + 8 * q + 3]));
-                u.z = pack_bf16(gelu_fast(v[8 * q + 4] + bl[c + 8 * q + 4]), gelu_fast(v[8 * q + 5] + bl[c + 8 * q + 5]));
-                u.w = pack_bf16(gelu_fast(v[8 * q + 6] + bl[c + 8 * q + 6]), gelu_fast(v[8 * q + 7] + bl[c + 8 * q + 7]));
-                *reinterpret_cast<uint4*>(hbuf + tc_off(row, c + 8 * q, kTile)) = u;
+                u.x = pack_bf16(gelu_fast(v[0] + ba.x), gelu_fast(v[1] + ba.y));
+                u.y = pack_bf16(gelu_fast(v[2] + ba.z), gelu_fast(v[3] + ba.w));
+                u.z = pack_bf16(gelu_fast(v[4] + bb.x), gelu_fast(v[5] + bb.y));
+                u.w = pack_bf16(gelu_fast(v[6] + bb.z), gelu_fast(v[7] + bb.w));
+                *reinterpret_cast<uint4*>(tbuf + tc_off(row, c + 8 * q, kTile)) = u;
             }
-        }
+        });
+    };
+    /* bias + running argmax over outputs [o0, o0 + cols); the first maximum wins */
+    auto epi_argmax = [&](int o0, int cols, float& best, int& bi) {
+        const float* bl = sb + 2 * HID + o0;
+        tmem_chunks(lane_base, cols, [&](uint32_t (&r)[16], int c) {
+            const float4* b4 = reinterpret_cast<const float4*>(bl + c); /* 16-byte aligned */
+#pragma unroll
+            for (int i = 0; i < 16; i += 4) {
+                const float4 b = b4[i / 4];
+                const float z0 = __uint_as_float(r[i]) + b.x, z1 = __uint_as_float(r[i + 1]) + b.y;
+                const float z2 = __uint_as_float(r[i + 2]) + b.z, z3 = __uint_as_float(r[i + 3]) + b.w;
+                if (z0 > best) { best = z0; bi = o0 + c + i; }
+                if (z1 > best) { best = z1; bi = o0 + c + i + 1; }
+                if (z2 > best) { best = z2; bi = o0 + c + i + 2; }
+                if (z3 > best) { best = z3; bi = o0 + c + i + 3; }
+            }
+        });
     };
 
     if (tile < ntiles) {
-        if (gt == 0) tma_tile(&tmX, aX, tile * kTile, mb_x);
+        if (gt == 0) tma_tile(&tmX, aT, tile * kTile, mb_x);
         x_pending = true;
     }
     while (!fail && tile < ntiles) {
         if (!wait(mb_x, ph_x, x_pending)) break;
-        mma(aX, aW1, IN, HID);
+        mma(aW1, IN, HID, HID);
         if (!wait(mb_mma, ph_mma, mma_pending)) break;
-        /* the features are consumed: request the group's next tile */
-        const int nxt = tile + 2 * (int)gridDim.x;
-        if (nxt < ntiles) {
-            if (gt == 0) tma_tile(&tmX, aX, nxt * kTile, mb_x);
-            x_pending = true;
-        }
         epi_hidden(sb);
-        mma(aH, aW2, HID, HID);
+        mma(aW2, HID, HID, HID);
         if (!wait(mb_mma, ph_mma, mma_pending)) break;
         epi_hidden(sb + HID);
-        mma(aH, aW3, HID, OUT);
+        /* layer 3: outputs 0..127, read out, then 128..159 in the same columns */
+        mma(aW3, HID, kOutA, OUT);
         if (!wait(mb_mma, ph_mma, mma_pending)) break;
-        /* bias + argmax over the 160 outputs; the first maximum wins */
-        const float* bl = sb + 2 * HID;
         float best = -INFINITY;
         int bi = 0;
-#pragma unroll 1
-        for (int c = 0; c < OUT; c += 32) {
-            float v[32];
-            tmem_ld32(lane_base + (uint32_t)c, v);
-#pragma unroll
-            for (int i = 0; i < 32; i++) {
-                const float z = v[i] + bl[c + i];
-                if (z > best) { best = z; bi = c + i; }
-            }
-        }
+        epi_argmax(0, kOutA, best, bi);
+        mma(aW3 + (uint32_t)(kOutA / 8) * 128u, HID, OUT - kOutA, OUT);
+        if (!wait(mb_mma, ph_mma, mma_pending)) break;
+        epi_argmax(kOutA, OUT - kOutA, best, bi);
         const int r = tile * kTile + row;
         if (r < n) cls[r] = (unsigned char)bi;
-        /* the accumulator is read out before the next tile's chain */
-        tc_fence_before();
-        group_sync(bar_id);
-        tc_fence_after();
-        tile = nxt;
+        /* the operand tile is free (the last chain has completed): the
+           group's next features go into it */
+        tile += kGroups * (int)gridDim.x;
+        if (tile < ntiles) {
+            if (gt == 0) tma_tile(&tmX, aT, tile * kTile, mb_x);
+            x_pending = true;
+        }
     }
     if (fail && gt == 0) atomicOr(err, errbit);
     /* nothing in flight may outlive the CTA: the group's copy and MMA chain

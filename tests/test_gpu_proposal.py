@@ -97,7 +97,7 @@ def test_mlp_predict_tensor_cores_matches_bf16_oracle(lib):
 
 
 def test_mlp_predict_pipelined_tiles_match_single_tiles(lib):
-    """many tiles per CTA (both pipeline slots, tiles that wait for their
+    """many tiles per CTA (every pipeline, tiles that wait for their
     features) give the classes that launches of a few tiles give"""
     torch = _torch()
     from ecmgenerator_gb300.proposal import ProposalModel
