@@ -405,7 +405,10 @@ def run_ours(args):
         e2e_steps = 0
         # every tick ends by writing the getters' host arrays
         sim.set_host_mirror(True)
-        _ = sim.view("position")
+        for _ in range(args.warmup):
+            sim.update()
+            _ = sim.view("position")
+            _ = sim.view("velocity")
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):

@@ -2643,8 +2643,7 @@ ecmg_status ecmg_set_host_mirror(ecmg_ctx* c, int on)
         }
     }
     c->mirror = on != 0;
-    c->mirror_stale = true;
-    c->graph_dirty = true; /* TickArgs::h_pos / h_vel */
+    c->mirror_stale = true; /* the copy after the tick, outside the graph: no recapture */
     return ECMG_OK;
 }
 
