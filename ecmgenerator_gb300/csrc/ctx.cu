@@ -258,14 +258,19 @@ struct ecmg_ctx {
         std::vector<std::vector<V2>> res;
         std::vector<char> ok;
         std::vector<int> fe;
-        /* a persistent helper thread that drives the planner pool */
+        /* a persistent helper thread: one search runs on it, several on the
+           planner pool (with the helper's own scratch for its share) */
         std::thread th;
         std::mutex mu;
         std::condition_variable cv, cv_done;
         bool work = false, stop = false;
         std::atomic<bool> done{true};
         bool active = false; /* started and not yet applied (calling thread only) */
-    } batch;
+        long long seq = 0;   /* start order */
+        PlanScratch scr;
+    } batch[2]; /* the last tick's searches and this tick's, in flight together */
+    long long batch_seq = 0;
+    std::mutex pool_mu; /* one user of the planner pool at a time */
     int replan_overlap = 1; /* 0 off, 1 when a search outlasts its tick, 2 always */
     long long batch_failed = 0; /* failed searches applied outside a tick, counted with the next one */
     DBuf<int> d_pend;
@@ -934,6 +939,7 @@ static void plan_jobs(ecmg_ctx* c, int m, const std::function<void(int, PlanScra
         for (int i = 0; i < m; i++) fn(i, c->scratch);
         return;
     }
+    std::lock_guard<std::mutex> l(c->pool_mu);
     c->pool.run(m, [&](int i, int w) { fn(i, c->pool.scratch[w]); });
 }
 
@@ -1013,7 +1019,7 @@ static ecmg_status plan_now(ecmg_ctx* c, const std::vector<int>& slot, const std
         ok[i] = plan(c, sc, start[i], c->paths[sl].back(), c->clear[sl], res[i], scr, &fe[i]) == ECMG_OK &&
                 !res[i].empty();
     };
-    if (c->batch.active) {
+    if (c->batch[0].active || c->batch[1].active) {
         for (int i = 0; i < m; i++) one(i, c->scratch);
     } else {
         plan_jobs(c, m, one);
@@ -1021,29 +1027,28 @@ static ecmg_status plan_now(ecmg_ctx* c, const std::vector<int>& slot, const std
     return apply_plans(c, slot, res, ok, fe, failed);
 }
 
-/* the searches of the current batch (on the helper thread) */
-static void batch_run(ecmg_ctx* c)
+/* the searches of batch b (on its helper thread) */
+static void batch_run(ecmg_ctx* c, ecmg_ctx::PlanBatch& b)
 {
-    ecmg_ctx::PlanBatch& b = c->batch;
     const int m = (int)b.slot.size();
     auto one = [&](int i, PlanScratch& scr) {
         SceneState* sc = c->scenes[c->slot_scene[b.slot[i]]].get();
         b.ok[i] = plan(c, sc, b.start[i], b.goal[i], b.clr[i], b.res[i], scr, &b.fe[i]) == ECMG_OK &&
                   !b.res[i].empty();
     };
-    if (c->pool.size() == 0) {
-        PlanScratch scr;
-        for (int i = 0; i < m; i++) one(i, scr);
+    if (m < 2 || c->pool.size() == 0) {
+        for (int i = 0; i < m; i++) one(i, b.scr);
     } else {
-        c->pool.run(m, [&](int i, int w) { one(i, c->pool.scratch[w]); });
+        std::lock_guard<std::mutex> l(c->pool_mu);
+        c->pool.run(m, [&](int i, int w) { one(i, w == 0 ? b.scr : c->pool.scratch[w]); });
     }
 }
 
-/* the re-plans of `slot` (ascending) on the helper thread, which drives the
-   pool of planner threads; goals and clearances are taken now */
-static void batch_start(ecmg_ctx* c, const std::vector<int>& slot, const std::vector<V2>& start)
+/* the re-plans of `slot` (ascending) on batch b's helper thread; goals and
+   clearances are taken now */
+static void batch_start(ecmg_ctx* c, ecmg_ctx::PlanBatch& b, const std::vector<int>& slot,
+                        const std::vector<V2>& start)
 {
-    ecmg_ctx::PlanBatch& b = c->batch;
     const int m = (int)slot.size();
     b.slot = slot;
     b.start = start;
@@ -1058,8 +1063,7 @@ static void batch_start(ecmg_ctx* c, const std::vector<int>& slot, const std::ve
     b.fe.assign(m, -1);
     c->pool.start(std::min(15, (int)std::max(1u, std::thread::hardware_concurrency()) - 1));
     if (!b.th.joinable())
-        b.th = std::thread([c] {
-            ecmg_ctx::PlanBatch& b = c->batch;
+        b.th = std::thread([c, &b] {
             for (;;) {
                 {
                     std::unique_lock<std::mutex> l(b.mu);
@@ -1067,7 +1071,7 @@ static void batch_start(ecmg_ctx* c, const std::vector<int>& slot, const std::ve
                     if (b.stop) return;
                     b.work = false;
                 }
-                batch_run(c);
+                batch_run(c, b);
                 {
                     std::lock_guard<std::mutex> l(b.mu);
                     b.done.store(true);
@@ -1076,6 +1080,7 @@ static void batch_start(ecmg_ctx* c, const std::vector<int>& slot, const std::ve
             }
         });
     b.active = true;
+    b.seq = ++c->batch_seq;
     {
         std::lock_guard<std::mutex> l(b.mu);
         b.done.store(false);
@@ -1084,10 +1089,9 @@ static void batch_start(ecmg_ctx* c, const std::vector<int>& slot, const std::ve
     b.cv.notify_one();
 }
 
-/* waits for the helper's searches and applies them */
-static ecmg_status batch_apply(ecmg_ctx* c, long long* failed)
+/* waits for batch b's searches and applies them */
+static ecmg_status batch_apply(ecmg_ctx* c, ecmg_ctx::PlanBatch& b, long long* failed)
 {
-    ecmg_ctx::PlanBatch& b = c->batch;
     if (!b.active) return ECMG_OK;
     {
         std::unique_lock<std::mutex> l(b.mu);
@@ -1097,25 +1101,44 @@ static ecmg_status batch_apply(ecmg_ctx* c, long long* failed)
     return apply_plans(c, b.slot, b.res, b.ok, b.fe, failed);
 }
 
-/* stops the helper thread (the context is going away) */
+/* the batch started first among those in flight (null: none) */
+static ecmg_ctx::PlanBatch* oldest_batch(ecmg_ctx* c)
+{
+    ecmg_ctx::PlanBatch *a = &c->batch[0], *b = &c->batch[1];
+    if (a->active && b->active) return a->seq < b->seq ? a : b;
+    return a->active ? a : b->active ? b : nullptr;
+}
+
+/* every batch in flight applied, in the order they were started */
+static ecmg_status batch_apply_all(ecmg_ctx* c, long long* failed)
+{
+    for (ecmg_ctx::PlanBatch* b; (b = oldest_batch(c)) != nullptr;) {
+        ecmg_status s = batch_apply(c, *b, failed);
+        if (s != ECMG_OK) return s;
+    }
+    return ECMG_OK;
+}
+
+/* stops the helper threads (the context is going away) */
 static void batch_stop(ecmg_ctx* c)
 {
-    ecmg_ctx::PlanBatch& b = c->batch;
-    if (!b.th.joinable()) return;
-    {
-        std::lock_guard<std::mutex> l(b.mu);
-        b.stop = true;
+    for (auto& b : c->batch) {
+        if (!b.th.joinable()) continue;
+        {
+            std::lock_guard<std::mutex> l(b.mu);
+            b.stop = true;
+        }
+        b.cv.notify_all();
+        b.th.join();
+        b.active = false;
     }
-    b.cv.notify_all();
-    b.th.join();
-    b.active = false;
 }
 
 /* every re-plan in flight applied: before anything that reads or changes
    paths, agents, the scene or the planner between ticks */
 static ecmg_status drain(ecmg_ctx* c)
 {
-    return c ? batch_apply(c, &c->batch_failed) : ECMG_OK;
+    return c ? batch_apply_all(c, &c->batch_failed) : ECMG_OK;
 }
 
 static cudaError_t ensure_check_buffers(ecmg_ctx* c)
@@ -2091,8 +2114,8 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         /* re-plans of the last tick still in flight: their agents are marked
            pending for this tick and stepped by k_fixup after it (the spawn
            stage needs the planner threads and the paths: apply them first) */
-        if (c->batch.active && (spawning || c->global_last() < 0)) {
-            ecmg_status ds = batch_apply(c, &st.replans_failed);
+        if (oldest_batch(c) && (spawning || c->global_last() < 0)) {
+            ecmg_status ds = batch_apply_all(c, &st.replans_failed);
             if (ds != ECMG_OK) return ds;
         }
         st.replans_failed += c->batch_failed;
@@ -2114,9 +2137,11 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             c->gate_left--;
             st.gated++;
         }
-        const int npend = c->batch.active ? (int)c->batch.slot.size() : 0;
+        /* at most one batch is in flight here: the last tick's */
+        ecmg_ctx::PlanBatch* carried = oldest_batch(c);
+        const int npend = carried ? (int)carried->slot.size() : 0;
         if (npend > 0) {
-            ecmg_status ps = stage_copy(c, c->d_pend.p, c->batch.slot.data(), sizeof(int) * (size_t)npend);
+            ecmg_status ps = stage_copy(c, c->d_pend.p, carried->slot.data(), sizeof(int) * (size_t)npend);
             if (ps != ECMG_OK) return ps;
             BinArgs bm;
             TickArgs tm;
@@ -2152,25 +2177,6 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             CK(enqueue_tick(c, last + 1, use_model));
         }
         CK(cudaEventRecord(c->ev_t1, c->stream));
-        if (npend > 0) {
-            auto hb = std::chrono::steady_clock::now();
-            /* the last tick's searches, their paths queued behind this tick's
-               kernels, then the pending agents' step of this tick */
-            ecmg_status bs = batch_apply(c, &st.replans_failed);
-            if (bs != ECMG_OK) return bs;
-            BinArgs bf;
-            TickArgs tf;
-            fill_args(c, bf, tf, use_model);
-            CK(launch_fixup(tf, c->d_pend.p, npend, c->stream));
-            CK(cudaMemcpyAsync(c->h_counters + kCounters, c->counters.p, sizeof(int) * kCounters,
-                               cudaMemcpyDeviceToHost, c->stream));
-            st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - hb).count();
-        }
-        /* the getters' host arrays: slots [0, last] are all this tick can
-           have moved (spawns included); the copy runs while the host does
-           the tick's bookkeeping */
-        if (c->mirror && !c->mirror_stale)
-            CK(launch_mirror(c->pos.p, c->vel.p, c->mirror_dev[0], c->mirror_dev[1], last + 1, c->sms, c->stream));
         /* the lists of the attraction kernel are final after it: bookkeeping
            and re-plans run on the host while the rest of the tick runs on the
            device; path uploads are queued behind the tick */
@@ -2235,12 +2241,30 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
             ecmg_status rs = replans(0, nr, r, rp);
             if (rs != ECMG_OK) return rs;
             if (overlap) {
-                batch_start(c, r, rp);
+                /* on the idle helper, beside the last tick's searches */
+                batch_start(c, c->batch[0].active ? c->batch[1] : c->batch[0], r, rp);
             } else {
                 rs = plan_now(c, r, rp, &st.replans_failed);
                 if (rs != ECMG_OK) return rs;
             }
         }
+        if (npend > 0) {
+            /* the last tick's searches, their paths queued behind this tick's
+               kernels, then the pending agents' step of this tick */
+            ecmg_status bs = batch_apply(c, *carried, &st.replans_failed);
+            if (bs != ECMG_OK) return bs;
+            BinArgs bf;
+            TickArgs tf;
+            fill_args(c, bf, tf, use_model);
+            CK(launch_fixup(tf, c->d_pend.p, npend, c->stream));
+            CK(cudaMemcpyAsync(c->h_counters + kCounters, c->counters.p, sizeof(int) * kCounters,
+                               cudaMemcpyDeviceToHost, c->stream));
+        }
+        /* the getters' host arrays: slots [0, last] are all this tick can
+           have moved (spawns included); the copy runs while the host does
+           the tick's bookkeeping */
+        if (c->mirror && !c->mirror_stale)
+            CK(launch_mirror(c->pos.p, c->vel.p, c->mirror_dev[0], c->mirror_dev[1], last + 1, c->sms, c->stream));
         st.host_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - h0).count();
         CK(cudaStreamSynchronize(c->stream));
         c->h_up_used = 0; /* every queued upload has been applied */
@@ -2266,10 +2290,11 @@ static ecmg_status run_ticks(ecmg_ctx* c, int n_ticks, ecmg_tick_stats* stats)
         st.replans_failed += fin[C_REPLAN_DEV];
         /* searches that ended while the tick's kernels ran are applied now, as
            re-plans served inside the tick; the others overlap the next tick */
-        if (c->batch.active && c->batch.done.load() && c->replan_overlap != 2) {
-            ecmg_status bs = batch_apply(c, &st.replans_failed);
-            if (bs != ECMG_OK) return bs;
-        }
+        if (ecmg_ctx::PlanBatch* nb = oldest_batch(c))
+            if (nb->done.load() && c->replan_overlap != 2) {
+                ecmg_status bs = batch_apply(c, *nb, &st.replans_failed);
+                if (bs != ECMG_OK) return bs;
+            }
         auto h1 = std::chrono::steady_clock::now();
         /* attraction and neighbour kernels run side by side: both are timed
            from their common start */
