@@ -167,7 +167,8 @@ ecmg_status ecmg_set_planner_mode(ecmg_ctx* ctx, int mode);
    after ecmg_tick returns, and the next tick skips those agents in its
    attraction and ORCA kernels and steps them, with their new paths, in a
    small launch after its own kernels -- the same inputs and functions, so the
-   same results, the searches overlapping a whole tick of device work.
+   same results, the searches overlapping a whole tick of device work (the
+   next tick's own searches start beside them).
    Mode 2: every search is carried into the next tick that way.  Mode 0: the
    tick waits for its searches.  Every entry point that reads or changes
    paths, agents, the scene or the planner waits for the searches first. */
