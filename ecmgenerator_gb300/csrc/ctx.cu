@@ -84,9 +84,7 @@ struct GoalAreaH {
 /* Host threads for the planner calls of a tick (re-plans, spawned agents):
    started once, idle on a condition variable between ticks.  run(m, fn)
    calls fn(i, w) for i in [0, m) on the calling thread (w = 0) and the
-   workers (w = 1..size()), each with its own planner scratch.  A run of m
-   jobs enlists at most m - 1 workers (tickets): a few searches do not wait
-   for every idle thread of the pool to wake up. */
+   workers (w = 1..size()), each with its own planner scratch. */
 class HostPool {
 public:
     ~HostPool()
@@ -112,20 +110,15 @@ public:
             for (int i = 0; i < m; i++) fn(i, 0);
             return;
         }
-        const int want = std::min(m - 1, (int)th_.size());
         {
             std::lock_guard<std::mutex> l(mu_);
             job_ = &fn;
             m_ = m;
             next_ = 0;
-            tickets_ = want;
-            busy_ = want;
+            busy_ = (int)th_.size();
             gen_++;
         }
-        if (want == (int)th_.size())
-            cv_.notify_all();
-        else
-            for (int q = 0; q < want; q++) cv_.notify_one();
+        cv_.notify_all();
         for (int i; (i = next_.fetch_add(1)) < m;) fn(i, 0);
         std::unique_lock<std::mutex> l(mu_);
         done_.wait(l, [this] { return busy_ == 0; });
@@ -141,10 +134,9 @@ private:
             int m;
             {
                 std::unique_lock<std::mutex> l(mu_);
-                cv_.wait(l, [&] { return stop_ || (gen_ != seen && tickets_ > 0); });
+                cv_.wait(l, [&] { return stop_ || gen_ != seen; });
                 if (stop_) return;
                 seen = gen_;
-                tickets_--;
                 job = job_;
                 m = m_;
             }
@@ -157,7 +149,7 @@ private:
     std::mutex mu_;
     std::condition_variable cv_, done_;
     const std::function<void(int, int)>* job_ = nullptr;
-    int m_ = 0, busy_ = 0, tickets_ = 0;
+    int m_ = 0, busy_ = 0;
     unsigned gen_ = 0;
     std::atomic<int> next_{0};
     bool stop_ = false;
