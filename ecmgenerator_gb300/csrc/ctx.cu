@@ -12,6 +12,7 @@
  */
 #include "../../include/ecmg.h"
 #include "ecmg_internal.h"
+#include "host_pool.h"
 #include "host_scene.h"
 
 #include <algorithm>
@@ -79,80 +80,6 @@ struct SpawnAreaH {
 struct GoalAreaH {
     int id = 0;
     float x = 0, y = 0, hw = 0, hh = 0;
-};
-
-/* Host threads for the planner calls of a tick (re-plans, spawned agents):
-   started once, idle on a condition variable between ticks.  run(m, fn)
-   calls fn(i, w) for i in [0, m) on the calling thread (w = 0) and the
-   workers (w = 1..size()), each with its own planner scratch. */
-class HostPool {
-public:
-    ~HostPool()
-    {
-        {
-            std::lock_guard<std::mutex> l(mu_);
-            stop_ = true;
-        }
-        cv_.notify_all();
-        for (auto& t : th_) t.join();
-    }
-    int size() const { return (int)th_.size(); }
-    std::vector<PlanScratch> scratch; /* [size() + 1] */
-    void start(int n)
-    {
-        if (!th_.empty() || n < 1) return;
-        scratch.resize((size_t)n + 1);
-        for (int w = 1; w <= n; w++) th_.emplace_back([this, w] { loop(w); });
-    }
-    void run(int m, const std::function<void(int, int)>& fn)
-    {
-        if (th_.empty() || m < 2) {
-            for (int i = 0; i < m; i++) fn(i, 0);
-            return;
-        }
-        {
-            std::lock_guard<std::mutex> l(mu_);
-            job_ = &fn;
-            m_ = m;
-            next_ = 0;
-            busy_ = (int)th_.size();
-            gen_++;
-        }
-        cv_.notify_all();
-        for (int i; (i = next_.fetch_add(1)) < m;) fn(i, 0);
-        std::unique_lock<std::mutex> l(mu_);
-        done_.wait(l, [this] { return busy_ == 0; });
-        job_ = nullptr;
-    }
-
-private:
-    void loop(int w)
-    {
-        unsigned seen = 0;
-        for (;;) {
-            const std::function<void(int, int)>* job;
-            int m;
-            {
-                std::unique_lock<std::mutex> l(mu_);
-                cv_.wait(l, [&] { return stop_ || gen_ != seen; });
-                if (stop_) return;
-                seen = gen_;
-                job = job_;
-                m = m_;
-            }
-            for (int i; (i = next_.fetch_add(1)) < m;) (*job)(i, w);
-            std::lock_guard<std::mutex> l(mu_);
-            if (--busy_ == 0) done_.notify_one();
-        }
-    }
-    std::vector<std::thread> th_;
-    std::mutex mu_;
-    std::condition_variable cv_, done_;
-    const std::function<void(int, int)>* job_ = nullptr;
-    int m_ = 0, busy_ = 0;
-    unsigned gen_ = 0;
-    std::atomic<int> next_{0};
-    bool stop_ = false;
 };
 
 struct SceneState {
@@ -240,7 +167,7 @@ struct ecmg_ctx {
     ecmg_plan_fn plan_fn = nullptr;
     void* plan_user = nullptr;
     PlanScratch scratch;
-    HostPool pool; /* planner threads (built-in planner only: it is re-entrant) */
+    HostPool<PlanScratch> pool; /* planner threads (built-in planner only: it is re-entrant) */
     int planner_mode = ECMG_PLANNER_REFERENCE; /* the reference's paths unless FAST is chosen */
     bool replan_enabled = true;
     bool spawn_enabled = true; /* off while the autotuner runs its trial ticks */
