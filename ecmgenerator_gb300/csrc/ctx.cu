@@ -190,7 +190,7 @@ struct ecmg_ctx {
         std::thread th;
         std::mutex mu;
         std::condition_variable cv, cv_done;
-        bool work = false, stop = false;
+        std::atomic<bool> work{false}, stop{false};
         std::atomic<bool> done{true};
         bool active = false; /* started and not yet applied (calling thread only) */
         long long seq = 0;   /* start order */
@@ -954,6 +954,18 @@ static ecmg_status plan_now(ecmg_ctx* c, const std::vector<int>& slot, const std
     return apply_plans(c, slot, res, ok, fe, failed);
 }
 
+/* polls flag (yielding the core between polls) until it is set or `limit`
+   has passed */
+constexpr std::chrono::microseconds kSpinWait{1000};
+static void spin_until(const std::atomic<bool>& flag, std::chrono::microseconds limit)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int it = 0; !flag.load(); it++) {
+        if ((it & 63) == 63 && std::chrono::steady_clock::now() - t0 > limit) return;
+        std::this_thread::yield();
+    }
+}
+
 /* the searches of batch b (on its helper thread) */
 static void batch_run(ecmg_ctx* c, ecmg_ctx::PlanBatch& b)
 {
@@ -992,9 +1004,13 @@ static void batch_start(ecmg_ctx* c, ecmg_ctx::PlanBatch& b, const std::vector<i
     if (!b.th.joinable())
         b.th = std::thread([c, &b] {
             for (;;) {
+                /* the next batch usually comes within a tick: poll for it a
+                   while before sleeping (a sleeping thread takes tens of
+                   microseconds to wake) */
+                spin_until(b.work, kSpinWait);
                 {
                     std::unique_lock<std::mutex> l(b.mu);
-                    b.cv.wait(l, [&] { return b.work || b.stop; });
+                    b.cv.wait(l, [&] { return b.work.load() || b.stop.load(); });
                     if (b.stop) return;
                     b.work = false;
                 }
@@ -1020,6 +1036,7 @@ static void batch_start(ecmg_ctx* c, ecmg_ctx::PlanBatch& b, const std::vector<i
 static ecmg_status batch_apply(ecmg_ctx* c, ecmg_ctx::PlanBatch& b, long long* failed)
 {
     if (!b.active) return ECMG_OK;
+    spin_until(b.done, kSpinWait); /* the caller has nothing else to do */
     {
         std::unique_lock<std::mutex> l(b.mu);
         b.cv_done.wait(l, [&] { return b.done.load(); });
